@@ -1,0 +1,270 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle is a CPU restatement of Bembel's H2 single-layer path (geometry,
+element tree, block partition, DuffyTrick quadrature, FMM moments/transfers,
+H2 assembly and matvec, dense Galerkin matrix, load vectors, potential,
+GMRES). It is used by tests/, the smoke check and bench.py's CPU-baseline leg
+only; the bembel_gb300 package never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+LAPLACE, HELMHOLTZ, MAXWELL, DUMMY = 0, 1, 2, 3
+DENSE, LOWRANK = 2, 1
+
+
+def build():
+    """Compile the oracle with its Makefile (portable flags, x86_64 and aarch64)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P, I, D, L_ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_long
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        lp = ctypes.POINTER(ctypes.c_long)
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [ctypes.c_char_p, I, I, I, D, D, I, D, I, I, I]
+        L.orc_destroy.argtypes = [P]
+        L.orc_info.argtypes = [P, lp]
+        L.orc_assemble_seconds.restype = D
+        L.orc_assemble_seconds.argtypes = [P]
+        L.orc_transform_csr.argtypes = [P, ip, ip, dp]
+        L.orc_elements.argtypes = [P, ip, dp]
+        L.orc_leaves.argtypes = [P, ip]
+        L.orc_leaf_matrix.argtypes = [P, L_, I, I, dp]
+        L.orc_element_pair.argtypes = [P, I, I, dp]
+        L.orc_pair_class.argtypes = [P, I, I, ip, dp]
+        L.orc_dummy_integrate.restype = D
+        L.orc_dummy_integrate.argtypes = [P, I, I, I, I, I, I]
+        L.orc_point_integrand.argtypes = [P, I, D, D, D, D, dp]
+        L.orc_surface_point.argtypes = [P, I, D, D, dp]
+        L.orc_transfer_matrices.argtypes = [I, dp]
+        L.orc_moment2d.argtypes = [I, I, I, I, I, I, dp]
+        L.orc_moments.argtypes = [P, I, dp]
+        L.orc_forward_transform.argtypes = [dp, I, I, dp, I, I, dp, I, dp]
+        L.orc_backward_transform.argtypes = [dp, I, I, dp, I, I, dp, I, dp]
+        L.orc_matvec.restype = I
+        L.orc_matvec.argtypes = [P, dp, dp, I]
+        L.orc_matvec_ss.restype = I
+        L.orc_matvec_ss.argtypes = [P, dp, dp]
+        L.orc_dense_ss.argtypes = [P, dp]
+        L.orc_load_vector.argtypes = [P, I, dp, dp]
+        L.orc_potential.argtypes = [P, dp, dp, I, dp]
+        L.orc_gmres.restype = I
+        L.orc_gmres.argtypes = [P, dp, dp, D, I, I]
+        L.orc_threads.restype = I
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def transfer_matrices(np_):
+    out = np.zeros((4 * np_ * np_, np_ * np_))  # column-major storage of np2 x 4np2
+    lib().orc_transfer_matrices(np_, _dp(out))
+    return out.T.copy()
+
+
+def moment2d(P, cluster_level, cluster_ref, np_, d1=False, d2=False):
+    rows = np_ * np_
+    cols = (P + 1) ** 2 * 4 ** cluster_ref
+    out = np.zeros((cols, rows))
+    lib().orc_moment2d(P, cluster_level, cluster_ref, np_, int(d1), int(d2), _dp(out))
+    return out.T.copy()
+
+
+def forward_transform(mom, T, steps, X):
+    np_ = int(round(np.sqrt(T.shape[0])))
+    mr, mc = mom.shape
+    xc = X.shape[1]
+    sizes = [mr * (xc // 4 ** i) for i in range(steps + 1)]
+    out = np.zeros(sum(sizes))
+    lib().orc_forward_transform(_dp(np.asfortranarray(mom)), mr, mc, _dp(np.asfortranarray(T)), np_, steps,
+                                _dp(np.asfortranarray(X)), xc, _dp(out))
+    res, o = [], 0
+    for i in range(steps + 1):
+        c = xc // 4 ** i
+        res.append(out[o:o + mr * c].reshape((mr, c), order="F"))
+        o += mr * c
+    return res
+
+
+def backward_transform(mom, T, steps, Z):
+    np_ = int(round(np.sqrt(T.shape[0])))
+    mr, mc = mom.shape
+    xc = Z[0].shape[1]
+    flat = np.concatenate([np.asfortranarray(z).ravel(order="F") for z in Z])
+    out = np.zeros(mc * xc)
+    lib().orc_backward_transform(_dp(np.asfortranarray(mom)), mr, mc, _dp(np.asfortranarray(T)), np_, steps,
+                                 _dp(flat), xc, _dp(out))
+    return out
+
+
+class Problem:
+    """Oracle discretisation: geometry file, refinement M, degree P, operator."""
+
+    def __init__(self, geo, M, P, kind=LAPLACE, kappa=0.0, np_=9, eta=1.6, mcl=1, assemble=True,
+                 dummy_fun=0):
+        kappa = complex(kappa)
+        self.h = lib().orc_create(geo.encode(), M, P, kind, kappa.real, kappa.imag, np_, eta, mcl,
+                                  int(assemble), dummy_fun)
+        if not self.h:
+            raise RuntimeError("oracle problem creation failed")
+        info = np.zeros(12, dtype=np.int64)
+        lib().orc_info(self.h, info.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+        (self.ne, self.S, self.N, self.n_leaves, self.n_dense, self.n_lowrank, self.vd, self.nc, self.np,
+         self.nnz, self.M, self.P) = [int(v) for v in info]
+        self.kind = kind
+        self.kappa = kappa
+        self.complex = kind in (HELMHOLTZ, MAXWELL)
+        self.dtype = np.complex128 if self.complex else np.float64
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    @property
+    def assemble_seconds(self):
+        return lib().orc_assemble_seconds(self.h)
+
+    def transform_csr(self):
+        ptr = np.zeros(self.S + 1, dtype=np.int32)
+        idx = np.zeros(self.nnz, dtype=np.int32)
+        val = np.zeros(self.nnz)
+        lib().orc_transform_csr(self.h, _ip(ptr), _ip(idx), _dp(val))
+        return ptr, idx, val
+
+    def transform_dense(self):
+        ptr, idx, val = self.transform_csr()
+        T = np.zeros((self.S, self.N))
+        for r in range(self.S):
+            for k in range(ptr[r], ptr[r + 1]):
+                T[r, idx[k]] += val[k]
+        return T
+
+    def elements(self):
+        ints = np.zeros((self.ne, 7), dtype=np.int32)
+        dbl = np.zeros((self.ne, 6))
+        lib().orc_elements(self.h, _ip(ints), _dp(dbl))
+        return ints, dbl
+
+    def leaves(self):
+        out = np.zeros((self.n_leaves, 7), dtype=np.int32)
+        lib().orc_leaves(self.h, _ip(out))
+        return out
+
+    def leaf_matrix(self, leaf, rc=0, cc=0):
+        lv = self.leaves()[leaf]
+        if lv[0] == DENSE:
+            n = lv[6] * (self.P + 1) ** 2
+        else:
+            n = self.nc * self.np * self.np
+        out = np.zeros((n, n), dtype=self.dtype)
+        buf = out.T.copy()  # column-major
+        if lib().orc_leaf_matrix(self.h, leaf, rc, cc, _dp(buf.view(np.float64))) != 0:
+            raise RuntimeError("H2 matrix not assembled")
+        return buf.T.copy()
+
+    def element_pair(self, id1, id2):
+        n = self.vd * (self.P + 1) ** 2
+        buf = np.zeros((n, n), dtype=self.dtype)
+        lib().orc_element_pair(self.h, id1, id2, _dp(buf.view(np.float64)))
+        return buf.T.copy()
+
+    def pair_class(self, id1, id2):
+        out = np.zeros(4, dtype=np.int32)
+        d = np.zeros(1)
+        lib().orc_pair_class(self.h, id1, id2, _ip(out), _dp(d))
+        return tuple(int(v) for v in out), float(d[0])
+
+    def dummy_integrate(self, which, id1, id2, qdeg, rot1=0, rot2=0):
+        return lib().orc_dummy_integrate(self.h, which, id1, id2, qdeg, rot1, rot2)
+
+    def point_integrand(self, id_, s1, t1, s2, t2):
+        n = self.vd * (self.P + 1) ** 2
+        buf = np.zeros((n, n), dtype=self.dtype)
+        lib().orc_point_integrand(self.h, id_, s1, t1, s2, t2, _dp(buf.view(np.float64)))
+        return buf.T.copy()
+
+    def surface_point(self, patch, s, t):
+        out = np.zeros(12)
+        lib().orc_surface_point(self.h, patch, s, t, _dp(out))
+        return out
+
+    def moments(self, comp=0):
+        rows = self.nc * self.np * self.np
+        cols = 4 * (self.P + 1) ** 2
+        out = np.zeros((cols, rows))
+        lib().orc_moments(self.h, comp, _dp(out))
+        return out.T.copy()
+
+    def matvec(self, x):
+        x = np.asarray(x, dtype=self.dtype)
+        squeeze = x.ndim == 1
+        X = np.asfortranarray(x.reshape(self.N, -1))
+        Y = np.zeros_like(X, order="F")
+        if lib().orc_matvec(self.h, _dp(X.view(np.float64)), _dp(Y.view(np.float64)), X.shape[1]) != 0:
+            raise RuntimeError("H2 matrix not assembled")
+        return Y[:, 0] if squeeze else Y
+
+    def matvec_ss(self, x):
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        y = np.zeros_like(x)
+        if lib().orc_matvec_ss(self.h, _dp(x.view(np.float64)), _dp(y.view(np.float64))) != 0:
+            raise RuntimeError("H2 matrix not assembled")
+        return y
+
+    def dense_ss(self):
+        out = np.zeros((self.S, self.S), dtype=self.dtype, order="F")
+        lib().orc_dense_ss(self.h, _dp(out.view(np.float64) if not self.complex else
+                                       out.reshape(-1, order="F").view(np.float64)))
+        return out
+
+    def dense(self):
+        D = self.dense_ss()
+        T = self.transform_dense()
+        return T.T @ D @ T
+
+    def load_vector(self, kind, prm):
+        p = np.zeros(8)
+        p[:len(prm)] = prm
+        out = np.zeros(self.N, dtype=self.dtype)
+        lib().orc_load_vector(self.h, kind, _dp(p), _dp(out.view(np.float64)))
+        return out
+
+    def potential(self, rho, pts):
+        rho = np.ascontiguousarray(rho, dtype=self.dtype)
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        out = np.zeros(pts.shape[0], dtype=self.dtype)
+        lib().orc_potential(self.h, _dp(rho.view(np.float64)), _dp(pts), pts.shape[0], _dp(out.view(np.float64)))
+        return out
+
+    def gmres(self, b, tol=1e-10, restart=100, maxit=1000):
+        b = np.ascontiguousarray(b, dtype=self.dtype)
+        x = np.zeros_like(b)
+        it = lib().orc_gmres(self.h, _dp(b.view(np.float64)), _dp(x.view(np.float64)), tol, restart, maxit)
+        return x, it
+
+
+def threads():
+    return lib().orc_threads()
