@@ -1,0 +1,331 @@
+"""bembel_gb300 — GB300-native H2 single-layer boundary element operator.
+
+Python mirror of the reference's user-facing interface for the H2 path
+(Geometry, AnsatzSpace, {Laplace,Helmholtz,Maxwell}SingleLayerOperator,
+DiscreteOperator<H2Matrix<S>, Op>, H2Matrix * x, DiscreteLinearForm,
+DiscretePotential), over the C ABI of include/bembel_gb300.h.
+
+    geo = Geometry("sphere.dat")
+    space = AnsatzSpace(geo, refinement_level=5, polynomial_degree=2)
+    op = DiscreteOperator(space, LaplaceSingleLayerOperator())
+    op.compute()
+    A = op.get_discrete_operator()
+    y = A @ x                       # FP64 H2 matvec on the GPU
+    x, stats = A.solve(b, tol=1e-8) # GMRES with FP64 iterative refinement
+
+Arrays may be numpy arrays (host memory) or CUDA torch tensors (device
+memory); blocks of right-hand sides are (N, nrhs).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import BembelError, H2Params, SolveParams, SolveStats
+
+__all__ = ["Context", "Geometry", "AnsatzSpace", "LaplaceSingleLayerOperator", "HelmholtzSingleLayerOperator",
+           "MaxwellSingleLayerOperator", "DiscreteOperator", "H2Matrix", "BembelError", "default_context"]
+
+_default_ctx = None
+
+
+class Context:
+    """One GPU (device >= 0) or a host-only context (device = -1) that can build
+    and inspect discretisations but runs no device work."""
+
+    def __init__(self, device=0):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        st = L.bg_context_create(device, ctypes.byref(h))
+        if st != _lib.BG_OK:
+            raise BembelError(st, "cannot create a context on device %d" % device)
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().bg_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        _lib.check(st, self.h)
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class Geometry:
+    """Geometry(filename): patches of a .dat file (Geometry/Geometry.hpp:89-102)."""
+
+    def __init__(self, filename, context=None):
+        self.ctx = context or default_context()
+        h = ctypes.c_void_p()
+        self.ctx.check(_lib.load().bg_geometry_load_dat(self.ctx.h, str(filename).encode(), ctypes.byref(h)))
+        self.h = h
+        self.filename = str(filename)
+
+    def surface_point(self, patch, s, t):
+        out = np.zeros(12)
+        self.ctx.check(_lib.load().bg_geometry_surface_point(self.h, patch, s, t, _dp(out)))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib.load().bg_geometry_destroy(self.h)
+            self.h = None
+
+
+class AnsatzSpace:
+    """AnsatzSpace(geometry, refinement_level, polynomial_degree) (AnsatzSpace.hpp:82-111)."""
+
+    def __init__(self, geometry, refinement_level, polynomial_degree, knot_repetition=1):
+        if knot_repetition != 1:
+            raise BembelError(_lib.BG_UNSUPPORTED, "knot repetition other than 1")
+        self.geometry = geometry
+        self.refinement_level = int(refinement_level)
+        self.polynomial_degree = int(polynomial_degree)
+
+
+class _SingleLayer:
+    kind = None
+    is_complex = False
+
+    def __init__(self):
+        self.wavenumber = 0j
+
+    def set_wavenumber(self, k):
+        self.wavenumber = complex(k)
+
+    def get_wavenumber(self):
+        return self.wavenumber
+
+
+class LaplaceSingleLayerOperator(_SingleLayer):
+    """1/(4 pi |x-y|) (Laplace/SingleLayerOperator.hpp)."""
+    kind = _lib.LAPLACE_SL
+
+
+class HelmholtzSingleLayerOperator(_SingleLayer):
+    """exp(-i k |x-y|)/(4 pi |x-y|) (Helmholtz/SingleLayerOperator.hpp)."""
+    kind = _lib.HELMHOLTZ_SL
+    is_complex = True
+
+
+class MaxwellSingleLayerOperator(_SingleLayer):
+    """Electric field integral operator (Maxwell/SingleLayerOperator.hpp)."""
+    kind = _lib.MAXWELL_SL
+    is_complex = True
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+class H2Matrix:
+    """Device-resident H2 matrix; rows() == cols() == number of DOFs."""
+
+    def __init__(self, dop):
+        self._dop = dop
+
+    @property
+    def h(self):
+        return self._dop.h
+
+    def rows(self):
+        return self._dop.N
+
+    def cols(self):
+        return self._dop.N
+
+    @property
+    def shape(self):
+        return (self._dop.N, self._dop.N)
+
+    @property
+    def dtype(self):
+        return np.complex128 if self._dop.is_complex else np.float64
+
+    def __matmul__(self, x):
+        return self.matvec(x)
+
+    def matvec(self, x, precision="fp64", out=None, alpha=1.0, beta=0.0):
+        """out = beta * out + alpha * A x (H2DenseProduct.hpp:268-290)."""
+        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_FP32
+        N = self._dop.N
+        a = np.array([complex(alpha).real, complex(alpha).imag])
+        b = np.array([complex(beta).real, complex(beta).imag])
+        if _is_torch(x):
+            import torch
+            squeeze = x.dim() == 1
+            X = (x.reshape(N, -1)).t().contiguous()  # (nrhs, N): column-major N x nrhs
+            Y = torch.empty_like(X) if out is None else out.reshape(N, -1).t().contiguous()
+            on_dev = 1 if X.is_cuda else 0
+            if not on_dev:
+                raise BembelError(_lib.BG_INVALID_ARG, "pass numpy arrays for host memory")
+            self._dop.ctx.check(_lib.load().bg_matvec(self.h, ctypes.c_void_p(X.data_ptr()), N,
+                                                      ctypes.c_void_p(Y.data_ptr()), N, X.shape[0], _dp(a), _dp(b),
+                                                      prec, on_dev))
+            Y = Y.t()
+            return Y.reshape(N) if squeeze else Y
+        x = np.asarray(x, dtype=self.dtype)
+        squeeze = x.ndim == 1
+        X = np.asfortranarray(x.reshape(N, -1))
+        Y = np.zeros_like(X, order="F") if out is None else np.asfortranarray(np.asarray(out, self.dtype).reshape(N, -1))
+        self._dop.ctx.check(_lib.load().bg_matvec(self.h, X.ctypes.data_as(ctypes.c_void_p), N,
+                                                  Y.ctypes.data_as(ctypes.c_void_p), N, X.shape[1], _dp(a), _dp(b),
+                                                  prec, 0))
+        return Y[:, 0].copy() if squeeze else Y
+
+    def solve(self, b, tol=1e-8, restart=60, max_iter=2000, inner="fp32", inner_tol=1e-5, max_refinements=12):
+        """GMRES with FP64 iterative refinement; returns (x, stats dict)."""
+        p = SolveParams()
+        _lib.load().bg_solve_params_default(ctypes.byref(p))
+        p.tol, p.restart, p.max_iter = tol, restart, max_iter
+        p.inner_precision = _lib.PREC_FP32 if inner == "fp32" else _lib.PREC_FP64
+        p.inner_tol, p.max_refinements = inner_tol, max_refinements
+        st = SolveStats()
+        N = self._dop.N
+        if _is_torch(b):
+            import torch
+            squeeze = b.dim() == 1
+            B = b.reshape(N, -1).t().contiguous()
+            X = torch.empty_like(B)
+            status = _lib.load().bg_solve(self.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                          B.shape[0], ctypes.byref(p), ctypes.byref(st), 1 if B.is_cuda else 0)
+            x = X.t()
+            x = x.reshape(N) if squeeze else x
+        else:
+            b = np.asarray(b, dtype=self.dtype)
+            squeeze = b.ndim == 1
+            B = np.asfortranarray(b.reshape(N, -1))
+            X = np.zeros_like(B, order="F")
+            status = _lib.load().bg_solve(self.h, B.ctypes.data_as(ctypes.c_void_p), X.ctypes.data_as(ctypes.c_void_p),
+                                          B.shape[1], ctypes.byref(p), ctypes.byref(st), 0)
+            x = X[:, 0].copy() if squeeze else X
+        stats = {k: getattr(st, k) for k, _ in SolveStats._fields_}
+        if status not in (_lib.BG_OK, _lib.BG_NOT_CONVERGED):
+            self._dop.ctx.check(status)
+        stats["converged"] = status == _lib.BG_OK
+        return x, stats
+
+
+class DiscreteOperator:
+    """DiscreteOperator<H2Matrix<S>, Op>(ansatz_space) (DiscreteOperator.hpp:107-145)."""
+
+    def __init__(self, ansatz_space, linear_operator, n_p=9, eta=1.6, min_cluster_level=1, store_fp64_far=True):
+        self.ansatz_space = ansatz_space
+        self.lin_op = linear_operator
+        self.ctx = ansatz_space.geometry.ctx
+        prm = H2Params()
+        _lib.load().bg_h2_params_default(ctypes.byref(prm))
+        prm.n_p, prm.eta, prm.min_cluster_level, prm.store_fp64_far = n_p, eta, min_cluster_level, int(store_fp64_far)
+        h = ctypes.c_void_p()
+        self.ctx.check(_lib.load().bg_operator_create(self.ctx.h, ansatz_space.geometry.h,
+                                                      ansatz_space.refinement_level, ansatz_space.polynomial_degree,
+                                                      linear_operator.kind, ctypes.byref(prm), ctypes.byref(h)))
+        self.h = h
+        info = self.info()
+        self.N = int(info[0])
+        self.S = int(info[1])
+        self.ne = int(info[2])
+        self.n_dense = int(info[3])
+        self.n_lowrank = int(info[4])
+        self.is_complex = bool(info[8])
+        self._matrix = H2Matrix(self)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _lib.load().bg_operator_destroy(self.h)
+            self.h = None
+
+    def info(self):
+        out = np.zeros(16, dtype=np.int64)
+        self.ctx.check(_lib.load().bg_operator_info(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
+        return out
+
+    def get_linear_operator(self):
+        return self.lin_op
+
+    def compute(self):
+        """Assemble the near and far field on the GPU (H2Matrix::init_H2Matrix)."""
+        if self.lin_op.is_complex:
+            k = complex(self.lin_op.wavenumber)
+            self.ctx.check(_lib.load().bg_operator_set_wavenumber(self.h, k.real, k.imag))
+        self.ctx.check(_lib.load().bg_operator_assemble(self.h))
+
+    def assembly_times(self):
+        t = np.zeros(3)
+        self.ctx.check(_lib.load().bg_operator_assembly_times(self.h, _dp(t)))
+        return {"near_s": t[0], "far_s": t[1], "total_s": t[2]}
+
+    def get_discrete_operator(self):
+        return self._matrix
+
+    # -- load vectors / potentials (DiscreteLinearForm, DiscretePotential) --
+    def load_vector(self, kind, params):
+        """Dirichlet-trace load vectors for analytic data: kind 0 point source
+        1/(4 pi r), 1 Helmholtz point source, 2 plane wave; params (nrhs, 3)."""
+        prm = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, 3))
+        k = prm.shape[0]
+        out = np.zeros((self.N, k), dtype=np.complex128 if self.is_complex else np.float64, order="F")
+        self.ctx.check(_lib.load().bg_load_vector(self.h, kind, _dp(prm), k, out.ctypes.data_as(ctypes.c_void_p), 0))
+        return out
+
+    def potential(self, rho, points):
+        rho = np.asfortranarray(np.asarray(rho, dtype=np.complex128 if self.is_complex else np.float64).reshape(self.N, -1))
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+        out = np.zeros((pts.shape[0], rho.shape[1]), dtype=rho.dtype, order="F")
+        self.ctx.check(_lib.load().bg_potential(self.h, rho.ctypes.data_as(ctypes.c_void_p), rho.shape[1], _dp(pts),
+                                                pts.shape[0], out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    # -- inspection --
+    def elements(self):
+        ints = np.zeros((self.ne, 5), dtype=np.int32)
+        dbl = np.zeros((self.ne, 6))
+        self.ctx.check(_lib.load().bg_operator_elements(self.h, ints.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                        _dp(dbl)))
+        return ints, dbl
+
+    def leaves(self):
+        out = np.zeros((self.n_dense + self.n_lowrank, 4), dtype=np.int32)
+        self.ctx.check(_lib.load().bg_operator_leaves(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out
+
+    def transform_csr(self):
+        info = self.info()
+        nnz = int(info[12])
+        ptr = np.zeros(self.S + 1, dtype=np.int32)
+        idx = np.zeros(nnz, dtype=np.int32)
+        val = np.zeros(nnz)
+        ip = ctypes.POINTER(ctypes.c_int)
+        self.ctx.check(_lib.load().bg_operator_transform(self.h, ptr.ctypes.data_as(ip), idx.ctypes.data_as(ip),
+                                                         _dp(val)))
+        return ptr, idx, val
+
+    def leaf_block(self, leaf, rc=0, cc=0):
+        lv = self.leaves()[leaf]
+        info = self.info()
+        p2 = (int(info[10]) + 1) ** 2
+        if lv[0] == 2:
+            n = int(info[11]) * p2
+        else:
+            n = int(info[6]) * int(info[7]) ** 2
+        dt = np.complex128 if self.is_complex else np.float64
+        buf = np.zeros(n * n, dtype=dt)
+        self.ctx.check(_lib.load().bg_operator_leaf_block(self.h, leaf, rc, cc, _dp(buf.view(np.float64))))
+        return buf.reshape((n, n), order="F")

@@ -1,0 +1,682 @@
+// C ABI of the GB300 H2 single-layer operator (include/bembel_gb300.h):
+// context, geometry and operator lifecycle, device tables, assembly and the
+// batched H2 matvec.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <new>
+
+#include "bg_operator.hpp"
+
+using namespace bg;
+
+bg_status set_error(bg_context* ctx, bg_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+bg_status cuda_status(bg_context* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return BG_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return set_error(ctx, BG_OOM, m);
+  return set_error(ctx, BG_DEVICE_ERROR, m);
+}
+#define BG_CHECK(expr, what)                                   \
+  do {                                                         \
+    bg_status _st = cuda_status(op->ctx, (expr), (what));      \
+    if (_st != BG_OK) return _st;                              \
+  } while (0)
+
+extern "C" {
+
+void bg_h2_params_default(bg_h2_params* p) {
+  if (!p) return;
+  p->n_p = 9;
+  p->eta = 1.6;
+  p->min_cluster_level = 1;
+  p->store_fp64_far = 1;
+}
+void bg_solve_params_default(bg_solve_params* p) {
+  if (!p) return;
+  p->tol = 1e-8;
+  p->restart = 60;
+  p->max_iter = 2000;
+  p->inner_precision = BG_PREC_FP32;
+  p->inner_tol = 1e-5;
+  p->max_refinements = 12;
+}
+
+bg_status bg_context_create(int device, bg_context** out) {
+  if (!out) return BG_INVALID_ARG;
+  *out = nullptr;
+  bg_context* ctx = new (std::nothrow) bg_context();
+  if (!ctx) return BG_OOM;
+  ctx->device = device;
+  if (device >= 0) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device >= n) {
+      delete ctx;
+      return BG_DEVICE_ERROR;
+    }
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ctx;
+      return BG_DEVICE_ERROR;
+    }
+  }
+  *out = ctx;
+  return BG_OK;
+}
+bg_status bg_context_destroy(bg_context* ctx) {
+  if (!ctx) return BG_INVALID_ARG;
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->stage_in.release();
+    ctx->stage_out.release();
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return BG_OK;
+}
+const char* bg_last_error_string(bg_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** out) {
+  if (!ctx || !path || !out) return BG_INVALID_ARG;
+  *out = nullptr;
+  bg_geometry* g = new (std::nothrow) bg_geometry();
+  if (!g) return BG_OOM;
+  std::string err;
+  if (!load_dat(path, &g->g, &err)) {
+    delete g;
+    return set_error(ctx, BG_INVALID_ARG, err);
+  }
+  g->ctx = ctx;
+  *out = g;
+  return BG_OK;
+}
+bg_status bg_geometry_destroy(bg_geometry* g) {
+  if (!g) return BG_INVALID_ARG;
+  delete g;
+  return BG_OK;
+}
+bg_status bg_geometry_surface_point(const bg_geometry* g, int patch, double s, double t, double* out12) {
+  if (!g || !out12 || patch < 0 || patch >= (int)g->g.patches.size()) return BG_INVALID_ARG;
+  out12[0] = s;
+  out12[1] = t;
+  out12[2] = 1.0;
+  patch_frame(g->g.patches[patch], s, t, out12 + 3);
+  return BG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+static void build_segments(bg_operator* op) {
+  const Partition& pt = op->part;
+  const int vd = op->vd;
+  // dense leaves
+  {
+    BsrSegment& s = op->dense;
+    const int ncl = op->nclusters(pt.dense_level);
+    const int ecl = pt.dense_level < 0 ? op->ne : (1 << (2 * (op->M - pt.dense_level)));
+    s.B = ecl * op->p2;
+    s.nrows = vd * ncl;
+    std::vector<std::vector<std::pair<int, int>>> rows(s.nrows);  // (col block, block id)
+    int li = 0, di = 0;
+    std::vector<int> leaf_index_of_dense;
+    for (size_t k = 0; k < pt.leaf_list.size(); k += 4, ++li)
+      if (pt.leaf_list[k] == 2) {
+        for (int rc = 0; rc < vd; ++rc)
+          for (int cc = 0; cc < vd; ++cc)
+            rows[rc * ncl + pt.dense_c1[di]].push_back({cc * ncl + pt.dense_c2[di], (li << 4) | (rc * vd + cc)});
+        ++di;
+      }
+    s.row_ptr.assign(1, 0);
+    for (auto& r : rows) {
+      std::stable_sort(r.begin(), r.end());
+      for (auto& e : r) {
+        s.col.push_back(e.first);
+        s.leaf.push_back(e.second >> 4);
+        s.comp.push_back(e.second & 15);
+      }
+      s.row_ptr.push_back((int)s.col.size());
+    }
+  }
+  // far levels
+  op->far.clear();
+  op->far.resize(op->leaf_level + 1);
+  std::vector<std::vector<std::vector<std::pair<int, int>>>> rows(op->leaf_level + 1);
+  for (int l = 0; l <= op->leaf_level; ++l) rows[l].resize(vd * op->nclusters(l));
+  std::vector<int> pos(op->leaf_level + 1, 0);
+  int li = 0;
+  for (size_t k = 0; k < pt.leaf_list.size(); k += 4, ++li)
+    if (pt.leaf_list[k] == 1) {
+      const int l = pt.leaf_list[k + 1], c1 = pt.leaf_list[k + 2], c2 = pt.leaf_list[k + 3];
+      const int ncl = op->nclusters(l);
+      for (int rc = 0; rc < vd; ++rc)
+        for (int cc = 0; cc < vd; ++cc) rows[l][rc * ncl + c1].push_back({cc * ncl + c2, (li << 4) | (rc * vd + cc)});
+    }
+  for (int l = 0; l <= op->leaf_level; ++l) {
+    BsrSegment& s = op->far[l];
+    s.B = op->R;
+    s.nrows = vd * op->nclusters(l);
+    s.row_ptr.assign(1, 0);
+    for (auto& r : rows[l]) {
+      std::stable_sort(r.begin(), r.end());
+      for (auto& e : r) {
+        s.col.push_back(e.first);
+        s.leaf.push_back(e.second >> 4);
+        s.comp.push_back(e.second & 15);
+      }
+      s.row_ptr.push_back((int)s.col.size());
+    }
+  }
+}
+
+static bg_status upload_tables(bg_operator* op) {
+  cudaStream_t s = op->ctx->stream;
+  std::vector<int> meta;
+  std::vector<double> cp;
+  for (const auto& P : op->geo.patches) {
+    meta.insert(meta.end(), {P.px, P.py, (int)cp.size()});
+    cp.insert(cp.end(), P.cp.begin(), P.cp.end());
+    while (cp.size() % 4) cp.push_back(0.0);
+  }
+  BG_CHECK(op->d_patch_meta.upload(meta, s), "upload patches");
+  BG_CHECK(op->d_patch_cp.upload(cp, s), "upload patches");
+  BG_CHECK(op->d_el_patch.upload(op->mesh.patch, s), "upload elements");
+  BG_CHECK(op->d_el_llc.upload(op->mesh.llc, s), "upload elements");
+  BG_CHECK(op->d_T_ptr.upload(op->T.ptr, s), "upload T");
+  BG_CHECK(op->d_T_idx.upload(op->T.idx, s), "upload T");
+  BG_CHECK(op->d_T_val.upload(op->T.val, s), "upload T");
+  BG_CHECK(op->d_Tt_ptr.upload(op->Tt.ptr, s), "upload T");
+  BG_CHECK(op->d_Tt_idx.upload(op->Tt.idx, s), "upload T");
+  BG_CHECK(op->d_Tt_val.upload(op->Tt.val, s), "upload T");
+  BG_CHECK(op->d_cheb.upload(cheb_points(op->np), s), "upload FMM");
+  BG_CHECK(op->dense.d_row_ptr.upload(op->dense.row_ptr, s), "upload partition");
+  BG_CHECK(op->dense.d_col.upload(op->dense.col, s), "upload partition");
+  for (auto& f : op->far) {
+    BG_CHECK(f.d_row_ptr.upload(f.row_ptr, s), "upload partition");
+    BG_CHECK(f.d_col.upload(f.col, s), "upload partition");
+  }
+  std::vector<std::vector<double>> mom = moment_matrices(op->kind == BG_MAXWELL_SL, op->P, op->leaf_level,
+                                                         std::min(op->mcl, op->M), op->np);
+  std::vector<double> tr = transfer_matrix(op->np);
+  for (auto& m : mom) {
+    DevBuf* a = new DevBuf();
+    DevBuf* b = new DevBuf();
+    op->d_mom64.push_back(a);
+    op->d_mom32.push_back(b);
+    BG_CHECK(a->upload(m, s), "upload moments");
+    std::vector<float> mf(m.begin(), m.end());
+    BG_CHECK(b->upload(mf, s), "upload moments");
+  }
+  BG_CHECK(op->d_tr64.upload(tr, s), "upload transfer");
+  std::vector<float> tf(tr.begin(), tr.end());
+  BG_CHECK(op->d_tr32.upload(tf, s), "upload transfer");
+  BG_CHECK(cudaStreamSynchronize(s), "upload tables");
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, int M, int P, int op_kind,
+                                        const bg_h2_params* params, bg_operator** out) {
+  if (!ctx || !g || !out) return BG_INVALID_ARG;
+  *out = nullptr;
+  if (M < 0 || M > 9) return set_error(ctx, BG_INVALID_ARG, "refinement level must be in [0, 9]");
+  if (P < 0 || P > 3) return set_error(ctx, BG_UNSUPPORTED, "polynomial degree must be in [0, 3]");
+  if (op_kind != BG_LAPLACE_SL && op_kind != BG_HELMHOLTZ_SL && op_kind != BG_MAXWELL_SL)
+    return set_error(ctx, BG_INVALID_ARG, "unknown operator kind");
+  bg_h2_params prm;
+  bg_h2_params_default(&prm);
+  if (params) prm = *params;
+  if (prm.n_p < 2 || prm.n_p > 12 || prm.eta <= 0 || prm.min_cluster_level < 0 || prm.min_cluster_level > 3)
+    return set_error(ctx, BG_INVALID_ARG, "invalid H2 parameters");
+  bg_operator* op = new (std::nothrow) bg_operator();
+  if (!op) return BG_OOM;
+  op->ctx = ctx;
+  op->kind = op_kind;
+  op->M = M;
+  op->P = P;
+  op->np = prm.n_p;
+  op->eta = prm.eta;
+  op->mcl = prm.min_cluster_level;
+  op->store_far = prm.store_fp64_far != 0;
+  op->cplx = op_kind != BG_LAPLACE_SL;
+  op->vd = op_kind == BG_MAXWELL_SL ? 2 : 1;
+  op->nc = op_kind == BG_MAXWELL_SL ? 2 : 1;
+  op->geo = g->g;
+  op->G = 2;
+  for (const auto& p : op->geo.patches) op->G = std::max(op->G, std::max(p.px, p.py));
+  if (op->G > 6) {
+    delete op;
+    return set_error(ctx, BG_UNSUPPORTED, "patch degree above 5 is not supported");
+  }
+  if (op->G == 4 || op->G == 6) op->G = op->G;  // supported by the point kernels
+  std::string err;
+  if (!build_mesh(op->geo, M, &op->mesh, &err) || !build_transform(op->mesh, P, op->vd == 2, &op->T, &err)) {
+    delete op;
+    return set_error(ctx, BG_INVALID_ARG, err);
+  }
+  op->Tt = transpose(op->T);
+  build_partition(op->mesh, op->eta, op->mcl, &op->part);
+  op->p2 = (P + 1) * (P + 1);
+  op->ne = op->mesh.ne;
+  op->S = op->T.rows;
+  op->N = op->T.cols;
+  op->leaf_level = std::max(M - op->mcl, 0);
+  op->nleaf_cl = op->nclusters(op->leaf_level);
+  op->Bq = (1 << (2 * std::min(op->mcl, M))) * op->p2;
+  op->R = op->nc * op->np * op->np;
+  build_segments(op);
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    bg_status st = upload_tables(op);
+    if (st != BG_OK) {
+      delete op;
+      return st;
+    }
+  }
+  *out = op;
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_destroy(bg_operator* op) {
+  if (!op) return BG_INVALID_ARG;
+  if (op->ctx && op->ctx->device >= 0) {
+    cudaSetDevice(op->ctx->device);
+    cudaStreamSynchronize(op->ctx->stream);
+  }
+  delete op;
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_set_wavenumber(bg_operator* op, double re, double im) {
+  if (!op) return BG_INVALID_ARG;
+  if (op->kind == BG_LAPLACE_SL) return set_error(op->ctx, BG_INVALID_ARG, "the Laplace operator has no wavenumber");
+  if (op->kind == BG_MAXWELL_SL && re == 0.0 && im == 0.0)
+    return set_error(op->ctx, BG_INVALID_ARG, "the Maxwell operator needs a nonzero wavenumber");
+  op->kre = re;
+  op->kim = im;
+  op->assembled = false;
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_info(const bg_operator* op, long* info) {
+  if (!op || !info) return BG_INVALID_ARG;
+  long nd = 0, nl = 0;
+  for (size_t k = 0; k < op->part.leaf_list.size(); k += 4) (op->part.leaf_list[k] == 2 ? nd : nl)++;
+  long far_bytes = 0;
+  for (const auto& f : op->far) far_bytes += (long)f.col.size() * f.B * f.B * (long)op->scalar_bytes(false);
+  if (!op->store_far) far_bytes = 0;
+  const long near_bytes = (long)op->dense.col.size() * op->dense.B * op->dense.B * (long)op->scalar_bytes(false);
+  long v[16] = {op->N, op->S, op->ne, nd, nl, op->vd, op->nc, op->np, op->cplx ? 1 : 0, op->M, op->P,
+                op->dense.B / std::max(op->p2, 1), (long)op->T.val.size(), far_bytes, near_bytes, op->near_pairs};
+  std::memcpy(info, v, sizeof(v));
+  return BG_OK;
+}
+extern "C" bg_status bg_operator_assembly_times(const bg_operator* op, double* t3) {
+  if (!op || !t3) return BG_INVALID_ARG;
+  t3[0] = op->t_near;
+  t3[1] = op->t_far;
+  t3[2] = op->t_total;
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_elements(const bg_operator* op, int* ints5, double* dbl6) {
+  if (!op || !ints5 || !dbl6) return BG_INVALID_ARG;
+  const Mesh& m = op->mesh;
+  for (int e = 0; e < m.ne; ++e) {
+    ints5[5 * e] = m.patch[e];
+    for (int k = 0; k < 4; ++k) ints5[5 * e + 1 + k] = m.vert[4 * e + k];
+    dbl6[6 * e] = m.llc[2 * e];
+    dbl6[6 * e + 1] = m.llc[2 * e + 1];
+    for (int k = 0; k < 4; ++k) dbl6[6 * e + 2 + k] = m.ball[m.M][4 * e + k];
+  }
+  return BG_OK;
+}
+extern "C" bg_status bg_operator_leaves(const bg_operator* op, int* out4) {
+  if (!op || !out4) return BG_INVALID_ARG;
+  std::copy(op->part.leaf_list.begin(), op->part.leaf_list.end(), out4);
+  return BG_OK;
+}
+extern "C" bg_status bg_operator_transform(const bg_operator* op, int* ptr, int* idx, double* val) {
+  if (!op || !ptr || !idx || !val) return BG_INVALID_ARG;
+  std::copy(op->T.ptr.begin(), op->T.ptr.end(), ptr);
+  std::copy(op->T.idx.begin(), op->T.idx.end(), idx);
+  std::copy(op->T.val.begin(), op->T.val.end(), val);
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, int rc, int cc, double* out) {
+  if (!op || !out || leaf < 0 || 4 * leaf >= (long)op->part.leaf_list.size() || rc < 0 || cc < 0 || rc >= op->vd ||
+      cc >= op->vd)
+    return BG_INVALID_ARG;
+  if (op->ctx->device < 0 || !op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
+  const int cls = op->part.leaf_list[4 * leaf];
+  const BsrSegment* seg = nullptr;
+  const DevBuf* data = nullptr;
+  if (cls == 2) {
+    seg = &op->dense;
+    data = &op->d_dense64;
+  } else {
+    if (!op->store_far) return set_error(op->ctx, BG_INVALID_ARG, "far field is not stored");
+    const int l = op->part.leaf_list[4 * leaf + 1];
+    seg = &op->far[l];
+    data = op->d_far64[l];
+  }
+  long k = -1;
+  for (size_t i = 0; i < seg->leaf.size(); ++i)
+    if (seg->leaf[i] == leaf && seg->comp[i] == rc * op->vd + cc) k = (long)i;
+  if (k < 0) return set_error(op->ctx, BG_INVALID_ARG, "leaf not found");
+  const size_t sb = op->scalar_bytes(false);
+  const size_t bytes = (size_t)seg->B * seg->B * sb;
+  cudaSetDevice(op->ctx->device);
+  cudaError_t e = cudaMemcpy(out, static_cast<const char*>(data->p) + k * bytes, bytes, cudaMemcpyDeviceToHost);
+  return cuda_status(op->ctx, e, "copy leaf block");
+}
+
+// ---------------------------------------------------------------------------
+// Assembly (H2Matrix::init_H2Matrix, H2Matrix.hpp:93-250)
+static bg_status assemble_far(bg_operator* op) {
+  cudaStream_t s = op->ctx->stream;
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  const int np2 = op->np * op->np;
+  bool any_far = false;
+  for (const auto& f : op->far) any_far |= !f.col.empty();
+  if (!any_far) return BG_OK;
+  for (int l = 0; l <= op->leaf_level; ++l) {
+    if ((int)op->d_pts64.size() <= l) {
+      op->d_pts64.push_back(new DevBuf());
+      op->d_pts32.push_back(new DevBuf());
+      op->d_far64.push_back(new DevBuf());
+    }
+    const int ncl = op->nclusters(l);
+    BG_CHECK(op->d_pts64[l]->alloc((size_t)ncl * np2 * sizeof(d4)), "cluster points");
+    BG_CHECK(op->d_pts32[l]->alloc((size_t)ncl * np2 * sizeof(float4)), "cluster points");
+    BG_CHECK(launch_cluster_points(op->G, pt, l, ncl, op->d_cheb.as<double>(), op->np, op->d_pts64[l]->as<d4>(),
+                                   op->d_pts32[l]->as<float4>(), s),
+             "cluster points");
+    if (!op->store_far || op->far[l].col.empty()) continue;
+    if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "stored far field of vector operators");
+    const BsrSegment& f = op->far[l];
+    std::vector<int2> pairs(f.col.size());
+    for (int r = 0; r < f.nrows; ++r)
+      for (int k = f.row_ptr[r]; k < f.row_ptr[r + 1]; ++k) pairs[k] = make_int2(r, f.col[k]);
+    DevBuf dp;
+    BG_CHECK(dp.upload(pairs, s), "far pairs");
+    const size_t bytes = (size_t)f.col.size() * f.B * f.B * op->scalar_bytes(false);
+    BG_CHECK(op->d_far64[l]->alloc(bytes), "far field storage");
+    BG_CHECK(launch_far_assemble(op->cplx, op->d_pts64[l]->as<d4>(), dp.as<int2>(), (int)pairs.size(), f.B, op->kre,
+                                 op->kim, op->d_far64[l]->p, s),
+             "far-field assembly");
+    BG_CHECK(cudaStreamSynchronize(s), "far-field assembly");
+  }
+  return BG_OK;
+}
+
+static bg_status assemble_near(bg_operator* op) {
+  cudaStream_t s = op->ctx->stream;
+  const BsrSegment& D = op->dense;
+  const int B = D.B, p2 = op->p2;
+  const int ecl = B / p2;
+  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "near field of vector operators");
+  const size_t sb = op->scalar_bytes(false);
+  BG_CHECK(op->d_dense64.alloc((size_t)D.col.size() * B * B * sb), "near-field storage");
+  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, (size_t)D.col.size() * B * B * sb, s), "near-field storage");
+  // classify every element pair of the dense leaves (host, FP64 like the reference)
+  std::map<int, std::vector<NearPair>> regular;                 // by degree
+  std::map<std::pair<int, int>, std::vector<NearPair>> singular;  // by (case, degree)
+  long npairs = 0;
+  for (int r = 0; r < D.nrows; ++r)
+    for (int k = D.row_ptr[r]; k < D.row_ptr[r + 1]; ++k) {
+      const int c1 = r, c2 = D.col[k];
+      for (int b = 0; b < ecl; ++b)
+        for (int a = 0; a < ecl; ++a) {
+          const int e1 = c1 * ecl + a, e2 = c2 * ecl + b;
+          PairClass pc = classify_pair(op->mesh, e1, e2, op->P);
+          NearPair np;
+          np.e1 = e1;
+          np.e2 = e2;
+          np.rot = (pc.rot1 & 15) | ((pc.rot2 & 15) << 4);
+          np.pad = 0;
+          np.dst = (long long)k * B * B + (long long)(b * p2) * B + a * p2;
+          if (pc.cs == 0) regular[pc.deg].push_back(np);
+          else singular[{pc.cs, pc.deg}].push_back(np);
+          ++npairs;
+        }
+    }
+  op->near_pairs = npairs;
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), 1.0 / double(1 << op->M)};
+  std::vector<DevBuf*> keep;  // buffers alive until the stream drains
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(s);
+    for (auto b : keep) delete b;
+  };
+  bg_status st = BG_OK;
+  for (auto& kv : regular) {
+    const int deg = kv.first, n1 = deg + 1, Q = n1 * n1;
+    const Rule1D& gr = gauss_rule(n1);
+    std::vector<double> basis((size_t)Q * p2);
+    for (int q = 0; q < Q; ++q) {
+      double bs[8], bt[8];
+      bernstein(op->P, gr.x[q / n1], bs);
+      bernstein(op->P, gr.x[q % n1], bt);
+      for (int iy = 0; iy <= op->P; ++iy)
+        for (int ix = 0; ix <= op->P; ++ix) basis[(size_t)q * p2 + iy * (op->P + 1) + ix] = bs[ix] * bt[iy];
+    }
+    DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dtab = new DevBuf(), *dbas = new DevBuf(), *dpairs = new DevBuf();
+    keep.insert(keep.end(), {dgx, dgw, dtab, dbas, dpairs});
+    cudaError_t e = dgx->upload(gr.x, s);
+    if (e == cudaSuccess) e = dgw->upload(gr.w, s);
+    if (e == cudaSuccess) e = dbas->upload(basis, s);
+    if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
+    if (e == cudaSuccess) e = dtab->alloc((size_t)op->ne * Q * sizeof(d4));
+    if (e == cudaSuccess) e = launch_quad_table(op->G, pt, et, op->ne, dgx->as<double>(), dgw->as<double>(), n1, dtab->as<d4>(), s);
+    if (e == cudaSuccess)
+      e = launch_near_regular(op->P, op->cplx, dpairs->as<NearPair>(), (int)kv.second.size(), dtab->as<d4>(), n1,
+                              dbas->as<double>(), op->kre, op->kim, op->d_dense64.p, B, s);
+    if ((st = cuda_status(op->ctx, e, "near-field regular pairs")) != BG_OK) {
+      cleanup();
+      return st;
+    }
+  }
+  for (auto& kv : singular) {
+    const int cs = kv.first.first, deg = kv.first.second, n1 = deg + 1;
+    const Rule1D& gr = gauss_rule(n1);
+    DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dpairs = new DevBuf();
+    keep.insert(keep.end(), {dgx, dgw, dpairs});
+    cudaError_t e = dgx->upload(gr.x, s);
+    if (e == cudaSuccess) e = dgw->upload(gr.w, s);
+    if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
+    if (e == cudaSuccess)
+      e = launch_near_duffy(op->G, op->P, op->cplx, cs, pt, et, dpairs->as<NearPair>(), (int)kv.second.size(),
+                            dgx->as<double>(), dgw->as<double>(), n1, op->kre, op->kim, op->d_dense64.p, B, s);
+    if ((st = cuda_status(op->ctx, e, "near-field singular pairs")) != BG_OK) {
+      cleanup();
+      return st;
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  cleanup();
+  if ((st = cuda_status(op->ctx, e, "near-field assembly")) != BG_OK) return st;
+  // FP32 copy for the mixed-precision inner operator
+  const long n = (long)D.col.size() * B * B * (op->cplx ? 2 : 1);
+  BG_CHECK(op->d_dense32.alloc(n * sizeof(float)), "near-field FP32 copy");
+  BG_CHECK(launch_convert(0, 2, op->d_dense64.p, n, op->d_dense32.p, s), "near-field FP32 copy");
+  BG_CHECK(cudaStreamSynchronize(s), "near-field FP32 copy");
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_assemble(bg_operator* op) {
+  if (!op) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
+  if (op->kind == BG_MAXWELL_SL) return set_error(op->ctx, BG_UNSUPPORTED, "Maxwell assembly is not available yet");
+  cudaSetDevice(op->ctx->device);
+  op->assembled = false;
+  auto t0 = std::chrono::steady_clock::now();
+  bg_status st = assemble_far(op);
+  if (st != BG_OK) return st;
+  auto t1 = std::chrono::steady_clock::now();
+  st = assemble_near(op);
+  if (st != BG_OK) return st;
+  auto t2 = std::chrono::steady_clock::now();
+  op->t_far = std::chrono::duration<double>(t1 - t0).count();
+  op->t_near = std::chrono::duration<double>(t2 - t1).count();
+  op->t_total = op->t_far + op->t_near;
+  op->assembled = true;
+  return BG_OK;
+}
+
+// ---------------------------------------------------------------------------
+bg_status ensure_work(bg_operator* op, int nrhs) {
+  if (nrhs <= op->cap) return BG_OK;
+  const size_t sb = op->scalar_bytes(false);  // FP64 sizes cover the FP32 path
+  BG_CHECK(op->w_xdof.alloc((size_t)op->N * nrhs * sb), "work vectors");
+  BG_CHECK(op->w_ydof.alloc((size_t)op->N * nrhs * sb), "work vectors");
+  BG_CHECK(op->w_xss.alloc((size_t)op->S * nrhs * sb), "work vectors");
+  BG_CHECK(op->w_yss.alloc((size_t)op->S * nrhs * sb), "work vectors");
+  while ((int)op->w_y.size() <= op->leaf_level) {
+    op->w_y.push_back(new DevBuf());
+    op->w_z.push_back(new DevBuf());
+  }
+  for (int l = 0; l <= op->leaf_level; ++l) {
+    const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
+    BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
+    BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
+  }
+  op->cap = nrhs;
+  return BG_OK;
+}
+
+// One H2 product on row-major work vectors (H2DenseProduct.hpp:33-165).
+bg_status apply_operator(bg_operator* op, int nrhs, bool fp32, const void* xdof, void* ydof) {
+  cudaStream_t s = op->ctx->stream;
+  const int S = op->stype(fp32);
+  const size_t sb = op->scalar_bytes(fp32);
+  const int np2 = op->np * op->np;
+  BG_CHECK(launch_csr_apply(S, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
+                            op->w_xss.p, nrhs, s),
+           "T x");
+  bool any_far = false;
+  for (const auto& f : op->far) any_far |= !f.col.empty();
+  const long comp_ss = (long)op->ne * op->p2;  // superspace rows per vector component
+  if (any_far) {
+    const int Ll = op->leaf_level;
+    for (int c = 0; c < op->vd; ++c) {
+      const void* mom = fp32 ? op->d_mom32[c]->p : op->d_mom64[c]->p;
+      BG_CHECK(launch_moment_fwd(S, mom, op->R, op->Bq, op->nleaf_cl,
+                                 static_cast<const char*>(op->w_xss.p) + c * comp_ss * nrhs * sb,
+                                 static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sb, nrhs, s),
+               "forward moments");
+      for (int l = Ll - 1; l >= 0; --l) {
+        const int ncl = op->nclusters(l);
+        BG_CHECK(launch_transfer_fwd(S, fp32 ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                     static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sb,
+                                     static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sb, nrhs, s),
+                 "forward transfer");
+      }
+    }
+  }
+  // near field
+  BG_CHECK(launch_bsr(S, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(),
+                      fp32 ? op->d_dense32.p : op->d_dense64.p, op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p,
+                      nrhs, 0, s),
+           "near-field product");
+  if (any_far) {
+    for (int l = 0; l <= op->leaf_level; ++l) {
+      const BsrSegment& f = op->far[l];
+      if (f.col.empty()) {
+        BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)f.nrows * f.B * nrhs * sb, s), "far field");
+        continue;
+      }
+      if (fp32) {
+        if (op->vd != 1 || op->nc != 1) return set_error(op->ctx, BG_UNSUPPORTED, "FP32 far field of vector operators");
+        BG_CHECK(launch_far_fused(op->cplx, op->d_pts32[l]->as<float4>(), op->d_pts32[l]->as<float4>(),
+                                  f.d_row_ptr.as<int>(), f.d_col.as<int>(), f.nrows, np2, (float)op->kre, (float)op->kim,
+                                  op->w_y[l]->p, op->w_z[l]->p, nrhs, s),
+                 "far-field product (FP32 fused)");
+      } else {
+        if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "FP64 product needs the stored far field");
+        BG_CHECK(launch_bsr(S, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p, f.nrows, f.B, op->w_y[l]->p,
+                            op->w_z[l]->p, nrhs, 0, s),
+                 "far-field product");
+      }
+    }
+    const int Ll = op->leaf_level;
+    for (int c = 0; c < op->vd; ++c) {
+      for (int l = 0; l < Ll; ++l) {
+        const int ncl = op->nclusters(l);
+        BG_CHECK(launch_transfer_bwd(S, fp32 ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                     static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sb,
+                                     static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sb, nrhs, s),
+                 "backward transfer");
+      }
+      const void* mom = fp32 ? op->d_mom32[c]->p : op->d_mom64[c]->p;
+      BG_CHECK(launch_moment_bwd(S, mom, op->R, op->Bq, op->nleaf_cl,
+                                 static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sb,
+                                 static_cast<char*>(op->w_yss.p) + c * comp_ss * nrhs * sb, nrhs, s),
+               "backward moments");
+    }
+  }
+  BG_CHECK(launch_csr_apply(S, op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(), op->N,
+                            op->w_yss.p, ydof, nrhs, s),
+           "T^T y");
+  return BG_OK;
+}
+
+static bg_status stage_host(bg_context* ctx, DevBuf* buf, const void* host, long ld, long rows, int ncols, size_t esz,
+                            bool to_device) {
+  cudaError_t e = buf->alloc((size_t)rows * ncols * esz);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "staging buffer");
+  if (to_device)
+    e = cudaMemcpy2DAsync(buf->p, rows * esz, host, ld * esz, rows * esz, ncols, cudaMemcpyHostToDevice, ctx->stream);
+  return cuda_status(ctx, e, "host to device copy");
+}
+
+extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
+                               const double* alpha, const double* beta, int precision, int on_device) {
+  if (!op || !x || !y || nrhs <= 0 || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
+  if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
+  if (precision != BG_PREC_FP64 && precision != BG_PREC_FP32) return set_error(op->ctx, BG_INVALID_ARG, "precision");
+  const double one[2] = {1.0, 0.0}, zero2[2] = {0.0, 0.0};
+  if (!alpha) alpha = one;
+  if (!beta) beta = zero2;
+  if (!op->cplx && (alpha[1] != 0.0 || beta[1] != 0.0))
+    return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
+  cudaSetDevice(op->ctx->device);
+  cudaStream_t s = op->ctx->stream;
+  const bool fp32 = precision == BG_PREC_FP32;
+  const size_t usz = op->cplx ? 16 : 8;
+  const int uS = op->cplx ? 1 : 0;
+  for (int c0 = 0; c0 < nrhs; c0 += 32) {
+    const int k = std::min(32, nrhs - c0);
+    bg_status st = ensure_work(op, k);
+    if (st != BG_OK) return st;
+    const char* xp = static_cast<const char*>(x) + (size_t)c0 * ldx * usz;
+    char* yp = static_cast<char*>(y) + (size_t)c0 * ldy * usz;
+    const void* xd = xp;
+    long lx = ldx, ly = ldy;
+    void* yd = yp;
+    if (!on_device) {
+      if ((st = stage_host(op->ctx, &op->ctx->stage_in, xp, ldx, op->N, k, usz, true)) != BG_OK) return st;
+      if ((st = stage_host(op->ctx, &op->ctx->stage_out, yp, ldy, op->N, k, usz,
+                           beta[0] != 0.0 || beta[1] != 0.0)) != BG_OK)
+        return st;
+      xd = op->ctx->stage_in.p;
+      yd = op->ctx->stage_out.p;
+      lx = ly = op->N;
+    }
+    BG_CHECK(launch_gather_in(uS, op->stype(fp32), xd, lx, op->N, k, op->w_xdof.p, s), "gather x");
+    if ((st = apply_operator(op, k, fp32, op->w_xdof.p, op->w_ydof.p)) != BG_OK) return st;
+    BG_CHECK(launch_scatter_out(op->stype(fp32), op->w_ydof.p, op->N, k, yd, ly, alpha, beta, s), "scatter y");
+    if (!on_device)
+      BG_CHECK(cudaMemcpy2DAsync(yp, ldy * usz, yd, op->N * usz, op->N * usz, k, cudaMemcpyDeviceToHost, s),
+               "device to host copy");
+  }
+  BG_CHECK(cudaStreamSynchronize(s), "H2 matvec");
+  return BG_OK;
+}

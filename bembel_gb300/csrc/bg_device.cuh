@@ -1,0 +1,186 @@
+// Device helpers shared by the GB300 kernels: complex arithmetic, the FP64
+// reciprocal square root, Bernstein bases and the surface map of a rational
+// Bezier patch (Patch::updateSurfacePoint, Geometry/Patch.hpp:294-365).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bg {
+
+struct cd {  // complex<double>, interleaved
+  double re, im;
+};
+struct cf {  // complex<float>
+  float re, im;
+};
+struct __align__(32) d4 {  // point + weight, one 32-byte load
+  double x, y, z, w;
+};
+__host__ __device__ inline cd operator+(cd a, cd b) { return {a.re + b.re, a.im + b.im}; }
+__host__ __device__ inline cd operator-(cd a, cd b) { return {a.re - b.re, a.im - b.im}; }
+__host__ __device__ inline cd operator*(cd a, cd b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__host__ __device__ inline cd operator*(cd a, double s) { return {a.re * s, a.im * s}; }
+__host__ __device__ inline cf operator+(cf a, cf b) { return {a.re + b.re, a.im + b.im}; }
+__host__ __device__ inline cf operator*(cf a, cf b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__host__ __device__ inline cf operator*(cf a, float s) { return {a.re * s, a.im * s}; }
+
+// zero / fma helpers working for real and complex scalars
+template <typename S> __device__ inline S zero();
+template <> __device__ inline double zero<double>() { return 0.0; }
+template <> __device__ inline float zero<float>() { return 0.0f; }
+template <> __device__ inline cd zero<cd>() { return {0.0, 0.0}; }
+template <> __device__ inline cf zero<cf>() { return {0.0f, 0.0f}; }
+__device__ inline double fmac(double acc, double a, double b) { return fma(a, b, acc); }
+__device__ inline float fmac(float acc, float a, float b) { return fmaf(a, b, acc); }
+__device__ inline cd fmac(cd acc, cd a, cd b) {
+  return {fma(a.re, b.re, fma(-a.im, b.im, acc.re)), fma(a.re, b.im, fma(a.im, b.re, acc.im))};
+}
+__device__ inline cf fmac(cf acc, cf a, cf b) {
+  return {fmaf(a.re, b.re, fmaf(-a.im, b.im, acc.re)), fmaf(a.re, b.im, fmaf(a.im, b.re, acc.im))};
+}
+__device__ inline cd fmac(cd acc, double a, cd b) { return {fma(a, b.re, acc.re), fma(a, b.im, acc.im)}; }
+__device__ inline cf fmac(cf acc, float a, cf b) { return {fmaf(a, b.re, acc.re), fmaf(a, b.im, acc.im)}; }
+__device__ inline cd fmac(cd acc, cd a, double b) { return {fma(a.re, b, acc.re), fma(a.im, b, acc.im)}; }
+__device__ inline cf fmac(cf acc, cf a, float b) { return {fmaf(a.re, b, acc.re), fmaf(a.im, b, acc.im)}; }
+
+// 1/sqrt(x) in FP64: single-precision estimate refined by two Newton-Raphson
+// steps y <- y (3 - x y^2) / 2 for f(y) = y^-2 - x. Each step squares the
+// relative error, so the FP32 seed (rel. error ~1e-7) reaches FP64 accuracy.
+// Valid for normal x in the FP32 range (all distances here).
+__device__ inline double rsqrt_nr(double x) {
+  double y = (double)rsqrtf((float)x);
+  double hx = 0.5 * x;
+  y = y * fma(-hx * y, y, 1.5);
+  y = y * fma(-hx * y, y, 1.5);
+  return y;
+}
+
+// 1/x in FP64: single-precision estimate refined by two Newton-Raphson steps
+// y <- y (2 - x y); valid for normal x in the FP32 range.
+__device__ inline double rcp_nr(double x) {
+  double y = (double)__frcp_rn((float)x);
+  y = y * fma(-x, y, 2.0);
+  y = y * fma(-x, y, 2.0);
+  return y;
+}
+
+// Bernstein basis of degree p at x (p <= N-1), built by the triangular
+// recurrence b_i <- (1-x) b_i + x b_{i-1}.
+template <int N>
+__device__ inline void bern(int p, double x, double* b) {
+  b[0] = 1.0;
+#pragma unroll
+  for (int k = 1; k < N; ++k) {
+    if (k <= p) {
+      double prev = 0.0;
+#pragma unroll
+      for (int i = 0; i < k; ++i) {
+        double t = b[i];
+        b[i] = fma(1.0 - x, t, prev);
+        prev = x * t;
+      }
+      b[k] = prev;
+    }
+  }
+}
+// Bernstein basis and its derivative, degree p (p <= N-1)
+template <int N>
+__device__ inline void bern_der(int p, double x, double* b, double* db) {
+  double lo[N];
+  bern<N>(p - 1 < 0 ? 0 : p - 1, x, lo);
+  if (p == 0) {
+    b[0] = 1.0;
+    db[0] = 0.0;
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    if (i <= p) {
+      double a = i > 0 ? lo[i - 1] : 0.0;
+      double c = i < p ? lo[i] : 0.0;
+      db[i] = p * (a - c);
+    }
+  }
+  bern<N>(p, x, b);
+}
+
+// Patches on the device: orders px, py <= G; control points at cp + off
+// (4 doubles per point, index 4 * (ix * py + iy) + k).
+struct PatchTable {
+  const int* meta;     // per patch: px, py, offset (in doubles)
+  const double* cp;
+};
+
+// Surface point at patch coordinates (s, t): x, dx, dy (9 doubles)
+template <int G>
+__device__ inline void surface_frame(const PatchTable& pt, int patch, double s, double t, double* x, double* dx,
+                                     double* dy) {
+  const int px = __ldg(&pt.meta[3 * patch]), py = __ldg(&pt.meta[3 * patch + 1]);
+  const double* cp = pt.cp + __ldg(&pt.meta[3 * patch + 2]);
+  double bs[G], dbs[G], bt[G], dbt[G];
+  bern_der<G>(px - 1, s, bs, dbs);
+  bern_der<G>(py - 1, t, bt, dbt);
+  double h[4] = {0, 0, 0, 0}, hs[4] = {0, 0, 0, 0}, ht[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int i = 0; i < G; ++i) {
+    if (i < px) {
+      // inner sum over t first: q = sum_j bt_j P_ij, qt = sum_j dbt_j P_ij
+      double q[4] = {0, 0, 0, 0}, qt[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int j = 0; j < G; ++j) {
+        if (j < py) {
+          const d4 c = *reinterpret_cast<const d4*>(cp + 4 * (i * py + j));
+          q[0] = fma(c.x, bt[j], q[0]); q[1] = fma(c.y, bt[j], q[1]);
+          q[2] = fma(c.z, bt[j], q[2]); q[3] = fma(c.w, bt[j], q[3]);
+          qt[0] = fma(c.x, dbt[j], qt[0]); qt[1] = fma(c.y, dbt[j], qt[1]);
+          qt[2] = fma(c.z, dbt[j], qt[2]); qt[3] = fma(c.w, dbt[j], qt[3]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        h[k] = fma(bs[i], q[k], h[k]);
+        hs[k] = fma(dbs[i], q[k], hs[k]);
+        ht[k] = fma(bs[i], qt[k], ht[k]);
+      }
+    }
+  }
+  const double iw = rcp_nr(h[3]);
+  const double iw2 = iw * iw;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    x[k] = h[k] * iw;
+    dx[k] = (hs[k] * h[3] - h[k] * hs[3]) * iw2;
+    dy[k] = (ht[k] * h[3] - h[k] * ht[3]) * iw2;
+  }
+}
+
+// surface measure |dx x dy|
+__device__ inline double surface_measure(const double* dx, const double* dy) {
+  double n0 = dx[1] * dy[2] - dx[2] * dy[1];
+  double n1 = dx[2] * dy[0] - dx[0] * dy[2];
+  double n2 = dx[0] * dy[1] - dx[1] * dy[0];
+  double n2s = n0 * n0 + n1 * n1 + n2 * n2;
+  return n2s * rsqrt_nr(n2s);
+}
+
+// tensor Bernstein basis of degree P at (s, t), local index iy*(P+1)+ix
+template <int P>
+__device__ inline void tensor_basis(double s, double t, double* phi) {
+  double bs[P + 1], bt[P + 1];
+  bern<P + 1>(P, s, bs);
+  bern<P + 1>(P, t, bt);
+#pragma unroll
+  for (int iy = 0; iy <= P; ++iy)
+#pragma unroll
+    for (int ix = 0; ix <= P; ++ix) phi[iy * (P + 1) + ix] = bs[ix] * bt[iy];
+}
+
+// the DuffyTrick rotation tau (DuffyTrick/tau.hpp:26-42)
+__device__ inline void tau(double x, double y, int c, double* o) {
+  if (c == 1) { o[0] = 1 - y; o[1] = x; }
+  else if (c == 2) { o[0] = 1 - x; o[1] = 1 - y; }
+  else if (c == 3) { o[0] = y; o[1] = 1 - x; }
+  else { o[0] = x; o[1] = y; }
+}
+
+}  // namespace bg

@@ -1,0 +1,71 @@
+// Kernel interfaces of the GB300 H2 single-layer operator. Implementations in
+// bg_nearfield.cu (near-field assembly), bg_farfield.cu (cluster points and
+// far-field assembly) and bg_matvec.cu (transforms, block-sparse products,
+// the fused FP32 far field and the Krylov vector kernels).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "bg_device.cuh"
+
+namespace bg {
+
+// element pair of a dense leaf: output block position dst (scalars) inside
+// the dense-block pool; rot packs rot1 | rot2 << 4
+struct NearPair {
+  int e1, e2, rot, pad;
+  long long dst;
+};
+
+struct ElementTable {
+  const int* patch;    // per element
+  const double* llc;   // 2 per element
+  double h;            // element size in patch coordinates
+};
+
+// ---- near field ----
+// per element e and 2D Gauss point q of an n1 x n1 rule: x, y, z, h*w*|dx x dy|
+cudaError_t launch_quad_table(int G, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                              const double* gw, int n1, d4* out, cudaStream_t s);
+// regular pairs (integrate0 / integrate1 of the DuffyTrick) from quad tables
+cudaError_t launch_near_regular(int P, bool cplx, const NearPair* pairs, int npairs, const d4* tab, int n1,
+                                const double* basis, double kre, double kim, void* out, int B, cudaStream_t s);
+// identical (cs = 2), common edge (3), common vertex (4) pairs
+cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable& pt, const ElementTable& et,
+                              const NearPair* pairs, int npairs, const double* gx, const double* gw, int n1,
+                              double kre, double kim, void* out, int B, cudaStream_t s);
+
+// ---- far field ----
+// interpolation points of every cluster of a level: x, y, z, |dx x dy| (FP64 and FP32)
+cudaError_t launch_cluster_points(int G, const PatchTable& pt, int level, int nclusters, const double* cheb, int np,
+                                  d4* out64, float4* out32, cudaStream_t s);
+// F blocks (B x B, column-major) for the listed cluster pairs of one level
+cudaError_t launch_far_assemble(bool cplx, const d4* pts, const int2* pairs, int nblocks, int B, double kre,
+                                double kim, void* out, cudaStream_t s);
+
+// ---- matvec building blocks (row-major work vectors, nrhs contiguous) ----
+// S: 0 double, 1 complex double, 2 float, 3 complex float
+cudaError_t launch_csr_apply(int S, const int* ptr, const int* idx, const double* val, int rows, const void* x,
+                             void* y, int nrhs, cudaStream_t s);
+cudaError_t launch_bsr(int S, const int* row_ptr, const int* col, const void* blocks, int nrows, int B, const void* x,
+                       void* y, int nrhs, int accumulate, cudaStream_t s);
+cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int nclusters, const void* xss, void* y, int nrhs,
+                              cudaStream_t s);
+cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int nclusters, const void* z, void* yss, int nrhs,
+                              cudaStream_t s);
+cudaError_t launch_transfer_fwd(int S, const void* T, int np2, int nc, int nparents, const void* ychild, void* yparent,
+                                int nrhs, cudaStream_t s);
+cudaError_t launch_transfer_bwd(int S, const void* T, int np2, int nc, int nparents, const void* zparent, void* zchild,
+                                int nrhs, cudaStream_t s);
+// fused FP32 far field: for each listed block, generate the coupling from
+// cluster points on the fly and accumulate into the row cluster's output
+cudaError_t launch_far_fused(bool cplx, const float4* pts_row, const float4* pts_col, const int* row_ptr,
+                             const int* col, int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs,
+                             cudaStream_t s);
+// user column-major block (ld) <-> row-major work vector, with precision change
+cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int rows, int nrhs, void* work,
+                             cudaStream_t s);
+cudaError_t launch_scatter_out(int Swork, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
+                               const double* beta, cudaStream_t s);
+cudaError_t launch_convert(int Sin, int Sout, const void* in, long n, void* out, cudaStream_t s);
+
+}  // namespace bg

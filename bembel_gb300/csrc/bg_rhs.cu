@@ -1,0 +1,290 @@
+// Load vectors and potentials on GB300.
+//
+// bg_load_vector: DiscreteLinearForm<DirichletTrace<S>, Op>::compute
+// (LinearForm/DiscreteLinearForm.hpp:44-83, LinearForm/DirichletTrace.hpp:38-66):
+// per element the (P+2)^2-point tensor Gauss rule, weight h*w, integrand
+// u(x) |dx x dy| phi_a, then the transpose of the transformation matrix.
+// bg_potential: DiscretePotential::evaluate (Potential/DiscretePotential.hpp:49-107)
+// for the Laplace / Helmholtz single layer potential.
+#include <algorithm>
+#include <vector>
+
+#include "bg_operator.hpp"
+
+using namespace bg;
+
+namespace {
+
+constexpr double kInv4Pi = 0.07957747154594767;
+
+// analytic Dirichlet data (examples/Data.hpp), kind 0/1/2, per right-hand side
+__device__ inline cd data_value(int kind, const double* prm, const double* x, double kre, double kim) {
+  if (kind == 2) {
+    const double dx = prm[0] * x[0] + prm[1] * x[1] + prm[2] * x[2];
+    // exp(-i k d.x), k = kre + i kim
+    double sn, cs;
+    sincos(kre * dx, &sn, &cs);
+    const double a = kim != 0.0 ? exp(kim * dx) : 1.0;
+    return {cs * a, -sn * a};
+  }
+  const double d0 = x[0] - prm[0], d1 = x[1] - prm[1], d2 = x[2] - prm[2];
+  const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const double inv = rsqrt_nr(r2);
+  if (kind == 0) return {inv * kInv4Pi, 0.0};
+  const double r = r2 * inv;
+  double sn, cs;
+  sincos(kre * r, &sn, &cs);
+  const double a = (kim != 0.0 ? exp(kim * r) : 1.0) * inv * kInv4Pi;
+  return {cs * a, -sn * a};
+}
+
+// thread per (element, rhs); output superspace rows e*p2 + a, row-major k
+template <int G, int P, bool CPLX>
+__global__ void k_load(PatchTable pt, ElementTable et, int ne, const double* __restrict__ gx,
+                       const double* __restrict__ gw, int n1, int kind, const double* __restrict__ prm, int k,
+                       double kre, double kim, double* __restrict__ out) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)ne * k) return;
+  const int e = (int)(t / k), c = (int)(t % k);
+  const double h = et.h;
+  double acc_re[P2], acc_im[P2];
+#pragma unroll
+  for (int a = 0; a < P2; ++a) acc_re[a] = acc_im[a] = 0.0;
+  for (int q = 0; q < n1 * n1; ++q) {
+    const double u = gx[q / n1], v = gx[q % n1], w = gw[q / n1] * gw[q % n1];
+    double x[3], dx[3], dy[3], phi[P2];
+    surface_frame<G>(pt, et.patch[e], et.llc[2 * e] + h * u, et.llc[2 * e + 1] + h * v, x, dx, dy);
+    const double wk = h * w * surface_measure(dx, dy);
+    const cd f = data_value(kind, prm + 3 * c, x, kre, kim);
+    tensor_basis<P>(u, v, phi);
+#pragma unroll
+    for (int a = 0; a < P2; ++a) {
+      acc_re[a] = fma(f.re * wk, phi[a], acc_re[a]);
+      acc_im[a] = fma(f.im * wk, phi[a], acc_im[a]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < P2; ++a) {
+    const long o = ((long)e * P2 + a) * k + c;
+    if (CPLX) {
+      out[2 * o] = acc_re[a];
+      out[2 * o + 1] = acc_im[a];
+    } else {
+      out[o] = acc_re[a];
+    }
+  }
+}
+
+// CTA per evaluation point: threads over (element, Gauss point) sum
+// k(x, y_q) c_q rho(y_q) with c_q = h w |J| and rho = sum_a coef phi_a (the
+// 1/h of FunctionEvaluatorEval and the h^2 of the weight leave h).
+template <int P, bool CPLX>
+__global__ void k_potential(const d4* __restrict__ tab, int ne, int Q, const double* __restrict__ basis,
+                            const double* __restrict__ coef, int k, const double* __restrict__ pts, double kre,
+                            double kim, double* __restrict__ out) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  __shared__ double red_re[256], red_im[256];
+  const int p = blockIdx.x;
+  const double px = pts[3 * p], py = pts[3 * p + 1], pz = pts[3 * p + 2];
+  for (int c = 0; c < k; ++c) {
+    double sre = 0, sim = 0;
+    for (long t = threadIdx.x; t < (long)ne * Q; t += blockDim.x) {
+      const int e = (int)(t / Q), q = (int)(t % Q);
+      const d4 y = tab[t];
+      const double d0 = px - y.x, d1 = py - y.y, d2 = pz - y.z;
+      const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+      const double inv = rsqrt_nr(r2);
+      double kr = inv * kInv4Pi * y.w, ki = 0.0;
+      if (CPLX) {
+        const double r = r2 * inv;
+        double sn, cs;
+        sincos(kre * r, &sn, &cs);
+        const double a = kim != 0.0 ? exp(kim * r) : 1.0;
+        ki = -sn * a * kr;
+        kr = cs * a * kr;
+      }
+      double rre = 0, rim = 0;
+#pragma unroll
+      for (int a = 0; a < P2; ++a) {
+        const long o = ((long)e * P2 + a) * k + c;
+        const double b = basis[q * P2 + a];
+        if (CPLX) {
+          rre = fma(coef[2 * o], b, rre);
+          rim = fma(coef[2 * o + 1], b, rim);
+        } else {
+          rre = fma(coef[o], b, rre);
+        }
+      }
+      sre += kr * rre - ki * rim;
+      sim += kr * rim + ki * rre;
+    }
+    red_re[threadIdx.x] = sre;
+    red_im[threadIdx.x] = sim;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        red_re[threadIdx.x] += red_re[threadIdx.x + w];
+        red_im[threadIdx.x] += red_im[threadIdx.x + w];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      if (CPLX) {
+        out[2 * ((long)c * gridDim.x + p)] = red_re[0];
+        out[2 * ((long)c * gridDim.x + p) + 1] = red_im[0];
+      } else {
+        out[(long)c * gridDim.x + p] = red_re[0];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int G, int P>
+cudaError_t run_load(bool cplx, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                     const double* gw, int n1, int kind, const double* prm, int k, double kre, double kim, double* out,
+                     cudaStream_t s) {
+  const long n = (long)ne * k;
+  const unsigned g = (unsigned)((n + 127) / 128);
+  if (cplx) k_load<G, P, true><<<g, 128, 0, s>>>(pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out);
+  else k_load<G, P, false><<<g, 128, 0, s>>>(pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out);
+  return cudaGetLastError();
+}
+template <int G>
+cudaError_t load_p(int P, bool cplx, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                   const double* gw, int n1, int kind, const double* prm, int k, double kre, double kim, double* out,
+                   cudaStream_t s) {
+  switch (P) {
+    case 0: return run_load<G, 0>(cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 1: return run_load<G, 1>(cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 2: return run_load<G, 2>(cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 3: return run_load<G, 3>(cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_load(int G, int P, bool cplx, const PatchTable& pt, const ElementTable& et, int ne,
+                        const double* gx, const double* gw, int n1, int kind, const double* prm, int k, double kre,
+                        double kim, double* out, cudaStream_t s) {
+  switch (G) {
+    case 2: return load_p<2>(P, cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 3: return load_p<3>(P, cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 4: return load_p<4>(P, cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 5: return load_p<5>(P, cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    case 6: return load_p<6>(P, cplx, pt, et, ne, gx, gw, n1, kind, prm, k, kre, kim, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+cudaError_t launch_potential(int P, bool cplx, const d4* tab, int ne, int Q, const double* basis, const double* coef,
+                             int k, const double* pts, int npts, double kre, double kim, double* out, cudaStream_t s) {
+#define BG_POT(PP)                                                                                              \
+  case PP:                                                                                                      \
+    if (cplx) k_potential<PP, true><<<npts, 256, 0, s>>>(tab, ne, Q, basis, coef, k, pts, kre, kim, out);      \
+    else k_potential<PP, false><<<npts, 256, 0, s>>>(tab, ne, Q, basis, coef, k, pts, kre, kim, out);          \
+    break;
+  switch (P) {
+    BG_POT(0)
+    BG_POT(1)
+    BG_POT(2)
+    BG_POT(3)
+    default: return cudaErrorInvalidValue;
+  }
+#undef BG_POT
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device) {
+  if (!op || !prm || !out || nrhs <= 0 || kind < 0 || kind > 2) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: load vectors need a GPU");
+  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "load vectors of vector operators");
+  if (!op->cplx && kind != 0) return set_error(op->ctx, BG_INVALID_ARG, "complex data for a real operator");
+  cudaSetDevice(op->ctx->device);
+  cudaStream_t s = op->ctx->stream;
+  const size_t usz = op->cplx ? 16 : 8;
+  const Rule1D& gr = gauss_rule(op->P + 2);
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), 1.0 / double(1 << op->M)};
+  for (int c0 = 0; c0 < nrhs; c0 += 32) {
+    const int k = std::min(32, nrhs - c0);
+    bg_status st = ensure_work(op, k);
+    if (st != BG_OK) return st;
+    DevBuf gx, gw, dp, dout;
+    std::vector<double> p(prm + 3 * c0, prm + 3 * (c0 + k));
+    cudaError_t e = gx.upload(gr.x, s);
+    if (e == cudaSuccess) e = gw.upload(gr.w, s);
+    if (e == cudaSuccess) e = dp.upload(p, s);
+    if (e == cudaSuccess)
+      e = launch_load(op->G, op->P, op->cplx, pt, et, op->ne, gx.as<double>(), gw.as<double>(), op->P + 2, kind,
+                      dp.as<double>(), k, op->kre, op->kim, op->w_yss.as<double>(), s);
+    if (e == cudaSuccess)
+      e = launch_csr_apply(op->stype(false), op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(),
+                           op->N, op->w_yss.p, op->w_ydof.p, k, s);
+    void* dst = static_cast<char*>(out) + (size_t)c0 * op->N * usz;
+    void* dd = dst;
+    if (!on_device && e == cudaSuccess) {
+      e = dout.alloc((size_t)op->N * k * usz);
+      dd = dout.p;
+    }
+    const double one[2] = {1, 0}, zero2[2] = {0, 0};
+    if (e == cudaSuccess) e = launch_scatter_out(op->stype(false), op->w_ydof.p, op->N, k, dd, op->N, one, zero2, s);
+    if (!on_device && e == cudaSuccess) e = cudaMemcpyAsync(dst, dd, (size_t)op->N * k * usz, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(op->ctx, e, "load vector");
+  }
+  return BG_OK;
+}
+
+extern "C" bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out) {
+  if (!op || !rho || !pts || !out || nrhs <= 0 || npts <= 0) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: potentials need a GPU");
+  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "potentials of vector operators");
+  cudaSetDevice(op->ctx->device);
+  cudaStream_t s = op->ctx->stream;
+  const size_t usz = op->cplx ? 16 : 8;
+  const int n1 = op->P + 2, Q = n1 * n1, p2 = op->p2;
+  const Rule1D& gr = gauss_rule(n1);
+  std::vector<double> basis((size_t)Q * p2);
+  for (int q = 0; q < Q; ++q) {
+    double bs[8], bt[8];
+    bernstein(op->P, gr.x[q / n1], bs);
+    bernstein(op->P, gr.x[q % n1], bt);
+    for (int iy = 0; iy <= op->P; ++iy)
+      for (int ix = 0; ix <= op->P; ++ix) basis[(size_t)q * p2 + iy * (op->P + 1) + ix] = bs[ix] * bt[iy];
+  }
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), 1.0 / double(1 << op->M)};
+  DevBuf gx, gw, tab, dbas, dpts, drho, dout;
+  std::vector<double> P3(pts, pts + 3 * npts);
+  cudaError_t e = gx.upload(gr.x, s);
+  if (e == cudaSuccess) e = gw.upload(gr.w, s);
+  if (e == cudaSuccess) e = dbas.upload(basis, s);
+  if (e == cudaSuccess) e = dpts.upload(P3, s);
+  if (e == cudaSuccess) e = tab.alloc((size_t)op->ne * Q * sizeof(d4));
+  if (e == cudaSuccess) e = launch_quad_table(op->G, pt, et, op->ne, gx.as<double>(), gw.as<double>(), n1, tab.as<d4>(), s);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "potential setup");
+  for (int c0 = 0; c0 < nrhs; c0 += 32) {
+    const int k = std::min(32, nrhs - c0);
+    bg_status st = ensure_work(op, k);
+    if (st != BG_OK) return st;
+    e = drho.alloc((size_t)op->N * k * usz);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(drho.p, static_cast<const char*>(rho) + (size_t)c0 * op->N * usz, (size_t)op->N * k * usz,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_gather_in(op->stype(false), op->stype(false), drho.p, op->N, op->N, k, op->w_xdof.p, s);
+    if (e == cudaSuccess)
+      e = launch_csr_apply(op->stype(false), op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(),
+                           op->S, op->w_xdof.p, op->w_xss.p, k, s);
+    if (e == cudaSuccess) e = dout.alloc((size_t)npts * k * usz);
+    if (e == cudaSuccess)
+      e = launch_potential(op->P, op->cplx, tab.as<d4>(), op->ne, Q, dbas.as<double>(), op->w_xss.as<double>(), k,
+                           dpts.as<double>(), npts, op->kre, op->kim, dout.as<double>(), s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<char*>(out) + (size_t)c0 * npts * usz, dout.p, (size_t)npts * k * usz,
+                          cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(op->ctx, e, "potential");
+  }
+  return BG_OK;
+}

@@ -1,0 +1,158 @@
+/*
+ * bembel_gb300 — C ABI of the GB300 (sm_103a) H2 single-layer operator.
+ *
+ * This is the drop-in boundary for Bembel's
+ *   DiscreteOperator<H2Matrix<Scalar>, {Laplace,Helmholtz,Maxwell}SingleLayerOperator>
+ * path: geometry -> discrete space -> H2 assembly -> H2 matvec -> Krylov solve.
+ * Every entry point names the reference interface it replaces (paths are
+ * relative to the Bembel source tree). Plain pointers and sizes only; no
+ * exceptions cross this boundary; every call returns a bg_status.
+ *
+ * Conventions
+ *  - Vectors are column-major blocks of nrhs columns with leading dimension
+ *    ld >= rows. Complex values are interleaved (re, im) doubles, the layout
+ *    of std::complex<double>.
+ *  - The row/column space of the operator is the reference's DOF space
+ *    (cols of AnsatzSpace::get_transformation_matrix(), AnsatzSpace.hpp:108).
+ *  - Helmholtz/Maxwell kernels use the reference sign exp(-i k r)/(4 pi r)
+ *    (Helmholtz/SingleLayerOperator.hpp:115-120).
+ */
+#ifndef BEMBEL_GB300_H_
+#define BEMBEL_GB300_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BG_OK = 0,
+  BG_INVALID_ARG = 1,
+  BG_OOM = 2,
+  BG_UNSUPPORTED = 3,
+  BG_DEVICE_ERROR = 4,
+  BG_TIMEOUT = 5,
+  BG_CANCELLED = 6,
+  BG_NOT_CONVERGED = 7
+} bg_status;
+
+typedef enum { BG_LAPLACE_SL = 0, BG_HELMHOLTZ_SL = 1, BG_MAXWELL_SL = 2 } bg_op_kind;
+
+/* Arithmetic of the far field in a product. BG_PREC_FP64 streams the stored
+ * FP64 couplings (the reference's H2Matrix); BG_PREC_FP32 generates the
+ * couplings on the fly in FP32 inside the fused matvec (no stored far field). */
+typedef enum { BG_PREC_FP64 = 0, BG_PREC_FP32 = 1 } bg_precision;
+
+typedef struct bg_context bg_context;
+typedef struct bg_geometry bg_geometry;
+typedef struct bg_operator bg_operator;
+
+/* H2 parameters. Defaults (bg_h2_params_default) are the reference's:
+ * number_of_points = 9 (H2Matrix.hpp:94-96), eta = 1.6 and
+ * min_cluster_level = 1 (BlockClusterTree.hpp:113-118). */
+typedef struct {
+  int n_p;               /* Chebyshev points per direction */
+  double eta;            /* admissibility constant */
+  int min_cluster_level; /* leaf clusters hold 4^min_cluster_level elements */
+  int store_fp64_far;    /* 1: assemble and store the FP64 far field */
+} bg_h2_params;
+
+/* Solve controls for bg_solve (GMRES with iterative refinement). */
+typedef struct {
+  double tol;            /* target ||b - A x|| / ||b|| per column */
+  int restart;           /* Krylov restart length */
+  int max_iter;          /* total inner iterations, all refinement steps */
+  int inner_precision;   /* bg_precision of the inner (correction) operator */
+  double inner_tol;      /* relative tolerance of each inner solve */
+  int max_refinements;   /* outer FP64 residual steps */
+} bg_solve_params;
+
+typedef struct {
+  int iterations;        /* inner Krylov iterations, summed */
+  int refinements;       /* FP64 residual evaluations */
+  int fp64_matvecs;
+  int low_matvecs;
+  double final_relres;   /* max over columns */
+} bg_solve_stats;
+
+void bg_h2_params_default(bg_h2_params* p);
+void bg_solve_params_default(bg_solve_params* p);
+
+/* Context: one GPU, its streams and scratch. Bembel has no counterpart; it is
+ * the owner of everything the reference keeps in process globals. */
+bg_status bg_context_create(int device, bg_context** out);
+bg_status bg_context_destroy(bg_context* ctx);
+const char* bg_last_error_string(bg_context* ctx);
+
+/* Geometry(const std::string&) with LoadGeometryFileDAT
+ * (Geometry/Geometry.hpp:89-102, Geometry/GeometryIO.hpp:25-122). */
+bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** out);
+bg_status bg_geometry_destroy(bg_geometry* g);
+/* Patch::updateSurfacePoint at patch coordinates (Geometry/Patch.hpp:294-365);
+ * out12 = [s, t, 1, x(3), dx(3), dy(3)]. Host evaluation. */
+bg_status bg_geometry_surface_point(const bg_geometry* g, int patch, double s, double t, double* out12);
+
+/* AnsatzSpace(geometry, M, P) + DiscreteOperator<H2Matrix<S>, Op>(ansatz_space)
+ * (AnsatzSpace/AnsatzSpace.hpp:102-111, LinearOperator/DiscreteOperator.hpp:107-145):
+ * builds the element tree, block cluster tree, transformation matrix, FMM
+ * moments/transfers and uploads the device tables. */
+bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, int M, int P, int op_kind,
+                             const bg_h2_params* params, bg_operator** out);
+/* HelmholtzSingleLayerOperator::set_wavenumber (Helmholtz/SingleLayerOperator.hpp:124-126). */
+bg_status bg_operator_set_wavenumber(bg_operator* op, double re, double im);
+/* DiscreteOperator::compute -> H2Matrix::init_H2Matrix (H2Matrix/H2Matrix.hpp:93-250):
+ * near-field (DuffyTrick) and far-field (interpolateKernel) assembly on the GPU. */
+bg_status bg_operator_assemble(bg_operator* op);
+bg_status bg_operator_destroy(bg_operator* op);
+/* info[0..15]: rows (= cols, H2Matrix.hpp:76-77), superspace size, elements,
+ * dense leaves, low-rank leaves, vector dimension, FMM components, n_p,
+ * is_complex, M, P, dense-leaf levels' cluster size, nnz(T), stored far-field
+ * bytes, near-field bytes, element pairs in the near field. */
+bg_status bg_operator_info(const bg_operator* op, long* info);
+/* seconds of the last bg_operator_assemble: [near field, far field, total] */
+bg_status bg_operator_assembly_times(const bg_operator* op, double* t3);
+
+/* H2_time_dense_product_impl::run via generic_product_impl::scaleAndAddTo
+ * (H2Matrix/EigenHelper/H2DenseProduct.hpp:33-165, 268-290):
+ *   Y = beta * Y + alpha * A X   for nrhs columns.
+ * x, y are host pointers when on_device == 0 (staged through pinned buffers),
+ * device pointers otherwise. alpha/beta are complex (re, im) pairs; for a real
+ * operator their imaginary parts must be 0. precision: bg_precision. */
+bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
+                    const double* alpha, const double* beta, int precision, int on_device);
+
+/* DiscreteLinearForm<DirichletTrace<S>, Op>::compute (LinearForm/DiscreteLinearForm.hpp:44-83,
+ * LinearForm/DirichletTrace.hpp:38-66) for analytic data (examples/Data.hpp):
+ *   kind 0: u(x) = 1/(4 pi |x - x0|), prm = x0 (3 doubles per column)
+ *   kind 1: u(x) = exp(-i k |x - x0|)/(4 pi |x - x0|), prm = x0 (3 per column)
+ *   kind 2: plane wave u(x) = exp(-i k d.x), prm = d (3 per column)
+ * Output: nrhs load vectors (N x nrhs, column-major, ld = N), host or device. */
+bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device);
+
+/* GMRES on the H2 operator with iterative refinement (replaces the Eigen
+ * solvers called at examples/LaplaceSingleLayerH2.cpp:78-81 and
+ * examples/HelmholtzSingleLayerH2.cpp:82-85). Residuals, the near field and the
+ * Krylov basis are FP64; the inner correction operator is params->inner_precision. */
+bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params* params,
+                   bg_solve_stats* stats, int on_device);
+
+/* DiscretePotential<...SingleLayerPotential>::evaluate (Potential/DiscretePotential.hpp:49-107)
+ * at npts points (3 doubles each) for nrhs densities rho (N x nrhs). */
+bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out);
+
+/* ---- inspection entry points used by the parity tests ---- */
+/* per element id: patch, vertex ids[4]; and llc[2], ball midpoint[3], radius */
+bg_status bg_operator_elements(const bg_operator* op, int* ints5, double* dbl6);
+/* per leaf: admissibility (2 dense, 1 low-rank), level, cluster1 id, cluster2 id */
+bg_status bg_operator_leaves(const bg_operator* op, int* out4);
+/* transformation matrix T (superspace x dofs) in CSR */
+bg_status bg_operator_transform(const bg_operator* op, int* ptr, int* idx, double* val);
+/* copy one assembled leaf block (row component rc, column component cc) to the
+ * host, column-major (complex interleaved); leaf indexes bg_operator_leaves */
+bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, int rc, int cc, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEMBEL_GB300_H_ */

@@ -339,7 +339,6 @@ int gmres(Problem& p, const S* b, S* x, double tol, int restart, int maxit) {
       } else {
         cs[j] = a / den;
         sn[j] = (H[j][j] / a) * (S(bb) / den);
-        if constexpr (!std::is_same<S, double>::value) sn[j] = std::conj(sn[j]);
       }
       H[j][j] = cs[j] * H[j][j] + sn[j] * H[j + 1][j];
       H[j + 1][j] = 0;

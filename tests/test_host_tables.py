@@ -1,0 +1,83 @@
+"""Host-side setup of the product (host-only context, no GPU) against the oracle:
+element tree, vertex topology, enclosing balls, block partition and the
+transformation matrix T."""
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, SPHERE, TORUS
+
+
+@pytest.fixture(scope="module")
+def bg_host():
+    import bembel_gb300 as bg
+    return bg, bg.Context(-1)
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+    from bembel_gb300 import _lib
+    header = open(ROOT + "/include/bembel_gb300.h").read()
+    names = set(re.findall(r"\b(bg_[a-z0-9_]+)\s*\(", header))
+    assert len(names) >= 20
+    L = ctypes.CDLL(_lib.LIB_PATH) if _lib._lib is None else _lib._lib
+    _lib.load()
+    missing = [n for n in sorted(names) if not hasattr(_lib.load(), n)]
+    assert not missing
+
+
+@pytest.mark.parametrize("geo,M,P", [(SPHERE, 3, 1), (SPHERE, 2, 2), (TORUS, 2, 2), (SPHERE, 1, 0), (SPHERE, 0, 1)])
+def test_tables_match_oracle(bg_host, oracle, geo, M, P):
+    bg, ctx = bg_host
+    g = bg.Geometry(geo, ctx)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(g, M, P), bg.LaplaceSingleLayerOperator(), n_p=6)
+    o = oracle.Problem(geo, M, P, oracle.LAPLACE, np_=6, assemble=False)
+    assert (d.N, d.S, d.n_dense, d.n_lowrank) == (o.N, o.S, o.n_dense, o.n_lowrank)
+    pi, pd = d.elements()
+    oi, od = o.elements()
+    assert np.array_equal(pi[:, 0], oi[:, 0])
+    # vertex numbering differs, the identification must be the same bijection
+    mp = {}
+    for e in range(d.ne):
+        for k in range(4):
+            assert mp.setdefault(int(pi[e, 1 + k]), int(oi[e, 3 + k])) == int(oi[e, 3 + k])
+    assert len(set(mp.values())) == len(mp)
+    assert np.array_equal(pd[:, :2], od[:, :2])
+    assert np.array_equal(pd[:, 2:], od[:, 2:])  # enclosing balls bit-identical
+    ps = set(map(tuple, d.leaves().tolist()))
+    os_ = set(map(tuple, o.leaves()[:, :4].tolist()))
+    assert ps == os_
+    a, b = d.transform_csr(), o.transform_csr()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.abs(a[2] - b[2]).max() < 1e-13
+
+
+def test_surface_point_matches_oracle(bg_host, oracle):
+    bg, ctx = bg_host
+    g = bg.Geometry(SPHERE, ctx)
+    o = oracle.Problem(SPHERE, 0, 0, oracle.LAPLACE, np_=6, assemble=False)
+    rng = np.random.default_rng(5)
+    for _ in range(50):
+        p, s, t = int(rng.integers(6)), rng.uniform(), rng.uniform()
+        assert np.abs(g.surface_point(p, s, t)[3:] - o.surface_point(p, s, t)[3:]).max() < 1e-14
+
+
+def test_host_only_context_refuses_device_work(bg_host):
+    bg, ctx = bg_host
+    g = bg.Geometry(SPHERE, ctx)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(g, 1, 1), bg.LaplaceSingleLayerOperator(), n_p=6)
+    with pytest.raises(bg.BembelError) as ei:
+        d.compute()
+    assert "host-only" in str(ei.value)
+
+
+def test_invalid_arguments(bg_host):
+    bg, ctx = bg_host
+    with pytest.raises(bg.BembelError):
+        bg.Geometry("/nonexistent/file.dat", ctx)
+    g = bg.Geometry(SPHERE, ctx)
+    with pytest.raises(bg.BembelError):
+        bg.DiscreteOperator(bg.AnsatzSpace(g, 1, 7), bg.LaplaceSingleLayerOperator())
+    with pytest.raises(bg.BembelError):
+        bg.DiscreteOperator(bg.AnsatzSpace(g, 1, 1), bg.LaplaceSingleLayerOperator(), n_p=1)
