@@ -80,9 +80,12 @@ class Geometry:
         return out
 
     def __del__(self):
-        if getattr(self, "h", None):
-            _lib.load().bg_geometry_destroy(self.h)
-            self.h = None
+        try:
+            if getattr(self, "h", None):
+                _lib.load().bg_geometry_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
 
 
 class AnsatzSpace:
@@ -163,8 +166,12 @@ class H2Matrix:
         return self.matvec(x)
 
     def matvec(self, x, precision="fp64", out=None, alpha=1.0, beta=0.0):
-        """out = beta * out + alpha * A x (H2DenseProduct.hpp:268-290)."""
-        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_FP32
+        """out = beta * out + alpha * A x (H2DenseProduct.hpp:268-290).
+        precision "fp64": the FP64 H2 matrix; "mixed": FP64 near field, FP32
+        on-the-fly far field."""
+        if precision not in ("fp64", "mixed"):
+            raise BembelError(_lib.BG_INVALID_ARG, "precision must be 'fp64' or 'mixed'")
+        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
         N = self._dop.N
         a = np.array([complex(alpha).real, complex(alpha).imag])
         b = np.array([complex(beta).real, complex(beta).imag])
@@ -190,12 +197,12 @@ class H2Matrix:
                                                   prec, 0))
         return Y[:, 0].copy() if squeeze else Y
 
-    def solve(self, b, tol=1e-8, restart=60, max_iter=2000, inner="fp32", inner_tol=1e-5, max_refinements=12):
+    def solve(self, b, tol=1e-8, restart=200, max_iter=3000, inner="mixed", inner_tol=1e-5, max_refinements=12):
         """GMRES with FP64 iterative refinement; returns (x, stats dict)."""
         p = SolveParams()
         _lib.load().bg_solve_params_default(ctypes.byref(p))
         p.tol, p.restart, p.max_iter = tol, restart, max_iter
-        p.inner_precision = _lib.PREC_FP32 if inner == "fp32" else _lib.PREC_FP64
+        p.inner_precision = _lib.PREC_MIXED if inner == "mixed" else _lib.PREC_FP64
         p.inner_tol, p.max_refinements = inner_tol, max_refinements
         st = SolveStats()
         N = self._dop.N
@@ -203,7 +210,7 @@ class H2Matrix:
             import torch
             squeeze = b.dim() == 1
             B = b.reshape(N, -1).t().contiguous()
-            X = torch.empty_like(B)
+            X = torch.empty_like(B) if B.is_cuda else torch.empty(B.shape, dtype=B.dtype, pin_memory=B.is_pinned())
             status = _lib.load().bg_solve(self.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
                                           B.shape[0], ctypes.byref(p), ctypes.byref(st), 1 if B.is_cuda else 0)
             x = X.t()
@@ -248,9 +255,12 @@ class DiscreteOperator:
         self._matrix = H2Matrix(self)
 
     def __del__(self):
-        if getattr(self, "h", None):
-            _lib.load().bg_operator_destroy(self.h)
-            self.h = None
+        try:
+            if getattr(self, "h", None):
+                _lib.load().bg_operator_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
 
     def info(self):
         out = np.zeros(16, dtype=np.int64)

@@ -14,7 +14,7 @@ BG_OK, BG_INVALID_ARG, BG_OOM, BG_UNSUPPORTED, BG_DEVICE_ERROR, BG_TIMEOUT, BG_C
 STATUS_NAMES = ["BG_OK", "BG_INVALID_ARG", "BG_OOM", "BG_UNSUPPORTED", "BG_DEVICE_ERROR", "BG_TIMEOUT",
                 "BG_CANCELLED", "BG_NOT_CONVERGED"]
 LAPLACE_SL, HELMHOLTZ_SL, MAXWELL_SL = 0, 1, 2
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
 
 
 class H2Params(ctypes.Structure):

@@ -11,6 +11,28 @@
 
 using namespace bg;
 
+static void context_free(bg_context* ctx) {
+  if (ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->stage_in.release();
+    ctx->stage_out.release();
+    for (int c = 0; c < 8; ++c)
+      for (auto& pr : ctx->pending[c]) {
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+      }
+    for (auto ev : ctx->event_pool) cudaEventDestroy(ev);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+}
+void context_retain(bg_context* ctx) { ++ctx->children; }
+void context_release(bg_context* ctx) {
+  if (--ctx->children == 0 && ctx->closing) context_free(ctx);
+}
+
 bg_status set_error(bg_context* ctx, bg_status st, const std::string& msg) {
   if (ctx) ctx->err = msg;
   return st;
@@ -39,9 +61,9 @@ void bg_h2_params_default(bg_h2_params* p) {
 void bg_solve_params_default(bg_solve_params* p) {
   if (!p) return;
   p->tol = 1e-8;
-  p->restart = 60;
+  p->restart = 200;
   p->max_iter = 2000;
-  p->inner_precision = BG_PREC_FP32;
+  p->inner_precision = BG_PREC_MIXED;
   p->inner_tol = 1e-5;
   p->max_refinements = 12;
 }
@@ -68,22 +90,49 @@ bg_status bg_context_create(int device, bg_context** out) {
   return BG_OK;
 }
 bg_status bg_context_destroy(bg_context* ctx) {
-  if (!ctx) return BG_INVALID_ARG;
-  if (ctx->device >= 0) {
-    cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
-    ctx->stage_in.release();
-    ctx->stage_out.release();
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    cudaStreamDestroy(ctx->stream);
-  }
-  delete ctx;
+  if (!ctx || ctx->closing) return BG_INVALID_ARG;
+  ctx->closing = true;
+  if (ctx->children == 0) context_free(ctx);
   return BG_OK;
 }
 const char* bg_last_error_string(bg_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
+bg_status bg_context_get_stream(bg_context* ctx, void** stream) {
+  if (!ctx || !stream) return BG_INVALID_ARG;
+  *stream = (void*)ctx->stream;
+  return BG_OK;
+}
+bg_status bg_profile_enable(bg_context* ctx, int enable) {
+  if (!ctx) return BG_INVALID_ARG;
+  if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context");
+  ctx->profiling = enable != 0;
+  return BG_OK;
+}
+bg_status bg_profile_read(bg_context* ctx, double* ms8, long* launches8) {
+  if (!ctx || !ms8 || !launches8) return BG_INVALID_ARG;
+  if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context");
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(ctx, e, "profile");
+  for (int c = 0; c < 8; ++c) {
+    for (auto& pr : ctx->pending[c]) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, pr.first, pr.second);
+      ctx->class_ms[c] += ms;
+      ctx->event_pool.push_back(pr.first);
+      ctx->event_pool.push_back(pr.second);
+    }
+    ctx->pending[c].clear();
+    ms8[c] = ctx->class_ms[c];
+    launches8[c] = ctx->class_launches[c];
+    ctx->class_ms[c] = 0;
+    ctx->class_launches[c] = 0;
+  }
+  return BG_OK;
+}
+
 bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** out) {
-  if (!ctx || !path || !out) return BG_INVALID_ARG;
+  if (!ctx || !path || !out || ctx->closing) return BG_INVALID_ARG;
   *out = nullptr;
   bg_geometry* g = new (std::nothrow) bg_geometry();
   if (!g) return BG_OOM;
@@ -93,12 +142,15 @@ bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** 
     return set_error(ctx, BG_INVALID_ARG, err);
   }
   g->ctx = ctx;
+  context_retain(ctx);
   *out = g;
   return BG_OK;
 }
 bg_status bg_geometry_destroy(bg_geometry* g) {
   if (!g) return BG_INVALID_ARG;
+  bg_context* ctx = g->ctx;
   delete g;
+  if (ctx) context_release(ctx);
   return BG_OK;
 }
 bg_status bg_geometry_surface_point(const bg_geometry* g, int patch, double s, double t, double* out12) {
@@ -222,7 +274,7 @@ static bg_status upload_tables(bg_operator* op) {
 
 extern "C" bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, int M, int P, int op_kind,
                                         const bg_h2_params* params, bg_operator** out) {
-  if (!ctx || !g || !out) return BG_INVALID_ARG;
+  if (!ctx || !g || !out || ctx->closing) return BG_INVALID_ARG;
   *out = nullptr;
   if (M < 0 || M > 9) return set_error(ctx, BG_INVALID_ARG, "refinement level must be in [0, 9]");
   if (P < 0 || P > 3) return set_error(ctx, BG_UNSUPPORTED, "polynomial degree must be in [0, 3]");
@@ -278,17 +330,20 @@ extern "C" bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, i
       return st;
     }
   }
+  context_retain(ctx);
   *out = op;
   return BG_OK;
 }
 
 extern "C" bg_status bg_operator_destroy(bg_operator* op) {
   if (!op) return BG_INVALID_ARG;
-  if (op->ctx && op->ctx->device >= 0) {
-    cudaSetDevice(op->ctx->device);
-    cudaStreamSynchronize(op->ctx->stream);
+  bg_context* ctx = op->ctx;
+  if (ctx && ctx->device >= 0) {
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
   }
   delete op;
+  if (ctx) context_release(ctx);
   return BG_OK;
 }
 
@@ -308,9 +363,9 @@ extern "C" bg_status bg_operator_info(const bg_operator* op, long* info) {
   long nd = 0, nl = 0;
   for (size_t k = 0; k < op->part.leaf_list.size(); k += 4) (op->part.leaf_list[k] == 2 ? nd : nl)++;
   long far_bytes = 0;
-  for (const auto& f : op->far) far_bytes += (long)f.col.size() * f.B * f.B * (long)op->scalar_bytes(false);
+  for (const auto& f : op->far) far_bytes += (long)f.col.size() * op->block_stride(f.B) * 8 * (op->cplx ? 2 : 1);
   if (!op->store_far) far_bytes = 0;
-  const long near_bytes = (long)op->dense.col.size() * op->dense.B * op->dense.B * (long)op->scalar_bytes(false);
+  const long near_bytes = (long)op->dense.col.size() * op->block_stride(op->dense.B) * (long)op->scalar_bytes(false);
   long v[16] = {op->N, op->S, op->ne, nd, nl, op->vd, op->nc, op->np, op->cplx ? 1 : 0, op->M, op->P,
                 op->dense.B / std::max(op->p2, 1), (long)op->T.val.size(), far_bytes, near_bytes, op->near_pairs};
   std::memcpy(info, v, sizeof(v));
@@ -372,8 +427,9 @@ extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, in
   if (k < 0) return set_error(op->ctx, BG_INVALID_ARG, "leaf not found");
   const size_t sb = op->scalar_bytes(false);
   const size_t bytes = (size_t)seg->B * seg->B * sb;
+  const size_t stride = (size_t)op->block_stride(seg->B) * sb;
   cudaSetDevice(op->ctx->device);
-  cudaError_t e = cudaMemcpy(out, static_cast<const char*>(data->p) + k * bytes, bytes, cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(out, static_cast<const char*>(data->p) + k * stride, bytes, cudaMemcpyDeviceToHost);
   return cuda_status(op->ctx, e, "copy leaf block");
 }
 
@@ -390,13 +446,18 @@ static bg_status assemble_far(bg_operator* op) {
     if ((int)op->d_pts64.size() <= l) {
       op->d_pts64.push_back(new DevBuf());
       op->d_pts32.push_back(new DevBuf());
+      op->d_centres.push_back(new DevBuf());
       op->d_far64.push_back(new DevBuf());
     }
     const int ncl = op->nclusters(l);
+    std::vector<double> cen(4 * (size_t)ncl);
+    for (int c = 0; c < ncl; ++c)
+      for (int q = 0; q < 3; ++q) cen[4 * c + q] = op->mesh.ball[l][4 * c + q];
+    BG_CHECK(op->d_centres[l]->upload(cen, s), "cluster centres");
     BG_CHECK(op->d_pts64[l]->alloc((size_t)ncl * np2 * sizeof(d4)), "cluster points");
     BG_CHECK(op->d_pts32[l]->alloc((size_t)ncl * np2 * sizeof(float4)), "cluster points");
-    BG_CHECK(launch_cluster_points(op->G, pt, l, ncl, op->d_cheb.as<double>(), op->np, op->d_pts64[l]->as<d4>(),
-                                   op->d_pts32[l]->as<float4>(), s),
+    BG_CHECK(timed_launch(op->ctx, KC_ASSEMBLY, [&] { return launch_cluster_points(op->G, pt, l, ncl, op->d_cheb.as<double>(), op->np, op->d_centres[l]->as<d4>(),
+                                   op->d_pts64[l]->as<d4>(), op->d_pts32[l]->as<float4>(), s); }),
              "cluster points");
     if (!op->store_far || op->far[l].col.empty()) continue;
     if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "stored far field of vector operators");
@@ -406,10 +467,10 @@ static bg_status assemble_far(bg_operator* op) {
       for (int k = f.row_ptr[r]; k < f.row_ptr[r + 1]; ++k) pairs[k] = make_int2(r, f.col[k]);
     DevBuf dp;
     BG_CHECK(dp.upload(pairs, s), "far pairs");
-    const size_t bytes = (size_t)f.col.size() * f.B * f.B * op->scalar_bytes(false);
+    const size_t bytes = (size_t)f.col.size() * op->block_stride(f.B) * op->scalar_bytes(false);
     BG_CHECK(op->d_far64[l]->alloc(bytes), "far field storage");
-    BG_CHECK(launch_far_assemble(op->cplx, op->d_pts64[l]->as<d4>(), dp.as<int2>(), (int)pairs.size(), f.B, op->kre,
-                                 op->kim, op->d_far64[l]->p, s),
+    BG_CHECK(timed_launch(op->ctx, KC_ASSEMBLY, [&] { return launch_far_assemble(op->cplx, op->d_pts64[l]->as<d4>(), dp.as<int2>(), (int)pairs.size(), f.B,
+                                 op->block_stride(f.B), op->kre, op->kim, op->d_far64[l]->p, s); }),
              "far-field assembly");
     BG_CHECK(cudaStreamSynchronize(s), "far-field assembly");
   }
@@ -423,8 +484,9 @@ static bg_status assemble_near(bg_operator* op) {
   const int ecl = B / p2;
   if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "near field of vector operators");
   const size_t sb = op->scalar_bytes(false);
-  BG_CHECK(op->d_dense64.alloc((size_t)D.col.size() * B * B * sb), "near-field storage");
-  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, (size_t)D.col.size() * B * B * sb, s), "near-field storage");
+  const long bstride = op->block_stride(B);
+  BG_CHECK(op->d_dense64.alloc((size_t)D.col.size() * bstride * sb), "near-field storage");
+  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, (size_t)D.col.size() * bstride * sb, s), "near-field storage");
   // classify every element pair of the dense leaves (host, FP64 like the reference)
   std::map<int, std::vector<NearPair>> regular;                 // by degree
   std::map<std::pair<int, int>, std::vector<NearPair>> singular;  // by (case, degree)
@@ -441,7 +503,7 @@ static bg_status assemble_near(bg_operator* op) {
           np.e2 = e2;
           np.rot = (pc.rot1 & 15) | ((pc.rot2 & 15) << 4);
           np.pad = 0;
-          np.dst = (long long)k * B * B + (long long)(b * p2) * B + a * p2;
+          np.dst = (long long)k * bstride + (long long)(b * p2) * B + a * p2;
           if (pc.cs == 0) regular[pc.deg].push_back(np);
           else singular[{pc.cs, pc.deg}].push_back(np);
           ++npairs;
@@ -502,11 +564,6 @@ static bg_status assemble_near(bg_operator* op) {
   cudaError_t e = cudaStreamSynchronize(s);
   cleanup();
   if ((st = cuda_status(op->ctx, e, "near-field assembly")) != BG_OK) return st;
-  // FP32 copy for the mixed-precision inner operator
-  const long n = (long)D.col.size() * B * B * (op->cplx ? 2 : 1);
-  BG_CHECK(op->d_dense32.alloc(n * sizeof(float)), "near-field FP32 copy");
-  BG_CHECK(launch_convert(0, 2, op->d_dense64.p, n, op->d_dense32.p, s), "near-field FP32 copy");
-  BG_CHECK(cudaStreamSynchronize(s), "near-field FP32 copy");
   return BG_OK;
 }
 
@@ -538,6 +595,8 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
   BG_CHECK(op->w_ydof.alloc((size_t)op->N * nrhs * sb), "work vectors");
   BG_CHECK(op->w_xss.alloc((size_t)op->S * nrhs * sb), "work vectors");
   BG_CHECK(op->w_yss.alloc((size_t)op->S * nrhs * sb), "work vectors");
+  BG_CHECK(op->w_xss32.alloc((size_t)op->S * nrhs * sb / 2), "work vectors");
+  BG_CHECK(op->w_yss32.alloc((size_t)op->S * nrhs * sb / 2), "work vectors");
   while ((int)op->w_y.size() <= op->leaf_level) {
     op->w_y.push_back(new DevBuf());
     op->w_z.push_back(new DevBuf());
@@ -551,78 +610,86 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
   return BG_OK;
 }
 
-// One H2 product on row-major work vectors (H2DenseProduct.hpp:33-165).
-bg_status apply_operator(bg_operator* op, int nrhs, bool fp32, const void* xdof, void* ydof) {
+// One H2 product on row-major FP64 work vectors (H2DenseProduct.hpp:33-165).
+bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof, void* ydof) {
   cudaStream_t s = op->ctx->stream;
-  const int S = op->stype(fp32);
-  const size_t sb = op->scalar_bytes(fp32);
+  const int S64 = op->stype(false), Sfar = op->stype(mixed);
+  const size_t sfar = op->scalar_bytes(mixed);
   const int np2 = op->np * op->np;
-  BG_CHECK(launch_csr_apply(S, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
-                            op->w_xss.p, nrhs, s),
+  const long ss_n = (long)op->S * nrhs;
+  BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
+                            op->w_xss.p, nrhs, s); }),
            "T x");
+  // near field, always FP64
+  BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
+                      op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p, nrhs, 0, s); }),
+           "near-field product");
   bool any_far = false;
   for (const auto& f : op->far) any_far |= !f.col.empty();
-  const long comp_ss = (long)op->ne * op->p2;  // superspace rows per vector component
   if (any_far) {
+    const long comp_ss = (long)op->ne * op->p2;  // superspace rows per vector component
+    const void* xfar = op->w_xss.p;
+    void* yfar = op->w_yss.p;
+    if (mixed) {
+      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
+      BG_CHECK(cudaMemsetAsync(op->w_yss32.p, 0, ss_n * sfar, s), "far field");
+      xfar = op->w_xss32.p;
+      yfar = op->w_yss32.p;
+    }
     const int Ll = op->leaf_level;
     for (int c = 0; c < op->vd; ++c) {
-      const void* mom = fp32 ? op->d_mom32[c]->p : op->d_mom64[c]->p;
-      BG_CHECK(launch_moment_fwd(S, mom, op->R, op->Bq, op->nleaf_cl,
-                                 static_cast<const char*>(op->w_xss.p) + c * comp_ss * nrhs * sb,
-                                 static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sb, nrhs, s),
+      const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_moment_fwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl,
+                                 static_cast<const char*>(xfar) + c * comp_ss * nrhs * sfar,
+                                 static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar,
+                                 nrhs, s); }),
                "forward moments");
       for (int l = Ll - 1; l >= 0; --l) {
         const int ncl = op->nclusters(l);
-        BG_CHECK(launch_transfer_fwd(S, fp32 ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
-                                     static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sb,
-                                     static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sb, nrhs, s),
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                     static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar,
+                                     static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar, nrhs, s); }),
                  "forward transfer");
       }
     }
-  }
-  // near field
-  BG_CHECK(launch_bsr(S, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(),
-                      fp32 ? op->d_dense32.p : op->d_dense64.p, op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p,
-                      nrhs, 0, s),
-           "near-field product");
-  if (any_far) {
     for (int l = 0; l <= op->leaf_level; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
-        BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)f.nrows * f.B * nrhs * sb, s), "far field");
+        BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)f.nrows * f.B * nrhs * sfar, s), "far field");
         continue;
       }
-      if (fp32) {
-        if (op->vd != 1 || op->nc != 1) return set_error(op->ctx, BG_UNSUPPORTED, "FP32 far field of vector operators");
-        BG_CHECK(launch_far_fused(op->cplx, op->d_pts32[l]->as<float4>(), op->d_pts32[l]->as<float4>(),
+      if (mixed) {
+        if (op->vd != 1 || op->nc != 1) return set_error(op->ctx, BG_UNSUPPORTED, "mixed far field of vector operators");
+        BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_fused(op->cplx, op->d_pts32[l]->as<float4>(), op->d_centres[l]->as<d4>(),
                                   f.d_row_ptr.as<int>(), f.d_col.as<int>(), f.nrows, np2, (float)op->kre, (float)op->kim,
-                                  op->w_y[l]->p, op->w_z[l]->p, nrhs, s),
+                                  op->w_y[l]->p, op->w_z[l]->p, nrhs, s); }),
                  "far-field product (FP32 fused)");
       } else {
-        if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "FP64 product needs the stored far field");
-        BG_CHECK(launch_bsr(S, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p, f.nrows, f.B, op->w_y[l]->p,
-                            op->w_z[l]->p, nrhs, 0, s),
+        if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "the FP64 product needs the stored far field");
+        BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(op->cplx, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
+                            op->block_stride(f.B), f.nrows, f.B, op->w_y[l]->p, op->w_z[l]->p, nrhs, 0, s); }),
                  "far-field product");
       }
     }
-    const int Ll = op->leaf_level;
     for (int c = 0; c < op->vd; ++c) {
       for (int l = 0; l < Ll; ++l) {
         const int ncl = op->nclusters(l);
-        BG_CHECK(launch_transfer_bwd(S, fp32 ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
-                                     static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sb,
-                                     static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sb, nrhs, s),
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                     static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar,
+                                     static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar,
+                                     nrhs, s); }),
                  "backward transfer");
       }
-      const void* mom = fp32 ? op->d_mom32[c]->p : op->d_mom64[c]->p;
-      BG_CHECK(launch_moment_bwd(S, mom, op->R, op->Bq, op->nleaf_cl,
-                                 static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sb,
-                                 static_cast<char*>(op->w_yss.p) + c * comp_ss * nrhs * sb, nrhs, s),
+      const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_moment_bwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl,
+                                 static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar,
+                                 static_cast<char*>(yfar) + c * comp_ss * nrhs * sfar, nrhs, s); }),
                "backward moments");
     }
+    if (mixed) BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_add_low(op->cplx, op->w_yss32.p, ss_n, op->w_yss.p, s); }), "far field to FP64");
   }
-  BG_CHECK(launch_csr_apply(S, op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(), op->N,
-                            op->w_yss.p, ydof, nrhs, s),
+  BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(), op->N,
+                            op->w_yss.p, ydof, nrhs, s); }),
            "T^T y");
   return BG_OK;
 }
@@ -641,7 +708,7 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
   if (!op || !x || !y || nrhs <= 0 || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
   if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
-  if (precision != BG_PREC_FP64 && precision != BG_PREC_FP32) return set_error(op->ctx, BG_INVALID_ARG, "precision");
+  if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED) return set_error(op->ctx, BG_INVALID_ARG, "precision");
   const double one[2] = {1.0, 0.0}, zero2[2] = {0.0, 0.0};
   if (!alpha) alpha = one;
   if (!beta) beta = zero2;
@@ -649,7 +716,7 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
     return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
   cudaSetDevice(op->ctx->device);
   cudaStream_t s = op->ctx->stream;
-  const bool fp32 = precision == BG_PREC_FP32;
+  const bool mixed = precision == BG_PREC_MIXED;
   const size_t usz = op->cplx ? 16 : 8;
   const int uS = op->cplx ? 1 : 0;
   for (int c0 = 0; c0 < nrhs; c0 += 32) {
@@ -670,9 +737,9 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
       yd = op->ctx->stage_out.p;
       lx = ly = op->N;
     }
-    BG_CHECK(launch_gather_in(uS, op->stype(fp32), xd, lx, op->N, k, op->w_xdof.p, s), "gather x");
-    if ((st = apply_operator(op, k, fp32, op->w_xdof.p, op->w_ydof.p)) != BG_OK) return st;
-    BG_CHECK(launch_scatter_out(op->stype(fp32), op->w_ydof.p, op->N, k, yd, ly, alpha, beta, s), "scatter y");
+    BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_gather_in(uS, uS, xd, lx, op->N, k, op->w_xdof.p, s); }), "gather x");
+    if ((st = apply_operator(op, k, mixed, op->w_xdof.p, op->w_ydof.p)) != BG_OK) return st;
+    BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_scatter_out(uS, op->w_ydof.p, op->N, k, yd, ly, alpha, beta, s); }), "scatter y");
     if (!on_device)
       BG_CHECK(cudaMemcpy2DAsync(yp, ldy * usz, yd, op->N * usz, op->N * usz, k, cudaMemcpyDeviceToHost, s),
                "device to host copy");

@@ -37,10 +37,11 @@ cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable&
 // ---- far field ----
 // interpolation points of every cluster of a level: x, y, z, |dx x dy| (FP64 and FP32)
 cudaError_t launch_cluster_points(int G, const PatchTable& pt, int level, int nclusters, const double* cheb, int np,
-                                  d4* out64, float4* out32, cudaStream_t s);
+                                  const d4* centres, d4* out64, float4* out32, cudaStream_t s);
 // F blocks (B x B, column-major) for the listed cluster pairs of one level
-cudaError_t launch_far_assemble(bool cplx, const d4* pts, const int2* pairs, int nblocks, int B, double kre,
-                                double kim, void* out, cudaStream_t s);
+// block k written at out + k * bstride scalars
+cudaError_t launch_far_assemble(bool cplx, const d4* pts, const int2* pairs, int nblocks, int B, long bstride,
+                                double kre, double kim, void* out, cudaStream_t s);
 
 // ---- matvec building blocks (row-major work vectors, nrhs contiguous) ----
 // S: 0 double, 1 complex double, 2 float, 3 complex float
@@ -48,6 +49,10 @@ cudaError_t launch_csr_apply(int S, const int* ptr, const int* idx, const double
                              void* y, int nrhs, cudaStream_t s);
 cudaError_t launch_bsr(int S, const int* row_ptr, const int* col, const void* blocks, int nrows, int B, const void* x,
                        void* y, int nrhs, int accumulate, cudaStream_t s);
+// FP64 (cplx: complex FP64) block-sparse product with a cp.async pipeline;
+// block k starts at blocks + k * bstride scalars (bstride * sizeof >= 16 B multiple)
+cudaError_t launch_bsr_fp64(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
 cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int nclusters, const void* xss, void* y, int nrhs,
                               cudaStream_t s);
 cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int nclusters, const void* z, void* yss, int nrhs,
@@ -58,14 +63,16 @@ cudaError_t launch_transfer_bwd(int S, const void* T, int np2, int nc, int npare
                                 int nrhs, cudaStream_t s);
 // fused FP32 far field: for each listed block, generate the coupling from
 // cluster points on the fly and accumulate into the row cluster's output
-cudaError_t launch_far_fused(bool cplx, const float4* pts_row, const float4* pts_col, const int* row_ptr,
-                             const int* col, int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs,
-                             cudaStream_t s);
+// (points are FP32 offsets from the FP64 cluster centres)
+cudaError_t launch_far_fused(bool cplx, const float4* pts, const d4* centres, const int* row_ptr, const int* col,
+                             int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs, cudaStream_t s);
 // user column-major block (ld) <-> row-major work vector, with precision change
 cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int rows, int nrhs, void* work,
                              cudaStream_t s);
 cudaError_t launch_scatter_out(int Swork, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
                                const double* beta, cudaStream_t s);
 cudaError_t launch_convert(int Sin, int Sout, const void* in, long n, void* out, cudaStream_t s);
+// out64[t] += (FP64) in32[t]
+cudaError_t launch_add_low(bool cplx, const void* in32, long n, void* out64, cudaStream_t s);
 
 }  // namespace bg

@@ -8,6 +8,7 @@
 //   y = T^T y_ss                         (:161-162)
 // Work vectors are row-major with the right-hand sides contiguous, so every
 // coupling entry streamed from HBM is reused across all right-hand sides.
+#include <algorithm>
 #include <type_traits>
 
 #include "bg_kernels.cuh"
@@ -34,6 +35,29 @@ __device__ inline double add(double a, double b) { return a + b; }
 __device__ inline float add(float a, float b) { return a + b; }
 __device__ inline cd add(cd a, cd b) { return a + b; }
 __device__ inline cf add(cf a, cf b) { return a + b; }
+
+// Neumaier's compensated summation step: sum + comp carries the running total
+__device__ inline void neumaier_add(float& sum, float& comp, float v) {
+  const float t = sum + v;
+  comp += (fabsf(sum) >= fabsf(v)) ? ((sum - t) + v) : ((v - t) + sum);
+  sum = t;
+}
+__device__ inline void neumaier_add(cf& sum, cf& comp, cf v) {
+  neumaier_add(sum.re, comp.re, v.re);
+  neumaier_add(sum.im, comp.im, v.im);
+}
+
+__device__ inline void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ inline void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
 // ---------------------------------------------------------------------------
 template <typename S>
@@ -81,6 +105,67 @@ __global__ void k_bsr(const int* __restrict__ row_ptr, const int* __restrict__ c
 #pragma unroll
     for (int c = 0; c < NR; ++c)
       if (c < nrhs) yo[c] = accumulate ? add(yo[c], acc[c]) : acc[c];
+  }
+}
+
+// Pipelined block-sparse product for FP64 / complex FP64 blocks. Thread t
+// owns row t % B and the NCOL right-hand sides of column group t / B. The
+// next block (coupling matrix and its x panel) is staged with cp.async while
+// the current one is multiplied from shared memory.
+template <typename S, int NCOL>
+__global__ void k_bsr_pipe(const int* __restrict__ row_ptr, const int* __restrict__ col, const S* __restrict__ blocks,
+                           long bstride, int B, const S* __restrict__ x, S* __restrict__ y, int nrhs, int accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const long fsz = (B * B * (long)sizeof(S) + 15) / 16 * 16;  // bytes per staged block
+  const long xsz = (B * nrhs * (long)sizeof(S) + 15) / 16 * 16;
+  unsigned char* st[2] = {smem_raw, smem_raw + fsz + xsz};
+  const int row = blockIdx.x, t = threadIdx.x;
+  const int i = t % B, cg = t / B;
+  const int c0 = cg * NCOL;
+  const bool active = c0 < nrhs && cg * B + i == t;
+  S acc[NCOL];
+#pragma unroll
+  for (int c = 0; c < NCOL; ++c) acc[c] = zero<S>();
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  auto issue = [&](int k, unsigned char* dst) {
+    const unsigned char* F = reinterpret_cast<const unsigned char*>(blocks + (long)k * bstride);
+    const long fbytes = (long)B * B * sizeof(S);
+    for (long off = 16L * t; off < fbytes; off += 16L * blockDim.x) cp_async16(dst + off, F + off);
+    const S* xs = x + (long)col[k] * B * nrhs;
+    S* xd = reinterpret_cast<S*>(dst + fsz);
+    for (int e = t; e < B * nrhs; e += blockDim.x) {
+      if (sizeof(S) == 16) cp_async16(xd + e, xs + e);
+      else cp_async8(xd + e, xs + e);
+    }
+    cp_async_commit();
+  };
+  if (kb < ke) issue(kb, st[0]);
+  for (int k = kb; k < ke; ++k) {
+    const int s = (k - kb) & 1;
+    if (k + 1 < ke) {
+      issue(k + 1, st[s ^ 1]);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    if (active) {
+      const S* F = reinterpret_cast<const S*>(st[s]);
+      const S* xs = reinterpret_cast<const S*>(st[s] + fsz);
+      for (int j = 0; j < B; ++j) {
+        const S f = F[j * B + i];
+#pragma unroll
+        for (int c = 0; c < NCOL; ++c)
+          if (c0 + c < nrhs) acc[c] = fmac(acc[c], f, xs[j * nrhs + c0 + c]);
+      }
+    }
+    __syncthreads();
+  }
+  if (active) {
+    S* yo = y + ((long)row * B + i) * nrhs;
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c)
+      if (c0 + c < nrhs) yo[c0 + c] = accumulate ? add(yo[c0 + c], acc[c]) : acc[c];
   }
 }
 
@@ -151,60 +236,223 @@ __global__ void k_transfer_bwd(const typename RealOf<S>::T* __restrict__ T, int 
   }
 }
 
+// Batched small GEMM with one shared real matrix (FMM moments and transfers):
+//   C[b] (=, +=) op(A) B[b],  op(A) = A (Mo x Ki) or A^T (A stored Ki x Mo),
+// B[b]: Ki x kk row-major, C[b]: Mo x kk row-major; complex vectors are real
+// matrices with kk = 2 * nrhs. Persistent CTAs stage A in shared memory once
+// (when it fits) and loop over batch items; each thread owns an RT x CT tile.
+template <typename T, bool TA, bool ACC, bool STAGE_A, int RT, int CT>
+__global__ void __launch_bounds__(256) k_bgemm(const T* __restrict__ A, int Mo, int Ki, const T* __restrict__ B,
+                                               long bstride, T* __restrict__ C, long cstride, int nbatch, int kk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);              // [q][i] (= op(A)^T), when staged
+  T* Bs = As + (STAGE_A ? (size_t)Mo * Ki : 0);        // [q][c]
+  if (STAGE_A) {
+    for (int t = threadIdx.x; t < Mo * Ki; t += blockDim.x) {
+      const int q = t / Mo, i = t - q * Mo;
+      As[t] = TA ? A[(long)q * Mo + i] : A[(long)i * Ki + q];
+    }
+  }
+  const int rtiles = (Mo + RT - 1) / RT, ctiles = (kk + CT - 1) / CT;
+  for (int b = blockIdx.x; b < nbatch; b += gridDim.x) {
+    __syncthreads();
+    const T* Bb = B + (long)b * bstride;
+    for (int t = threadIdx.x; t < Ki * kk; t += blockDim.x) Bs[t] = Bb[t];
+    __syncthreads();
+    T* Cb = C + (long)b * cstride;
+    for (int tile = threadIdx.x; tile < rtiles * ctiles; tile += blockDim.x) {
+      const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+      T acc[RT][CT];
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[r][c] = (T)0;
+      for (int q = 0; q < Ki; ++q) {
+        T a[RT], bv[CT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) {
+          const int i = i0 + r < Mo ? i0 + r : Mo - 1;
+          a[r] = STAGE_A ? As[(long)q * Mo + i] : (TA ? __ldg(&A[(long)q * Mo + i]) : __ldg(&A[(long)i * Ki + q]));
+        }
+#pragma unroll
+        for (int c = 0; c < CT; ++c) bv[c] = Bs[q * kk + (c0 + c < kk ? c0 + c : kk - 1)];
+#pragma unroll
+        for (int r = 0; r < RT; ++r)
+#pragma unroll
+          for (int c = 0; c < CT; ++c) acc[r][c] = fmac(acc[r][c], a[r], bv[c]);
+      }
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+          if (i0 + r < Mo && c0 + c < kk) {
+            T* o = Cb + (long)(i0 + r) * kk + c0 + c;
+            *o = ACC ? *o + acc[r][c] : acc[r][c];
+          }
+    }
+  }
+}
+
+template <typename T>
+static cudaError_t bgemm(bool ta, bool acc, const T* A, int Mo, int Ki, const T* B, long bstride, T* C, long cstride,
+                         int nbatch, int kk, cudaStream_t s) {
+  if (nbatch == 0) return cudaSuccess;
+  const size_t a_bytes = (size_t)Mo * Ki * sizeof(T), b_bytes = (size_t)Ki * kk * sizeof(T);
+  const bool stage = a_bytes + b_bytes <= 200 * 1024;
+  if (!stage && b_bytes > 200 * 1024) return cudaErrorInvalidValue;
+  const size_t smem = (stage ? a_bytes : 0) + b_bytes;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = std::min(nbatch, stage ? sms : 4 * sms);
+#define BG_GEMM(TA_, AC_, ST_)                                                                             \
+  {                                                                                                        \
+    auto kf = k_bgemm<T, TA_, AC_, ST_, 3, 4>;                                                             \
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
+    if (e != cudaSuccess) return e;                                                                        \
+    kf<<<grid, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, nbatch, kk);                             \
+    return cudaGetLastError();                                                                             \
+  }
+  if (!ta && !acc && stage) BG_GEMM(false, false, true)
+  if (!ta && !acc && !stage) BG_GEMM(false, false, false)
+  if (ta && acc && stage) BG_GEMM(true, true, true)
+  if (ta && acc && !stage) BG_GEMM(true, true, false)
+#undef BG_GEMM
+  return cudaErrorInvalidValue;
+}
+
 // Fused FP32 far field: the coupling F_ij = k(x_i, y_j) |J_i| |J_j| is
-// generated from the clusters' interpolation points inside the product.
-template <bool CPLX, int NR>
-__global__ void k_far_fused(const float4* __restrict__ prow, const float4* __restrict__ pcol,
-                            const int* __restrict__ row_ptr, const int* __restrict__ col, int np2, float kre, float kim,
-                            const void* __restrict__ yv, void* __restrict__ zv, int nrhs) {
+// generated from the clusters' interpolation points inside the product, so the
+// far field is never stored. One CTA (128 threads) per block row (cluster c1).
+// Per block: the next block's points and right-hand sides are prefetched with
+// cp.async while the CTA writes the np2 x np2 coupling tile to shared memory
+// ([j][i], conflict-free) and contracts it; each thread owns ROWS rows x NC
+// right-hand sides. Block results are summed with Neumaier compensation.
+// Points are FP32 offsets from FP64 cluster centres (centre differences in
+// FP64), which keeps near-admissible distances accurate to FP32 rounding.
+template <bool CPLX, int NP2, int NC>
+__global__ void __launch_bounds__(128) k_far_fused(const float4* __restrict__ pts, const d4* __restrict__ centres,
+                                                   const int* __restrict__ row_ptr, const int* __restrict__ col,
+                                                   float kre, float kim, const void* __restrict__ yv,
+                                                   void* __restrict__ zv, int nrhs) {
   typedef typename std::conditional<CPLX, cf, float>::type S;
+  typedef typename std::conditional<CPLX, float2, float>::type FT;
+  constexpr int ROWS = (NP2 + 31) / 32;
+  constexpr int LD = 4 * NC;  // padded right-hand-side row length
   const S* y = static_cast<const S*>(yv);
   S* z = static_cast<S*>(zv);
+  __shared__ float4 prs[NP2];
+  __shared__ float4 pcs[2][NP2];
+  __shared__ __align__(16) S ys[2][NP2 * LD];
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float4* ps = reinterpret_cast<float4*>(smem_raw);
-  S* ys = reinterpret_cast<S*>(ps + np2);
-  const int row = blockIdx.x, i = threadIdx.x;
-  float4 xi = make_float4(0, 0, 0, 0);
-  if (i < np2) xi = prow[(long)row * np2 + i];
-  S acc[NR];
-#pragma unroll
-  for (int c = 0; c < NR; ++c) acc[c] = zero<S>();
-  for (int k = row_ptr[row]; k < row_ptr[row + 1]; ++k) {
+  FT* F = reinterpret_cast<FT*>(smem_raw);  // [j][i]
+  const int row = blockIdx.x;
+  const int lane = threadIdx.x & 31, cg = threadIdx.x >> 5;
+  const int c0 = cg * NC;
+  for (int t = threadIdx.x; t < NP2; t += blockDim.x) prs[t] = pts[(long)row * NP2 + t];
+  const d4 crow = centres[row];
+  const bool dense_rhs = (nrhs == LD);
+  auto issue = [&](int k, int b) {
     const int c2 = col[k];
-    __syncthreads();
-    for (int t = threadIdx.x; t < np2; t += blockDim.x) ps[t] = pcol[(long)c2 * np2 + t];
-    for (int t = threadIdx.x; t < np2 * nrhs; t += blockDim.x) ys[t] = y[(long)c2 * np2 * nrhs + t];
-    __syncthreads();
-    if (i < np2) {
-      for (int j = 0; j < np2; ++j) {
-        const float4 yj = ps[j];
-        const float d0 = xi.x - yj.x, d1 = xi.y - yj.y, d2 = xi.z - yj.z;
-        const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
-        const float inv = rsqrtf(r2);
-        const float amp = inv * 0.0795774715f * xi.w * yj.w;
-        if constexpr (CPLX) {
-          const float r = r2 * inv;
-          float sn, cs;
-          sincosf(kre * r, &sn, &cs);
-          float a = amp;
-          if (kim != 0.0f) a *= expf(kim * r);
-          const cf f = {cs * a, -sn * a};
-#pragma unroll
-          for (int c = 0; c < NR; ++c)
-            if (c < nrhs) acc[c] = fmac(acc[c], f, ys[j * nrhs + c]);
+    for (int t = threadIdx.x; t < NP2; t += blockDim.x) cp_async16(&pcs[b][t], &pts[(long)c2 * NP2 + t]);
+    const S* src = y + (long)c2 * NP2 * nrhs;
+    if (dense_rhs) {
+      constexpr int CH = (int)(NP2 * LD * sizeof(S) / 16);
+      for (int t = threadIdx.x; t < CH; t += blockDim.x)
+        cp_async16(reinterpret_cast<unsigned char*>(ys[b]) + 16 * t, reinterpret_cast<const unsigned char*>(src) + 16 * t);
+    } else {
+      for (int t = threadIdx.x; t < NP2 * LD; t += blockDim.x) {
+        const int j = t / LD, c = t - j * LD;
+        if (c < nrhs) {
+          if (sizeof(S) == 8) cp_async8(&ys[b][t], &src[j * nrhs + c]);
+          else ys[b][t] = src[j * nrhs + c];
         } else {
-#pragma unroll
-          for (int c = 0; c < NR; ++c)
-            if (c < nrhs) acc[c] = fmac(acc[c], amp, ys[j * nrhs + c]);
+          ys[b][t] = zero<S>();
         }
       }
     }
-  }
-  if (i < np2) {
-    S* zo = z + ((long)row * np2 + i) * nrhs;
+    cp_async_commit();
+  };
+  S sum[ROWS][NC], cmp[ROWS][NC];
 #pragma unroll
-    for (int c = 0; c < NR; ++c)
-      if (c < nrhs) zo[c] = acc[c];
+  for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sum[r][c] = cmp[r][c] = zero<S>();
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  if (kb < ke) issue(kb, 0);
+  for (int k = kb; k < ke; ++k) {
+    const int b = (k - kb) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // block k staged; every thread is done with F and buffer b^1
+    if (k + 1 < ke) issue(k + 1, b ^ 1);
+    const d4 ccol = centres[col[k]];
+    const float dcx = (float)(crow.x - ccol.x), dcy = (float)(crow.y - ccol.y), dcz = (float)(crow.z - ccol.z);
+    for (int e = threadIdx.x; e < NP2 * NP2; e += blockDim.x) {
+      const int j = e / NP2, i = e - j * NP2;
+      const float4 xi = prs[i], yj = pcs[b][j];
+      const float d0 = dcx + (xi.x - yj.x), d1 = dcy + (xi.y - yj.y), d2 = dcz + (xi.z - yj.z);
+      const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+      const float inv = rsqrtf(r2);
+      const float amp = inv * 0.0795774715f * xi.w * yj.w;
+      if constexpr (CPLX) {
+        const float r = r2 * inv;
+        float sn, cs;
+        sincosf(kre * r, &sn, &cs);
+        float a = amp;
+        if (kim != 0.0f) a *= expf(kim * r);
+        F[e] = make_float2(cs * a, -sn * a);
+      } else {
+        F[e] = amp;
+      }
+    }
+    __syncthreads();  // coupling tile complete
+    S acc[ROWS][NC];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[r][c] = zero<S>();
+#pragma unroll 3
+    for (int j = 0; j < NP2; ++j) {
+      S yl[NC];
+      if constexpr ((NC * sizeof(S)) % 16 == 0) {
+        const float4* src = reinterpret_cast<const float4*>(&ys[b][j * LD + c0]);
+#pragma unroll
+        for (int v = 0; v < (int)(NC * sizeof(S) / 16); ++v) {
+          const float4 q = src[v];
+          float* d = reinterpret_cast<float*>(yl) + 4 * v;
+          d[0] = q.x; d[1] = q.y; d[2] = q.z; d[3] = q.w;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) yl[c] = ys[b][j * LD + c0 + c];
+      }
+#pragma unroll
+      for (int r = 0; r < ROWS; ++r) {
+        const int i = lane + 32 * r;
+        if (i < NP2) {
+          const FT f = F[j * NP2 + i];
+#pragma unroll
+          for (int c = 0; c < NC; ++c) {
+            if constexpr (CPLX) acc[r][c] = fmac(acc[r][c], cf{f.x, f.y}, yl[c]);
+            else acc[r][c] = fmac(acc[r][c], f, yl[c]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+      for (int c = 0; c < NC; ++c) neumaier_add(sum[r][c], cmp[r][c], acc[r][c]);
+  }
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r) {
+    const int i = lane + 32 * r;
+    if (i < NP2) {
+      S* zo = z + ((long)row * NP2 + i) * nrhs;
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c0 + c < nrhs) zo[c0 + c] = add(sum[r][c], cmp[r][c]);
+    }
   }
 }
 
@@ -236,6 +484,11 @@ __global__ void k_scatter_out_cplx(const S* __restrict__ work, int rows, int nrh
   cd v = alpha * w;
   if (beta.re != 0.0 || beta.im != 0.0) v = v + beta * (*u);
   *u = v;
+}
+template <typename S64, typename S32>
+__global__ void k_add_low(const S32* __restrict__ in, long n, S64* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) out[t] = add(out[t], Conv<S32, S64>::run(in[t]));
 }
 template <typename Sin, typename Sout>
 __global__ void k_convert(const Sin* __restrict__ in, long n, Sout* __restrict__ out) {
@@ -297,6 +550,50 @@ cudaError_t launch_bsr(int S, const int* row_ptr, const int* col, const void* bl
 }
 
 template <typename S>
+static cudaError_t bsr_pipe_typed(const int* row_ptr, const int* col, const S* blocks, long bstride, int nrows, int B,
+                                  const S* x, S* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (nrows == 0) return cudaSuccess;
+  // column groups: enough threads to cover B rows x nrhs, at most 1024 threads
+  int ncol = nrhs <= 1 ? 1 : (nrhs <= 2 ? 2 : (nrhs <= 4 ? 4 : 8));
+  int groups = (nrhs + ncol - 1) / ncol;
+  while (B * groups > 1024) {
+    ncol *= 2;
+    groups = (nrhs + ncol - 1) / ncol;
+  }
+  if (ncol > 32) return cudaErrorInvalidValue;
+  const int threads = ((B * groups + 31) / 32) * 32;
+  const size_t fsz = ((size_t)B * B * sizeof(S) + 15) / 16 * 16, xsz = ((size_t)B * nrhs * sizeof(S) + 15) / 16 * 16;
+  const size_t smem = 2 * (fsz + xsz);
+  if (smem > 220 * 1024) {
+    // too large to double-buffer: single-stage kernel on contiguous blocks
+    if (bstride != (long)B * B) return cudaErrorInvalidValue;
+    return bsr_typed<S>(row_ptr, col, blocks, nrows, B, x, y, nrhs, accumulate, s);
+  }
+#define BG_PIPE(NC)                                                                                         \
+  if (ncol == NC) {                                                                                         \
+    auto kf = k_bsr_pipe<S, NC>;                                                                            \
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+    if (e != cudaSuccess) return e;                                                                         \
+    kf<<<nrows, threads, smem, s>>>(row_ptr, col, blocks, bstride, B, x, y, nrhs, accumulate);              \
+    return cudaGetLastError();                                                                              \
+  }
+  BG_PIPE(1)
+  BG_PIPE(2)
+  BG_PIPE(4)
+  BG_PIPE(8)
+  BG_PIPE(16)
+  BG_PIPE(32)
+#undef BG_PIPE
+  return cudaErrorInvalidValue;
+}
+cudaError_t launch_bsr_fp64(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (cplx)
+    return bsr_pipe_typed<cd>(row_ptr, col, (const cd*)blocks, bstride, nrows, B, (const cd*)x, (cd*)y, nrhs, accumulate, s);
+  return bsr_pipe_typed<double>(row_ptr, col, (const double*)blocks, bstride, nrows, B, (const double*)x, (double*)y,
+                                nrhs, accumulate, s);
+}
+template <typename S>
 static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void* xss, void* y, int nrhs, cudaStream_t s) {
   if (ncl == 0) return cudaSuccess;
   const size_t smem = (size_t)Bq * nrhs * sizeof(S);
@@ -308,6 +605,12 @@ static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void
 }
 cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int ncl, const void* xss, void* y, int nrhs,
                               cudaStream_t s) {
+  // Y[c] (R x k) = Mom (R x Bq) X[c] (Bq x k); complex vectors as 2k real columns
+  const int kk = (S & 1) ? 2 * nrhs : nrhs;
+  if (S < 2) return bgemm<double>(false, false, (const double*)mom, R, Bq, (const double*)xss, (long)Bq * kk, (double*)y,
+                                  (long)R * kk, ncl, kk, s);
+  return bgemm<float>(false, false, (const float*)mom, R, Bq, (const float*)xss, (long)Bq * kk, (float*)y, (long)R * kk,
+                      ncl, kk, s);
   switch (S) {
     case 0: return mom_fwd_t<double>(mom, R, Bq, ncl, xss, y, nrhs, s);
     case 1: return mom_fwd_t<cd>(mom, R, Bq, ncl, xss, y, nrhs, s);
@@ -328,6 +631,12 @@ static cudaError_t mom_bwd_t(const void* mom, int R, int Bq, int ncl, const void
 }
 cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int ncl, const void* z, void* yss, int nrhs,
                               cudaStream_t s) {
+  // Yss[c] (Bq x k) += Mom^T (Bq x R) Z[c] (R x k)
+  const int kk = (S & 1) ? 2 * nrhs : nrhs;
+  if (S < 2) return bgemm<double>(true, true, (const double*)mom, Bq, R, (const double*)z, (long)R * kk, (double*)yss,
+                                  (long)Bq * kk, ncl, kk, s);
+  return bgemm<float>(true, true, (const float*)mom, Bq, R, (const float*)z, (long)R * kk, (float*)yss, (long)Bq * kk,
+                      ncl, kk, s);
   switch (S) {
     case 0: return mom_bwd_t<double>(mom, R, Bq, ncl, z, yss, nrhs, s);
     case 1: return mom_bwd_t<cd>(mom, R, Bq, ncl, z, yss, nrhs, s);
@@ -339,6 +648,15 @@ cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int ncl, co
 cudaError_t launch_transfer_fwd(int S, const void* T, int np2, int nc, int np_, const void* yc, void* yp, int nrhs,
                                 cudaStream_t s) {
   if (np_ == 0) return cudaSuccess;
+  if (nc == 1) {
+    // parent p (np2 x k) = T (np2 x 4np2) [children 4p..4p+3 stacked] (4np2 x k)
+    const int kk = (S & 1) ? 2 * nrhs : nrhs;
+    if (S < 2)
+      return bgemm<double>(false, false, (const double*)T, np2, 4 * np2, (const double*)yc, 4L * np2 * kk, (double*)yp,
+                           (long)np2 * kk, np_, kk, s);
+    return bgemm<float>(false, false, (const float*)T, np2, 4 * np2, (const float*)yc, 4L * np2 * kk, (float*)yp,
+                        (long)np2 * kk, np_, kk, s);
+  }
   switch (S) {
     case 0: k_transfer_fwd<double><<<np_, 256, 0, s>>>((const double*)T, np2, nc, (const double*)yc, (double*)yp, nrhs); break;
     case 1: k_transfer_fwd<cd><<<np_, 256, 0, s>>>((const double*)T, np2, nc, (const cd*)yc, (cd*)yp, nrhs); break;
@@ -351,6 +669,15 @@ cudaError_t launch_transfer_fwd(int S, const void* T, int np2, int nc, int np_, 
 cudaError_t launch_transfer_bwd(int S, const void* T, int np2, int nc, int np_, const void* zp, void* zc, int nrhs,
                                 cudaStream_t s) {
   if (np_ == 0) return cudaSuccess;
+  if (nc == 1) {
+    // children 4p..4p+3 stacked (4np2 x k) += T^T (4np2 x np2) parent p (np2 x k)
+    const int kk = (S & 1) ? 2 * nrhs : nrhs;
+    if (S < 2)
+      return bgemm<double>(true, true, (const double*)T, 4 * np2, np2, (const double*)zp, (long)np2 * kk, (double*)zc,
+                           4L * np2 * kk, np_, kk, s);
+    return bgemm<float>(true, true, (const float*)T, 4 * np2, np2, (const float*)zp, (long)np2 * kk, (float*)zc,
+                        4L * np2 * kk, np_, kk, s);
+  }
   switch (S) {
     case 0: k_transfer_bwd<double><<<np_, 256, 0, s>>>((const double*)T, np2, nc, (const double*)zp, (double*)zc, nrhs); break;
     case 1: k_transfer_bwd<cd><<<np_, 256, 0, s>>>((const double*)T, np2, nc, (const cd*)zp, (cd*)zc, nrhs); break;
@@ -361,61 +688,50 @@ cudaError_t launch_transfer_bwd(int S, const void* T, int np2, int nc, int np_, 
   return cudaGetLastError();
 }
 
-template <bool CPLX>
-static cudaError_t far_fused_t(const float4* prow, const float4* pcol, const int* row_ptr, const int* col, int nrows,
-                               int np2, float kre, float kim, const void* y, void* z, int nrhs, cudaStream_t s) {
-  if (nrows == 0) return cudaSuccess;
-  const int bs = ((np2 + 31) / 32) * 32;
-  const size_t smem = np2 * sizeof(float4) + (size_t)np2 * nrhs * (CPLX ? sizeof(cf) : sizeof(float));
-#define BG_FF(NRV)                                                                                          \
+template <bool CPLX, int NP2>
+static cudaError_t far_fused_t(const float4* pts, const d4* centres, const int* row_ptr, const int* col, int nrows,
+                               float kre, float kim, const void* y, void* z, int nrhs, cudaStream_t s) {
+  const size_t smem = (size_t)NP2 * NP2 * (CPLX ? sizeof(float2) : sizeof(float));
+#define BG_FF(NCV)                                                                                          \
   {                                                                                                         \
-    auto kf = k_far_fused<CPLX, NRV>;                                                                       \
+    auto kf = k_far_fused<CPLX, NP2, NCV>;                                                                  \
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
     if (e != cudaSuccess) return e;                                                                         \
-    kf<<<nrows, bs, smem, s>>>(prow, pcol, row_ptr, col, np2, kre, kim, y, z, nrhs);                        \
+    kf<<<nrows, 128, smem, s>>>(pts, centres, row_ptr, col, kre, kim, y, z, nrhs);                          \
     return cudaGetLastError();                                                                              \
   }
-  if (nrhs <= 1) BG_FF(1)
-  if (nrhs <= 2) BG_FF(2)
-  if (nrhs <= 4) BG_FF(4)
-  if (nrhs <= 8) BG_FF(8)
-  if (nrhs <= 16) BG_FF(16)
-  if (nrhs <= 32) BG_FF(32)
+  if (nrhs <= 4) BG_FF(1)
+  if (nrhs <= 8) BG_FF(2)
+  if (nrhs <= 16) BG_FF(4)
+  if (nrhs <= 32) BG_FF(8)
 #undef BG_FF
   return cudaErrorInvalidValue;
 }
-cudaError_t launch_far_fused(bool cplx, const float4* prow, const float4* pcol, const int* row_ptr, const int* col,
-                             int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs,
-                             cudaStream_t s) {
-  return cplx ? far_fused_t<true>(prow, pcol, row_ptr, col, nrows, np2, kre, kim, y, z, nrhs, s)
-              : far_fused_t<false>(prow, pcol, row_ptr, col, nrows, np2, kre, kim, y, z, nrhs, s);
-}
-
-cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int rows, int nrhs, void* work,
-                             cudaStream_t s) {
-  const long n = (long)rows * nrhs;
-  if (n == 0) return cudaSuccess;
-  const unsigned g = blocks_for(n, 256);
-  if (Sin == 0 && Sout == 0) k_gather_in<double, double><<<g, 256, 0, s>>>((const double*)user, ld, rows, nrhs, (double*)work);
-  else if (Sin == 0 && Sout == 2) k_gather_in<double, float><<<g, 256, 0, s>>>((const double*)user, ld, rows, nrhs, (float*)work);
-  else if (Sin == 1 && Sout == 1) k_gather_in<cd, cd><<<g, 256, 0, s>>>((const cd*)user, ld, rows, nrhs, (cd*)work);
-  else if (Sin == 1 && Sout == 3) k_gather_in<cd, cf><<<g, 256, 0, s>>>((const cd*)user, ld, rows, nrhs, (cf*)work);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
-}
-cudaError_t launch_scatter_out(int Sw, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
-                               const double* beta, cudaStream_t s) {
-  const long n = (long)rows * nrhs;
-  if (n == 0) return cudaSuccess;
-  const unsigned g = blocks_for(n, 256);
-  const cd a = {alpha[0], alpha[1]}, b = {beta[0], beta[1]};
-  switch (Sw) {
-    case 0: k_scatter_out_real<double><<<g, 256, 0, s>>>((const double*)work, rows, nrhs, (double*)user, ld, alpha[0], beta[0]); break;
-    case 2: k_scatter_out_real<float><<<g, 256, 0, s>>>((const float*)work, rows, nrhs, (double*)user, ld, alpha[0], beta[0]); break;
-    case 1: k_scatter_out_cplx<cd><<<g, 256, 0, s>>>((const cd*)work, rows, nrhs, (cd*)user, ld, a, b); break;
-    case 3: k_scatter_out_cplx<cf><<<g, 256, 0, s>>>((const cf*)work, rows, nrhs, (cd*)user, ld, a, b); break;
+cudaError_t launch_far_fused(bool cplx, const float4* pts, const d4* centres, const int* row_ptr, const int* col,
+                             int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs, cudaStream_t s) {
+  if (nrows == 0) return cudaSuccess;
+#define BG_FR(N2)                                                                                    \
+  case N2:                                                                                           \
+    return cplx ? far_fused_t<true, N2>(pts, centres, row_ptr, col, nrows, kre, kim, y, z, nrhs, s)  \
+                : far_fused_t<false, N2>(pts, centres, row_ptr, col, nrows, kre, kim, y, z, nrhs, s);
+  switch (np2) {
+    BG_FR(16)
+    BG_FR(25)
+    BG_FR(36)
+    BG_FR(49)
+    BG_FR(64)
+    BG_FR(81)
+    BG_FR(100)
+    BG_FR(121)
     default: return cudaErrorInvalidValue;
   }
+#undef BG_FR
+}
+cudaError_t launch_add_low(bool cplx, const void* in32, long n, void* out64, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(n, 256);
+  if (cplx) k_add_low<cd, cf><<<g, 256, 0, s>>>((const cf*)in32, n, (cd*)out64);
+  else k_add_low<double, float><<<g, 256, 0, s>>>((const float*)in32, n, (double*)out64);
   return cudaGetLastError();
 }
 cudaError_t launch_convert(int Sin, int Sout, const void* in, long n, void* out, cudaStream_t s) {

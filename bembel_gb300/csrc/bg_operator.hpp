@@ -59,12 +59,50 @@ struct DevBuf {
 
 struct bg_context {
   int device = -1;  // -1: host-only context (setup and inspection, no device work)
+  int children = 0;      // live geometries and operators
+  bool closing = false;  // bg_context_destroy was called; free with the last child
   cudaStream_t stream = nullptr;
   std::string err;
   DevBuf stage_in, stage_out;   // device staging of host operands
   void* pinned = nullptr;       // pinned host staging
   size_t pinned_bytes = 0;
+  // kernel-class timing with CUDA events on `stream` (bg_profile)
+  bool profiling = false;
+  long launches = 0;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[8];
+  double class_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long class_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t get_event() {
+    if (event_pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = event_pool.back();
+    event_pool.pop_back();
+    return e;
+  }
 };
+
+// kernel classes reported by bg_profile_read
+enum { KC_NEAR = 0, KC_FAR64 = 1, KC_FAR_FUSED = 2, KC_TRANSFORM = 3, KC_TAPPLY = 4, KC_KRYLOV = 5, KC_OTHER = 6,
+       KC_ASSEMBLY = 7 };
+
+// launch f() on ctx->stream, counting it and, when profiling, bracketing it
+// with events of class cls
+template <typename F>
+cudaError_t timed_launch(bg_context* ctx, int cls, F&& f) {
+  ++ctx->launches;
+  ++ctx->class_launches[cls];
+  if (!ctx->profiling) return f();
+  cudaEvent_t a = ctx->get_event(), b = ctx->get_event();
+  cudaEventRecord(a, ctx->stream);
+  cudaError_t e = f();
+  cudaEventRecord(b, ctx->stream);
+  ctx->pending[cls].push_back({a, b});
+  return e;
+}
 
 struct bg_geometry {
   bg::Geometry g;
@@ -106,27 +144,35 @@ struct bg_operator {
   DevBuf d_patch_meta, d_patch_cp, d_el_patch, d_el_llc;
   DevBuf d_T_ptr, d_T_idx, d_T_val, d_Tt_ptr, d_Tt_idx, d_Tt_val;
   DevBuf d_cheb;
-  std::vector<DevBuf*> d_pts64, d_pts32;  // per level
-  DevBuf d_dense64, d_dense32;            // dense blocks
+  std::vector<DevBuf*> d_pts64, d_pts32, d_centres;  // per level
+  DevBuf d_dense64;                       // dense blocks (FP64)
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
   // work vectors (sized for the largest nrhs seen)
   int cap = 0;
-  DevBuf w_xdof, w_xss, w_yss, w_ydof;
+  DevBuf w_xdof, w_xss, w_yss, w_ydof, w_xss32, w_yss32;
   std::vector<DevBuf*> w_y, w_z;  // per level
 
   ~bg_operator() {
-    for (auto v : {&d_pts64, &d_pts32, &d_far64, &d_mom64, &d_mom32, &w_y, &w_z})
+    for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_far64, &d_mom64, &d_mom32, &w_y, &w_z})
       for (auto b : *v) delete b;
   }
   size_t scalar_bytes(bool fp32) const { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }
+  // scalars between consecutive stored FP64 blocks of size B x B: rounded up
+  // so that every block starts on a 16-byte boundary
+  long block_stride(int B) const { return cplx ? (long)B * B : ((long)B * B + 1) / 2 * 2; }
   int stype(bool fp32) const { return (fp32 ? 2 : 0) + (cplx ? 1 : 0); }
   int nclusters(int level) const { return level < 0 ? 1 : mesh.npatch << (2 * level); }
 };
 
 bg_status set_error(bg_context* ctx, bg_status st, const std::string& msg);
+// child bookkeeping: a context is released only after its last child
+void context_retain(bg_context* ctx);
+void context_release(bg_context* ctx);
 bg_status cuda_status(bg_context* ctx, cudaError_t e, const char* what);
 bg_status ensure_work(bg_operator* op, int nrhs);
-// y_dof (row-major work, FP64 or FP32 per precision) = A x_dof
-bg_status apply_operator(bg_operator* op, int nrhs, bool fp32, const void* xdof, void* ydof);
+// y_dof = A x_dof on row-major FP64 work vectors. mixed = false: the FP64
+// H2 matrix (stored far field); mixed = true: FP64 near field plus the FP32
+// fused far field (forward/backward transforms in FP32).
+bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof, void* ydof);

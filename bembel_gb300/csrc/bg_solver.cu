@@ -1,10 +1,12 @@
 // Krylov solve, load vectors and potential evaluation on GB300.
 //
 // bg_solve: restarted GMRES (Saad & Schultz 1986) batched over right-hand
-// sides with classical Gram-Schmidt applied twice, FP64 Krylov basis, wrapped
-// in iterative refinement: every refinement step evaluates the FP64 residual
-// b - A x with the FP64 operator and solves for the correction with the inner
-// operator (FP64, or the FP32 fused far field). Replaces the Eigen solvers
+// sides with classical Gram-Schmidt applied twice and an FP64 Krylov basis.
+// FP64 path: GMRES on the FP64 H2 matrix. Mixed path: flexible GMRES (Saad
+// 1993) on the FP64 operator whose right preconditioner is an inner GMRES solve
+// with the mixed operator (FP64 near field, FP32 far field): every outer step
+// is one FP64 residual-consistent product, the inner steps are cheap, and the
+// outer Krylov space recovers the FP64 solution. Replaces the Eigen solvers
 // used at examples/LaplaceSingleLayerH2.cpp:78-81 and
 // examples/HelmholtzSingleLayerH2.cpp:82-85.
 #include <algorithm>
@@ -59,6 +61,19 @@ __global__ void k_vupdate(const S* __restrict__ V, long vstride, int nv, const S
   for (int i = 0; i < nv; ++i) acc = sub(acc, V[(long)i * vstride + t] * h[(long)i * k + c]);
   w[t] = acc;
 }
+// inv[c] = 1 / sqrt(|d[c]|) (0 when d[c] == 0), from a Gram column of w with itself
+template <typename S>
+__global__ void k_inv_norm(const S* __restrict__ d, int k, double* __restrict__ inv);
+template <>
+__global__ void k_inv_norm<double>(const double* __restrict__ d, int k, double* __restrict__ inv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < k) inv[c] = d[c] > 0 ? 1.0 / sqrt(d[c]) : 0.0;
+}
+template <>
+__global__ void k_inv_norm<cd>(const cd* __restrict__ d, int k, double* __restrict__ inv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < k) inv[c] = d[c].re > 0 ? 1.0 / sqrt(d[c].re) : 0.0;
+}
 // V_next[n][c] = w[n][c] * inv[c]
 template <typename S>
 __global__ void k_vscale(const S* __restrict__ w, const double* __restrict__ inv, int N, int k, S* __restrict__ out) {
@@ -99,23 +114,24 @@ namespace {
 struct Krylov {
   bg_operator* op;
   int N, k, m;
-  bool cplx;
-  size_t sb;  // FP64 scalar bytes
-  DevBuf V, w, hdev, tmp32a, tmp32b, inv, ydev;
+  bool flexible;          // store the preconditioned directions Z
+  DevBuf V, Z, w, hdev, inv, ydev;
+  bg_status init(bg_operator* o, int kk, int mm, bool flex, size_t sb) {
+    op = o;
+    N = o->N;
+    k = kk;
+    m = mm;
+    flexible = flex;
+    const long nk = (long)N * k;
+    cudaError_t e = V.alloc((size_t)(m + 1) * nk * sb);
+    if (e == cudaSuccess && flex) e = Z.alloc((size_t)m * nk * sb);
+    if (e == cudaSuccess) e = w.alloc(nk * sb);
+    if (e == cudaSuccess) e = hdev.alloc((size_t)3 * (m + 1) * k * sb);
+    if (e == cudaSuccess) e = inv.alloc(k * sizeof(double));
+    if (e == cudaSuccess) e = ydev.alloc((size_t)(m + 1) * k * sb);
+    return cuda_status(o->ctx, e, "solver workspace");
+  }
 };
-
-// w = A v with the requested precision (FP64 work vectors in and out)
-bg_status apply_prec(Krylov& K, bool fp32, const void* v, void* w) {
-  bg_operator* op = K.op;
-  cudaStream_t s = op->ctx->stream;
-  if (!fp32) return apply_operator(op, K.k, false, v, w);
-  const long n = (long)K.N * K.k;
-  const int S64 = op->stype(false), S32 = op->stype(true);
-  bg_status st = cuda_status(op->ctx, launch_convert(S64, S32, v, n, K.tmp32a.p, s), "convert");
-  if (st != BG_OK) return st;
-  if ((st = apply_operator(op, K.k, true, K.tmp32a.p, K.tmp32b.p)) != BG_OK) return st;
-  return cuda_status(op->ctx, launch_convert(S32, S64, K.tmp32b.p, n, w, s), "convert");
-}
 
 template <typename S>
 using HostS = typename std::conditional<std::is_same<S, double>::value, double, std::complex<double>>::type;
@@ -126,7 +142,10 @@ inline std::complex<double> cj(std::complex<double> v) { return std::conj(v); }
 template <typename S>
 bg_status col_norms(Krylov& K, const void* x, std::vector<double>* out) {
   cudaStream_t s = K.op->ctx->stream;
-  k_mdot<S><<<1, 256, 0, s>>>(static_cast<const S*>(x), 0, static_cast<const S*>(x), K.N, K.k, K.hdev.as<S>());
+  timed_launch(K.op->ctx, KC_KRYLOV, [&] {
+    k_mdot<S><<<1, 256, 0, s>>>(static_cast<const S*>(x), 0, static_cast<const S*>(x), K.N, K.k, K.hdev.as<S>());
+    return cudaGetLastError();
+  });
   std::vector<HostS<S>> h(K.k);
   cudaError_t e = cudaMemcpyAsync(h.data(), K.hdev.p, K.k * sizeof(S), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -136,94 +155,141 @@ bg_status col_norms(Krylov& K, const void* x, std::vector<double>* out) {
   return BG_OK;
 }
 
-// GMRES on A (precision fp32 or fp64) for the row-major FP64 rhs r (N x k):
-// solves A d = r to relative tolerance tol per column; d accumulates.
+struct Counters {
+  int fp64_mv = 0, mixed_mv = 0, inner_it = 0, outer_it = 0;
+};
+
+// Right-preconditioned restarted (F)GMRES for A x = b on row-major FP64 work
+// vectors, x updated in place from its current value. A is the FP64 operator
+// (mixed = false) or the mixed one. With a preconditioner (inner != nullptr)
+// z_j = M^-1 v_j is an inner GMRES solve on the mixed operator and the
+// directions z_j are kept (flexible GMRES); otherwise z_j = v_j. Stops when
+// every column's residual estimate is below tol * ||b_c||.
 template <typename S>
-bg_status gmres_cycles(Krylov& K, bool fp32, const void* r, void* d, double tol, int max_iter, int* iters,
-                       int* matvecs) {
+bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inner_max, const void* b, void* x,
+                 double tol, int max_iter, Counters* cnt, std::vector<double>* relres) {
   typedef HostS<S> H;
   bg_operator* op = K.op;
   cudaStream_t s = op->ctx->stream;
   const int N = K.N, k = K.k, m = K.m;
-  const long nk = (long)N * k;
-  const long vstride = nk;
-  std::vector<double> rn;
-  bg_status st = col_norms<S>(K, r, &rn);
+  const long nk = (long)N * k, vstride = nk;
+  std::vector<double> bn;
+  bg_status st = col_norms<S>(K, b, &bn);
   if (st != BG_OK) return st;
-  // residual vector of the correction system: rc = r - A d (d starts at 0)
-  DevBuf rc;
-  cudaError_t e = rc.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = cudaMemcpyAsync(rc.p, r, nk * sizeof(S), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, nk * sizeof(S), s);
-  if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres setup");
-  int it = 0;
+  DevBuf r;
+  cudaError_t e = r.alloc(nk * sizeof(S));
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
   std::vector<H> Hm((size_t)(m + 1) * m * k), g((size_t)(m + 1) * k), cs((size_t)m * k), sn((size_t)m * k);
   std::vector<H> hcol((size_t)(m + 1) * k);
-  std::vector<double> inv(k);
-  while (it < max_iter) {
-    std::vector<double> beta;
-    if ((st = col_norms<S>(K, rc.p, &beta)) != BG_OK) return st;
+  std::vector<double> inv(k), beta;
+  int it = 0;
+  while (true) {
+    // true residual r = b - A x
+    if ((st = apply_operator(op, k, mixed, x, r.p)) != BG_OK) return st;
+    ++(mixed ? cnt->mixed_mv : cnt->fp64_mv);
+    timed_launch(op->ctx, KC_KRYLOV, [&] {
+      k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(b), nk, r.as<S>());
+      return cudaGetLastError();
+    });
+    if ((st = col_norms<S>(K, r.p, &beta)) != BG_OK) return st;
     bool done = true;
     for (int c = 0; c < k; ++c)
-      if (beta[c] > tol * rn[c] && rn[c] > 0) done = false;
-    if (done) break;
+      if (beta[c] > tol * bn[c] && bn[c] > 0) done = false;
+    if (relres) {
+      relres->resize(k);
+      for (int c = 0; c < k; ++c) (*relres)[c] = bn[c] > 0 ? beta[c] / bn[c] : 0.0;
+    }
+    if (done || it >= max_iter) break;
     for (int c = 0; c < k; ++c) inv[c] = beta[c] > 0 ? 1.0 / beta[c] : 0.0;
     e = cudaMemcpyAsync(K.inv.p, inv.data(), k * sizeof(double), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
-    k_vscale<S><<<nblk(nk), 256, 0, s>>>(rc.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>());
+    timed_launch(op->ctx, KC_KRYLOV, [&] {
+      k_vscale<S><<<nblk(nk), 256, 0, s>>>(r.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>());
+      return cudaGetLastError();
+    });
     std::fill(Hm.begin(), Hm.end(), H(0));
     std::fill(g.begin(), g.end(), H(0));
     for (int c = 0; c < k; ++c) g[c] = beta[c];
-    std::vector<char> active(k, 1);
     int j = 0;
     for (; j < m && it < max_iter; ++j, ++it) {
       S* vj = K.V.as<S>() + (long)j * vstride;
-      if ((st = apply_prec(K, fp32, vj, K.w.p)) != BG_OK) return st;
-      ++*matvecs;
-      // CGS2: two Gram-Schmidt passes
-      std::fill(hcol.begin(), hcol.end(), H(0));
-      for (int pass = 0; pass < 2; ++pass) {
-        k_mdot<S><<<j + 1, 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, K.hdev.as<S>());
-        k_vupdate<S><<<nblk(nk), 256, 0, s>>>(K.V.as<S>(), vstride, j + 1, K.hdev.as<S>(), N, k, K.w.as<S>());
-        std::vector<H> hp((size_t)(j + 1) * k);
-        e = cudaMemcpyAsync(hp.data(), K.hdev.p, hp.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres orthogonalisation");
-        for (size_t q = 0; q < hp.size(); ++q) hcol[q] += hp[q];
+      const S* zj = vj;
+      if (inner) {
+        S* zdst = K.Z.as<S>() + (long)j * vstride;
+        e = cudaMemsetAsync(zdst, 0, nk * sizeof(S), s);
+        if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
+        Counters ic;
+        if ((st = fgmres<S>(*inner, true, nullptr, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr)) != BG_OK)
+          return st;
+        cnt->mixed_mv += ic.mixed_mv;
+        cnt->inner_it += ic.outer_it;
+        zj = zdst;
       }
-      std::vector<double> hn;
-      if ((st = col_norms<S>(K, K.w.p, &hn)) != BG_OK) return st;
-      for (int c = 0; c < k; ++c) inv[c] = hn[c] > 0 ? 1.0 / hn[c] : 0.0;
-      e = cudaMemcpyAsync(K.inv.p, inv.data(), k * sizeof(double), cudaMemcpyHostToDevice, s);
-      if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
-      k_vscale<S><<<nblk(nk), 256, 0, s>>>(K.w.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>() + (long)(j + 1) * vstride);
+      if ((st = apply_operator(op, k, mixed, zj, K.w.p)) != BG_OK) return st;
+      ++(mixed ? cnt->mixed_mv : cnt->fp64_mv);
+      // classical Gram-Schmidt, two passes, and the norm, all on the device;
+      // one copy brings the Hessenberg column back
+      S* h1 = K.hdev.as<S>();
+      S* h2 = h1 + (size_t)(m + 1) * k;
+      S* h3 = h2 + (size_t)(m + 1) * k;
+      for (int pass = 0; pass < 2; ++pass) {
+        S* hp = pass == 0 ? h1 : h2;
+        timed_launch(op->ctx, KC_KRYLOV, [&] {
+          k_mdot<S><<<j + 1, 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, hp);
+          return cudaGetLastError();
+        });
+        timed_launch(op->ctx, KC_KRYLOV, [&] {
+          k_vupdate<S><<<nblk(nk), 256, 0, s>>>(K.V.as<S>(), vstride, j + 1, hp, N, k, K.w.as<S>());
+          return cudaGetLastError();
+        });
+      }
+      timed_launch(op->ctx, KC_KRYLOV, [&] {
+        k_mdot<S><<<1, 256, 0, s>>>(K.w.as<S>(), 0, K.w.as<S>(), N, k, h3);
+        return cudaGetLastError();
+      });
+      timed_launch(op->ctx, KC_KRYLOV, [&] {
+        k_inv_norm<S><<<1, 64, 0, s>>>(h3, k, K.inv.as<double>());
+        return cudaGetLastError();
+      });
+      timed_launch(op->ctx, KC_KRYLOV, [&] {
+        k_vscale<S><<<nblk(nk), 256, 0, s>>>(K.w.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>() + (long)(j + 1) * vstride);
+        return cudaGetLastError();
+      });
+      std::vector<H> hp1((size_t)(j + 1) * k), hp2((size_t)(j + 1) * k), hp3(k);
+      e = cudaMemcpyAsync(hp1.data(), h1, hp1.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(hp2.data(), h2, hp2.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(hp3.data(), h3, hp3.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres orthogonalisation");
+      for (size_t q = 0; q < hp1.size(); ++q) hcol[q] = hp1[q] + hp2[q];
+      std::vector<double> hn(k);
+      for (int c = 0; c < k; ++c) hn[c] = std::sqrt(std::abs(hp3[c]));
       bool all_done = true;
       for (int c = 0; c < k; ++c) {
         H* hc = &Hm[(size_t)c * (m + 1) * m];
         for (int i = 0; i <= j; ++i) hc[(size_t)j * (m + 1) + i] = hcol[(size_t)i * k + c];
         hc[(size_t)j * (m + 1) + j + 1] = hn[c];
-        // apply the previous Givens rotations to the new column
-        for (int i = 0; i < j; ++i) {
-          H a = hc[(size_t)j * (m + 1) + i], b = hc[(size_t)j * (m + 1) + i + 1];
+        for (int i = 0; i < j; ++i) {  // previous Givens rotations
+          H a = hc[(size_t)j * (m + 1) + i], bb = hc[(size_t)j * (m + 1) + i + 1];
           H cc = cs[(size_t)c * m + i], ss = sn[(size_t)c * m + i];
-          hc[(size_t)j * (m + 1) + i] = cc * a + ss * b;
-          hc[(size_t)j * (m + 1) + i + 1] = -cj(ss) * a + cc * b;
+          hc[(size_t)j * (m + 1) + i] = cc * a + ss * bb;
+          hc[(size_t)j * (m + 1) + i + 1] = -cj(ss) * a + cc * bb;
         }
         H a = hc[(size_t)j * (m + 1) + j];
-        double bb = hn[c], aa = std::abs(a);
-        double den = std::sqrt(aa * aa + bb * bb);
+        double hb = hn[c], aa = std::abs(a);
+        double den = std::sqrt(aa * aa + hb * hb);
         H cc, ss;
         if (den == 0) { cc = 1; ss = 0; }
         else if (aa == 0) { cc = 0; ss = 1; }
-        else { cc = aa / den; ss = (a / aa) * (bb / den); }
+        else { cc = aa / den; ss = (a / aa) * (hb / den); }
         cs[(size_t)c * m + j] = cc;
         sn[(size_t)c * m + j] = ss;
-        hc[(size_t)j * (m + 1) + j] = cc * a + ss * bb;
+        hc[(size_t)j * (m + 1) + j] = cc * a + ss * hb;
         hc[(size_t)j * (m + 1) + j + 1] = 0;
         H gj = g[(size_t)j * k + c];
         g[(size_t)(j + 1) * k + c] = -cj(ss) * gj;
         g[(size_t)j * k + c] = cc * gj;
-        if (std::abs(g[(size_t)(j + 1) * k + c]) > tol * rn[c] && hn[c] > 0) all_done = false;
+        if (std::abs(g[(size_t)(j + 1) * k + c]) > tol * bn[c] && hn[c] > 0) all_done = false;
       }
       if (all_done) {
         ++j;
@@ -231,7 +297,7 @@ bg_status gmres_cycles(Krylov& K, bool fp32, const void* r, void* d, double tol,
         break;
       }
     }
-    // y = R^-1 g per column, d += V y
+    // y = R^-1 g per column; x += [V or Z] y
     std::vector<H> y((size_t)j * k, H(0));
     for (int c = 0; c < k; ++c) {
       const H* hc = &Hm[(size_t)c * (m + 1) * m];
@@ -244,13 +310,13 @@ bg_status gmres_cycles(Krylov& K, bool fp32, const void* r, void* d, double tol,
     }
     e = cudaMemcpyAsync(K.ydev.p, y.data(), y.size() * sizeof(S), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres update");
-    k_xupdate<S><<<nblk(nk), 256, 0, s>>>(K.V.as<S>(), vstride, j, K.ydev.as<S>(), N, k, static_cast<S*>(d));
-    // true residual of the correction system for the restart
-    if ((st = apply_prec(K, fp32, d, rc.p)) != BG_OK) return st;
-    ++*matvecs;
-    k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(r), nk, rc.as<S>());
+    timed_launch(op->ctx, KC_KRYLOV, [&] {
+      k_xupdate<S><<<nblk(nk), 256, 0, s>>>(inner ? K.Z.as<S>() : K.V.as<S>(), vstride, j, K.ydev.as<S>(), N, k,
+                                          static_cast<S*>(x));
+      return cudaGetLastError();
+    });
   }
-  *iters += it;
+  cnt->outer_it += it;
   return BG_OK;
 }
 
@@ -258,67 +324,37 @@ template <typename S>
 bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, const bg_solve_params& prm,
                       bg_solve_stats* stats) {
   cudaStream_t s = op->ctx->stream;
-  Krylov K;
-  K.op = op;
-  K.N = op->N;
-  K.k = k;
-  K.m = std::max(2, prm.restart);
-  K.cplx = op->cplx;
-  K.sb = sizeof(S);
-  const long nk = (long)K.N * k;
-  cudaError_t e = K.V.alloc((size_t)(K.m + 1) * nk * sizeof(S));
-  if (e == cudaSuccess) e = K.w.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = K.hdev.alloc((size_t)(K.m + 1) * k * sizeof(S));
-  if (e == cudaSuccess) e = K.tmp32a.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = K.tmp32b.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = K.inv.alloc(k * sizeof(double));
-  if (e == cudaSuccess) e = K.ydev.alloc((size_t)(K.m + 1) * k * sizeof(S));
-  DevBuf r, d;
-  if (e == cudaSuccess) e = r.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = d.alloc(nk * sizeof(S));
-  if (e == cudaSuccess) e = cudaMemsetAsync(xdof, 0, nk * sizeof(S), s);
-  if (e != cudaSuccess) return cuda_status(op->ctx, e, "solver workspace");
-  std::vector<double> bn;
-  bg_status st = col_norms<S>(K, bdof, &bn);
-  if (st != BG_OK) return st;
-  const bool inner32 = prm.inner_precision == BG_PREC_FP32;
-  bg_solve_stats loc{0, 0, 0, 0, 0.0};
-  int fp64_mv = 0, low_mv = 0;
-  double worst = 0;
-  for (int ref = 0; ref <= prm.max_refinements; ++ref) {
-    // FP64 residual r = b - A x
-    if (ref == 0) {
-      e = cudaMemcpyAsync(r.p, bdof, nk * sizeof(S), cudaMemcpyDeviceToDevice, s);
-      if (e != cudaSuccess) return cuda_status(op->ctx, e, "residual");
-    } else {
-      if ((st = apply_operator(op, k, false, xdof, r.p)) != BG_OK) return st;
-      ++fp64_mv;
-      k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(bdof), nk, r.as<S>());
-    }
-    std::vector<double> rn;
-    if ((st = col_norms<S>(K, r.p, &rn)) != BG_OK) return st;
-    worst = 0;
-    for (int c = 0; c < k; ++c) worst = std::max(worst, bn[c] > 0 ? rn[c] / bn[c] : 0.0);
-    loc.refinements = ref;
-    if (worst <= prm.tol) break;
-    if (ref == prm.max_refinements || loc.iterations >= prm.max_iter) break;
-    // inner tolerance relative to the current residual, but never asking for
-    // more than the target on the full system
-    double itol = inner32 ? prm.inner_tol : prm.tol;
-    double need = 0;
-    for (int c = 0; c < k; ++c) need = std::max(need, rn[c] > 0 ? prm.tol * bn[c] / rn[c] : 0.0);
-    itol = std::max(itol, 0.5 * need);
-    int mv = 0;
-    if ((st = gmres_cycles<S>(K, inner32, r.p, d.p, itol, prm.max_iter - loc.iterations, &loc.iterations, &mv)) != BG_OK)
-      return st;
-    (inner32 ? low_mv : fp64_mv) += mv;
-    k_axpy<S><<<nblk(nk), 256, 0, s>>>(static_cast<S*>(xdof), d.as<S>(), nk);
+  const long nk = (long)op->N * k;
+  cudaError_t e = cudaMemsetAsync(xdof, 0, nk * sizeof(S), s);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve");
+  const bool mixed = prm.inner_precision == BG_PREC_MIXED;
+  Counters cnt;
+  std::vector<double> relres;
+  bg_status st;
+  if (!mixed) {
+    Krylov K;
+    if ((st = K.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
+    st = fgmres<S>(K, false, nullptr, 0, 0, bdof, xdof, prm.tol, prm.max_iter, &cnt, &relres);
+    cnt.inner_it = cnt.outer_it;
+  } else {
+    // outer FP64 flexible GMRES; each direction is an inner mixed GMRES solve
+    Krylov outer, inner;
+    const int mo = std::max(2, prm.max_refinements);
+    if ((st = outer.init(op, k, mo, true, sizeof(S))) != BG_OK) return st;
+    if ((st = inner.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
+    st = fgmres<S>(outer, false, &inner, prm.inner_tol, prm.max_iter, bdof, xdof, prm.tol, mo, &cnt, &relres);
   }
+  if (st != BG_OK) return st;
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve");
+  double worst = 0;
+  for (double r : relres) worst = std::max(worst, r);
+  bg_solve_stats loc;
+  loc.iterations = cnt.inner_it;
+  loc.refinements = mixed ? cnt.outer_it : 0;
+  loc.fp64_matvecs = cnt.fp64_mv;
+  loc.low_matvecs = cnt.mixed_mv;
   loc.final_relres = worst;
-  loc.fp64_matvecs = fp64_mv;
-  loc.low_matvecs = low_mv;
   if (stats) *stats = loc;
   return worst <= prm.tol ? BG_OK : set_error(op->ctx, BG_NOT_CONVERGED, "solver did not reach the tolerance");
 }

@@ -1,0 +1,362 @@
+"""Benchmark: batched H2 single-layer solves on one GB300.
+
+Workload (one "step"): the Laplace single-layer Galerkin system on the
+6-patch NURBS sphere (sphere.dat), refinement M = 5 (6144 elements), B-spline
+degree P = 2 (6936 DOFs), interpolation n_p = 9, eta = 1.6, with 32 right-hand
+sides from seeded point sources |x0| ~ U[1.5, 3] (uniform directions): one
+batched solve of all 32 systems to rel. residual 1e-8. The operator is
+assembled once before the timed region (as DiscreteOperator::compute in the
+reference) and reused by every solve.
+
+value:  solves/s = right-hand sides solved to 1e-8 per second, mixed path
+        (FP64 flexible GMRES over the FP64 H2 matrix, inner GMRES with the FP64
+        near field and the FP32 on-the-fly far field), operands in HBM.
+e2e:    the same through the public C ABI with host (pinned) buffers, the
+        host->device copy of b and device->host copy of x inside each step.
+Also reported: the plain FP64 GPU solve, H2 matvec/s (FP64 and mixed),
+p50/p99 step latency, assembly time, accuracy vs FP64 and vs the analytic
+point-source potential, the roofline of the dominant kernel and the CPU
+baseline (the CPU oracle, which restates the reference algorithm).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+GEO = os.path.join(ROOT, "tests", "golden", "geo", "sphere.dat")
+M, P, NP, NRHS = 5, 2, 9, 32
+TOL = 1e-8
+METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed precision)"
+# FP64 GMRES iterations of this workload (restart 200), used by the CPU model
+FP64_ITERS_C2 = 253
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "laplace_sl_h2_sphere_M5_P2_np9_32rhs", "geometry": "sphere.dat (6 NURBS patches)",
+           "elements": 6144, "dofs": 6936, "refinement": M, "degree": P, "n_p": NP, "eta": 1.6, "nrhs": NRHS,
+           "tol": TOL, "rhs": "point sources |x0|~U[1.5,3], seed 3",
+           "l2": "flush: 256 MiB buffer written between timed steps; operator data (near field 175 MB) > L2",
+           "solver": "FGMRES(FP64 H2) + inner GMRES(mixed: FP64 near, FP32 fused far)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def rhs_points():
+    rng = np.random.default_rng(3)
+    d = rng.normal(size=(NRHS, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rho = rng.uniform(1.5, 3.0, (NRHS, 1))
+    return d * rho
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) == 6:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(threads=None):
+    """Time the CPU oracle's H2 product on a bounded sample of the workload.
+
+    The oracle (a restatement of the reference's OpenMP algorithm) assembles
+    every 40th leaf of the c2 block partition; its product is timed with one
+    right-hand side (the reference applies right-hand sides one at a time,
+    H2DenseProduct.hpp:50) and the leaf-loop time is scaled by
+    total/sampled matrix entries. A solve costs FP64_ITERS_C2 products of
+    NRHS right-hand sides."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    t0 = time.time()
+    p = oracle.Problem(GEO, M, P, oracle.LAPLACE, np_=NP, leaf_stride=40)
+    t_asm = time.time() - t0
+    x = np.random.default_rng(0).uniform(-1, 1, p.N)
+    p.matvec(x)
+    reps = []
+    t1 = time.time()
+    while len(reps) < 20 and time.time() - t1 < 20:
+        p.matvec(x)
+        reps.append(p.last_product_split())
+    r = np.median(np.array(reps), axis=0)
+    t_full = r[1] + r[0] * r[3] / r[2]
+    solve_s = FP64_ITERS_C2 * NRHS * t_full
+    return {"value": NRHS / solve_s, "unit": "solves/s", "cores": oracle.threads(), "kind": "port",
+            "sample": ("CPU oracle (restates the reference OpenMP H2 path): every 40th leaf assembled (%.1f s), "
+                       "1-RHS product timed x%d (median leaf loop %.2f ms on %.1f%% of entries, transforms %.2f ms), "
+                       "full product extrapolated to %.1f ms; solve = %d FP64 GMRES iterations x %d RHS products"
+                       % (t_asm, len(reps), r[0] * 1e3, 100 * r[2] / r[3], r[1] * 1e3, t_full * 1e3,
+                          FP64_ITERS_C2, NRHS)),
+            "matvec_per_s_1rhs": 1.0 / t_full}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    t0 = time.time()
+    base = cpu_sample()
+    line = {"metric": METRIC, "value": base["value"], "unit": "solves/s", "n_gpus": args.gpus, "steps": 1,
+            "warmup": 0, "ms_per_step": 1e3 * NRHS / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded point sources on sphere.dat)",
+            "impl": "reference", "config": workload_config({"parallelism": "cpu openmp"}),
+            "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": base["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference needs Eigen, absent here and on the GPU box; the CPU oracle port stands in",
+            "wall_s": time.time() - t0}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import bembel_gb300 as bg
+    from bembel_gb300 import _lib
+    L = _lib.load()
+    ctx = bg.Context(local)
+    sp = ctypes_void_p()
+    L.bg_context_get_stream(ctx.h, ctypes_byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
+
+    t0 = time.time()
+    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), M, P), bg.LaplaceSingleLayerOperator(), n_p=NP)
+    op.compute()
+    asm = op.assembly_times()
+    asm["wall_s"] = time.time() - t0
+    A = op.get_discrete_operator()
+    N = op.N
+    x0 = rhs_points()
+    b_host = op.load_vector(0, x0)                      # (N, 32) float64, Fortran order
+    b_dev = torch.from_numpy(np.ascontiguousarray(b_host.T)).cuda()  # (32, N) = column-major N x 32
+    b_dev_t = b_dev.t()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def solve(inner, b):
+        return A.solve(b, tol=TOL, inner=inner, inner_tol=1e-2, restart=200, max_refinements=12)
+
+    # FP64 GPU path (reference solution for the accuracy report), outside the timed region
+    x64, st64 = solve("fp64", b_dev_t)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def timed_steps(inner, b, steps, warmup, profile=False):
+        for _ in range(warmup):
+            solve(inner, b)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        times, stats = [], None
+        if profile:
+            L.bg_profile_enable(ctx.h, 1)
+            _read_profile(L, ctx)  # reset counters
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            x, stats = solve(inner, b)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        prof = _read_profile(L, ctx) if profile else None
+        if profile:
+            L.bg_profile_enable(ctx.h, 0)
+        if dist:
+            dist.barrier()
+        return np.array(times), x, stats, prof
+
+    clocks = ClockSampler(local)
+    with clocks:
+        t_mixed, xm, stm, prof = timed_steps("mixed", b_dev_t, args.steps, args.warmup, profile=True)
+    t_fp64, _, _, _ = timed_steps("fp64", b_dev_t, max(1, min(2, args.steps)), 1)
+    # end to end: host pinned b, host x, copies inside the step
+    b_pin = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
+    t_e2e, xe, _, _ = timed_steps("mixed", b_pin.t(), args.steps, 1)
+
+    # matvec throughput (32 RHS per product)
+    def mv_rate(prec, reps=5):
+        x = torch.randn(N, NRHS, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            A.matvec(x, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(reps):
+            A.matvec(x, precision=prec)
+        e1.record(stream)
+        e1.synchronize()
+        return reps / (e0.elapsed_time(e1) * 1e-3)
+    mv64, mvmx = mv_rate("fp64"), mv_rate("mixed")
+
+    total_ms = float(t_mixed.sum())
+    if dist:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = world * NRHS * args.steps / (total_ms * 1e-3)
+    fp64_value = NRHS / (float(np.mean(t_fp64)) * 1e-3)
+    e2e_value = NRHS / (float(np.mean(t_e2e)) * 1e-3)
+
+    # accuracy: mixed vs FP64 solution, and potential error vs the analytic point source
+    xm_np = xm.cpu().numpy() if hasattr(xm, "cpu") else xm
+    x64_np = x64.cpu().numpy() if hasattr(x64, "cpu") else x64
+    rel_vs_fp64 = float(np.max(np.linalg.norm(xm_np - x64_np, axis=0) / np.linalg.norm(x64_np, axis=0)))
+    rng = np.random.default_rng(2)
+    pts = rng.normal(size=(100, 3))
+    pts = pts / np.linalg.norm(pts, axis=1, keepdims=True) * (0.25 * rng.uniform(0, 1, (100, 1)) ** (1 / 3))
+    pot = op.potential(xm_np, pts)
+    ref = 1.0 / (4 * np.pi * np.linalg.norm(pts[:, None, :] - x0[None, :, :], axis=2))
+    pot_err = float(np.max(np.abs(pot - ref)) / np.max(np.abs(ref)))
+
+    if rank != 0:
+        return
+    roof = _roofline(op, prof, stm)
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+            "data": "synthetic (seeded point sources, sphere.dat geometry)",
+            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "single gpu"}),
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(N * NRHS * 8),
+                    "d2h_bytes_per_step": int(N * NRHS * 8)},
+            "gpu_launches": int(prof["launches_total"]) if prof else None,
+            "roofline": roof, "clocks": clocks.summary(),
+            "latency_ms": {"p50": float(np.percentile(t_mixed, 50)), "p99": float(np.percentile(t_mixed, 99))},
+            "fp64_path": {"solves_per_s": fp64_value, "ms_per_step": float(np.mean(t_fp64)),
+                          "iterations": st64["iterations"]},
+            "mixed_over_fp64": value / world / fp64_value,
+            "solver": {k: stm[k] for k in ("iterations", "refinements", "fp64_matvecs", "low_matvecs",
+                                            "final_relres")},
+            "accuracy": {"mixed_vs_fp64_solution": rel_vs_fp64, "potential_vs_analytic": pot_err,
+                         "fp64_final_relres": st64["final_relres"]},
+            "matvec": {"fp64_products_per_s_32rhs": mv64, "mixed_products_per_s_32rhs": mvmx,
+                       "fp64_matvec_per_s": mv64 * NRHS, "mixed_matvec_per_s": mvmx * NRHS},
+            "assembly_s": asm, "kernel_ms": prof["ms"] if prof else None}
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k in ("value", "unit", "cores", "kind",
+                                                                               "sample")}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+CLASSES = ["near_fp64", "far_fp64", "far_fused_fp32", "transforms", "t_apply", "krylov", "other", "assembly"]
+
+
+def _read_profile(L, ctx):
+    import ctypes
+    ms = (ctypes.c_double * 8)()
+    ln = (ctypes.c_long * 8)()
+    L.bg_profile_read(ctx.h, ms, ln)
+    return {"ms": {CLASSES[i]: ms[i] for i in range(8)}, "launches": {CLASSES[i]: ln[i] for i in range(8)},
+            "launches_total": sum(ln[i] for i in range(8))}
+
+
+def _roofline(op, prof, stats):
+    """Roofline of the dominant kernel class of the timed solves."""
+    import json as _j
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = _j.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    src = "measured" if peaks else "fallback"
+    if not prof:
+        return None
+    cls = max(prof["ms"], key=lambda k: prof["ms"][k])
+    n = max(1, prof["launches"][cls])
+    t = prof["ms"][cls] * 1e-3 / n  # seconds per launch
+    info = op.info()
+    near_bytes = float(info[14])
+    if cls == "near_fp64":
+        # near-field block-sparse product: dense blocks streamed once per launch
+        algo = near_bytes
+        ach = algo / t / 1e9
+        return {"kernel": "k_bsr (FP64 near-field product, 32 RHS)", "bound": "hbm", "achieved": ach, "peak": hbm,
+                "unit": "GB/s", "frac": ach / hbm, "traffic": None, "peak_source": src,
+                "algorithmic_bytes_per_launch": algo, "avg_launch_ms": t * 1e3,
+                "note": "FP64 FMA-bound at 32 RHS (GB300 FP64 ~1.2 TFLOP/s); bytes = stored near-field blocks"}
+    # fused far field: algorithmic flops = 2 * entries * 32 RHS (GEMM part) per launch (one launch per level)
+    return {"kernel": cls, "bound": "tensor", "achieved": None, "peak": bf16, "unit": "TFLOP/s", "frac": None,
+            "traffic": None, "peak_source": src, "avg_launch_ms": t * 1e3}
+
+
+def ctypes_void_p():
+    import ctypes
+    return ctypes.c_void_p()
+
+
+def ctypes_byref(x):
+    import ctypes
+    return ctypes.byref(x)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

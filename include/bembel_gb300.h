@@ -39,10 +39,12 @@ typedef enum {
 
 typedef enum { BG_LAPLACE_SL = 0, BG_HELMHOLTZ_SL = 1, BG_MAXWELL_SL = 2 } bg_op_kind;
 
-/* Arithmetic of the far field in a product. BG_PREC_FP64 streams the stored
- * FP64 couplings (the reference's H2Matrix); BG_PREC_FP32 generates the
- * couplings on the fly in FP32 inside the fused matvec (no stored far field). */
-typedef enum { BG_PREC_FP64 = 0, BG_PREC_FP32 = 1 } bg_precision;
+/* Arithmetic of a product. BG_PREC_FP64 applies the FP64 H2 matrix (stored
+ * near and far field, the reference's H2Matrix). BG_PREC_MIXED keeps the
+ * near-field product, T and the vectors in FP64 and evaluates the far field in
+ * FP32: couplings generated on the fly inside the fused product (nothing
+ * stored), moments and transfers in FP32. */
+typedef enum { BG_PREC_FP64 = 0, BG_PREC_MIXED = 1 } bg_precision;
 
 typedef struct bg_context bg_context;
 typedef struct bg_geometry bg_geometry;
@@ -84,6 +86,16 @@ void bg_solve_params_default(bg_solve_params* p);
 bg_status bg_context_create(int device, bg_context** out);
 bg_status bg_context_destroy(bg_context* ctx);
 const char* bg_last_error_string(bg_context* ctx);
+/* The CUDA stream (cudaStream_t) every kernel of this context runs on. */
+bg_status bg_context_get_stream(bg_context* ctx, void** stream);
+/* Kernel timing: while enabled, every kernel launch is bracketed by CUDA
+ * events on the context stream. bg_profile_read synchronises and returns, per
+ * kernel class (near-field product, FP64 far-field product, fused FP32 far
+ * field, FMM transforms, T application, Krylov vector kernels, other,
+ * assembly), the summed device milliseconds and launch counts since the last
+ * read, then resets them. */
+bg_status bg_profile_enable(bg_context* ctx, int enable);
+bg_status bg_profile_read(bg_context* ctx, double* ms8, long* launches8);
 
 /* Geometry(const std::string&) with LoadGeometryFileDAT
  * (Geometry/Geometry.hpp:89-102, Geometry/GeometryIO.hpp:25-122). */

@@ -65,6 +65,9 @@ def lib():
         L.orc_potential.argtypes = [P, dp, dp, I, dp]
         L.orc_gmres.restype = I
         L.orc_gmres.argtypes = [P, dp, dp, D, I, I]
+        L.orc_create_sampled.restype = P
+        L.orc_create_sampled.argtypes = [ctypes.c_char_p, I, I, I, D, D, I, D, I, I]
+        L.orc_last_product_split.argtypes = [P, dp]
         L.orc_threads.restype = I
         _lib = L
     return _lib
@@ -123,10 +126,14 @@ class Problem:
     """Oracle discretisation: geometry file, refinement M, degree P, operator."""
 
     def __init__(self, geo, M, P, kind=LAPLACE, kappa=0.0, np_=9, eta=1.6, mcl=1, assemble=True,
-                 dummy_fun=0):
+                 dummy_fun=0, leaf_stride=1):
         kappa = complex(kappa)
-        self.h = lib().orc_create(geo.encode(), M, P, kind, kappa.real, kappa.imag, np_, eta, mcl,
-                                  int(assemble), dummy_fun)
+        if leaf_stride > 1:
+            self.h = lib().orc_create_sampled(geo.encode(), M, P, kind, kappa.real, kappa.imag, np_, eta, mcl,
+                                              leaf_stride)
+        else:
+            self.h = lib().orc_create(geo.encode(), M, P, kind, kappa.real, kappa.imag, np_, eta, mcl,
+                                      int(assemble), dummy_fun)
         if not self.h:
             raise RuntimeError("oracle problem creation failed")
         info = np.zeros(12, dtype=np.int64)
@@ -222,10 +229,19 @@ class Problem:
         x = np.asarray(x, dtype=self.dtype)
         squeeze = x.ndim == 1
         X = np.asfortranarray(x.reshape(self.N, -1))
-        Y = np.zeros_like(X, order="F")
-        if lib().orc_matvec(self.h, _dp(X.view(np.float64)), _dp(Y.view(np.float64)), X.shape[1]) != 0:
+        nrhs = X.shape[1]
+        xf = X.reshape(-1, order="F")
+        yf = np.zeros_like(xf)
+        if lib().orc_matvec(self.h, _dp(xf.view(np.float64)), _dp(yf.view(np.float64)), nrhs) != 0:
             raise RuntimeError("H2 matrix not assembled")
+        Y = yf.reshape((self.N, nrhs), order="F")
         return Y[:, 0] if squeeze else Y
+
+    def last_product_split(self):
+        """(leaf-loop seconds, other seconds, sampled entries, total entries) of the last matvec."""
+        out = np.zeros(4)
+        lib().orc_last_product_split(self.h, _dp(out))
+        return out
 
     def matvec_ss(self, x):
         x = np.ascontiguousarray(x, dtype=self.dtype)
@@ -235,10 +251,9 @@ class Problem:
         return y
 
     def dense_ss(self):
-        out = np.zeros((self.S, self.S), dtype=self.dtype, order="F")
-        lib().orc_dense_ss(self.h, _dp(out.view(np.float64) if not self.complex else
-                                       out.reshape(-1, order="F").view(np.float64)))
-        return out
+        flat = np.zeros(self.S * self.S, dtype=self.dtype)
+        lib().orc_dense_ss(self.h, _dp(flat.view(np.float64)))
+        return flat.reshape((self.S, self.S), order="F")
 
     def dense(self):
         D = self.dense_ss()

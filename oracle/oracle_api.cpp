@@ -34,6 +34,9 @@ struct Problem {
   std::vector<H2Leaf<cplx>> leaves_c;
   std::vector<std::vector<SurfacePoint>> ffq;
   double t_assemble = 0;
+  int leaf_stride = 1;   // assemble only leaves with index % leaf_stride == 0
+  double t_leaves = 0, t_other = 0;  // split of the last product's time
+  long sampled_entries = 0, total_entries = 0;
   std::string err;
 
   int vd() const { return op.vd(); }
@@ -55,6 +58,15 @@ void assemble_h2(Problem& p) {
   const int vd = p.vd(), n = p.ss.p2();
   auto& L = leaves_of<S>(p);
   L.resize(p.bct.leaves.size());
+  p.total_entries = p.sampled_entries = 0;
+  for (long li = 0; li < (long)p.bct.leaves.size(); ++li) {
+    const BlockLeaf& bl = p.bct.leaves[li];
+    long ent = bl.cc == kDense ? (long)p.ss.et.cluster_size(bl.c1) * n * p.ss.et.cluster_size(bl.c2) * n
+                               : (long)p.op.nc() * p.np * p.np * p.op.nc() * p.np * p.np;
+    ent *= vd * vd;
+    p.total_entries += ent;
+    if (li % p.leaf_stride == 0) p.sampled_entries += ent;
+  }
 #pragma omp parallel for schedule(dynamic, 1)
   for (long li = 0; li < (long)p.bct.leaves.size(); ++li) {
     const BlockLeaf& bl = p.bct.leaves[li];
@@ -62,6 +74,7 @@ void assemble_h2(Problem& p) {
     out.cc = bl.cc;
     out.c1 = bl.c1;
     out.c2 = bl.c2;
+    if (li % p.leaf_stride != 0) continue;  // sampled assembly: leaf left empty
     if (bl.cc == kDense) {
       int n1 = p.ss.et.cluster_size(bl.c1), f1 = p.ss.et.cluster_first(bl.c1);
       int n2 = p.ss.et.cluster_size(bl.c2), f2 = p.ss.et.cluster_first(bl.c2);
@@ -106,7 +119,9 @@ void h2_product_ss(Problem& p, const S* xss, S* yss) {
       std::vector<S> dst(comp, S(0));
       std::vector<Mat<S>> bw;
       for (auto& f : fwd) bw.emplace_back(f.rows, f.cols);
+      auto tl0 = std::chrono::steady_clock::now();
       for (auto& lf : L) {
+        if (lf.F.empty()) continue;  // not assembled (sampled operator)
         const Mat<S>& F = lf.F[rc * vd + cc];
         const Node& c1 = p.ss.et.nodes[lf.c1];
         const Node& c2 = p.ss.et.nodes[lf.c2];
@@ -126,6 +141,7 @@ void h2_product_ss(Problem& p, const S* xss, S* yss) {
           }
         }
       }
+      p.t_leaves += std::chrono::duration<double>(std::chrono::steady_clock::now() - tl0).count();
       std::vector<S> back = backward_transform<S>(p.mom[rc], p.transfer, steps, bw);
       for (int i = 0; i < comp; ++i) yss[(size_t)rc * comp + i] += dst[i] + back[i];
     }
@@ -272,12 +288,15 @@ void potential(Problem& p, const S* rho, const double* pts, int npts, S* out) {
 // DOF-level product y = A x for nrhs columns (column-major, leading dim N)
 template <typename S>
 void h2_matvec(Problem& p, const S* x, S* y, int nrhs) {
+  auto t0 = std::chrono::steady_clock::now();
+  p.t_leaves = 0;
   std::vector<S> xs(p.S()), ys(p.S());
   for (int c = 0; c < nrhs; ++c) {
     p.T.apply(x + (size_t)c * p.N(), xs.data());
     h2_product_ss<S>(p, xs.data(), ys.data());
     p.T.apply_t(ys.data(), y + (size_t)c * p.N());
   }
+  p.t_other = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() - p.t_leaves;
 }
 
 inline double absval(double v) { return std::fabs(v); }
@@ -413,6 +432,27 @@ void* orc_create(const char* geo, int M, int P, int kind, double kre, double kim
   }
 }
 void orc_destroy(void* h) { delete static_cast<Problem*>(h); }
+
+// As orc_create with assembly, but only every leaf_stride-th leaf of the block
+// partition is assembled (a bounded sample of the H2 matrix for CPU timing).
+void* orc_create_sampled(const char* geo, int M, int P, int kind, double kre, double kim, int np, double eta, int mcl,
+                         int leaf_stride) {
+  Problem* p = static_cast<Problem*>(orc_create(geo, M, P, kind, kre, kim, np, eta, mcl, 0, 0));
+  if (!p) return nullptr;
+  p->leaf_stride = leaf_stride < 1 ? 1 : leaf_stride;
+  auto t0 = std::chrono::steady_clock::now();
+  if (p->op.is_complex()) assemble_h2<cplx>(*p); else assemble_h2<double>(*p);
+  p->t_assemble = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return p;
+}
+// times of the last product: [leaf loop s, transforms and T s, sampled entries, total entries]
+void orc_last_product_split(void* h, double* out4) {
+  Problem& p = *static_cast<Problem*>(h);
+  out4[0] = p.t_leaves;
+  out4[1] = p.t_other;
+  out4[2] = (double)p.sampled_entries;
+  out4[3] = (double)p.total_entries;
+}
 
 // info[0..11]: ne, S, N, n_leaves, n_dense, n_lowrank, vd, nc, np, T nnz, M, P
 void orc_info(void* h, long* info) {

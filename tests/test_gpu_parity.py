@@ -11,7 +11,7 @@ from conftest import SPHERE, TORUS
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
-FP32_TOL = 1e-5
+FP32_TOL = 1e-5  # mixed: FP64 near field, FP32 far field
 
 
 @pytest.fixture(scope="module")
@@ -49,7 +49,7 @@ def test_leaf_blocks(ctx, oracle, geo, M, P, kind, kappa, np_):
 
 
 @pytest.mark.parametrize("geo,M,P,kind,kappa,np_", CASES)
-def test_matvec_fp64_and_fp32(ctx, oracle, geo, M, P, kind, kappa, np_):
+def test_matvec_fp64_and_mixed(ctx, oracle, geo, M, P, kind, kappa, np_):
     d, o = _pair(ctx, oracle, geo, M, P, kind, kappa, np_)
     rng = np.random.default_rng(7)
     for nrhs in (1, 5):
@@ -59,7 +59,7 @@ def test_matvec_fp64_and_fp32(ctx, oracle, geo, M, P, kind, kappa, np_):
         ref = o.matvec(x)
         A = d.get_discrete_operator()
         y64 = A.matvec(x)
-        y32 = A.matvec(x, precision="fp32")
+        y32 = A.matvec(x, precision="mixed")
         assert np.linalg.norm(y64 - ref) / np.linalg.norm(ref) < FP64_TOL
         assert np.linalg.norm(y32 - ref) / np.linalg.norm(ref) < FP32_TOL
 
@@ -97,7 +97,7 @@ def test_potential(ctx, oracle):
         assert np.linalg.norm(got[:, c] - ref) / np.linalg.norm(ref) < FP64_TOL
 
 
-@pytest.mark.parametrize("inner", ["fp64", "fp32"])
+@pytest.mark.parametrize("inner", ["fp64", "mixed"])
 def test_solve_reaches_tolerance(ctx, oracle, inner):
     d, o = _pair(ctx, oracle, SPHERE, 3, 1, 0, 0.0, 6)
     x0 = np.array([[0.0, 0.2, 1.8], [1.0, 1.5, -1.2], [-2.0, 0.3, 0.1]])
