@@ -727,6 +727,33 @@ cudaError_t launch_far_fused(bool cplx, const float4* pts, const d4* centres, co
   }
 #undef BG_FR
 }
+cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int rows, int nrhs, void* work,
+                             cudaStream_t s) {
+  const long n = (long)rows * nrhs;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(n, 256);
+  if (Sin == 0 && Sout == 0) k_gather_in<double, double><<<g, 256, 0, s>>>((const double*)user, ld, rows, nrhs, (double*)work);
+  else if (Sin == 0 && Sout == 2) k_gather_in<double, float><<<g, 256, 0, s>>>((const double*)user, ld, rows, nrhs, (float*)work);
+  else if (Sin == 1 && Sout == 1) k_gather_in<cd, cd><<<g, 256, 0, s>>>((const cd*)user, ld, rows, nrhs, (cd*)work);
+  else if (Sin == 1 && Sout == 3) k_gather_in<cd, cf><<<g, 256, 0, s>>>((const cd*)user, ld, rows, nrhs, (cf*)work);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+cudaError_t launch_scatter_out(int Sw, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
+                               const double* beta, cudaStream_t s) {
+  const long n = (long)rows * nrhs;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = blocks_for(n, 256);
+  const cd a = {alpha[0], alpha[1]}, b = {beta[0], beta[1]};
+  switch (Sw) {
+    case 0: k_scatter_out_real<double><<<g, 256, 0, s>>>((const double*)work, rows, nrhs, (double*)user, ld, alpha[0], beta[0]); break;
+    case 2: k_scatter_out_real<float><<<g, 256, 0, s>>>((const float*)work, rows, nrhs, (double*)user, ld, alpha[0], beta[0]); break;
+    case 1: k_scatter_out_cplx<cd><<<g, 256, 0, s>>>((const cd*)work, rows, nrhs, (cd*)user, ld, a, b); break;
+    case 3: k_scatter_out_cplx<cf><<<g, 256, 0, s>>>((const cf*)work, rows, nrhs, (cd*)user, ld, a, b); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
 cudaError_t launch_add_low(bool cplx, const void* in32, long n, void* out64, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const unsigned g = blocks_for(n, 256);
