@@ -293,31 +293,111 @@ __global__ void __launch_bounds__(256) k_bgemm(const T* __restrict__ A, int Mo, 
   }
 }
 
+// K-chunked variant: one CTA per batch item, A and B staged KC rows of the
+// inner dimension at a time (small shared footprint, many CTAs per SM).
+template <typename T, bool TA, bool ACC, int RT, int CT, int KC>
+__global__ void __launch_bounds__(256) k_bgemm_kc(const T* __restrict__ A, int Mo, int Ki, const T* __restrict__ B,
+                                                  long bstride, T* __restrict__ C, long cstride, int kk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);  // [q][i], KC x Mo
+  T* Bs = As + (size_t)KC * Mo;            // [q][c], KC x kk
+  const int b = blockIdx.x;
+  const T* Bb = B + (long)b * bstride;
+  T* Cb = C + (long)b * cstride;
+  const int rtiles = (Mo + RT - 1) / RT, ctiles = (kk + CT - 1) / CT, ntiles = rtiles * ctiles;
+  constexpr int MAXT = 4;  // tiles per thread
+  T acc[MAXT][RT][CT];
+#pragma unroll
+  for (int u = 0; u < MAXT; ++u)
+#pragma unroll
+    for (int r = 0; r < RT; ++r)
+#pragma unroll
+      for (int c = 0; c < CT; ++c) acc[u][r][c] = (T)0;
+  for (int q0 = 0; q0 < Ki; q0 += KC) {
+    const int qn = min(KC, Ki - q0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < qn * Mo; t += blockDim.x) {
+      const int q = t / Mo, i = t - q * Mo;
+      As[t] = TA ? A[(long)(q0 + q) * Mo + i] : A[(long)i * Ki + q0 + q];
+    }
+    for (int t = threadIdx.x; t < qn * kk; t += blockDim.x) Bs[t] = Bb[(long)q0 * kk + t];
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < MAXT; ++u) {
+      const int tile = threadIdx.x + u * blockDim.x;
+      if (tile < ntiles) {
+        const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+        for (int q = 0; q < qn; ++q) {
+          T a[RT], bv[CT];
+#pragma unroll
+          for (int r = 0; r < RT; ++r) a[r] = As[q * Mo + min(i0 + r, Mo - 1)];
+#pragma unroll
+          for (int c = 0; c < CT; ++c) bv[c] = Bs[q * kk + min(c0 + c, kk - 1)];
+#pragma unroll
+          for (int r = 0; r < RT; ++r)
+#pragma unroll
+            for (int c = 0; c < CT; ++c) acc[u][r][c] = fmac(acc[u][r][c], a[r], bv[c]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < MAXT; ++u) {
+    const int tile = threadIdx.x + u * blockDim.x;
+    if (tile < ntiles) {
+      const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+          if (i0 + r < Mo && c0 + c < kk) {
+            T* o = Cb + (long)(i0 + r) * kk + c0 + c;
+            *o = ACC ? *o + acc[u][r][c] : acc[u][r][c];
+          }
+    }
+  }
+}
+
 template <typename T>
 static cudaError_t bgemm(bool ta, bool acc, const T* A, int Mo, int Ki, const T* B, long bstride, T* C, long cstride,
                          int nbatch, int kk, cudaStream_t s) {
   if (nbatch == 0) return cudaSuccess;
-  const size_t a_bytes = (size_t)Mo * Ki * sizeof(T), b_bytes = (size_t)Ki * kk * sizeof(T);
-  const bool stage = a_bytes + b_bytes <= 200 * 1024;
-  if (!stage && b_bytes > 200 * 1024) return cudaErrorInvalidValue;
-  const size_t smem = (stage ? a_bytes : 0) + b_bytes;
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int grid = std::min(nbatch, stage ? sms : 4 * sms);
+  constexpr int RT = 3, CT = 4, KC = 32;
+  const long ntiles = (long)((Mo + RT - 1) / RT) * ((kk + CT - 1) / CT);
+  if (ntiles > 4 * 256) {
+    // large outputs: persistent kernel with the whole A staged
+    const size_t a_bytes = (size_t)Mo * Ki * sizeof(T), b_bytes = (size_t)Ki * kk * sizeof(T);
+    const bool stage = a_bytes + b_bytes <= 200 * 1024;
+    if (!stage && b_bytes > 200 * 1024) return cudaErrorInvalidValue;
+    const size_t smem = (stage ? a_bytes : 0) + b_bytes;
+    const int grid = std::min(nbatch, 4 * 152);
 #define BG_GEMM(TA_, AC_, ST_)                                                                             \
+    {                                                                                                      \
+      auto kf = k_bgemm<T, TA_, AC_, ST_, 3, 4>;                                                           \
+      cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);    \
+      if (e != cudaSuccess) return e;                                                                      \
+      kf<<<grid, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, nbatch, kk);                           \
+      return cudaGetLastError();                                                                           \
+    }
+    if (!ta && !acc && stage) BG_GEMM(false, false, true)
+    if (!ta && !acc && !stage) BG_GEMM(false, false, false)
+    if (ta && acc && stage) BG_GEMM(true, true, true)
+    if (ta && acc && !stage) BG_GEMM(true, true, false)
+#undef BG_GEMM
+    return cudaErrorInvalidValue;
+  }
+  const size_t smem = (size_t)KC * (Mo + kk) * sizeof(T);
+#define BG_KC(TA_, AC_)                                                                                    \
   {                                                                                                        \
-    auto kf = k_bgemm<T, TA_, AC_, ST_, 3, 4>;                                                             \
+    auto kf = k_bgemm_kc<T, TA_, AC_, RT, CT, KC>;                                                         \
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
     if (e != cudaSuccess) return e;                                                                        \
-    kf<<<grid, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, nbatch, kk);                             \
+    kf<<<nbatch, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, kk);                                   \
     return cudaGetLastError();                                                                             \
   }
-  if (!ta && !acc && stage) BG_GEMM(false, false, true)
-  if (!ta && !acc && !stage) BG_GEMM(false, false, false)
-  if (ta && acc && stage) BG_GEMM(true, true, true)
-  if (ta && acc && !stage) BG_GEMM(true, true, false)
-#undef BG_GEMM
+  if (!ta && !acc) BG_KC(false, false)
+  if (ta && acc) BG_KC(true, true)
+#undef BG_KC
   return cudaErrorInvalidValue;
 }
 

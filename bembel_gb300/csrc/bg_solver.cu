@@ -50,6 +50,40 @@ __global__ void k_mdot(const S* __restrict__ V, long vstride, const S* __restric
     out[(long)i * k + threadIdx.x] = s;
   }
 }
+// Blocked dot products for many vectors at once: CTA (i, chunk) reduces rows
+// [chunk*rows_per, ...) of V_i^H w for all k columns into part[(i*nch + chunk)*k + c];
+// k_reduce_parts then sums the chunks in a fixed order (deterministic).
+template <typename S>
+__global__ void k_mdot_part(const S* __restrict__ V, long vstride, const S* __restrict__ w, int N, int k, int rows_per,
+                            S* __restrict__ part) {
+  __shared__ S red[256];
+  const int i = blockIdx.x, ch = blockIdx.y, nch = gridDim.y;
+  const int groups = blockDim.x / k;
+  const int c = threadIdx.x % k, g = threadIdx.x / k;
+  const int n0 = ch * rows_per, n1 = min(N, n0 + rows_per);
+  S acc = zero<S>();
+  if (g < groups) {
+    const S* v = V + (long)i * vstride;
+    for (int n = n0 + g; n < n1; n += groups) acc = addv(acc, conj_mul(v[(long)n * k + c], w[(long)n * k + c]));
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x < k) {
+    S s2 = zero<S>();
+    for (int gg = 0; gg < groups; ++gg) s2 = addv(s2, red[gg * k + threadIdx.x]);
+    part[((long)i * nch + ch) * k + threadIdx.x] = s2;
+  }
+}
+template <typename S>
+__global__ void k_reduce_parts(const S* __restrict__ part, int nv, int nch, int k, S* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nv * k) return;
+  const int i = t / k, c = t % k;
+  S s2 = zero<S>();
+  for (int ch = 0; ch < nch; ++ch) s2 = addv(s2, part[((long)i * nch + ch) * k + c]);
+  out[(long)i * k + c] = s2;
+}
+
 // w[n][c] -= sum_{i<nv} V[i][n][c] h[i][c]
 template <typename S>
 __global__ void k_vupdate(const S* __restrict__ V, long vstride, int nv, const S* __restrict__ h, int N, int k,
@@ -115,7 +149,7 @@ struct Krylov {
   bg_operator* op;
   int N, k, m;
   bool flexible;          // store the preconditioned directions Z
-  DevBuf V, Z, w, hdev, inv, ydev;
+  DevBuf V, Z, w, hdev, inv, ydev, part;
   bg_status init(bg_operator* o, int kk, int mm, bool flex, size_t sb) {
     op = o;
     N = o->N;
@@ -127,6 +161,7 @@ struct Krylov {
     if (e == cudaSuccess && flex) e = Z.alloc((size_t)m * nk * sb);
     if (e == cudaSuccess) e = w.alloc(nk * sb);
     if (e == cudaSuccess) e = hdev.alloc((size_t)3 * (m + 1) * k * sb);
+    if (e == cudaSuccess) e = part.alloc((size_t)(m + 1) * 64 * k * sb);
     if (e == cudaSuccess) e = inv.alloc(k * sizeof(double));
     if (e == cudaSuccess) e = ydev.alloc((size_t)(m + 1) * k * sb);
     return cuda_status(o->ctx, e, "solver workspace");
@@ -234,8 +269,16 @@ bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inn
       S* h3 = h2 + (size_t)(m + 1) * k;
       for (int pass = 0; pass < 2; ++pass) {
         S* hp = pass == 0 ? h1 : h2;
+        // split the rows over enough CTAs to fill the GPU
+        const int nch = std::max(1, std::min(64, (4 * 152 + j) / (j + 1)));
+        const int rows_per = (N + nch - 1) / nch;
         timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_mdot<S><<<j + 1, 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, hp);
+          k_mdot_part<S><<<dim3(j + 1, nch), 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, rows_per,
+                                                          K.part.as<S>());
+          return cudaGetLastError();
+        });
+        timed_launch(op->ctx, KC_KRYLOV, [&] {
+          k_reduce_parts<S><<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.part.as<S>(), j + 1, nch, k, hp);
           return cudaGetLastError();
         });
         timed_launch(op->ctx, KC_KRYLOV, [&] {
@@ -243,10 +286,17 @@ bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inn
           return cudaGetLastError();
         });
       }
-      timed_launch(op->ctx, KC_KRYLOV, [&] {
-        k_mdot<S><<<1, 256, 0, s>>>(K.w.as<S>(), 0, K.w.as<S>(), N, k, h3);
-        return cudaGetLastError();
-      });
+      {
+        const int nch = 64, rows_per = (N + nch - 1) / nch;
+        timed_launch(op->ctx, KC_KRYLOV, [&] {
+          k_mdot_part<S><<<dim3(1, nch), 256, 0, s>>>(K.w.as<S>(), 0, K.w.as<S>(), N, k, rows_per, K.part.as<S>());
+          return cudaGetLastError();
+        });
+        timed_launch(op->ctx, KC_KRYLOV, [&] {
+          k_reduce_parts<S><<<1, 256, 0, s>>>(K.part.as<S>(), 1, nch, k, h3);
+          return cudaGetLastError();
+        });
+      }
       timed_launch(op->ctx, KC_KRYLOV, [&] {
         k_inv_norm<S><<<1, 64, 0, s>>>(h3, k, K.inv.as<double>());
         return cudaGetLastError();
