@@ -134,6 +134,26 @@ bg_status bg_operator_assembly_times(const bg_operator* op, double* t3);
 bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
                     const double* alpha, const double* beta, int precision, int on_device);
 
+/* y = A x for ONE right-hand side without allocating any device memory. This
+ * entry point has no counterpart in the reference; it exists for callers that
+ * may not call cudaMalloc when they need a product (a host that owns a fixed
+ * memory budget and counts every allocation, code inside a pooled allocator it
+ * must not disturb, a serving loop that forbids allocation after warm-up
+ * because an allocation can stall the device). bg_matvec grows per-operator
+ * work vectors on demand and so may allocate.
+ * x, y: device pointers to N scalars of the operator's type (double, or
+ * interleaved complex double), aligned to that type, not overlapping.
+ * precision: bg_precision. The call returns once y is written.
+ * Intermediate vectors come from one fixed 16 MiB device array in the library
+ * (held on every GPU that loads it until the process exits). An operator whose
+ * intermediates do not fit is rejected with BG_INVALID_ARG and a message giving
+ * the bytes it would need (sphere, M = 5, P = 2, n_p = 9 needs about 4 MB).
+ * All calls on a device share that array, so calls that overlap on the GPU
+ * (other threads, other contexts, other streams) race and give wrong results.
+ * The first call on each device looks up the array's device address; make it
+ * before any stream capture. */
+bg_status bg_matvec_noalloc(bg_operator* op, const void* x, void* y, int precision);
+
 /* DiscreteLinearForm<DirichletTrace<S>, Op>::compute (LinearForm/DiscreteLinearForm.hpp:44-83,
  * LinearForm/DirichletTrace.hpp:38-66) for analytic data (examples/Data.hpp):
  *   kind 0: u(x) = 1/(4 pi |x - x0|), prm = x0 (3 doubles per column)
