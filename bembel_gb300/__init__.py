@@ -168,10 +168,10 @@ class H2Matrix:
     def matvec(self, x, precision="fp64", out=None, alpha=1.0, beta=0.0):
         """out = beta * out + alpha * A x (H2DenseProduct.hpp:268-290).
         precision "fp64": the FP64 H2 matrix; "mixed": FP64 near field, FP32
-        on-the-fly far field."""
-        if precision not in ("fp64", "mixed"):
-            raise BembelError(_lib.BG_INVALID_ARG, "precision must be 'fp64' or 'mixed'")
-        prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_MIXED
+        on-the-fly far field; "fp32": near and far field in FP32."""
+        if precision not in _lib.PRECISIONS:
+            raise BembelError(_lib.BG_INVALID_ARG, "precision must be one of %s" % sorted(_lib.PRECISIONS))
+        prec = _lib.PRECISIONS[precision]
         N = self._dop.N
         a = np.array([complex(alpha).real, complex(alpha).imag])
         b = np.array([complex(beta).real, complex(beta).imag])
@@ -202,7 +202,9 @@ class H2Matrix:
         p = SolveParams()
         _lib.load().bg_solve_params_default(ctypes.byref(p))
         p.tol, p.restart, p.max_iter = tol, restart, max_iter
-        p.inner_precision = _lib.PREC_MIXED if inner == "mixed" else _lib.PREC_FP64
+        if inner not in _lib.PRECISIONS:
+            raise BembelError(_lib.BG_INVALID_ARG, "inner must be one of %s" % sorted(_lib.PRECISIONS))
+        p.inner_precision = _lib.PRECISIONS[inner]
         p.inner_tol, p.max_refinements = inner_tol, max_refinements
         st = SolveStats()
         N = self._dop.N

@@ -14,7 +14,8 @@ BG_OK, BG_INVALID_ARG, BG_OOM, BG_UNSUPPORTED, BG_DEVICE_ERROR, BG_TIMEOUT, BG_C
 STATUS_NAMES = ["BG_OK", "BG_INVALID_ARG", "BG_OOM", "BG_UNSUPPORTED", "BG_DEVICE_ERROR", "BG_TIMEOUT",
                 "BG_CANCELLED", "BG_NOT_CONVERGED"]
 LAPLACE_SL, HELMHOLTZ_SL, MAXWELL_SL = 0, 1, 2
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "fp32": PREC_FP32}
 
 
 class H2Params(ctypes.Structure):

@@ -579,6 +579,16 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
   auto t1 = std::chrono::steady_clock::now();
   st = assemble_near(op);
   if (st != BG_OK) return st;
+  {
+    // FP32 copy of the near field for BG_PREC_FP32 products
+    const long nb = (long)op->dense.col.size(), B = op->dense.B;
+    cudaError_t e = op->d_dense32.alloc((size_t)nb * op->block_stride32((int)B) * op->scalar_bytes(true));
+    if (e == cudaSuccess)
+      e = launch_convert_blocks(op->cplx, op->d_dense64.p, op->block_stride((int)B), op->d_dense32.p,
+                                op->block_stride32((int)B), B * B, nb, op->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(op->ctx->stream);
+    if ((st = cuda_status(op->ctx, e, "FP32 near field")) != BG_OK) return st;
+  }
   auto t2 = std::chrono::steady_clock::now();
   op->t_far = std::chrono::duration<double>(t1 - t0).count();
   op->t_near = std::chrono::duration<double>(t2 - t1).count();
@@ -611,8 +621,10 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
 }
 
 // One H2 product on row-major FP64 work vectors (H2DenseProduct.hpp:33-165).
-bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof, void* ydof) {
+bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
   cudaStream_t s = op->ctx->stream;
+  const bool mixed = prec != BG_PREC_FP64;   // far field and transforms in FP32
+  const bool near32 = prec == BG_PREC_FP32;  // near field in FP32 too
   const int S64 = op->stype(false), Sfar = op->stype(mixed);
   const size_t sfar = op->scalar_bytes(mixed);
   const int np2 = op->np * op->np;
@@ -620,19 +632,28 @@ bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof
   BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
                             op->w_xss.p, nrhs, s); }),
            "T x");
-  // near field, always FP64
-  BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
-                      op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p, nrhs, 0, s); }),
-           "near-field product");
   bool any_far = false;
   for (const auto& f : op->far) any_far |= !f.col.empty();
+  if (near32) {
+    // FP32 near field into the FP32 accumulator the far field adds to
+    BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
+    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp32(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense32.p,
+                        op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss32.p, op->w_yss32.p, nrhs, 0, s); }),
+             "near-field product (FP32)");
+  } else {
+    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
+                        op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p, nrhs, 0, s); }),
+             "near-field product");
+  }
   if (any_far) {
     const long comp_ss = (long)op->ne * op->p2;  // superspace rows per vector component
     const void* xfar = op->w_xss.p;
     void* yfar = op->w_yss.p;
     if (mixed) {
-      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
-      BG_CHECK(cudaMemsetAsync(op->w_yss32.p, 0, ss_n * sfar, s), "far field");
+      if (!near32) {
+        BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
+        BG_CHECK(cudaMemsetAsync(op->w_yss32.p, 0, ss_n * sfar, s), "far field");
+      }
       xfar = op->w_xss32.p;
       yfar = op->w_yss32.p;
     }
@@ -686,8 +707,11 @@ bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof
                                  static_cast<char*>(yfar) + c * comp_ss * nrhs * sfar, nrhs, s); }),
                "backward moments");
     }
-    if (mixed) BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_add_low(op->cplx, op->w_yss32.p, ss_n, op->w_yss.p, s); }), "far field to FP64");
+    if (mixed && !near32)
+      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_add_low(op->cplx, op->w_yss32.p, ss_n, op->w_yss.p, s); }), "far field to FP64");
   }
+  if (near32)
+    BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(Sfar, S64, op->w_yss32.p, ss_n, op->w_yss.p, s); }), "y to FP64");
   BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(), op->N,
                             op->w_yss.p, ydof, nrhs, s); }),
            "T^T y");
@@ -708,7 +732,8 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
   if (!op || !x || !y || nrhs <= 0 || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
   if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
-  if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED) return set_error(op->ctx, BG_INVALID_ARG, "precision");
+  if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED && precision != BG_PREC_FP32)
+    return set_error(op->ctx, BG_INVALID_ARG, "precision");
   const double one[2] = {1.0, 0.0}, zero2[2] = {0.0, 0.0};
   if (!alpha) alpha = one;
   if (!beta) beta = zero2;
@@ -716,7 +741,6 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
     return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
   cudaSetDevice(op->ctx->device);
   cudaStream_t s = op->ctx->stream;
-  const bool mixed = precision == BG_PREC_MIXED;
   const size_t usz = op->cplx ? 16 : 8;
   const int uS = op->cplx ? 1 : 0;
   for (int c0 = 0; c0 < nrhs; c0 += 32) {
@@ -738,7 +762,7 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
       lx = ly = op->N;
     }
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_gather_in(uS, uS, xd, lx, op->N, k, op->w_xdof.p, s); }), "gather x");
-    if ((st = apply_operator(op, k, mixed, op->w_xdof.p, op->w_ydof.p)) != BG_OK) return st;
+    if ((st = apply_operator(op, k, precision, op->w_xdof.p, op->w_ydof.p)) != BG_OK) return st;
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_scatter_out(uS, op->w_ydof.p, op->N, k, yd, ly, alpha, beta, s); }), "scatter y");
     if (!on_device)
       BG_CHECK(cudaMemcpy2DAsync(yp, ldy * usz, yd, op->N * usz, op->N * usz, k, cudaMemcpyDeviceToHost, s),

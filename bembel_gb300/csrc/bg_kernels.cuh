@@ -71,6 +71,12 @@ cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int r
                              cudaStream_t s);
 cudaError_t launch_scatter_out(int Swork, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
                                const double* beta, cudaStream_t s);
+// FP32 / complex-FP32 blocks; same layout rules as launch_bsr_fp64
+cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
+// out[b*sout + e] = (FP32) in[b*sin + e], e < B2, b < nblocks
+cudaError_t launch_convert_blocks(bool cplx, const void* in, long sin, void* out, long sout, long B2, long nblocks,
+                                  cudaStream_t s);
 cudaError_t launch_convert(int Sin, int Sout, const void* in, long n, void* out, cudaStream_t s);
 // out64[t] += (FP64) in32[t]
 cudaError_t launch_add_low(bool cplx, const void* in32, long n, void* out64, cudaStream_t s);

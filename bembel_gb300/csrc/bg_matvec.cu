@@ -55,6 +55,10 @@ __device__ inline void cp_async8(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem));
 }
+__device__ inline void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
 __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
@@ -135,7 +139,8 @@ __global__ void k_bsr_pipe(const int* __restrict__ row_ptr, const int* __restric
     S* xd = reinterpret_cast<S*>(dst + fsz);
     for (int e = t; e < B * nrhs; e += blockDim.x) {
       if (sizeof(S) == 16) cp_async16(xd + e, xs + e);
-      else cp_async8(xd + e, xs + e);
+      else if (sizeof(S) == 8) cp_async8(xd + e, xs + e);
+      else cp_async4(xd + e, xs + e);
     }
     cp_async_commit();
   };
@@ -673,6 +678,33 @@ cudaError_t launch_bsr_fp64(bool cplx, const int* row_ptr, const int* col, const
   return bsr_pipe_typed<double>(row_ptr, col, (const double*)blocks, bstride, nrows, B, (const double*)x, (double*)y,
                                 nrhs, accumulate, s);
 }
+cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (cplx)
+    return bsr_pipe_typed<cf>(row_ptr, col, (const cf*)blocks, bstride, nrows, B, (const cf*)x, (cf*)y, nrhs, accumulate, s);
+  return bsr_pipe_typed<float>(row_ptr, col, (const float*)blocks, bstride, nrows, B, (const float*)x, (float*)y,
+                               nrhs, accumulate, s);
+}
+
+// FP32 copy of FP64 blocks with a different block stride (in scalars)
+template <typename S64, typename S32>
+__global__ void k_convert_blocks(const S64* __restrict__ in, long sin, S32* __restrict__ out, long sout, long B2,
+                                 long nblocks) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nblocks * B2) return;
+  const long b = t / B2, e = t % B2;
+  out[b * sout + e] = Conv<S64, S32>::run(in[b * sin + e]);
+}
+cudaError_t launch_convert_blocks(bool cplx, const void* in, long sin, void* out, long sout, long B2, long nblocks,
+                                  cudaStream_t s) {
+  const long n = nblocks * B2;
+  if (n == 0) return cudaSuccess;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  if (cplx) k_convert_blocks<cd, cf><<<g, 256, 0, s>>>((const cd*)in, sin, (cf*)out, sout, B2, nblocks);
+  else k_convert_blocks<double, float><<<g, 256, 0, s>>>((const double*)in, sin, (float*)out, sout, B2, nblocks);
+  return cudaGetLastError();
+}
+
 template <typename S>
 static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void* xss, void* y, int nrhs, cudaStream_t s) {
   if (ncl == 0) return cudaSuccess;

@@ -146,6 +146,7 @@ struct bg_operator {
   DevBuf d_cheb;
   std::vector<DevBuf*> d_pts64, d_pts32, d_centres;  // per level
   DevBuf d_dense64;                       // dense blocks (FP64)
+  DevBuf d_dense32;                       // FP32 copy of the dense blocks (BG_PREC_FP32)
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
@@ -162,6 +163,8 @@ struct bg_operator {
   // scalars between consecutive stored FP64 blocks of size B x B: rounded up
   // so that every block starts on a 16-byte boundary
   long block_stride(int B) const { return cplx ? (long)B * B : ((long)B * B + 1) / 2 * 2; }
+  // FP32 blocks: stride a multiple of 16 bytes
+  long block_stride32(int B) const { return cplx ? ((long)B * B + 1) / 2 * 2 : ((long)B * B + 3) / 4 * 4; }
   int stype(bool fp32) const { return (fp32 ? 2 : 0) + (cplx ? 1 : 0); }
   int nclusters(int level) const { return level < 0 ? 1 : mesh.npatch << (2 * level); }
 };
@@ -172,7 +175,8 @@ void context_retain(bg_context* ctx);
 void context_release(bg_context* ctx);
 bg_status cuda_status(bg_context* ctx, cudaError_t e, const char* what);
 bg_status ensure_work(bg_operator* op, int nrhs);
-// y_dof = A x_dof on row-major FP64 work vectors. mixed = false: the FP64
-// H2 matrix (stored far field); mixed = true: FP64 near field plus the FP32
-// fused far field (forward/backward transforms in FP32).
-bg_status apply_operator(bg_operator* op, int nrhs, bool mixed, const void* xdof, void* ydof);
+// y_dof = A x_dof on row-major FP64 work vectors. prec (bg_precision):
+// BG_PREC_FP64 the FP64 H2 matrix (stored far field); BG_PREC_MIXED FP64 near
+// field plus the FP32 fused far field (forward/backward transforms in FP32);
+// BG_PREC_FP32 as MIXED with the near field in FP32 as well.
+bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof);

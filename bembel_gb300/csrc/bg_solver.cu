@@ -4,7 +4,8 @@
 // sides with classical Gram-Schmidt applied twice and an FP64 Krylov basis.
 // FP64 path: GMRES on the FP64 H2 matrix. Mixed path: flexible GMRES (Saad
 // 1993) on the FP64 operator whose right preconditioner is an inner GMRES solve
-// with the mixed operator (FP64 near field, FP32 far field): every outer step
+// with a low-precision operator (BG_PREC_MIXED: FP64 near field, FP32 far
+// field; BG_PREC_FP32: both in FP32): every outer step
 // is one FP64 residual-consistent product, the inner steps are cheap, and the
 // outer Krylov space recovers the FP64 solution. Replaces the Eigen solvers
 // used at examples/LaplaceSingleLayerH2.cpp:78-81 and
@@ -197,12 +198,13 @@ struct Counters {
 // Right-preconditioned restarted (F)GMRES for A x = b on row-major FP64 work
 // vectors, x updated in place from its current value. A is the FP64 operator
 // (mixed = false) or the mixed one. With a preconditioner (inner != nullptr)
-// z_j = M^-1 v_j is an inner GMRES solve on the mixed operator and the
+// z_j = M^-1 v_j is an inner GMRES solve on the low-precision operator and the
 // directions z_j are kept (flexible GMRES); otherwise z_j = v_j. Stops when
 // every column's residual estimate is below tol * ||b_c||.
 template <typename S>
-bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inner_max, const void* b, void* x,
-                 double tol, int max_iter, Counters* cnt, std::vector<double>* relres) {
+bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inner_tol, int inner_max, const void* b,
+                 void* x, double tol, int max_iter, Counters* cnt, std::vector<double>* relres) {
+  const bool low = prec != BG_PREC_FP64;
   typedef HostS<S> H;
   bg_operator* op = K.op;
   cudaStream_t s = op->ctx->stream;
@@ -220,8 +222,8 @@ bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inn
   int it = 0;
   while (true) {
     // true residual r = b - A x
-    if ((st = apply_operator(op, k, mixed, x, r.p)) != BG_OK) return st;
-    ++(mixed ? cnt->mixed_mv : cnt->fp64_mv);
+    if ((st = apply_operator(op, k, prec, x, r.p)) != BG_OK) return st;
+    ++(low ? cnt->mixed_mv : cnt->fp64_mv);
     timed_launch(op->ctx, KC_KRYLOV, [&] {
       k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(b), nk, r.as<S>());
       return cudaGetLastError();
@@ -254,14 +256,15 @@ bg_status fgmres(Krylov& K, bool mixed, Krylov* inner, double inner_tol, int inn
         e = cudaMemsetAsync(zdst, 0, nk * sizeof(S), s);
         if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
         Counters ic;
-        if ((st = fgmres<S>(*inner, true, nullptr, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr)) != BG_OK)
+        if ((st = fgmres<S>(*inner, inner_prec, nullptr, 0, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr)) !=
+            BG_OK)
           return st;
         cnt->mixed_mv += ic.mixed_mv;
         cnt->inner_it += ic.outer_it;
         zj = zdst;
       }
-      if ((st = apply_operator(op, k, mixed, zj, K.w.p)) != BG_OK) return st;
-      ++(mixed ? cnt->mixed_mv : cnt->fp64_mv);
+      if ((st = apply_operator(op, k, prec, zj, K.w.p)) != BG_OK) return st;
+      ++(low ? cnt->mixed_mv : cnt->fp64_mv);
       // classical Gram-Schmidt, two passes, and the norm, all on the device;
       // one copy brings the Hessenberg column back
       S* h1 = K.hdev.as<S>();
@@ -377,14 +380,14 @@ bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, cons
   const long nk = (long)op->N * k;
   cudaError_t e = cudaMemsetAsync(xdof, 0, nk * sizeof(S), s);
   if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve");
-  const bool mixed = prm.inner_precision == BG_PREC_MIXED;
+  const bool mixed = prm.inner_precision != BG_PREC_FP64;
   Counters cnt;
   std::vector<double> relres;
   bg_status st;
   if (!mixed) {
     Krylov K;
     if ((st = K.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
-    st = fgmres<S>(K, false, nullptr, 0, 0, bdof, xdof, prm.tol, prm.max_iter, &cnt, &relres);
+    st = fgmres<S>(K, BG_PREC_FP64, nullptr, 0, 0, 0, bdof, xdof, prm.tol, prm.max_iter, &cnt, &relres);
     cnt.inner_it = cnt.outer_it;
   } else {
     // outer FP64 flexible GMRES; each direction is an inner mixed GMRES solve
@@ -392,7 +395,8 @@ bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, cons
     const int mo = std::max(2, prm.max_refinements);
     if ((st = outer.init(op, k, mo, true, sizeof(S))) != BG_OK) return st;
     if ((st = inner.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
-    st = fgmres<S>(outer, false, &inner, prm.inner_tol, prm.max_iter, bdof, xdof, prm.tol, mo, &cnt, &relres);
+    st = fgmres<S>(outer, BG_PREC_FP64, &inner, prm.inner_precision, prm.inner_tol, prm.max_iter, bdof, xdof, prm.tol,
+                   mo, &cnt, &relres);
   }
   if (st != BG_OK) return st;
   e = cudaStreamSynchronize(s);
@@ -419,7 +423,9 @@ extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs,
   bg_solve_params prm;
   bg_solve_params_default(&prm);
   if (params) prm = *params;
-  if (prm.tol <= 0 || prm.restart < 1 || prm.max_iter < 1) return set_error(op->ctx, BG_INVALID_ARG, "solve parameters");
+  if (prm.tol <= 0 || prm.restart < 1 || prm.max_iter < 1 || prm.inner_precision < BG_PREC_FP64 ||
+      prm.inner_precision > BG_PREC_FP32)
+    return set_error(op->ctx, BG_INVALID_ARG, "solve parameters");
   cudaSetDevice(op->ctx->device);
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;

@@ -8,9 +8,11 @@ batched solve of all 32 systems to rel. residual 1e-8. The operator is
 assembled once before the timed region (as DiscreteOperator::compute in the
 reference) and reused by every solve.
 
-value:  solves/s = right-hand sides solved to 1e-8 per second, mixed path
-        (FP64 flexible GMRES over the FP64 H2 matrix, inner GMRES with the FP64
-        near field and the FP32 on-the-fly far field), operands in HBM.
+value:  solves/s = right-hand sides solved to 1e-8 per second: FP64 flexible
+        GMRES over the FP64 H2 matrix, preconditioned by an inner GMRES (tol
+        1e-2) on a low-precision operator (--inner fp32: FP32 near field and
+        FP32 on-the-fly far field, default; --inner mixed: FP64 near field),
+        operands in HBM. Every solve meets 1e-8 in the FP64 residual.
 e2e:    the same through the public C ABI with host (pinned) buffers, the
         host->device copy of b and device->host copy of x inside each step.
 Also reported: the plain FP64 GPU solve, H2 matvec/s (FP64 and mixed),
@@ -38,6 +40,9 @@ TOL = 1e-8
 METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed precision)"
 # FP64 GMRES iterations of this workload (restart 200), used by the CPU model
 FP64_ITERS_C2 = 253
+# FP32 FMA throughput of one GB300 measured with an FMA-chain probe (TFLOP/s)
+FP32_FMA_TFLOPS = 75.0
+INNER_DESC = {"mixed": "inner GMRES(FP64 near, FP32 fused far)", "fp32": "inner GMRES(FP32 near, FP32 fused far)"}
 
 
 def workload_config(extra=None):
@@ -45,7 +50,7 @@ def workload_config(extra=None):
            "elements": 6144, "dofs": 6936, "refinement": M, "degree": P, "n_p": NP, "eta": 1.6, "nrhs": NRHS,
            "tol": TOL, "rhs": "point sources |x0|~U[1.5,3], seed 3",
            "l2": "flush: 256 MiB buffer written between timed steps; operator data (near field 175 MB) > L2",
-           "solver": "FGMRES(FP64 H2) + inner GMRES(mixed: FP64 near, FP32 fused far)"}
+           "solver": "FGMRES(FP64 H2) preconditioned by an inner GMRES(1e-2) on a low-precision operator"}
     if extra:
         cfg.update(extra)
     return cfg
@@ -220,13 +225,16 @@ def run_gpu(args):
             dist.barrier()
         return np.array(times), x, stats, prof
 
+    inner = args.inner
+    other = "mixed" if inner == "fp32" else "fp32"
     clocks = ClockSampler(local)
     with clocks:
-        t_mixed, xm, stm, prof = timed_steps("mixed", b_dev_t, args.steps, args.warmup, profile=True)
+        t_mixed, xm, stm, prof = timed_steps(inner, b_dev_t, args.steps, args.warmup, profile=True)
     t_fp64, _, _, _ = timed_steps("fp64", b_dev_t, max(1, min(2, args.steps)), 1)
+    t_other, _, st_other, _ = timed_steps(other, b_dev_t, max(1, min(2, args.steps)), 1)
     # end to end: host pinned b, host x, copies inside the step
     b_pin = torch.from_numpy(np.ascontiguousarray(b_host.T)).pin_memory()
-    t_e2e, xe, _, _ = timed_steps("mixed", b_pin.t(), args.steps, 1)
+    t_e2e, xe, _, _ = timed_steps(inner, b_pin.t(), args.steps, 1)
 
     # matvec throughput (32 RHS per product)
     def mv_rate(prec, reps=5):
@@ -241,7 +249,7 @@ def run_gpu(args):
         e1.record(stream)
         e1.synchronize()
         return reps / (e0.elapsed_time(e1) * 1e-3)
-    mv64, mvmx = mv_rate("fp64"), mv_rate("mixed")
+    mv64, mvmx, mv32 = mv_rate("fp64"), mv_rate("mixed"), mv_rate("fp32")
 
     total_ms = float(t_mixed.sum())
     if dist:
@@ -265,12 +273,13 @@ def run_gpu(args):
 
     if rank != 0:
         return
-    roof = _roofline(op, prof, stm)
+    roof = _roofline(op, prof, stm, args.steps)
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
             "data": "synthetic (seeded point sources, sphere.dat geometry)",
-            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "single gpu"}),
+            "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "single gpu",
+                                       "inner_operator": INNER_DESC[inner]}),
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(N * NRHS * 8),
                     "d2h_bytes_per_step": int(N * NRHS * 8)},
             "gpu_launches": int(prof["launches_total"]) if prof else None,
@@ -279,12 +288,15 @@ def run_gpu(args):
             "fp64_path": {"solves_per_s": fp64_value, "ms_per_step": float(np.mean(t_fp64)),
                           "iterations": st64["iterations"]},
             "mixed_over_fp64": value / world / fp64_value,
+            "other_inner": {"inner": other, "solves_per_s": NRHS / (float(np.mean(t_other)) * 1e-3),
+                            "iterations": st_other["iterations"], "refinements": st_other["refinements"]},
             "solver": {k: stm[k] for k in ("iterations", "refinements", "fp64_matvecs", "low_matvecs",
                                             "final_relres")},
             "accuracy": {"mixed_vs_fp64_solution": rel_vs_fp64, "potential_vs_analytic": pot_err,
                          "fp64_final_relres": st64["final_relres"]},
             "matvec": {"fp64_products_per_s_32rhs": mv64, "mixed_products_per_s_32rhs": mvmx,
-                       "fp64_matvec_per_s": mv64 * NRHS, "mixed_matvec_per_s": mvmx * NRHS},
+                       "fp32_products_per_s_32rhs": mv32, "fp64_matvec_per_s": mv64 * NRHS,
+                       "mixed_matvec_per_s": mvmx * NRHS, "fp32_matvec_per_s": mv32 * NRHS},
             "assembly_s": asm, "kernel_ms": prof["ms"] if prof else None}
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k in ("value", "unit", "cores", "kind",
@@ -306,32 +318,47 @@ def _read_profile(L, ctx):
             "launches_total": sum(ln[i] for i in range(8))}
 
 
-def _roofline(op, prof, stats):
-    """Roofline of the dominant kernel class of the timed solves."""
+def _roofline(op, prof, stats, steps):
+    """Roofline of the dominant kernel class of the timed solves.
+
+    achieved = algorithmic bytes (or flops) of the class over the timed region
+    / its summed CUDA-event time on the library stream (= per launch figure /
+    average launch time)."""
     import json as _j
+    if not prof:
+        return None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = _j.load(open(peaks_path)) if os.path.exists(peaks_path) else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
-    bf16 = peaks.get("bf16_tflops", 1900.0)
-    src = "measured" if peaks else "fallback"
-    if not prof:
-        return None
+    src = "measured (MEASURED_PEAKS.json)" if peaks else "fallback"
     cls = max(prof["ms"], key=lambda k: prof["ms"][k])
     n = max(1, prof["launches"][cls])
-    t = prof["ms"][cls] * 1e-3 / n  # seconds per launch
+    ms = prof["ms"][cls]
+    t = ms * 1e-3 / n  # seconds per launch
     info = op.info()
-    near_bytes = float(info[14])
+    nlow = float(info[4])
+    block_entries = float(info[7]) ** 4  # (n_p^2)^2 couplings per low-rank block
+    base = {"kernel_class": cls, "launches": n, "avg_launch_ms": t * 1e3, "class_ms": ms}
     if cls == "near_fp64":
-        # near-field block-sparse product: dense blocks streamed once per launch
-        algo = near_bytes
+        algo = float(info[14])  # stored FP64 near-field blocks, streamed once per launch
         ach = algo / t / 1e9
-        return {"kernel": "k_bsr (FP64 near-field product, 32 RHS)", "bound": "hbm", "achieved": ach, "peak": hbm,
-                "unit": "GB/s", "frac": ach / hbm, "traffic": None, "peak_source": src,
-                "algorithmic_bytes_per_launch": algo, "avg_launch_ms": t * 1e3,
-                "note": "FP64 FMA-bound at 32 RHS (GB300 FP64 ~1.2 TFLOP/s); bytes = stored near-field blocks"}
-    # fused far field: algorithmic flops = 2 * entries * 32 RHS (GEMM part) per launch (one launch per level)
-    return {"kernel": cls, "bound": "tensor", "achieved": None, "peak": bf16, "unit": "TFLOP/s", "frac": None,
-            "traffic": None, "peak_source": src, "avg_launch_ms": t * 1e3}
+        base.update({"kernel": "k_bsr_pipe (near-field block-sparse product, 32 RHS)", "bound": "hbm",
+                     "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "peak_source": src, "algorithmic_bytes_per_launch": algo})
+        return base
+    if cls == "far_fused_fp32":
+        # 2 flops per coupling entry per right-hand side; one launch per level
+        products = steps * stats["low_matvecs"]
+        flops = products * 2.0 * nlow * block_entries * NRHS
+        ach = flops / (ms * 1e-3) / 1e12
+        base.update({"kernel": "k_far_fused (FP32 couplings generated on the fly + contraction, 32 RHS)",
+                     "bound": "fp32-fma", "achieved": ach, "peak": FP32_FMA_TFLOPS, "unit": "TFLOP/s",
+                     "frac": ach / FP32_FMA_TFLOPS, "traffic": None,
+                     "peak_source": "FP32 FMA throughput probe on this GB300 (CUDA cores; kernel not on tensor cores)",
+                     "algorithmic_flops_per_product": 2.0 * nlow * block_entries * NRHS})
+        return base
+    base.update({"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None})
+    return base
 
 
 def ctypes_void_p():
@@ -351,6 +378,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--inner", default="fp32", choices=["mixed", "fp32"],
+                    help="precision of the inner (preconditioning) operator")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -43,8 +43,11 @@ typedef enum { BG_LAPLACE_SL = 0, BG_HELMHOLTZ_SL = 1, BG_MAXWELL_SL = 2 } bg_op
  * near and far field, the reference's H2Matrix). BG_PREC_MIXED keeps the
  * near-field product, T and the vectors in FP64 and evaluates the far field in
  * FP32: couplings generated on the fly inside the fused product (nothing
- * stored), moments and transfers in FP32. */
-typedef enum { BG_PREC_FP64 = 0, BG_PREC_MIXED = 1 } bg_precision;
+ * stored), moments and transfers in FP32. BG_PREC_FP32 also applies the near
+ * field in FP32 (an FP32 copy of the assembled FP64 blocks); T and the input and
+ * output vectors stay FP64. FP32 is meant for the inner operator of the solver,
+ * whose outer FP64 iteration removes its rounding. */
+typedef enum { BG_PREC_FP64 = 0, BG_PREC_MIXED = 1, BG_PREC_FP32 = 2 } bg_precision;
 
 typedef struct bg_context bg_context;
 typedef struct bg_geometry bg_geometry;
@@ -143,7 +146,7 @@ bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy,
  * work vectors on demand and so may allocate.
  * x, y: device pointers to N scalars of the operator's type (double, or
  * interleaved complex double), aligned to that type, not overlapping.
- * precision: bg_precision. The call returns once y is written.
+ * precision: BG_PREC_FP64 or BG_PREC_MIXED. The call returns once y is written.
  * Intermediate vectors come from one fixed 16 MiB device array in the library
  * (held on every GPU that loads it until the process exits). An operator whose
  * intermediates do not fit is rejected with BG_INVALID_ARG and a message giving

@@ -1,7 +1,8 @@
 """GPU parity against the CPU oracle, through the C ABI.
 
 FP64 path: assembled leaf blocks and the H2 matvec agree with the oracle to
-1e-12 relative (Frobenius / 2-norm). FP32 fused far field: 1e-5 relative.
+1e-12 relative (Frobenius / 2-norm). FP32 fused far field (with the near
+field in FP64 or FP32): 1e-5 relative.
 """
 import numpy as np
 import pytest
@@ -60,8 +61,10 @@ def test_matvec_fp64_and_mixed(ctx, oracle, geo, M, P, kind, kappa, np_):
         A = d.get_discrete_operator()
         y64 = A.matvec(x)
         y32 = A.matvec(x, precision="mixed")
+        yf = A.matvec(x, precision="fp32")
         assert np.linalg.norm(y64 - ref) / np.linalg.norm(ref) < FP64_TOL
         assert np.linalg.norm(y32 - ref) / np.linalg.norm(ref) < FP32_TOL
+        assert np.linalg.norm(yf - ref) / np.linalg.norm(ref) < FP32_TOL
 
 
 def test_matvec_alpha_beta(ctx, oracle):
@@ -97,7 +100,7 @@ def test_potential(ctx, oracle):
         assert np.linalg.norm(got[:, c] - ref) / np.linalg.norm(ref) < FP64_TOL
 
 
-@pytest.mark.parametrize("inner", ["fp64", "mixed"])
+@pytest.mark.parametrize("inner", ["fp64", "mixed", "fp32"])
 def test_solve_reaches_tolerance(ctx, oracle, inner):
     d, o = _pair(ctx, oracle, SPHERE, 3, 1, 0, 0.0, 6)
     x0 = np.array([[0.0, 0.2, 1.8], [1.0, 1.5, -1.2], [-2.0, 0.3, 0.1]])
