@@ -268,6 +268,21 @@ static bg_status upload_tables(bg_operator* op) {
   BG_CHECK(op->d_tr64.upload(tr, s), "upload transfer");
   std::vector<float> tf(tr.begin(), tr.end());
   BG_CHECK(op->d_tr32.upload(tf, s), "upload transfer");
+  {
+    // every row of every far-field level, rows with more blocks first so the
+    // longest CTAs start in the first wave
+    std::vector<std::pair<int, int2>> items;
+    for (int l = 0; l < (int)op->far.size() && l < kMaxFarLevels; ++l)
+      for (int r = 0; r < op->far[l].nrows; ++r)
+        items.push_back({op->far[l].row_ptr[r + 1] - op->far[l].row_ptr[r], make_int2(l, r)});
+    std::stable_sort(items.begin(), items.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    std::vector<int2> work(items.size());
+    for (size_t i = 0; i < items.size(); ++i) work[i] = items[i].second;
+    BG_CHECK(op->d_far_work.upload(work, s), "far-field work list");
+    op->n_far_work = (int)work.size();
+  }
+  BG_CHECK(op->d_err.alloc(sizeof(int)), "error flag");
+  BG_CHECK(cudaMemsetAsync(op->d_err.p, 0, sizeof(int), s), "error flag");
   BG_CHECK(cudaStreamSynchronize(s), "upload tables");
   return BG_OK;
 }
@@ -673,7 +688,24 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                  "forward transfer");
       }
     }
-    for (int l = 0; l <= op->leaf_level; ++l) {
+    const bool tc = mixed && op->vd == 1 && op->nc == 1 && op->leaf_level < kMaxFarLevels &&
+                    far_tc_supported(op->cplx, np2, nrhs);
+    if (tc) {
+      // all levels in one tensor-core launch; it writes every row of Z
+      FarTcLevels L{};
+      for (int l = 0; l <= op->leaf_level; ++l) {
+        L.row_ptr[l] = op->far[l].d_row_ptr.as<int>();
+        L.col[l] = op->far[l].d_col.as<int>();
+        L.pts[l] = op->d_pts32[l]->as<float4>();
+        L.cen[l] = op->d_centres[l]->as<d4>();
+        L.y[l] = static_cast<const float*>(op->w_y[l]->p);
+        L.z[l] = static_cast<float*>(op->w_z[l]->p);
+      }
+      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_tc(L, op->d_far_work.as<int2>(), op->n_far_work, np2, nrhs,
+                                                                      op->d_err.as<int>(), s); }),
+               "far-field product (tensor cores)");
+    }
+    for (int l = 0; l <= op->leaf_level && !tc; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
         BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)f.nrows * f.B * nrhs * sfar, s), "far field");
@@ -716,6 +748,18 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                             op->w_yss.p, ydof, nrhs, s); }),
            "T^T y");
   return BG_OK;
+}
+
+// Reads (and clears) the flag a kernel sets when one of its bounded waits ran
+// out; call after the stream has been synchronised.
+bg_status check_device_flag(bg_operator* op) {
+  if (!op->d_err.p) return BG_OK;
+  int code = 0;
+  BG_CHECK(cudaMemcpy(&code, op->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "error flag");
+  if (code == 0) return BG_OK;
+  BG_CHECK(cudaMemset(op->d_err.p, 0, sizeof(int)), "error flag");
+  return set_error(op->ctx, BG_TIMEOUT,
+                   "a bounded wait of the tensor-core far-field kernel ran out (code " + std::to_string(code) + ")");
 }
 
 static bg_status stage_host(bg_context* ctx, DevBuf* buf, const void* host, long ld, long rows, int ncols, size_t esz,
@@ -769,5 +813,5 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
                "device to host copy");
   }
   BG_CHECK(cudaStreamSynchronize(s), "H2 matvec");
-  return BG_OK;
+  return check_device_flag(op);
 }

@@ -1,0 +1,426 @@
+// Far-field product on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// For every target cluster row i of every FMM level:
+//   Z_i = sum_j F_ij Y_j,  F_ij[m][k] = |J(x_m)| |J(y_k)| / (4 pi |x_m - y_k|)
+// (H2Multipole.hpp:336-375 for the couplings, H2DenseProduct.hpp:88-121 for
+// the product), with F_ij generated on the fly in FP32 and never stored.
+//
+// One CTA per (level, row) from a work list sorted by block count, all levels
+// in one launch. Warp roles: 16 generator warps and one MMA warp.
+//  - Generators write the n_p^2 x n_p^2 coupling tile of each far-field block
+//    straight into shared memory in the UMMA K-major no-swizzle core-matrix
+//    layout (8 rows x 16 bytes per core matrix, core matrices contiguous along
+//    K), split into a TF32 high part and an FP32 remainder; Y_j (staged one
+//    block ahead with cp.async) is split the same way. Point arrays are padded
+//    with distant zero-weight points, so the padded rows and columns of a tile
+//    come out as exact zeros without branches.
+//  - The MMA warp issues tcgen05.mma kind::tf32 (M = 128, N = 32, K = 8) for
+//    hi*hi and, into a second accumulator, hi*lo + lo*hi, which keeps about 21
+//    bits of every product.
+//  - The tensor core's FP32 accumulation is not round-to-nearest, so chains
+//    are kept short: every block starts fresh tensor-memory accumulators (two
+//    buffers alternate) and the generators fold each finished block into
+//    per-row register sums with Neumaier compensation (each thread owns 8 of
+//    the 32 columns of one row) while later blocks run.
+// Two shared-memory stages let the generation of block k+1 overlap the MMAs
+// of block k; mbarriers hand stages between the roles (full: all generator
+// threads arrive; done: tcgen05.commit). Every wait is bounded: on timeout the
+// kernel records an error code, waits (bounded) for its MMAs, frees its tensor
+// memory and returns.
+#include <cstdint>
+
+#include "bg_kernels.cuh"
+
+namespace bg {
+
+namespace {
+
+constexpr int kGenWarps = 16;                 // warps generating the tiles
+constexpr int kGenThreads = 32 * kGenWarps;   // the MMA warp follows them
+constexpr int kThreads = kGenThreads + 32;
+constexpr int kN = 32;                        // MMA N: right-hand sides per tile
+constexpr int kYStride = 40;                  // floats per staged Y_j row (conflict-free reads)
+// FP32 accumulators: 2 buffers x {hi*hi, hi*lo + lo*hi} x 32 columns
+constexpr uint32_t kTmemCols = 128;
+constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
+constexpr float kFar = 1.0e18f;                  // padding points: finite r^2 (< 1.2e37), weight 0
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// K-major, no swizzle: LBO = byte distance of core matrices adjacent in K,
+// SBO = byte distance of core matrices adjacent in M (or N); version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;  // base offset 0, relative LBO, layout SWIZZLE_NONE
+}
+
+// kind::tf32 instruction descriptor: D FP32, A and B TF32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// round to the nearest TF32 value (10 explicit mantissa bits), ties away
+__device__ __forceinline__ float tf32_hi(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+
+__device__ __forceinline__ void gen_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(kGenThreads) : "memory"); }
+
+// 32 lanes x 8 consecutive FP32 columns of tensor memory, one lane per thread
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void neumaier(float& sum, float& comp, float v) {
+  const float t = sum + v;
+  comp += fabsf(sum) >= fabsf(v) ? (sum - t) + v : (v - t) + sum;
+  sum = t;
+}
+
+// Generator warp w owns tensor-memory lanes 32 (w % 4) .. +31 (the lanes its
+// warp may access) and columns 8 (w / 4) .. +7: fold accumulator buffer buf
+// (one finished block) into its row sums.
+__device__ __forceinline__ void drain_block(uint32_t tmem, int warp, int buf, float* sum, float* comp) {
+  float hh[8], cr[8];
+  const uint32_t base = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(64 * buf + 8 * (warp >> 2));
+  tmem_ld8(base, hh);
+  tmem_ld8(base + 32, cr);
+#pragma unroll
+  for (int n = 0; n < 8; ++n) neumaier(sum[n], comp[n], hh[n] + cr[n]);
+}
+
+// Compile-time tile geometry and shared-memory plan (bytes) for n_p^2 = NP2.
+// An A tile holds MG row groups of 8; the tensor core also reads row groups
+// MG..15 (rows beyond n_p^2, whose results are discarded), which land in the
+// following buffers or the tail, always inside the allocation (TOTAL >= NEED).
+template <int NP2>
+struct TcShape {
+  static constexpr int KP = (NP2 + 7) / 8 * 8;  // K padded to the MMA K step
+  static constexpr int KC = KP / 4;             // 16-byte core-matrix columns along K
+  static constexpr int MG = (NP2 + 7) / 8;      // 8-row groups holding the targets
+  static constexpr uint32_t SBO = KC * 128;
+  static constexpr uint32_t A_BYTES = MG * SBO, B_BYTES = 4 * SBO;
+  static constexpr uint32_t STAGE = 2 * A_BYTES + 2 * B_BYTES, TILES = 2 * STAGE;
+  static constexpr uint32_t NEED = STAGE + A_BYTES + 16 * SBO;
+  static constexpr int NPRS = (MG + 1) * 8;     // padded target points (one spare group)
+  static constexpr uint32_t PTS_OFF = TILES;    // prs [NPRS], pcs [2][KP]
+  static constexpr uint32_t YS_OFF = PTS_OFF + (NPRS + 2 * KP) * 16;
+  static constexpr uint32_t END = YS_OFF + 2 * KP * kYStride * 4;
+  static constexpr uint32_t TOTAL = END > NEED ? END : NEED;
+};
+
+}  // namespace
+
+template <int NP2>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_far_tc(FarTcLevels L, const int2* __restrict__ work, int nrhs, int* __restrict__ err) {
+  using G = TcShape<NP2>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full_bar[2], done_bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int2 w = work[blockIdx.x];
+  const int lev = w.x, row = w.y;
+  const int* row_ptr = L.row_ptr[lev];
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  float* z = L.z[lev];
+  if (kb == ke) {  // no far-field block in this row (uniform over the CTA)
+    for (int e = tid; e < NP2 * nrhs; e += kThreads) z[(long)row * NP2 * nrhs + e] = 0.0f;
+    return;
+  }
+  const int* col = L.col[lev];
+  const float4* pts = L.pts[lev];
+  const d4* cen = L.cen[lev];
+  const float* y = L.y[lev];
+  float4* prs = reinterpret_cast<float4*>(smem + G::PTS_OFF);
+  float4* pcs = prs + G::NPRS;                             // [2][KP]
+  float* ys = reinterpret_cast<float*>(smem + G::YS_OFF);  // [2][KP][kYStride]
+  const int nblk = ke - kb;
+
+  // stage the source points and Y_j of block column c2 into stage st
+  auto issue_stage = [&](int st, int c2) {
+    float4* pd = pcs + st * G::KP;
+    for (int t = tid; t < NP2; t += kGenThreads) cp_async16(&pd[t], &pts[(long)c2 * NP2 + t]);
+    float* yd = ys + st * G::KP * kYStride;
+    const float* src = y + (long)c2 * NP2 * nrhs;
+    if (nrhs == kN) {
+      for (int t = tid; t < NP2 * (kN / 4); t += kGenThreads) {
+        const int k = t >> 3, q = t & 7;
+        cp_async16(yd + k * kYStride + 4 * q, src + k * kN + 4 * q);
+      }
+    } else {
+      for (int t = tid; t < NP2 * nrhs; t += kGenThreads) {
+        const int k = t / nrhs, n = t - k * nrhs;
+        cp_async4(yd + k * kYStride + n, src + t);
+      }
+    }
+  };
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    mbar_init(&full_bar[0], kGenThreads);
+    mbar_init(&full_bar[1], kGenThreads);
+    mbar_init(&done_bar[0], 1);
+    mbar_init(&done_bar[1], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (tid < kGenThreads) {
+    // padded points, and the zero padding of the Y staging (never copied into)
+    for (int t = tid; t < G::NPRS; t += kGenThreads)
+      prs[t] = t < NP2 ? pts[(long)row * NP2 + t] : make_float4(kFar, kFar, kFar, 0.0f);
+    if constexpr (G::KP > NP2) {
+      constexpr int PAD = G::KP - NP2;
+      for (int t = tid; t < 2 * PAD; t += kGenThreads)
+        pcs[(t / PAD) * G::KP + NP2 + t % PAD] = make_float4(-kFar, -kFar, -kFar, 0.0f);
+    }
+    for (int t = tid; t < 2 * G::KP * kYStride; t += kGenThreads) {
+      const int k = (t / kYStride) % G::KP, n = t % kYStride;
+      if (k >= NP2 || n >= nrhs) ys[t] = 0.0f;
+    }
+    issue_stage(0, col[kb]);
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();  // the only CTA-wide barrier: the MMA warp leaves after its loop
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == kGenWarps) {
+    // ---- MMA warp: one thread issues every tensor-core instruction ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(128, kN);
+      const uint32_t base = smem_u32(smem);
+      for (int it = 0; it < nblk; ++it) {
+        const int s = it & 1;
+        if (!mbar_wait(&full_bar[s], (uint32_t)((it >> 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 3);
+          break;
+        }
+        if (*abort_v) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t a0 = base + s * G::STAGE, a1 = a0 + G::A_BYTES;
+        const uint32_t b0 = a0 + 2 * G::A_BYTES, b1 = b0 + G::B_BYTES;
+        const uint32_t d_hh = tmem + (uint32_t)(64 * s), d_cr = d_hh + 32;
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) {
+          uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
+          uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
+          const uint32_t dd = pass == 0 ? d_hh : d_cr;
+#pragma unroll
+          for (int ks = 0; ks < G::KP / 8; ++ks) {
+            mma_tf32(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
+            ad += 16;  // next K step: 256 bytes, in 16-byte units of the start-address field
+            bd += 16;
+          }
+        }
+        mma_commit(&done_bar[s]);
+      }
+    }
+    return;
+  }
+
+  // ---- generator warps ----
+  float sum[8], comp[8];  // this thread's row (lane) and 8 of the 32 columns
+#pragma unroll
+  for (int n = 0; n < 8; ++n) sum[n] = comp[n] = 0.0f;
+  const d4 crow = cen[row];
+  constexpr int AU = G::MG * G::KC, BU = 4 * G::KC;  // core matrices of A and B
+  const int a_begin = (warp * AU) / kGenWarps, a_end = ((warp + 1) * AU) / kGenWarps;
+  const int b_begin = (warp * BU) / kGenWarps, b_end = ((warp + 1) * BU) / kGenWarps;
+  int it = 0;
+  bool aborted = false;
+  for (; it < nblk; ++it) {
+    const int s = it & 1, k = kb + it;
+    if (tid == 0 && it >= 2 && !mbar_wait(&done_bar[s], (uint32_t)(((it >> 1) - 1) & 1))) {
+      *abort_v = 1;
+      atomicExch(err, 1);
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    gen_sync();  // stage s and accumulator buffer s free; block k staged; abort flag visible
+    if (*abort_v) {
+      aborted = true;
+      break;
+    }
+    if (it >= 2) {  // block it-2 is complete: fold buffer s into the row sums
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      drain_block(tmem, warp, s, sum, comp);
+    }
+    if (it + 1 < nblk) issue_stage(s ^ 1, col[k + 1]);
+    asm volatile("cp.async.commit_group;\n" ::);
+    float* ahi = reinterpret_cast<float*>(smem + s * G::STAGE);
+    float* alo = ahi + G::A_BYTES / 4;
+    float* bhi = ahi + 2 * (G::A_BYTES / 4);
+    float* blo = bhi + G::B_BYTES / 4;
+    // B = Y_j^T (N x K, K-major): core matrix cm = ng * KC + kg, lane = 4 (n % 8) + kk % 4
+    {
+      const float* yst = ys + s * G::KP * kYStride + (lane & 3) * kYStride + (lane >> 2);
+#pragma unroll 2
+      for (int cm = b_begin; cm < b_end; ++cm) {
+        const int ng = cm / G::KC, kg = cm - ng * G::KC;
+        const float v = yst[kg * 4 * kYStride + ng * 8];
+        const float h = tf32_hi(v);
+        bhi[cm * 32 + lane] = h;
+        blo[cm * 32 + lane] = v - h;
+      }
+    }
+    // A = F_ij (M x K, K-major): core matrix cm = mg * KC + kg, lane = 4 (m % 8) + kk % 4
+    {
+      const float4* pc = pcs + s * G::KP + (lane & 3);
+      const d4 ccol = cen[col[k]];
+      const float dcx = (float)(crow.x - ccol.x), dcy = (float)(crow.y - ccol.y), dcz = (float)(crow.z - ccol.z);
+      int cm = a_begin;
+      int mg = cm / G::KC, kg = cm - mg * G::KC;
+      float4 xi = prs[mg * 8 + (lane >> 2)];
+      float x0 = dcx + xi.x, x1 = dcy + xi.y, x2 = dcz + xi.z, wm = xi.w * 0.0795774715f;
+      float* ph = ahi + cm * 32 + lane;
+      float* pl = alo + cm * 32 + lane;
+#pragma unroll 4
+      for (; cm < a_end; ++cm) {
+        const float4 yj = pc[kg * 4];
+        const float d0 = x0 - yj.x, d1 = x1 - yj.y, d2 = x2 - yj.z;
+        const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+        const float f = rsqrtf(r2) * (wm * yj.w);
+        const float h = tf32_hi(f);
+        *ph = h;
+        *pl = f - h;
+        ph += 32;
+        pl += 32;
+        if (++kg == G::KC) {  // next row group (the spare padded group after the last)
+          kg = 0;
+          ++mg;
+          xi = prs[mg * 8 + (lane >> 2)];
+          x0 = dcx + xi.x;
+          x1 = dcy + xi.y;
+          x2 = dcz + xi.z;
+          wm = xi.w * 0.0795774715f;
+        }
+      }
+    }
+    // publish stage s to the tensor core: every generator thread arrives
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    mbar_arrive(&full_bar[s]);
+  }
+  // wait for the tensor core: the last block's commit covers every earlier MMA
+  if (tid == 0 && it > 0) {
+    const int last = it - 1;
+    if (!mbar_wait(&done_bar[last & 1], (uint32_t)((last >> 1) & 1))) {
+      *abort_v = 1;
+      atomicExch(err, 2);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  gen_sync();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (!aborted && !*abort_v) {
+    // blocks not folded in the loop: nblk-2 (if any) and nblk-1
+    for (int b = nblk >= 2 ? nblk - 2 : 0; b < nblk; ++b) drain_block(tmem, warp, b & 1, sum, comp);
+    const int m = (warp & 3) * 32 + lane, c0 = 8 * (warp >> 2);
+    if (m < NP2) {
+      float* zo = z + ((long)row * NP2 + m) * nrhs + c0;
+#pragma unroll
+      for (int n = 0; n < 8; ++n)
+        if (c0 + n < nrhs) zo[n] = sum[n] + comp[n];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  gen_sync();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+}
+
+template <int NP2>
+static cudaError_t launch_np(const FarTcLevels& L, const int2* work, int nwork, int nrhs, int* err, cudaStream_t s) {
+  constexpr uint32_t smem = TcShape<NP2>::TOTAL;
+  static_assert(smem <= 227 * 1024, "tensor-core far field: shared memory plan too large");
+  cudaError_t e = cudaFuncSetAttribute(k_far_tc<NP2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_far_tc<NP2><<<nwork, kThreads, smem, s>>>(L, work, nrhs, err);
+  return cudaGetLastError();
+}
+
+bool far_tc_supported(bool cplx, int np2, int nrhs) {
+  const bool shape = np2 == 4 || np2 == 9 || np2 == 16 || np2 == 25 || np2 == 36 || np2 == 49 || np2 == 64 || np2 == 81;
+  return !cplx && shape && nrhs >= 1 && nrhs <= kN;
+}
+
+cudaError_t launch_far_tc(const FarTcLevels& L, const int2* work, int nwork, int np2, int nrhs, int* err,
+                          cudaStream_t s) {
+  if (nwork == 0) return cudaSuccess;
+  if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
+  switch (np2) {
+    case 4: return launch_np<4>(L, work, nwork, nrhs, err, s);
+    case 9: return launch_np<9>(L, work, nwork, nrhs, err, s);
+    case 16: return launch_np<16>(L, work, nwork, nrhs, err, s);
+    case 25: return launch_np<25>(L, work, nwork, nrhs, err, s);
+    case 36: return launch_np<36>(L, work, nwork, nrhs, err, s);
+    case 49: return launch_np<49>(L, work, nwork, nrhs, err, s);
+    case 64: return launch_np<64>(L, work, nwork, nrhs, err, s);
+    case 81: return launch_np<81>(L, work, nwork, nrhs, err, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace bg

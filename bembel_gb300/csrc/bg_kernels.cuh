@@ -64,6 +64,24 @@ cudaError_t launch_transfer_bwd(int S, const void* T, int np2, int nc, int npare
 // fused FP32 far field: for each listed block, generate the coupling from
 // cluster points on the fly and accumulate into the row cluster's output
 // (points are FP32 offsets from the FP64 cluster centres)
+// Per-level tables of the tensor-core far-field product (one launch for all
+// FMM levels). y/z: FP32 coefficient blocks [cluster][n_p^2][nrhs].
+constexpr int kMaxFarLevels = 12;
+struct FarTcLevels {
+  const int* row_ptr[kMaxFarLevels];
+  const int* col[kMaxFarLevels];
+  const float4* pts[kMaxFarLevels];
+  const d4* cen[kMaxFarLevels];
+  const float* y[kMaxFarLevels];
+  float* z[kMaxFarLevels];
+};
+// real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32
+bool far_tc_supported(bool cplx, int np2, int nrhs);
+
+// work: (level, row) per CTA, every row of every level in L exactly once;
+// err: set to a nonzero code if a bounded wait of the kernel ran out
+cudaError_t launch_far_tc(const FarTcLevels& L, const int2* work, int nwork, int np2, int nrhs, int* err,
+                          cudaStream_t s);
 cudaError_t launch_far_fused(bool cplx, const float4* pts, const d4* centres, const int* row_ptr, const int* col,
                              int nrows, int np2, float kre, float kim, const void* y, void* z, int nrhs, cudaStream_t s);
 // user column-major block (ld) <-> row-major work vector, with precision change

@@ -150,6 +150,10 @@ struct bg_operator {
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
+  // tensor-core far field: (level, row) work list, heaviest rows first
+  DevBuf d_far_work;
+  int n_far_work = 0;
+  DevBuf d_err;  // int: nonzero after a bounded device wait ran out
   // work vectors (sized for the largest nrhs seen)
   int cap = 0;
   DevBuf w_xdof, w_xss, w_yss, w_ydof, w_xss32, w_yss32;
@@ -175,6 +179,7 @@ void context_retain(bg_context* ctx);
 void context_release(bg_context* ctx);
 bg_status cuda_status(bg_context* ctx, cudaError_t e, const char* what);
 bg_status ensure_work(bg_operator* op, int nrhs);
+bg_status check_device_flag(bg_operator* op);
 // y_dof = A x_dof on row-major FP64 work vectors. prec (bg_precision):
 // BG_PREC_FP64 the FP64 H2 matrix (stored far field); BG_PREC_MIXED FP64 near
 // field plus the FP32 fused far field (forward/backward transforms in FP32);

@@ -479,5 +479,6 @@ extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs,
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve");
   if (stats) *stats = total;
-  return result;
+  const bg_status flag = check_device_flag(op);
+  return flag != BG_OK ? flag : result;
 }

@@ -371,6 +371,31 @@ def ctypes_byref(x):
     return ctypes.byref(x)
 
 
+def run_profile_case(args):
+    """Small fixed cases for ncu (not a bench line): 'matvec' assembles the
+    workload's operator without the stored FP64 far field and applies five
+    32-column products at --precision; 'solve' runs one batched solve with the
+    chosen inner operator."""
+    import torch
+    import bembel_gb300 as bg
+    ctx = bg.Context(0)
+    store = args.profile == "solve"
+    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), M, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
+                             store_fp64_far=store)
+    op.compute()
+    A = op.get_discrete_operator()
+    if args.profile == "matvec":
+        x = torch.randn(op.N, NRHS, dtype=torch.float64, device="cuda")
+        for _ in range(5):
+            A.matvec(x, precision=args.precision)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "matvec", "precision": args.precision, "N": op.N, "products": 5}))
+    else:
+        b = op.load_vector(0, rhs_points())
+        _, st = A.solve(b, tol=TOL, inner=args.inner, inner_tol=1e-2, restart=200, max_refinements=12)
+        print(json.dumps({"profile": "solve", "inner": args.inner, "N": op.N, "stats": st}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,8 +405,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--inner", default="fp32", choices=["mixed", "fp32"],
                     help="precision of the inner (preconditioning) operator")
+    ap.add_argument("--profile", choices=["matvec", "solve"], default=None,
+                    help="run a small fixed case for ncu instead of the benchmark")
+    ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
+                    help="product precision of --profile matvec")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
