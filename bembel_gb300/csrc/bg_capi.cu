@@ -269,6 +269,43 @@ static bg_status upload_tables(bg_operator* op) {
   std::vector<float> tf(tr.begin(), tr.end());
   BG_CHECK(op->d_tr32.upload(tf, s), "upload transfer");
   {
+    // transposed, padded copies for launch_tgemm: AT[q][i] = op(A)[i][q]
+    const int R = op->R, Bq = op->Bq, np2 = op->np * op->np;
+    auto ld_for = [](int Mo) { const int r = (Mo + 2) / 3 * 3; return (r + 3) / 4 * 4; };
+    auto build = [&](int Mo, int Ki, auto opA, DevBuf* d64, DevBuf* d32, TGemmA* a64, TGemmA* a32) -> bg_status {
+      const int ld = ld_for(Mo);
+      std::vector<double> at((size_t)Ki * ld, 0.0);
+      for (int q = 0; q < Ki; ++q)
+        for (int i = 0; i < Mo; ++i) at[(size_t)q * ld + i] = opA(i, q);
+      std::vector<float> af(at.begin(), at.end());
+      BG_CHECK(d64->upload(at, s), "upload transforms");
+      BG_CHECK(d32->upload(af, s), "upload transforms");
+      *a64 = TGemmA{d64->p, ld, Mo, Ki};
+      *a32 = TGemmA{d32->p, ld, Mo, Ki};
+      return BG_OK;
+    };
+    bg_status st;
+    for (size_t c = 0; c < mom.size() && c < 2; ++c) {
+      const std::vector<double>& m = mom[c];  // R x Bq, row-major
+      if ((st = build(R, Bq, [&](int i, int q) { return m[(size_t)i * Bq + q]; }, &op->tm[0].mom_f[c],
+                      &op->tm[1].mom_f[c], &op->tm[0].a_mom_f[c], &op->tm[1].a_mom_f[c])) != BG_OK)
+        return st;
+      if ((st = build(Bq, R, [&](int i, int q) { return m[(size_t)q * Bq + i]; }, &op->tm[0].mom_b[c],
+                      &op->tm[1].mom_b[c], &op->tm[0].a_mom_b[c], &op->tm[1].a_mom_b[c])) != BG_OK)
+        return st;
+    }
+    // transfer matrix np2 x 4 np2, row-major
+    if ((st = build(np2, 4 * np2, [&](int i, int q) { return tr[(size_t)i * 4 * np2 + q]; }, &op->tm[0].tr_f,
+                    &op->tm[1].tr_f, &op->tm[0].a_tr_f, &op->tm[1].a_tr_f)) != BG_OK)
+      return st;
+    if ((st = build(4 * np2, np2, [&](int i, int q) { return tr[(size_t)q * 4 * np2 + i]; }, &op->tm[0].tr_b,
+                    &op->tm[1].tr_b, &op->tm[0].a_tr_b, &op->tm[1].a_tr_b)) != BG_OK)
+      return st;
+    // every output row tile count within the kernel's 4 x 256 tiles of 3 x 4
+    auto fits = [&](int Mo) { return (Mo + 2) / 3 * 8 <= 4 * 256; };
+    op->use_tgemm = op->nc == 1 && mom.size() <= 2 && fits(R) && fits(Bq) && fits(np2) && fits(4 * np2);
+  }
+  {
     // every row of every far-field level, rows with more blocks first so the
     // longest CTAs start in the first wave
     std::vector<std::pair<int, int2>> items;
@@ -673,18 +710,23 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
       yfar = op->w_yss32.p;
     }
     const int Ll = op->leaf_level;
+    const bg_operator::TransformMats& tm = op->tm[mixed ? 1 : 0];
     for (int c = 0; c < op->vd; ++c) {
       const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
-      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_moment_fwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl,
-                                 static_cast<const char*>(xfar) + c * comp_ss * nrhs * sfar,
-                                 static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar,
-                                 nrhs, s); }),
+      const char* xc = static_cast<const char*>(xfar) + c * comp_ss * nrhs * sfar;
+      char* yl = static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                 return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_mom_f[c], xc, op->Bq, yl, op->R, op->nleaf_cl, nrhs, s)
+                                      : launch_moment_fwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl, xc, yl, nrhs, s); }),
                "forward moments");
       for (int l = Ll - 1; l >= 0; --l) {
         const int ncl = op->nclusters(l);
-        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
-                                     static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar,
-                                     static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar, nrhs, s); }),
+        const char* ych = static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar;
+        char* ypa = static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, ych, 4L * op->R, ypa, op->R, ncl, nrhs, s)
+                                        : launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                                              ych, ypa, nrhs, s); }),
                  "forward transfer");
       }
     }
@@ -727,16 +769,20 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     for (int c = 0; c < op->vd; ++c) {
       for (int l = 0; l < Ll; ++l) {
         const int ncl = op->nclusters(l);
-        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
-                                     static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar,
-                                     static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar,
-                                     nrhs, s); }),
+        const char* zpa = static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;
+        char* zch = static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar;
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, zpa, op->R, zch, 4L * op->R, ncl, nrhs, s)
+                                        : launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
+                                                              zpa, zch, nrhs, s); }),
                  "backward transfer");
       }
       const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
-      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_moment_bwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl,
-                                 static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar,
-                                 static_cast<char*>(yfar) + c * comp_ss * nrhs * sfar, nrhs, s); }),
+      const char* zl = static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
+      char* yc = static_cast<char*>(yfar) + c * comp_ss * nrhs * sfar;
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                 return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_mom_b[c], zl, op->R, yc, op->Bq, op->nleaf_cl, nrhs, s)
+                                      : launch_moment_bwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl, zl, yc, nrhs, s); }),
                "backward moments");
     }
     if (mixed && !near32)

@@ -125,6 +125,14 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 1/sqrt(x) by the hardware approximation (relative error below 2^-22); x is
+// a squared distance of admissible clusters or a padding value, never subnormal
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;\n" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ void neumaier(float& sum, float& comp, float v) {
   const float t = sum + v;
   comp += fabsf(sum) >= fabsf(v) ? (sum - t) + v : (v - t) + sum;
@@ -330,32 +338,31 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float4* pc = pcs + s * G::KP + (lane & 3);
       const d4 ccol = cen[col[k]];
       const float dcx = (float)(crow.x - ccol.x), dcy = (float)(crow.y - ccol.y), dcz = (float)(crow.z - ccol.z);
+      // this warp's core matrices [a_begin, a_end) as segments of whole or
+      // partial row groups
       int cm = a_begin;
       int mg = cm / G::KC, kg = cm - mg * G::KC;
-      float4 xi = prs[mg * 8 + (lane >> 2)];
-      float x0 = dcx + xi.x, x1 = dcy + xi.y, x2 = dcz + xi.z, wm = xi.w * 0.0795774715f;
-      float* ph = ahi + cm * 32 + lane;
-      float* pl = alo + cm * 32 + lane;
+      while (cm < a_end) {
+        const float4 xi = prs[mg * 8 + (lane >> 2)];
+        const float x0 = dcx + xi.x, x1 = dcy + xi.y, x2 = dcz + xi.z, wm = xi.w * 0.0795774715f;
+        const int kend = min(G::KC, kg + (a_end - cm));
+        float* ph = ahi + cm * 32 + lane;
+        float* pl = alo + cm * 32 + lane;
+        const float4* py = pc + kg * 4;
+        const int cnt = kend - kg;
 #pragma unroll 4
-      for (; cm < a_end; ++cm) {
-        const float4 yj = pc[kg * 4];
-        const float d0 = x0 - yj.x, d1 = x1 - yj.y, d2 = x2 - yj.z;
-        const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
-        const float f = rsqrtf(r2) * (wm * yj.w);
-        const float h = tf32_hi(f);
-        *ph = h;
-        *pl = f - h;
-        ph += 32;
-        pl += 32;
-        if (++kg == G::KC) {  // next row group (the spare padded group after the last)
-          kg = 0;
-          ++mg;
-          xi = prs[mg * 8 + (lane >> 2)];
-          x0 = dcx + xi.x;
-          x1 = dcy + xi.y;
-          x2 = dcz + xi.z;
-          wm = xi.w * 0.0795774715f;
+        for (int q = 0; q < cnt; ++q) {
+          const float4 yj = py[4 * q];
+          const float d0 = x0 - yj.x, d1 = x1 - yj.y, d2 = x2 - yj.z;
+          const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+          const float f = rsqrt_approx(r2) * (wm * yj.w);
+          const float h = tf32_hi(f);
+          ph[32 * q] = h;
+          pl[32 * q] = f - h;
         }
+        cm += cnt;
+        kg = 0;
+        ++mg;
       }
     }
     // publish stage s to the tensor core: every generator thread arrives

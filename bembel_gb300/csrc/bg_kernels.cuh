@@ -89,6 +89,16 @@ cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int r
                              cudaStream_t s);
 cudaError_t launch_scatter_out(int Swork, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
                                const double* beta, cudaStream_t s);
+// op(A) of an FMM transform, stored transposed: AT[q][i], q < Ki, i < ld
+// (ld a multiple of 4, at least Mo rounded up to 3, zero beyond Mo)
+struct TGemmA {
+  const void* at;
+  int ld, Mo, Ki;
+};
+// C[b] (=, += if acc) op(A) B[b] for nbatch items; B[b] = B + b * bstride_rows
+// rows of the vector type S (bg stype), C likewise; nrhs columns
+cudaError_t launch_tgemm(int S, bool acc, const TGemmA& A, const void* B, long bstride_rows, void* C,
+                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s);
 // FP32 / complex-FP32 blocks; same layout rules as launch_bsr_fp64
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
                             int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);

@@ -406,6 +406,143 @@ static cudaError_t bgemm(bool ta, bool acc, const T* A, int Mo, int Ki, const T*
   return cudaErrorInvalidValue;
 }
 
+// FMM transforms as batched GEMMs with one shared matrix:
+//   C[b] (=, +=) op(A) B[b]   (op(A): Mo x Ki; B[b]: Ki x kk; C[b]: Mo x kk)
+// op(A) is given transposed and padded, AT[q][i] with row length ld (a
+// multiple of 4 and at least Mo rounded up to 3, zero beyond Mo), so its
+// chunks stage with coalesced 16-byte cp.async. One CTA per batch item and 32
+// columns; K is staged 16 rows at a time, double-buffered; each thread owns up
+// to 4 tiles of 3 rows x 4 columns.
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T* v) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    const double2 q0 = *reinterpret_cast<const double2*>(p), q1 = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+  }
+}
+
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(256) k_tgemm(const T* __restrict__ AT, int ld, int Mo, int Ki,
+                                               const T* __restrict__ B, long bstride, T* __restrict__ C, long cstride,
+                                               int kk, int vec_b) {
+  constexpr int KC = 16, RT = 3, CT = 4, NCOL = 32, MAXT = 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);  // [2][KC][ld]
+  T* Bs = As + 2 * KC * ld;                // [2][KC][NCOL]
+  const int b = blockIdx.x, cbase = NCOL * blockIdx.y;
+  const int ncol = min(NCOL, kk - cbase);
+  const T* Bb = B + (long)b * bstride + cbase;
+  const int tid = threadIdx.x;
+  // columns beyond ncol are never copied into: zero them once in both buffers
+  if (ncol < NCOL)
+    for (int t = tid; t < 2 * KC * NCOL; t += blockDim.x)
+      if ((t % NCOL) >= ncol) Bs[t] = (T)0;
+  auto stage = [&](int q0, int buf) {
+    const int qn = min(KC, Ki - q0);
+    const unsigned char* asrc = reinterpret_cast<const unsigned char*>(AT + (long)q0 * ld);
+    unsigned char* adst = reinterpret_cast<unsigned char*>(As + buf * KC * ld);
+    const int abytes = qn * ld * (int)sizeof(T);
+    for (int o = 16 * tid; o < abytes; o += 16 * blockDim.x) cp_async16(adst + o, asrc + o);
+    T* bdst = Bs + buf * KC * NCOL;
+    if (vec_b) {
+      const int per_row = ncol * (int)sizeof(T) / 16;
+      for (int t = tid; t < qn * per_row; t += blockDim.x) {
+        const int q = t / per_row, v = t - q * per_row;
+        cp_async16(reinterpret_cast<unsigned char*>(bdst + q * NCOL) + 16 * v,
+                   reinterpret_cast<const unsigned char*>(Bb + (long)(q0 + q) * kk) + 16 * v);
+      }
+    } else {
+      for (int t = tid; t < qn * ncol; t += blockDim.x) {
+        const int q = t / ncol, c = t - q * ncol;
+        bdst[q * NCOL + c] = Bb[(long)(q0 + q) * kk + c];
+      }
+    }
+    cp_async_commit();
+  };
+  const int rtiles = (Mo + RT - 1) / RT, ctiles = (ncol + CT - 1) / CT, ntiles = rtiles * ctiles;
+  T acc[MAXT][RT][CT];
+#pragma unroll
+  for (int u = 0; u < MAXT; ++u)
+#pragma unroll
+    for (int r = 0; r < RT; ++r)
+#pragma unroll
+      for (int c = 0; c < CT; ++c) acc[u][r][c] = (T)0;
+  stage(0, 0);
+  const int nchunks = (Ki + KC - 1) / KC;
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int buf = ch & 1, q0 = ch * KC, qn = min(KC, Ki - q0);
+    cp_async_wait<0>();
+    __syncthreads();  // chunk ch staged; everyone is done with buffer buf^1
+    if (ch + 1 < nchunks) stage(q0 + KC, buf ^ 1);
+    const T* as = As + buf * KC * ld;
+    const T* bs = Bs + buf * KC * NCOL;
+#pragma unroll
+    for (int u = 0; u < MAXT; ++u) {
+      const int tile = tid + u * blockDim.x;
+      if (tile < ntiles) {
+        const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+        for (int q = 0; q < qn; ++q) {
+          T a[RT], bv[CT];
+#pragma unroll
+          for (int r = 0; r < RT; ++r) a[r] = as[q * ld + i0 + r];
+          load4(bs + q * NCOL + c0, bv);
+#pragma unroll
+          for (int r = 0; r < RT; ++r)
+#pragma unroll
+            for (int c = 0; c < CT; ++c) acc[u][r][c] = fma(a[r], bv[c], acc[u][r][c]);
+        }
+      }
+    }
+  }
+  T* Cb = C + (long)b * cstride + cbase;
+#pragma unroll
+  for (int u = 0; u < MAXT; ++u) {
+    const int tile = tid + u * blockDim.x;
+    if (tile < ntiles) {
+      const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c)
+          if (i0 + r < Mo && c0 + c < ncol) {
+            T* o = Cb + (long)(i0 + r) * kk + c0 + c;
+            *o = ACC ? *o + acc[u][r][c] : acc[u][r][c];
+          }
+    }
+  }
+}
+
+template <typename T>
+static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, T* C, long cstride, int nbatch, int kk,
+                           cudaStream_t s) {
+  if (nbatch == 0) return cudaSuccess;
+  const int rtiles = (A.Mo + 2) / 3;
+  if (rtiles * 8 > 4 * 256 || A.ld < rtiles * 3 || A.ld % 4 != 0) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)2 * 16 * (A.ld + 32) * sizeof(T);
+  const int vec_b = (kk * sizeof(T)) % 16 == 0 && (bstride * sizeof(T)) % 16 == 0 &&
+                    (reinterpret_cast<uintptr_t>(B) % 16) == 0;
+  const dim3 grid(nbatch, (kk + 31) / 32);
+  auto kf = acc ? k_tgemm<T, true> : k_tgemm<T, false>;
+  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kf<<<grid, 256, smem, s>>>(static_cast<const T*>(A.at), A.ld, A.Mo, A.Ki, B, bstride, C, cstride, kk, vec_b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tgemm(int S, bool acc, const TGemmA& A, const void* B, long bstride_rows, void* C,
+                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s) {
+  // complex vectors are real matrices with 2 nrhs columns
+  const int kk = (S & 1) ? 2 * nrhs : nrhs;
+  if (S < 2)
+    return tgemm_t<double>(acc, A, static_cast<const double*>(B), bstride_rows * kk, static_cast<double*>(C),
+                           cstride_rows * kk, nbatch, kk, s);
+  return tgemm_t<float>(acc, A, static_cast<const float*>(B), bstride_rows * kk, static_cast<float*>(C),
+                        cstride_rows * kk, nbatch, kk, s);
+}
+
 // Fused FP32 far field: the coupling F_ij = k(x_i, y_j) |J_i| |J_j| is
 // generated from the clusters' interpolation points inside the product, so the
 // far field is never stored. One CTA (128 threads) per block row (cluster c1).

@@ -150,6 +150,14 @@ struct bg_operator {
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
+  // FMM matrices transposed and padded for launch_tgemm, per precision
+  // (0 FP64, 1 FP32): moments forward/backward per component, transfers
+  struct TransformMats {
+    DevBuf mom_f[2], mom_b[2], tr_f, tr_b;
+    bg::TGemmA a_mom_f[2], a_mom_b[2], a_tr_f, a_tr_b;
+  };
+  TransformMats tm[2];
+  bool use_tgemm = false;
   // tensor-core far field: (level, row) work list, heaviest rows first
   DevBuf d_far_work;
   int n_far_work = 0;
