@@ -500,6 +500,7 @@ static bg_status assemble_far(bg_operator* op) {
       op->d_pts32.push_back(new DevBuf());
       op->d_centres.push_back(new DevBuf());
       op->d_far64.push_back(new DevBuf());
+      op->d_far_df.push_back(new DevBuf());
     }
     const int ncl = op->nclusters(l);
     std::vector<double> cen(4 * (size_t)ncl);
@@ -524,6 +525,12 @@ static bg_status assemble_far(bg_operator* op) {
     BG_CHECK(timed_launch(op->ctx, KC_ASSEMBLY, [&] { return launch_far_assemble(op->cplx, op->d_pts64[l]->as<d4>(), dp.as<int2>(), (int)pairs.size(), f.B,
                                  op->block_stride(f.B), op->kre, op->kim, op->d_far64[l]->p, s); }),
              "far-field assembly");
+    if (!op->cplx) {
+      // (hi, lo) FP32 pairs of the same blocks for the double-float FP64 product
+      BG_CHECK(op->d_far_df[l]->alloc(bytes), "far field storage");
+      BG_CHECK(launch_split_df(op->d_far64[l]->p, (long)f.col.size() * op->block_stride(f.B), op->d_far_df[l]->p, s),
+               "far-field split");
+    }
     BG_CHECK(cudaStreamSynchronize(s), "far-field assembly");
   }
   return BG_OK;
@@ -662,11 +669,13 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
   while ((int)op->w_y.size() <= op->leaf_level) {
     op->w_y.push_back(new DevBuf());
     op->w_z.push_back(new DevBuf());
+    op->w_ydf.push_back(new DevBuf());
   }
   for (int l = 0; l <= op->leaf_level; ++l) {
     const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
     BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
+    if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
   }
   op->cap = nrhs;
   return BG_OK;
@@ -761,9 +770,18 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                  "far-field product (FP32 fused)");
       } else {
         if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "the FP64 product needs the stored far field");
-        BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(op->cplx, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
-                            op->block_stride(f.B), f.nrows, f.B, op->w_y[l]->p, op->w_z[l]->p, nrhs, 0, s); }),
-                 "far-field product");
+        if (!op->cplx && op->d_far_df[l]->p) {
+          BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df(op->w_y[l]->p, (long)op->nclusters(l) * op->R * nrhs,
+                                                                         op->w_ydf[l]->p, s); }),
+                   "far-field split of Y");
+          BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_df(f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far_df[l]->p,
+                              op->block_stride(f.B), f.nrows, f.B, op->w_ydf[l]->p, op->w_z[l]->p, nrhs, 0, s); }),
+                   "far-field product (double-float)");
+        }
+        else
+          BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(op->cplx, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
+                              op->block_stride(f.B), f.nrows, f.B, op->w_y[l]->p, op->w_z[l]->p, nrhs, 0, s); }),
+                   "far-field product");
       }
     }
     for (int c = 0; c < op->vd; ++c) {

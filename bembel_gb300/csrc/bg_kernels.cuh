@@ -89,6 +89,12 @@ cudaError_t launch_gather_in(int Sin, int Sout, const void* user, long ld, int r
                              cudaStream_t s);
 cudaError_t launch_scatter_out(int Swork, const void* work, int rows, int nrhs, void* user, long ld, const double* alpha,
                                const double* beta, cudaStream_t s);
+// Double-float product of real FP64 blocks stored as FP32 (hi, lo) pairs
+// (launch_split_df), FP64 x and y; bstride in pairs, even
+cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
+                          const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
+// out[t] = (hi, lo) of in[t] (FP64), t < n
+cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s);
 // op(A) of an FMM transform, stored transposed: AT[q][i], q < Ki, i < ld
 // (ld a multiple of 4, at least Mo rounded up to 3, zero beyond Mo)
 struct TGemmA {

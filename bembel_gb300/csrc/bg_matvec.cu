@@ -815,6 +815,136 @@ cudaError_t launch_bsr_fp64(bool cplx, const int* row_ptr, const int* col, const
   return bsr_pipe_typed<double>(row_ptr, col, (const double*)blocks, bstride, nrows, B, (const double*)x, (double*)y,
                                 nrhs, accumulate, s);
 }
+// Double-float block-sparse product for real operators. Blocks are stored as
+// FP32 pairs (hi, lo) with hi + lo equal to the FP64 coupling to 2^-48 and x
+// arrives split the same way (launch_split_df). Every multiply-add forms
+// hi*hi exactly (product plus its fmaf error), adds the cross terms
+// hi*lo + lo*hi, and sums with TwoSum into an FP32 pair per output, so the
+// result matches the FP64 product to about 1e-14 relative while running on
+// the FP32 pipes (GB300's FP64 rate is 1/64 of its FP32 rate).
+// Thread t owns row t % B and NCOL right-hand sides of column group t / B.
+// The block is read from global memory directly (each element once per
+// column group, coalesced along a block column; the groups share it through
+// L1); only the x panels are staged, double-buffered with cp.async, so
+// several CTAs fit on an SM.
+template <int NCOL, bool FULL>
+__global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr, const int* __restrict__ col,
+                                                const float2* __restrict__ blocks, long bstride, int B,
+                                                const float2* __restrict__ x, double* __restrict__ y, int nrhs,
+                                                int accumulate) {
+  extern __shared__ __align__(16) float2 xsm[];  // [2][B * nrhs]
+  const int row = blockIdx.x, t = threadIdx.x;
+  const int i = t % B, cg = t / B, c0 = cg * NCOL;
+  const bool active = c0 < nrhs && cg * B + i == t;
+  const int panel = B * nrhs;
+  float s[NCOL], cc[NCOL];
+#pragma unroll
+  for (int c = 0; c < NCOL; ++c) s[c] = cc[c] = 0.0f;
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  auto issue = [&](int k, int buf) {
+    const float2* src = x + (long)col[k] * panel;
+    float2* dst = xsm + buf * panel;
+    if ((panel & 1) == 0) {
+      for (int e = 2 * t; e < panel; e += 2 * blockDim.x) cp_async16(dst + e, src + e);
+    } else {
+      for (int e = t; e < panel; e += blockDim.x) cp_async8(dst + e, src + e);
+    }
+    cp_async_commit();
+  };
+  if (kb < ke) issue(kb, 0);
+  for (int k = kb; k < ke; ++k) {
+    const int buf = (k - kb) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // panel k staged; everyone is done with panel k-1
+    if (k + 1 < ke) issue(k + 1, buf ^ 1);
+    if (active) {
+      const float2* F = blocks + (long)k * bstride + i;
+      const float2* xp = xsm + buf * panel + c0;
+#pragma unroll 4
+      for (int j = 0; j < B; ++j) {
+        const float2 f = __ldg(F + (long)j * B);
+        const float2* xv = xp + j * nrhs;
+#pragma unroll
+        for (int c = 0; c < NCOL; ++c) {
+          if (FULL || c0 + c < nrhs) {
+            const float2 b = xv[c];
+            const float p = f.x * b.x;
+            float e = fmaf(f.x, b.x, -p);
+            e = fmaf(f.x, b.y, e);
+            e = fmaf(f.y, b.x, e);
+            const float tt = s[c] + p, z = tt - s[c];
+            cc[c] += ((s[c] - (tt - z)) + (p - z)) + e;
+            s[c] = tt;
+          }
+        }
+      }
+    }
+  }
+  if (active) {
+    double* yo = y + ((long)row * B + i) * nrhs;
+#pragma unroll
+    for (int c = 0; c < NCOL; ++c)
+      if (FULL || c0 + c < nrhs) {
+        const double v = (double)s[c] + (double)cc[c];
+        yo[c0 + c] = accumulate ? yo[c0 + c] + v : v;
+      }
+  }
+}
+
+cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
+                          const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (nrows == 0) return cudaSuccess;
+  int ncol = nrhs <= 1 ? 1 : (nrhs <= 2 ? 2 : (nrhs <= 4 ? 4 : 8));
+  int groups = (nrhs + ncol - 1) / ncol;
+  while (B * groups > 352) {
+    ncol *= 2;
+    groups = (nrhs + ncol - 1) / ncol;
+  }
+  if (ncol > 32) return cudaErrorInvalidValue;
+  const int threads = ((B * groups + 31) / 32) * 32;
+  const size_t smem = (size_t)2 * B * nrhs * sizeof(float2);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
+  const bool full = nrhs % ncol == 0;
+  const float2* bl = static_cast<const float2*>(blocks);
+  const float2* xx = static_cast<const float2*>(x);
+  double* yy = static_cast<double*>(y);
+#define BG_DF(NC, FU)                                                                                       \
+  if (ncol == NC && full == FU) {                                                                           \
+    auto kf = k_bsr_df<NC, FU>;                                                                             \
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+    if (e != cudaSuccess) return e;                                                                         \
+    kf<<<nrows, threads, smem, s>>>(row_ptr, col, bl, bstride, B, xx, yy, nrhs, accumulate);                \
+    return cudaGetLastError();                                                                              \
+  }
+  BG_DF(1, true)
+  BG_DF(2, true)
+  BG_DF(2, false)
+  BG_DF(4, true)
+  BG_DF(4, false)
+  BG_DF(8, true)
+  BG_DF(8, false)
+  BG_DF(16, true)
+  BG_DF(16, false)
+  BG_DF(32, true)
+  BG_DF(32, false)
+#undef BG_DF
+  return cudaErrorInvalidValue;
+}
+
+__global__ void k_split_df(const double* __restrict__ in, long n, float2* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double v = in[t];
+  const float h = (float)v;
+  out[t] = make_float2(h, (float)(v - (double)h));
+}
+cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_split_df<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const double*>(in), n,
+                                                           static_cast<float2*>(out));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
                             int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
   if (cplx)

@@ -379,8 +379,9 @@ def run_profile_case(args):
     import torch
     import bembel_gb300 as bg
     ctx = bg.Context(0)
-    store = args.profile == "solve"
-    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), M, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
+    store = args.profile == "solve" or args.precision == "fp64"
+    m = args.profile_m if args.profile_m is not None else M
+    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
                              store_fp64_far=store)
     op.compute()
     A = op.get_discrete_operator()
@@ -389,7 +390,7 @@ def run_profile_case(args):
         for _ in range(5):
             A.matvec(x, precision=args.precision)
         torch.cuda.synchronize()
-        print(json.dumps({"profile": "matvec", "precision": args.precision, "N": op.N, "products": 5}))
+        print(json.dumps({"profile": "matvec", "precision": args.precision, "M": m, "N": op.N, "products": 5}))
     else:
         b = op.load_vector(0, rhs_points())
         _, st = A.solve(b, tol=TOL, inner=args.inner, inner_tol=1e-2, restart=200, max_refinements=12)
@@ -409,6 +410,7 @@ def main():
                     help="run a small fixed case for ncu instead of the benchmark")
     ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
                     help="product precision of --profile matvec")
+    ap.add_argument("--profile-m", type=int, default=None, help="refinement level of --profile cases (default 5)")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args)
