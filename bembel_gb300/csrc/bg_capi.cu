@@ -492,7 +492,12 @@ static bg_status assemble_far(bg_operator* op) {
   PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
   const int np2 = op->np * op->np;
   bool any_far = false;
-  for (const auto& f : op->far) any_far |= !f.col.empty();
+  int far_levels = 0, tiled_levels = 0;
+  for (const auto& f : op->far) {
+    any_far |= !f.col.empty();
+    far_levels += !f.col.empty();
+  }
+  op->far_tiles = false;
   if (!any_far) return BG_OK;
   for (int l = 0; l <= op->leaf_level; ++l) {
     if ((int)op->d_pts64.size() <= l) {
@@ -501,6 +506,7 @@ static bg_status assemble_far(bg_operator* op) {
       op->d_centres.push_back(new DevBuf());
       op->d_far64.push_back(new DevBuf());
       op->d_far_df.push_back(new DevBuf());
+      op->d_far_atiles.push_back(new DevBuf());
     }
     const int ncl = op->nclusters(l);
     std::vector<double> cen(4 * (size_t)ncl);
@@ -530,9 +536,19 @@ static bg_status assemble_far(bg_operator* op) {
       BG_CHECK(op->d_far_df[l]->alloc(bytes), "far field storage");
       BG_CHECK(launch_split_df(op->d_far64[l]->p, (long)f.col.size() * op->block_stride(f.B), op->d_far_df[l]->p, s),
                "far-field split");
+      // TF32 hi / FP32 lo tiles in the tensor-core operand layout
+      const size_t tb = far_tc_atile_bytes(np2);
+      if (tb > 0 && op->vd == 1 && op->nc == 1) {
+        BG_CHECK(op->d_far_atiles[l]->alloc(tb * f.col.size()), "far field tiles");
+        BG_CHECK(launch_build_atiles(np2, op->d_far64[l]->as<double>(), op->block_stride(f.B), (long)f.col.size(),
+                                     op->d_far_atiles[l]->p, s),
+                 "far-field tiles");
+        ++tiled_levels;
+      }
     }
     BG_CHECK(cudaStreamSynchronize(s), "far-field assembly");
   }
+  op->far_tiles = tiled_levels == far_levels && op->leaf_level < kMaxFarLevels;
   return BG_OK;
 }
 
@@ -670,12 +686,15 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     op->w_y.push_back(new DevBuf());
     op->w_z.push_back(new DevBuf());
     op->w_ydf.push_back(new DevBuf());
+    op->w_btiles.push_back(new DevBuf());
   }
   for (int l = 0; l <= op->leaf_level; ++l) {
     const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
     BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
     if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
+    const size_t tb = far_tc_btile_bytes(op->np * op->np);
+    if (!op->cplx && tb > 0) BG_CHECK(op->w_btiles[l]->alloc(tb * op->nclusters(l)), "work vectors");
   }
   op->cap = nrhs;
   return BG_OK;
@@ -741,7 +760,25 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     }
     const bool tc = mixed && op->vd == 1 && op->nc == 1 && op->leaf_level < kMaxFarLevels &&
                     far_tc_supported(op->cplx, np2, nrhs);
-    if (tc) {
+    if (tc && op->far_tiles) {
+      // stored tiles streamed by TMA bulk copies; all levels in one launch,
+      // which writes every row of Z
+      FarTcTiles T{};
+      for (int l = 0; l <= op->leaf_level; ++l) {
+        T.row_ptr[l] = op->far[l].d_row_ptr.as<int>();
+        T.col[l] = op->far[l].d_col.as<int>();
+        T.a[l] = static_cast<const unsigned char*>(op->d_far_atiles[l]->p);
+        T.b[l] = static_cast<unsigned char*>(op->w_btiles[l]->p);
+        T.y[l] = static_cast<const float*>(op->w_y[l]->p);
+        T.z[l] = static_cast<float*>(op->w_z[l]->p);
+        T.ncl[l] = op->nclusters(l);
+      }
+      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
+               "right-hand-side tiles");
+      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_tc_stored(T, op->d_far_work.as<int2>(), op->n_far_work,
+                                                                             np2, nrhs, op->d_err.as<int>(), s); }),
+               "far-field product (stored tiles, tensor cores)");
+    } else if (tc) {
       // all levels in one tensor-core launch; it writes every row of Z
       FarTcLevels L{};
       for (int l = 0; l <= op->leaf_level; ++l) {

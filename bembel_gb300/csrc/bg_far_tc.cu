@@ -408,6 +408,310 @@ static cudaError_t launch_np(const FarTcLevels& L, const int2* work, int nwork, 
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Stored-tile variant. The FP64 couplings of every low-rank block are split
+// once, at assembly, into TF32 high / FP32 remainder tiles already in the UMMA
+// core-matrix layout (2 x 11 x 2816 bytes per 81 x 81 block); per product the
+// split right-hand-side tiles of every cluster are built once
+// (launch_build_btiles). The product then moves whole tiles with 1-D TMA bulk
+// copies and does no per-entry work on the CUDA cores. Roles: warp 0 (one
+// thread) issues the bulk copies, warp 1 (one thread) the MMAs, warps 2-5
+// fold the accumulators of each finished block into Neumaier-compensated row
+// sums (one tensor-memory lane quadrant each). Stages and accumulator buffers
+// change hands through mbarriers: full (copies landed, by transaction bytes),
+// done (tcgen05.commit) and free (the epilogue drained the buffer). Every wait
+// is bounded, as in k_far_tc.
+constexpr int kStoredThreads = 192;
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion counted on bar (16-byte aligned
+// addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int NP2>
+struct StoredPlan {
+  using G = TcShape<NP2>;
+  static constexpr uint32_t A2 = 2 * G::A_BYTES, B2 = 2 * G::B_BYTES;  // bytes per block / per cluster
+  static constexpr uint32_t SMEM = 2 * G::STAGE > G::NEED ? 2 * G::STAGE : G::NEED;
+};
+
+template <int NP2>
+__global__ void __launch_bounds__(kStoredThreads, 1)
+    k_far_tc_stored(FarTcTiles T, const int2* __restrict__ work, int nrhs, int* __restrict__ err) {
+  using G = TcShape<NP2>;
+  constexpr uint32_t A2 = StoredPlan<NP2>::A2, B2 = StoredPlan<NP2>::B2;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full_bar[2], done_bar[2], free_bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int2 w = work[blockIdx.x];
+  const int lev = w.x, row = w.y;
+  const int* row_ptr = T.row_ptr[lev];
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  float* z = T.z[lev];
+  if (kb == ke) {  // no far-field block in this row (uniform over the CTA)
+    for (int e = tid; e < NP2 * nrhs; e += kStoredThreads) z[(long)row * NP2 * nrhs + e] = 0.0f;
+    return;
+  }
+  const int* col = T.col[lev];
+  const unsigned char* atiles = T.a[lev];
+  const unsigned char* btiles = T.b[lev];
+  const int nblk = ke - kb;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&full_bar[b], 1);
+      mbar_init(&done_bar[b], 1);
+      mbar_init(&free_bar[b], 4);
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ---- producer: whole tiles by 1-D TMA bulk copies ----
+    if (lane == 0) {
+      for (int it = 0; it < nblk; ++it) {
+        const int s = it & 1, k = kb + it;
+        if (it >= 2 && !mbar_wait(&done_bar[s], (uint32_t)(((it >> 1) - 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 4);
+          break;
+        }
+        if (*abort_v) break;
+        unsigned char* st = smem + s * G::STAGE;
+        const unsigned char* ga = atiles + (size_t)k * A2;
+        const unsigned char* gb = btiles + (size_t)col[k] * B2;
+        mbar_expect_tx(&full_bar[s], A2 + B2);
+        bulk_g2s(st, ga, G::A_BYTES, &full_bar[s]);
+        bulk_g2s(st + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[s]);
+        bulk_g2s(st + A2, gb, G::B_BYTES, &full_bar[s]);
+        bulk_g2s(st + A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[s]);
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(128, kN);
+      const uint32_t base = smem_u32(smem);
+      for (int it = 0; it < nblk; ++it) {
+        const int s = it & 1;
+        if (!mbar_wait(&full_bar[s], (uint32_t)((it >> 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 5);
+          break;
+        }
+        if (it >= 2 && !mbar_wait(&free_bar[s], (uint32_t)(((it >> 1) - 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 6);
+          break;
+        }
+        if (*abort_v) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t a0 = base + s * G::STAGE, a1 = a0 + G::A_BYTES;
+        const uint32_t b0 = a0 + A2, b1 = b0 + G::B_BYTES;
+        const uint32_t d_hh = tmem + (uint32_t)(64 * s), d_cr = d_hh + 32;
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) {
+          uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
+          uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
+          const uint32_t dd = pass == 0 ? d_hh : d_cr;
+#pragma unroll
+          for (int ks = 0; ks < G::KP / 8; ++ks) {
+            mma_tf32(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
+            ad += 16;
+            bd += 16;
+          }
+        }
+        mma_commit(&done_bar[s]);
+      }
+    }
+  } else {
+    // ---- epilogue warps 2-5: tensor-memory lanes 32 (warp % 4) .. +31 ----
+    float sum[32], comp[32];
+#pragma unroll
+    for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    bool ok = true;
+    for (int it = 0; it < nblk; ++it) {
+      const int s = it & 1;
+      int got = 1;
+      if (lane == 0) got = mbar_wait(&done_bar[s], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        if (lane == 0) {
+          *abort_v = 1;
+          atomicExch(err, 7);
+        }
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      float hh[32], cr[32];
+      tmem_ld32(lane_base + (uint32_t)(64 * s), hh);
+      tmem_ld32(lane_base + (uint32_t)(64 * s + 32), cr);
+#pragma unroll
+      for (int n = 0; n < 32; ++n) neumaier(sum[n], comp[n], hh[n] + cr[n]);
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&free_bar[s]);
+    }
+    const int m = (warp & 3) * 32 + lane;
+    if (ok && m < NP2) {
+      float* zo = z + ((long)row * NP2 + m) * nrhs;
+#pragma unroll
+      for (int n = 0; n < 32; ++n)
+        if (n < nrhs) zo[n] = sum[n] + comp[n];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// A tiles of nblocks FP64 blocks (column-major, stride bstride doubles): per
+// block [hi tile][lo tile], entry (m, k) in core matrix (m / 8) * KC + k / 4 at
+// lane 4 (m % 8) + k % 4; zero beyond n_p^2.
+template <int NP2>
+__global__ void k_build_atiles(const double* __restrict__ F, long bstride, long nblocks, float* __restrict__ tiles) {
+  using G = TcShape<NP2>;
+  constexpr int AF = G::A_BYTES / 4;  // floats per tile
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nblocks * AF) return;
+  const long b = t / AF;
+  const int e = (int)(t - b * AF), cm = e >> 5, lane = e & 31;
+  const int m = (cm / G::KC) * 8 + (lane >> 2), k = (cm % G::KC) * 4 + (lane & 3);
+  const double v = (m < NP2 && k < NP2) ? F[b * bstride + (long)k * NP2 + m] : 0.0;
+  const float h = tf32_hi((float)v);
+  tiles[b * 2 * AF + e] = h;
+  tiles[b * 2 * AF + AF + e] = (float)(v - (double)h);
+}
+
+// B tiles of every cluster of every level: Y_c^T (32 x n_p^2, K-major) split
+// into [hi tile][lo tile]; columns beyond nrhs and rows beyond n_p^2 are zero.
+template <int NP2>
+__global__ void k_build_btiles(FarTcTiles T, int nlev, int nrhs) {
+  using G = TcShape<NP2>;
+  constexpr int BF = G::B_BYTES / 4;
+  int c = blockIdx.x, lev = 0;
+  while (lev + 1 < nlev && c >= T.ncl[lev]) c -= T.ncl[lev++];
+  const float* y = T.y[lev] + (long)c * NP2 * nrhs;
+  float* out = reinterpret_cast<float*>(T.b[lev]) + (long)c * 2 * BF;
+  for (int e = threadIdx.x; e < BF; e += blockDim.x) {
+    const int cm = e >> 5, lane = e & 31;
+    const int n = (cm / G::KC) * 8 + (lane >> 2), k = (cm % G::KC) * 4 + (lane & 3);
+    const float v = (n < nrhs && k < NP2) ? y[k * nrhs + n] : 0.0f;
+    const float h = tf32_hi(v);
+    out[e] = h;
+    out[BF + e] = v - h;
+  }
+}
+
+#define BG_TC_SHAPES(X) X(4) X(9) X(16) X(25) X(36) X(49) X(64) X(81)
+
+size_t far_tc_atile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return StoredPlan<N>::A2;
+    BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+size_t far_tc_btile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return StoredPlan<N>::B2;
+    BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+
+cudaError_t launch_build_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  const long n = nblocks * (long)(far_tc_atile_bytes(np2) / 8);
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  switch (np2) {
+#define BG_T(N) \
+  case N: k_build_atiles<N><<<grid, 256, 0, s>>>(F, bstride, nblocks, static_cast<float*>(tiles)); break;
+    BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_btiles(const FarTcTiles& T, int nlev, int np2, int nrhs, cudaStream_t s) {
+  if (nlev < 1 || nlev > kMaxFarLevels || nrhs < 1 || nrhs > kN) return cudaErrorInvalidValue;
+  int ncl_total = 0;
+  for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
+  if (ncl_total == 0) return cudaSuccess;
+  switch (np2) {
+#define BG_T(N) \
+  case N: k_build_btiles<N><<<ncl_total, 256, 0, s>>>(T, nlev, nrhs); break;
+    BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_far_tc_stored(const FarTcTiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
+                                 cudaStream_t s) {
+  if (nwork == 0) return cudaSuccess;
+  if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
+  switch (np2) {
+#define BG_T(N)                                                                                             \
+  case N: {                                                                                                 \
+    constexpr uint32_t smem = StoredPlan<N>::SMEM;                                                          \
+    static_assert(smem <= 227 * 1024, "stored far field: shared memory plan too large");                    \
+    cudaError_t e = cudaFuncSetAttribute(k_far_tc_stored<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                         (int)smem);                                                        \
+    if (e != cudaSuccess) return e;                                                                         \
+    k_far_tc_stored<N><<<nwork, kStoredThreads, smem, s>>>(T, work, nrhs, err);                             \
+    return cudaGetLastError();                                                                              \
+  }
+    BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 bool far_tc_supported(bool cplx, int np2, int nrhs) {
   const bool shape = np2 == 4 || np2 == 9 || np2 == 16 || np2 == 25 || np2 == 36 || np2 == 49 || np2 == 64 || np2 == 81;
   return !cplx && shape && nrhs >= 1 && nrhs <= kN;

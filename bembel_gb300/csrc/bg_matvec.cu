@@ -860,10 +860,7 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
     if (active) {
       const float2* F = blocks + (long)k * bstride + i;
       const float2* xp = xsm + buf * panel + c0;
-#pragma unroll 4
-      for (int j = 0; j < B; ++j) {
-        const float2 f = __ldg(F + (long)j * B);
-        const float2* xv = xp + j * nrhs;
+      auto madd = [&](const float2 f, const float2* xv) {
 #pragma unroll
         for (int c = 0; c < NCOL; ++c) {
           if (FULL || c0 + c < nrhs) {
@@ -877,7 +874,23 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
             s[c] = tt;
           }
         }
+      };
+      // block columns in groups of 4, the next group's couplings loaded
+      // while the current one is multiplied
+      constexpr int G = 4;
+      const int jg = B / G * G;
+      float2 fa[G], fb[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) fa[u] = u < jg ? __ldg(F + (long)u * B) : make_float2(0.f, 0.f);
+      for (int j = 0; j < jg; j += G) {
+#pragma unroll
+        for (int u = 0; u < G; ++u) fb[u] = j + G + u < jg ? __ldg(F + (long)(j + G + u) * B) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < G; ++u) madd(fa[u], xp + (j + u) * nrhs);
+#pragma unroll
+        for (int u = 0; u < G; ++u) fa[u] = fb[u];
       }
+      for (int j = jg; j < B; ++j) madd(__ldg(F + (long)j * B), xp + j * nrhs);
     }
   }
   if (active) {
