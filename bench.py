@@ -42,6 +42,11 @@ METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed p
 FP64_ITERS_C2 = 253
 # FP32 FMA throughput of one GB300 measured with an FMA-chain probe (TFLOP/s)
 FP32_FMA_TFLOPS = 75.0
+# DRAM bytes (read + write) per low-rank block of k_far_tc_stored, from one ncu
+# capture of the same kernel on the M=4 sphere (1.1413 GB for 17 616 blocks,
+# 64 785 bytes per block against 61 952 bytes of A tiles; the rest is the
+# right-hand-side tiles and the output)
+FAR_TILE_DRAM_BYTES_PER_BLOCK = 1.1413e9 / 17616
 INNER_DESC = {"mixed": "inner GMRES(FP64 near, FP32 fused far)", "fp32": "inner GMRES(FP32 near, FP32 fused far)"}
 
 
@@ -318,6 +323,14 @@ def _read_profile(L, ctx):
             "launches_total": sum(ln[i] for i in range(8))}
 
 
+def far_tile_bytes(np2):
+    """Bytes of the TF32 hi + lo operand tiles of one low-rank block: row
+    groups of 8 targets x K padded to 8 sources, 4 bytes each."""
+    mg = (np2 + 7) // 8
+    kp = (np2 + 7) // 8 * 8
+    return 2 * mg * 8 * kp * 4
+
+
 def _roofline(op, prof, stats, steps):
     """Roofline of the dominant kernel class of the timed solves.
 
@@ -347,15 +360,17 @@ def _roofline(op, prof, stats, steps):
                      "peak_source": src, "algorithmic_bytes_per_launch": algo})
         return base
     if cls == "far_fused_fp32":
-        # 2 flops per coupling entry per right-hand side; one launch per level
-        products = steps * stats["low_matvecs"]
-        flops = products * 2.0 * nlow * block_entries * NRHS
-        ach = flops / (ms * 1e-3) / 1e12
-        base.update({"kernel": "k_far_fused (FP32 couplings generated on the fly + contraction, 32 RHS)",
-                     "bound": "fp32-fma", "achieved": ach, "peak": FP32_FMA_TFLOPS, "unit": "TFLOP/s",
-                     "frac": ach / FP32_FMA_TFLOPS, "traffic": None,
-                     "peak_source": "FP32 FMA throughput probe on this GB300 (CUDA cores; kernel not on tensor cores)",
-                     "algorithmic_flops_per_product": 2.0 * nlow * block_entries * NRHS})
+        # k_far_tc_stored: one launch per product streams the split operand
+        # tiles of every low-rank block once (TMA bulk copies) into tcgen05.mma
+        np2 = int(info[7]) ** 2
+        tile = far_tile_bytes(np2)
+        algo = nlow * tile
+        ach = algo / t / 1e9
+        base.update({"kernel": "k_far_tc_stored (stored TF32 hi/lo tiles, TMA bulk copy -> tcgen05.mma, 32 RHS)",
+                     "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": nlow * FAR_TILE_DRAM_BYTES_PER_BLOCK, "peak_source": src,
+                     "algorithmic_bytes_per_launch": algo, "tile_bytes_per_block": tile,
+                     "contraction_tflops": 2.0 * nlow * block_entries * NRHS / t / 1e12})
         return base
     base.update({"bound": None, "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None})
     return base
@@ -373,13 +388,13 @@ def ctypes_byref(x):
 
 def run_profile_case(args):
     """Small fixed cases for ncu (not a bench line): 'matvec' assembles the
-    workload's operator without the stored FP64 far field and applies five
-    32-column products at --precision; 'solve' runs one batched solve with the
-    chosen inner operator."""
+    workload's operator (refinement --profile-m) and applies five 32-column
+    products at --precision; 'solve' runs one batched solve with the chosen
+    inner operator."""
     import torch
     import bembel_gb300 as bg
     ctx = bg.Context(0)
-    store = args.profile == "solve" or args.precision == "fp64"
+    store = True  # the tensor-core far field streams tiles built from the stored FP64 blocks
     m = args.profile_m if args.profile_m is not None else M
     op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
                              store_fp64_far=store)
