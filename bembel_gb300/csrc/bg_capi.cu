@@ -507,6 +507,7 @@ static bg_status assemble_far(bg_operator* op) {
       op->d_far64.push_back(new DevBuf());
       op->d_far_df.push_back(new DevBuf());
       op->d_far_atiles.push_back(new DevBuf());
+      op->d_far_ainv.push_back(new DevBuf());
     }
     const int ncl = op->nclusters(l);
     std::vector<double> cen(4 * (size_t)ncl);
@@ -536,12 +537,13 @@ static bg_status assemble_far(bg_operator* op) {
       BG_CHECK(op->d_far_df[l]->alloc(bytes), "far field storage");
       BG_CHECK(launch_split_df(op->d_far64[l]->p, (long)f.col.size() * op->block_stride(f.B), op->d_far_df[l]->p, s),
                "far-field split");
-      // TF32 hi / FP32 lo tiles in the tensor-core operand layout
-      const size_t tb = far_tc_atile_bytes(np2);
+      // scaled FP16 hi / lo tiles in the tensor-core operand layout
+      const size_t tb = far_h16_atile_bytes(np2);
       if (tb > 0 && op->vd == 1 && op->nc == 1) {
         BG_CHECK(op->d_far_atiles[l]->alloc(tb * f.col.size()), "far field tiles");
-        BG_CHECK(launch_build_atiles(np2, op->d_far64[l]->as<double>(), op->block_stride(f.B), (long)f.col.size(),
-                                     op->d_far_atiles[l]->p, s),
+        BG_CHECK(op->d_far_ainv[l]->alloc(sizeof(float) * f.col.size()), "far field tiles");
+        BG_CHECK(launch_build_h16_atiles(np2, op->d_far64[l]->as<double>(), op->block_stride(f.B), (long)f.col.size(),
+                                         op->d_far_atiles[l]->p, op->d_far_ainv[l]->as<float>(), s),
                  "far-field tiles");
         ++tiled_levels;
       }
@@ -687,14 +689,18 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     op->w_z.push_back(new DevBuf());
     op->w_ydf.push_back(new DevBuf());
     op->w_btiles.push_back(new DevBuf());
+    op->w_binv.push_back(new DevBuf());
   }
   for (int l = 0; l <= op->leaf_level; ++l) {
     const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
     BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
     if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
-    const size_t tb = far_tc_btile_bytes(op->np * op->np);
-    if (!op->cplx && tb > 0) BG_CHECK(op->w_btiles[l]->alloc(tb * op->nclusters(l)), "work vectors");
+    const size_t tb = far_h16_btile_bytes(op->np * op->np);
+    if (!op->cplx && tb > 0) {
+      BG_CHECK(op->w_btiles[l]->alloc(tb * op->nclusters(l)), "work vectors");
+      BG_CHECK(op->w_binv[l]->alloc(sizeof(float) * 32 * op->nclusters(l)), "work vectors");
+    }
   }
   op->cap = nrhs;
   return BG_OK;
@@ -761,23 +767,25 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     const bool tc = mixed && op->vd == 1 && op->nc == 1 && op->leaf_level < kMaxFarLevels &&
                     far_tc_supported(op->cplx, np2, nrhs);
     if (tc && op->far_tiles) {
-      // stored tiles streamed by TMA bulk copies; all levels in one launch,
-      // which writes every row of Z
-      FarTcTiles T{};
+      // stored FP16 tiles streamed by TMA bulk copies; all levels in one
+      // launch, which writes every row of Z
+      FarH16Tiles T{};
       for (int l = 0; l <= op->leaf_level; ++l) {
         T.row_ptr[l] = op->far[l].d_row_ptr.as<int>();
         T.col[l] = op->far[l].d_col.as<int>();
         T.a[l] = static_cast<const unsigned char*>(op->d_far_atiles[l]->p);
+        T.ainv[l] = op->d_far_ainv[l]->as<float>();
         T.b[l] = static_cast<unsigned char*>(op->w_btiles[l]->p);
+        T.binv[l] = op->w_binv[l]->as<float>();
         T.y[l] = static_cast<const float*>(op->w_y[l]->p);
         T.z[l] = static_cast<float*>(op->w_z[l]->p);
         T.ncl[l] = op->nclusters(l);
       }
-      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
+      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
                "right-hand-side tiles");
-      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_tc_stored(T, op->d_far_work.as<int2>(), op->n_far_work,
-                                                                             np2, nrhs, op->d_err.as<int>(), s); }),
-               "far-field product (stored tiles, tensor cores)");
+      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->d_far_work.as<int2>(), op->n_far_work,
+                                                                       np2, nrhs, op->d_err.as<int>(), s); }),
+               "far-field product (stored FP16 tiles, tensor cores)");
     } else if (tc) {
       // all levels in one tensor-core launch; it writes every row of Z
       FarTcLevels L{};

@@ -27,6 +27,8 @@
 // threads arrive; done: tcgen05.commit). Every wait is bounded: on timeout the
 // kernel records an error code, waits (bounded) for its MMAs, frees its tensor
 // memory and returns.
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "bg_kernels.cuh"
@@ -707,6 +709,351 @@ cudaError_t launch_far_tc_stored(const FarTcTiles& T, const int2* work, int nwor
     return cudaGetLastError();                                                                              \
   }
     BG_TC_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP16 stored-tile variant (the one the product uses). Each low-rank block is
+// scaled by a power of two sA (largest coupling in [2^13, 2^14)) and split into
+// FP16 hi + lo, which keeps 22 bits of every coupling at 4 bytes per entry;
+// each right-hand-side column of a cluster is scaled and split the same way
+// (sB[n]). tcgen05.mma kind::f16 (M = 128, N = 32, K = 16) forms hi*hi and
+// hi*lo + lo*hi exactly into FP32 tensor memory; the epilogue multiplies by
+// 1/(sA sB[n]) (exact) before the compensated row sums. Four shared-memory
+// stages of tiles move by 1-D TMA bulk copies; two accumulator buffers.
+constexpr int kH16Stages = 4;
+
+template <int NP2>
+struct H16Shape {
+  static constexpr int KP = (NP2 + 15) / 16 * 16;  // K padded to the f16 MMA K step
+  static constexpr int KC = KP / 8;                // 16-byte core-matrix columns (8 halves)
+  static constexpr int MG = (NP2 + 7) / 8;
+  static constexpr uint32_t SBO = KC * 128;
+  static constexpr uint32_t A_BYTES = MG * SBO, B_BYTES = 4 * SBO;
+  static constexpr uint32_t A2 = 2 * A_BYTES, B2 = 2 * B_BYTES;
+  static constexpr uint32_t STAGE = A2 + B2;
+  static constexpr uint32_t TILES = kH16Stages * STAGE;
+  static constexpr uint32_t NEED = (kH16Stages - 1) * STAGE + A_BYTES + 16 * SBO;
+  static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
+};
+
+// kind::f16 instruction descriptor: D FP32, A and B FP16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// power of two s with max_abs * s in [2^13, 2^14) (1 for zero or non-finite)
+__device__ __forceinline__ float h16_scale(float max_abs) {
+  if (!(max_abs > 0.0f) || !isfinite(max_abs)) return 1.0f;
+  int e;
+  frexpf(max_abs, &e);  // max_abs = f 2^e, f in [0.5, 1)
+  return ldexpf(1.0f, 14 - e);
+}
+
+template <int NP2>
+__global__ void __launch_bounds__(kStoredThreads, 1)
+    k_far_h16(FarH16Tiles T, const int2* __restrict__ work, int nrhs, int* __restrict__ err) {
+  using G = H16Shape<NP2>;
+  constexpr int S = kH16Stages;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full_bar[S], done_bar[S], free_bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int2 w = work[blockIdx.x];
+  const int lev = w.x, row = w.y;
+  const int* row_ptr = T.row_ptr[lev];
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  float* z = T.z[lev];
+  if (kb == ke) {  // no far-field block in this row (uniform over the CTA)
+    for (int e = tid; e < NP2 * nrhs; e += kStoredThreads) z[(long)row * NP2 * nrhs + e] = 0.0f;
+    return;
+  }
+  const int* col = T.col[lev];
+  const int nblk = ke - kb;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < S; ++b) {
+      mbar_init(&full_bar[b], 1);
+      mbar_init(&done_bar[b], 1);
+    }
+    mbar_init(&free_bar[0], 4);
+    mbar_init(&free_bar[1], 4);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ---- producer: whole tiles by 1-D TMA bulk copies ----
+    if (lane == 0) {
+      const unsigned char* atiles = T.a[lev];
+      const unsigned char* btiles = T.b[lev];
+      for (int it = 0; it < nblk; ++it) {
+        const int st = it % S, k = kb + it;
+        if (it >= S && !mbar_wait(&done_bar[st], (uint32_t)((it / S - 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 4);
+          break;
+        }
+        if (*abort_v) break;
+        unsigned char* sm = smem + st * G::STAGE;
+        const unsigned char* ga = atiles + (size_t)k * G::A2;
+        const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
+        mbar_expect_tx(&full_bar[st], G::STAGE);
+        bulk_g2s(sm, ga, G::A_BYTES, &full_bar[st]);
+        bulk_g2s(sm + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[st]);
+        bulk_g2s(sm + G::A2, gb, G::B_BYTES, &full_bar[st]);
+        bulk_g2s(sm + G::A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_f16(128, kN);
+      const uint32_t base = smem_u32(smem);
+      for (int it = 0; it < nblk; ++it) {
+        const int st = it % S, ab = it & 1;
+        if (!mbar_wait(&full_bar[st], (uint32_t)((it / S) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 5);
+          break;
+        }
+        if (it >= 2 && !mbar_wait(&free_bar[ab], (uint32_t)(((it >> 1) - 1) & 1))) {
+          *abort_v = 1;
+          atomicExch(err, 6);
+          break;
+        }
+        if (*abort_v) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t a0 = base + st * G::STAGE, a1 = a0 + G::A_BYTES;
+        const uint32_t b0 = a0 + G::A2, b1 = b0 + G::B_BYTES;
+        const uint32_t d_hh = tmem + (uint32_t)(64 * ab), d_cr = d_hh + 32;
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) {
+          uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
+          uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
+          const uint32_t dd = pass == 0 ? d_hh : d_cr;
+#pragma unroll
+          for (int ks = 0; ks < G::KP / 16; ++ks) {
+            mma_f16(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
+            ad += 16;  // next K step: two core matrices = 256 bytes
+            bd += 16;
+          }
+        }
+        mma_commit(&done_bar[st]);
+      }
+    }
+  } else {
+    // ---- epilogue warps 2-5: tensor-memory lanes 32 (warp % 4) .. +31 ----
+    float sum[32], comp[32];
+#pragma unroll
+    for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const float* ainv = T.ainv[lev];
+    const float* binv = T.binv[lev];
+    bool ok = true;
+    for (int it = 0; it < nblk; ++it) {
+      const int st = it % S, ab = it & 1, k = kb + it;
+      int got = 1;
+      if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        if (lane == 0) {
+          *abort_v = 1;
+          atomicExch(err, 7);
+        }
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      float hh[32], cr[32];
+      tmem_ld32(lane_base + (uint32_t)(64 * ab), hh);
+      tmem_ld32(lane_base + (uint32_t)(64 * ab + 32), cr);
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&free_bar[ab]);
+      const float sa = __ldg(&ainv[k]);
+      const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 b4 = __ldg(&sb[q]);
+        neumaier(sum[4 * q + 0], comp[4 * q + 0], (hh[4 * q + 0] + cr[4 * q + 0]) * (sa * b4.x));
+        neumaier(sum[4 * q + 1], comp[4 * q + 1], (hh[4 * q + 1] + cr[4 * q + 1]) * (sa * b4.y));
+        neumaier(sum[4 * q + 2], comp[4 * q + 2], (hh[4 * q + 2] + cr[4 * q + 2]) * (sa * b4.z));
+        neumaier(sum[4 * q + 3], comp[4 * q + 3], (hh[4 * q + 3] + cr[4 * q + 3]) * (sa * b4.w));
+      }
+    }
+    const int m = (warp & 3) * 32 + lane;
+    if (ok && m < NP2) {
+      float* zo = z + ((long)row * NP2 + m) * nrhs;
+#pragma unroll
+      for (int n = 0; n < 32; ++n)
+        if (n < nrhs) zo[n] = sum[n] + comp[n];
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// A tiles of nblocks FP64 blocks (column-major, stride bstride): one CTA per
+// block finds the largest coupling, picks sA, writes [hi tile][lo tile] with
+// entry (m, k) in core matrix (m / 8) * KC + k / 8 at row m % 8, element k % 8,
+// and 1/sA to ainv[b].
+template <int NP2>
+__global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restrict__ F, long bstride,
+                                                          __half* __restrict__ tiles, float* __restrict__ ainv) {
+  using G = H16Shape<NP2>;
+  constexpr int AH = G::A_BYTES / 2;  // halves per tile
+  __shared__ float red[8];
+  const long b = blockIdx.x;
+  const double* Fb = F + b * bstride;
+  float mx = 0.0f;
+  for (int e = threadIdx.x; e < NP2 * NP2; e += blockDim.x) mx = fmaxf(mx, (float)fabs(Fb[e]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) mx = fmaxf(mx, red[i]);
+  const float sa = h16_scale(mx * 1.0000001f);
+  __half* out = tiles + b * 2 * AH;
+  for (int e = threadIdx.x; e < AH; e += blockDim.x) {
+    const int cm = e >> 6, r = (e >> 3) & 7, c = e & 7;
+    const int m = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + c;
+    const double v = (m < NP2 && k < NP2) ? Fb[(long)k * NP2 + m] * (double)sa : 0.0;
+    const __half h = __double2half(v);
+    out[e] = h;
+    out[AH + e] = __double2half(v - (double)__half2float(h));
+  }
+  if (threadIdx.x == 0) ainv[b] = 1.0f / sa;
+}
+
+// B tiles of every cluster of every level (one CTA each): per right-hand-side
+// column n a scale sB[n], Y_c^T scaled and split into [hi tile][lo tile], and
+// 1/sB[n] to binv (32 per cluster, zero-padded columns have scale 1).
+template <int NP2>
+__global__ void __launch_bounds__(256) k_build_h16_btiles(FarH16Tiles T, int nlev, int nrhs) {
+  using G = H16Shape<NP2>;
+  constexpr int BH = G::B_BYTES / 2;
+  __shared__ float cmax[8][kN];
+  __shared__ float scale[kN];
+  int c = blockIdx.x, lev = 0;
+  while (lev + 1 < nlev && c >= T.ncl[lev]) c -= T.ncl[lev++];
+  const float* y = T.y[lev] + (long)c * NP2 * nrhs;
+  // column maxima: thread (q, n) scans rows q, q + 8, ...
+  {
+    const int n = threadIdx.x & 31, q = threadIdx.x >> 5;
+    float mx = 0.0f;
+    if (n < nrhs)
+      for (int k = q; k < NP2; k += 8) mx = fmaxf(mx, fabsf(y[k * nrhs + n]));
+    cmax[q][n] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    float mx = 0.0f;
+    for (int q = 0; q < 8; ++q) mx = fmaxf(mx, cmax[q][threadIdx.x]);
+    const float sb = h16_scale(mx * 1.0000001f);
+    scale[threadIdx.x] = sb;
+    T.binv[lev][(long)c * kN + threadIdx.x] = 1.0f / sb;
+  }
+  __syncthreads();
+  __half* out = reinterpret_cast<__half*>(T.b[lev]) + (long)c * 2 * BH;
+  for (int e = threadIdx.x; e < BH; e += blockDim.x) {
+    const int cm = e >> 6, r = (e >> 3) & 7, cc = e & 7;
+    const int n = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + cc;
+    const float v = (n < nrhs && k < NP2) ? y[k * nrhs + n] * scale[n] : 0.0f;
+    const __half h = __float2half_rn(v);
+    out[e] = h;
+    out[BH + e] = __float2half_rn(v - __half2float(h));
+  }
+}
+
+#define BG_H16_SHAPES(X) X(4) X(9) X(16) X(25) X(36) X(49) X(64) X(81)
+
+size_t far_h16_atile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return H16Shape<N>::A2;
+    BG_H16_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+size_t far_h16_btile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return H16Shape<N>::B2;
+    BG_H16_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+
+cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, float* ainv,
+                                    cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  switch (np2) {
+#define BG_T(N)                                                                                               \
+  case N:                                                                                                     \
+    k_build_h16_atiles<N><<<(unsigned)nblocks, 256, 0, s>>>(F, bstride, static_cast<__half*>(tiles), ainv); \
+    break;
+    BG_H16_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s) {
+  if (nlev < 1 || nlev > kMaxFarLevels || nrhs < 1 || nrhs > kN) return cudaErrorInvalidValue;
+  int ncl_total = 0;
+  for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
+  if (ncl_total == 0) return cudaSuccess;
+  switch (np2) {
+#define BG_T(N) \
+  case N: k_build_h16_btiles<N><<<ncl_total, 256, 0, s>>>(T, nlev, nrhs); break;
+    BG_H16_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
+                           cudaStream_t s) {
+  if (nwork == 0) return cudaSuccess;
+  if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
+  switch (np2) {
+#define BG_T(N)                                                                                             \
+  case N: {                                                                                                 \
+    constexpr uint32_t smem = H16Shape<N>::SMEM;                                                            \
+    static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
+    cudaError_t e = cudaFuncSetAttribute(k_far_h16<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e;                                                                         \
+    k_far_h16<N><<<nwork, kStoredThreads, smem, s>>>(T, work, nrhs, err);                                   \
+    return cudaGetLastError();                                                                              \
+  }
+    BG_H16_SHAPES(BG_T)
 #undef BG_T
     default: return cudaErrorInvalidValue;
   }

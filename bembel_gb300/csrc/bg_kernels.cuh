@@ -94,6 +94,27 @@ cudaError_t launch_build_btiles(const FarTcTiles& T, int nlev, int np2, int nrhs
 // every row of every level in work; err as for launch_far_tc
 cudaError_t launch_far_tc_stored(const FarTcTiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
                                  cudaStream_t s);
+// FP16 stored-tile far field: as FarTcTiles plus the inverse block scales
+// (ainv, one per low-rank block) and inverse column scales (binv, 32 per
+// cluster, written by launch_build_h16_btiles)
+struct FarH16Tiles {
+  const int* row_ptr[kMaxFarLevels];
+  const int* col[kMaxFarLevels];
+  const unsigned char* a[kMaxFarLevels];
+  const float* ainv[kMaxFarLevels];
+  unsigned char* b[kMaxFarLevels];
+  float* binv[kMaxFarLevels];
+  const float* y[kMaxFarLevels];
+  float* z[kMaxFarLevels];
+  int ncl[kMaxFarLevels];
+};
+size_t far_h16_atile_bytes(int np2);  // per low-rank block (0: shape not supported)
+size_t far_h16_btile_bytes(int np2);  // per cluster
+cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, float* ainv,
+                                    cudaStream_t s);
+cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s);
+cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
+                           cudaStream_t s);
 // real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32
 bool far_tc_supported(bool cplx, int np2, int nrhs);
 

@@ -149,7 +149,8 @@ struct bg_operator {
   DevBuf d_dense32;                       // FP32 copy of the dense blocks (BG_PREC_FP32)
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_far_df;          // per level: FP32 (hi, lo) pairs of d_far64 (real operators)
-  std::vector<DevBuf*> d_far_atiles;      // per level: split tensor-core operand tiles of the low-rank blocks
+  std::vector<DevBuf*> d_far_atiles;      // per level: FP16 hi/lo tensor-core tiles of the low-rank blocks
+  std::vector<DevBuf*> d_far_ainv;        // per level: inverse power-of-two scale of every tile
   bool far_tiles = false;                 // every far-field level has its tiles
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
@@ -170,11 +171,12 @@ struct bg_operator {
   DevBuf w_xdof, w_xss, w_yss, w_ydof, w_xss32, w_yss32;
   std::vector<DevBuf*> w_y, w_z;  // per level
   std::vector<DevBuf*> w_ydf;     // per level: FP32 (hi, lo) split of w_y for the double-float product
-  std::vector<DevBuf*> w_btiles;  // per level: split right-hand-side tiles of every cluster
+  std::vector<DevBuf*> w_btiles;  // per level: FP16 hi/lo right-hand-side tiles of every cluster
+  std::vector<DevBuf*> w_binv;    // per level: inverse column scales of those tiles (32 per cluster)
 
   ~bg_operator() {
-    for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_far64, &d_far_df, &d_far_atiles, &d_mom64, &d_mom32, &w_y, &w_z, &w_ydf,
-                   &w_btiles})
+    for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv, &d_mom64, &d_mom32, &w_y,
+                   &w_z, &w_ydf, &w_btiles, &w_binv})
       for (auto b : *v) delete b;
   }
   size_t scalar_bytes(bool fp32) const { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }

@@ -324,11 +324,11 @@ def _read_profile(L, ctx):
 
 
 def far_tile_bytes(np2):
-    """Bytes of the TF32 hi + lo operand tiles of one low-rank block: row
-    groups of 8 targets x K padded to 8 sources, 4 bytes each."""
+    """Bytes of the FP16 hi + lo operand tiles of one low-rank block: row
+    groups of 8 targets x K padded to 16 sources, 2 bytes each."""
     mg = (np2 + 7) // 8
-    kp = (np2 + 7) // 8 * 8
-    return 2 * mg * 8 * kp * 4
+    kp = (np2 + 15) // 16 * 16
+    return 2 * mg * 8 * kp * 2
 
 
 def _roofline(op, prof, stats, steps):
@@ -360,13 +360,13 @@ def _roofline(op, prof, stats, steps):
                      "peak_source": src, "algorithmic_bytes_per_launch": algo})
         return base
     if cls == "far_fused_fp32":
-        # k_far_tc_stored: one launch per product streams the split operand
+        # k_far_h16: one launch per product streams the split operand
         # tiles of every low-rank block once (TMA bulk copies) into tcgen05.mma
         np2 = int(info[7]) ** 2
         tile = far_tile_bytes(np2)
         algo = nlow * tile
         ach = algo / t / 1e9
-        base.update({"kernel": "k_far_tc_stored (stored TF32 hi/lo tiles, TMA bulk copy -> tcgen05.mma, 32 RHS)",
+        base.update({"kernel": "k_far_h16 (stored scaled FP16 hi/lo tiles, TMA bulk copy -> tcgen05.mma, 32 RHS)",
                      "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                      "traffic": nlow * FAR_TILE_DRAM_BYTES_PER_BLOCK, "peak_source": src,
                      "algorithmic_bytes_per_launch": algo, "tile_bytes_per_block": tile,
