@@ -29,6 +29,7 @@
 // memory and returns.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "bg_kernels.cuh"
@@ -411,18 +412,7 @@ static cudaError_t launch_np(const FarTcLevels& L, const int2* work, int nwork, 
 }
 
 // ---------------------------------------------------------------------------
-// Stored-tile variant. The FP64 couplings of every low-rank block are split
-// once, at assembly, into TF32 high / FP32 remainder tiles already in the UMMA
-// core-matrix layout (2 x 11 x 2816 bytes per 81 x 81 block); per product the
-// split right-hand-side tiles of every cluster are built once
-// (launch_build_btiles). The product then moves whole tiles with 1-D TMA bulk
-// copies and does no per-entry work on the CUDA cores. Roles: warp 0 (one
-// thread) issues the bulk copies, warp 1 (one thread) the MMAs, warps 2-5
-// fold the accumulators of each finished block into Neumaier-compensated row
-// sums (one tensor-memory lane quadrant each). Stages and accumulator buffers
-// change hands through mbarriers: full (copies landed, by transaction bytes),
-// done (tcgen05.commit) and free (the epilogue drained the buffer). Every wait
-// is bounded, as in k_far_tc.
+// Stored-tile helpers: 1-D TMA bulk copies and wide tensor-memory loads.
 constexpr int kStoredThreads = 192;
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -451,267 +441,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-template <int NP2>
-struct StoredPlan {
-  using G = TcShape<NP2>;
-  static constexpr uint32_t A2 = 2 * G::A_BYTES, B2 = 2 * G::B_BYTES;  // bytes per block / per cluster
-  static constexpr uint32_t SMEM = 2 * G::STAGE > G::NEED ? 2 * G::STAGE : G::NEED;
-};
-
-template <int NP2>
-__global__ void __launch_bounds__(kStoredThreads, 1)
-    k_far_tc_stored(FarTcTiles T, const int2* __restrict__ work, int nrhs, int* __restrict__ err) {
-  using G = TcShape<NP2>;
-  constexpr uint32_t A2 = StoredPlan<NP2>::A2, B2 = StoredPlan<NP2>::B2;
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint64_t full_bar[2], done_bar[2], free_bar[2];
-  __shared__ uint32_t tmem_slot;
-  __shared__ int abort_flag;
-  volatile int* abort_v = &abort_flag;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int2 w = work[blockIdx.x];
-  const int lev = w.x, row = w.y;
-  const int* row_ptr = T.row_ptr[lev];
-  const int kb = row_ptr[row], ke = row_ptr[row + 1];
-  float* z = T.z[lev];
-  if (kb == ke) {  // no far-field block in this row (uniform over the CTA)
-    for (int e = tid; e < NP2 * nrhs; e += kStoredThreads) z[(long)row * NP2 * nrhs + e] = 0.0f;
-    return;
-  }
-  const int* col = T.col[lev];
-  const unsigned char* atiles = T.a[lev];
-  const unsigned char* btiles = T.b[lev];
-  const int nblk = ke - kb;
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
-  }
-  if (tid == 0) {
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&full_bar[b], 1);
-      mbar_init(&done_bar[b], 1);
-      mbar_init(&free_bar[b], 4);
-    }
-    abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = tmem_slot;
-
-  if (warp == 0) {
-    // ---- producer: whole tiles by 1-D TMA bulk copies ----
-    if (lane == 0) {
-      for (int it = 0; it < nblk; ++it) {
-        const int s = it & 1, k = kb + it;
-        if (it >= 2 && !mbar_wait(&done_bar[s], (uint32_t)(((it >> 1) - 1) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 4);
-          break;
-        }
-        if (*abort_v) break;
-        unsigned char* st = smem + s * G::STAGE;
-        const unsigned char* ga = atiles + (size_t)k * A2;
-        const unsigned char* gb = btiles + (size_t)col[k] * B2;
-        mbar_expect_tx(&full_bar[s], A2 + B2);
-        bulk_g2s(st, ga, G::A_BYTES, &full_bar[s]);
-        bulk_g2s(st + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[s]);
-        bulk_g2s(st + A2, gb, G::B_BYTES, &full_bar[s]);
-        bulk_g2s(st + A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[s]);
-      }
-    }
-  } else if (warp == 1) {
-    // ---- MMA issuer ----
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_tf32(128, kN);
-      const uint32_t base = smem_u32(smem);
-      for (int it = 0; it < nblk; ++it) {
-        const int s = it & 1;
-        if (!mbar_wait(&full_bar[s], (uint32_t)((it >> 1) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 5);
-          break;
-        }
-        if (it >= 2 && !mbar_wait(&free_bar[s], (uint32_t)(((it >> 1) - 1) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 6);
-          break;
-        }
-        if (*abort_v) break;
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const uint32_t a0 = base + s * G::STAGE, a1 = a0 + G::A_BYTES;
-        const uint32_t b0 = a0 + A2, b1 = b0 + G::B_BYTES;
-        const uint32_t d_hh = tmem + (uint32_t)(64 * s), d_cr = d_hh + 32;
-#pragma unroll
-        for (int pass = 0; pass < 3; ++pass) {
-          uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
-          uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
-          const uint32_t dd = pass == 0 ? d_hh : d_cr;
-#pragma unroll
-          for (int ks = 0; ks < G::KP / 8; ++ks) {
-            mma_tf32(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
-            ad += 16;
-            bd += 16;
-          }
-        }
-        mma_commit(&done_bar[s]);
-      }
-    }
-  } else {
-    // ---- epilogue warps 2-5: tensor-memory lanes 32 (warp % 4) .. +31 ----
-    float sum[32], comp[32];
-#pragma unroll
-    for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
-    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    bool ok = true;
-    for (int it = 0; it < nblk; ++it) {
-      const int s = it & 1;
-      int got = 1;
-      if (lane == 0) got = mbar_wait(&done_bar[s], (uint32_t)((it >> 1) & 1)) ? 1 : 0;
-      got = __shfl_sync(0xffffffffu, got, 0);
-      if (!got) {
-        if (lane == 0) {
-          *abort_v = 1;
-          atomicExch(err, 7);
-        }
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      float hh[32], cr[32];
-      tmem_ld32(lane_base + (uint32_t)(64 * s), hh);
-      tmem_ld32(lane_base + (uint32_t)(64 * s + 32), cr);
-#pragma unroll
-      for (int n = 0; n < 32; ++n) neumaier(sum[n], comp[n], hh[n] + cr[n]);
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&free_bar[s]);
-    }
-    const int m = (warp & 3) * 32 + lane;
-    if (ok && m < NP2) {
-      float* zo = z + ((long)row * NP2 + m) * nrhs;
-#pragma unroll
-      for (int n = 0; n < 32; ++n)
-        if (n < nrhs) zo[n] = sum[n] + comp[n];
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
-}
-
-// A tiles of nblocks FP64 blocks (column-major, stride bstride doubles): per
-// block [hi tile][lo tile], entry (m, k) in core matrix (m / 8) * KC + k / 4 at
-// lane 4 (m % 8) + k % 4; zero beyond n_p^2.
-template <int NP2>
-__global__ void k_build_atiles(const double* __restrict__ F, long bstride, long nblocks, float* __restrict__ tiles) {
-  using G = TcShape<NP2>;
-  constexpr int AF = G::A_BYTES / 4;  // floats per tile
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nblocks * AF) return;
-  const long b = t / AF;
-  const int e = (int)(t - b * AF), cm = e >> 5, lane = e & 31;
-  const int m = (cm / G::KC) * 8 + (lane >> 2), k = (cm % G::KC) * 4 + (lane & 3);
-  const double v = (m < NP2 && k < NP2) ? F[b * bstride + (long)k * NP2 + m] : 0.0;
-  const float h = tf32_hi((float)v);
-  tiles[b * 2 * AF + e] = h;
-  tiles[b * 2 * AF + AF + e] = (float)(v - (double)h);
-}
-
-// B tiles of every cluster of every level: Y_c^T (32 x n_p^2, K-major) split
-// into [hi tile][lo tile]; columns beyond nrhs and rows beyond n_p^2 are zero.
-template <int NP2>
-__global__ void k_build_btiles(FarTcTiles T, int nlev, int nrhs) {
-  using G = TcShape<NP2>;
-  constexpr int BF = G::B_BYTES / 4;
-  int c = blockIdx.x, lev = 0;
-  while (lev + 1 < nlev && c >= T.ncl[lev]) c -= T.ncl[lev++];
-  const float* y = T.y[lev] + (long)c * NP2 * nrhs;
-  float* out = reinterpret_cast<float*>(T.b[lev]) + (long)c * 2 * BF;
-  for (int e = threadIdx.x; e < BF; e += blockDim.x) {
-    const int cm = e >> 5, lane = e & 31;
-    const int n = (cm / G::KC) * 8 + (lane >> 2), k = (cm % G::KC) * 4 + (lane & 3);
-    const float v = (n < nrhs && k < NP2) ? y[k * nrhs + n] : 0.0f;
-    const float h = tf32_hi(v);
-    out[e] = h;
-    out[BF + e] = v - h;
-  }
-}
-
-#define BG_TC_SHAPES(X) X(4) X(9) X(16) X(25) X(36) X(49) X(64) X(81)
-
-size_t far_tc_atile_bytes(int np2) {
-  switch (np2) {
-#define BG_T(N) \
-  case N: return StoredPlan<N>::A2;
-    BG_TC_SHAPES(BG_T)
-#undef BG_T
-    default: return 0;
-  }
-}
-size_t far_tc_btile_bytes(int np2) {
-  switch (np2) {
-#define BG_T(N) \
-  case N: return StoredPlan<N>::B2;
-    BG_TC_SHAPES(BG_T)
-#undef BG_T
-    default: return 0;
-  }
-}
-
-cudaError_t launch_build_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, cudaStream_t s) {
-  if (nblocks == 0) return cudaSuccess;
-  const long n = nblocks * (long)(far_tc_atile_bytes(np2) / 8);
-  const unsigned grid = (unsigned)((n + 255) / 256);
-  switch (np2) {
-#define BG_T(N) \
-  case N: k_build_atiles<N><<<grid, 256, 0, s>>>(F, bstride, nblocks, static_cast<float*>(tiles)); break;
-    BG_TC_SHAPES(BG_T)
-#undef BG_T
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-cudaError_t launch_build_btiles(const FarTcTiles& T, int nlev, int np2, int nrhs, cudaStream_t s) {
-  if (nlev < 1 || nlev > kMaxFarLevels || nrhs < 1 || nrhs > kN) return cudaErrorInvalidValue;
-  int ncl_total = 0;
-  for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
-  if (ncl_total == 0) return cudaSuccess;
-  switch (np2) {
-#define BG_T(N) \
-  case N: k_build_btiles<N><<<ncl_total, 256, 0, s>>>(T, nlev, nrhs); break;
-    BG_TC_SHAPES(BG_T)
-#undef BG_T
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-cudaError_t launch_far_tc_stored(const FarTcTiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                                 cudaStream_t s) {
-  if (nwork == 0) return cudaSuccess;
-  if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
-  switch (np2) {
-#define BG_T(N)                                                                                             \
-  case N: {                                                                                                 \
-    constexpr uint32_t smem = StoredPlan<N>::SMEM;                                                          \
-    static_assert(smem <= 227 * 1024, "stored far field: shared memory plan too large");                    \
-    cudaError_t e = cudaFuncSetAttribute(k_far_tc_stored<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
-                                         (int)smem);                                                        \
-    if (e != cudaSuccess) return e;                                                                         \
-    k_far_tc_stored<N><<<nwork, kStoredThreads, smem, s>>>(T, work, nrhs, err);                             \
-    return cudaGetLastError();                                                                              \
-  }
-    BG_TC_SHAPES(BG_T)
-#undef BG_T
-    default: return cudaErrorInvalidValue;
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -762,7 +491,10 @@ __device__ __forceinline__ float h16_scale(float max_abs) {
 
 template <int NP2>
 __global__ void __launch_bounds__(kStoredThreads, 1)
-    k_far_h16(FarH16Tiles T, const int2* __restrict__ work, int nrhs, int* __restrict__ err) {
+    k_far_h16(FarH16Tiles T, const int2* __restrict__ work, int nwork, int nrhs, int* __restrict__ err) {
+  // Persistent: CTA c takes the rows c, c + gridDim.x, ... of the work list
+  // (sorted by block count) and all three roles walk the same flattened
+  // sequence of blocks, so the copy pipeline runs on across row boundaries.
   using G = H16Shape<NP2>;
   constexpr int S = kH16Stages;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -771,17 +503,6 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
   __shared__ int abort_flag;
   volatile int* abort_v = &abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int2 w = work[blockIdx.x];
-  const int lev = w.x, row = w.y;
-  const int* row_ptr = T.row_ptr[lev];
-  const int kb = row_ptr[row], ke = row_ptr[row + 1];
-  float* z = T.z[lev];
-  if (kb == ke) {  // no far-field block in this row (uniform over the CTA)
-    for (int e = tid; e < NP2 * nrhs; e += kStoredThreads) z[(long)row * NP2 * nrhs + e] = 0.0f;
-    return;
-  }
-  const int* col = T.col[lev];
-  const int nblk = ke - kb;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
                  "r"(kTmemCols));
@@ -805,24 +526,30 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
   if (warp == 0) {
     // ---- producer: whole tiles by 1-D TMA bulk copies ----
     if (lane == 0) {
-      const unsigned char* atiles = T.a[lev];
-      const unsigned char* btiles = T.b[lev];
-      for (int it = 0; it < nblk; ++it) {
-        const int st = it % S, k = kb + it;
-        if (it >= S && !mbar_wait(&done_bar[st], (uint32_t)((it / S - 1) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 4);
-          break;
+      int it = 0;
+      for (int wi = blockIdx.x; wi < nwork && !*abort_v; wi += gridDim.x) {
+        const int lev = work[wi].x, row = work[wi].y;
+        const int kb = T.row_ptr[lev][row], ke = T.row_ptr[lev][row + 1];
+        const int* col = T.col[lev];
+        const unsigned char* atiles = T.a[lev];
+        const unsigned char* btiles = T.b[lev];
+        for (int k = kb; k < ke; ++k, ++it) {
+          const int st = it % S;
+          if (it >= S && !mbar_wait(&done_bar[st], (uint32_t)((it / S - 1) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 4);
+            break;
+          }
+          if (*abort_v) break;
+          unsigned char* sm = smem + st * G::STAGE;
+          const unsigned char* ga = atiles + (size_t)k * G::A2;
+          const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
+          mbar_expect_tx(&full_bar[st], G::STAGE);
+          bulk_g2s(sm, ga, G::A_BYTES, &full_bar[st]);
+          bulk_g2s(sm + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[st]);
+          bulk_g2s(sm + G::A2, gb, G::B_BYTES, &full_bar[st]);
+          bulk_g2s(sm + G::A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
         }
-        if (*abort_v) break;
-        unsigned char* sm = smem + st * G::STAGE;
-        const unsigned char* ga = atiles + (size_t)k * G::A2;
-        const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
-        mbar_expect_tx(&full_bar[st], G::STAGE);
-        bulk_g2s(sm, ga, G::A_BYTES, &full_bar[st]);
-        bulk_g2s(sm + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[st]);
-        bulk_g2s(sm + G::A2, gb, G::B_BYTES, &full_bar[st]);
-        bulk_g2s(sm + G::A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
       }
     }
   } else if (warp == 1) {
@@ -830,84 +557,95 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_f16(128, kN);
       const uint32_t base = smem_u32(smem);
-      for (int it = 0; it < nblk; ++it) {
-        const int st = it % S, ab = it & 1;
-        if (!mbar_wait(&full_bar[st], (uint32_t)((it / S) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 5);
-          break;
-        }
-        if (it >= 2 && !mbar_wait(&free_bar[ab], (uint32_t)(((it >> 1) - 1) & 1))) {
-          *abort_v = 1;
-          atomicExch(err, 6);
-          break;
-        }
-        if (*abort_v) break;
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const uint32_t a0 = base + st * G::STAGE, a1 = a0 + G::A_BYTES;
-        const uint32_t b0 = a0 + G::A2, b1 = b0 + G::B_BYTES;
-        const uint32_t d_hh = tmem + (uint32_t)(64 * ab), d_cr = d_hh + 32;
-#pragma unroll
-        for (int pass = 0; pass < 3; ++pass) {
-          uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
-          uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
-          const uint32_t dd = pass == 0 ? d_hh : d_cr;
-#pragma unroll
-          for (int ks = 0; ks < G::KP / 16; ++ks) {
-            mma_f16(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
-            ad += 16;  // next K step: two core matrices = 256 bytes
-            bd += 16;
+      int it = 0;
+      for (int wi = blockIdx.x; wi < nwork && !*abort_v; wi += gridDim.x) {
+        const int lev = work[wi].x, row = work[wi].y;
+        const int nb = T.row_ptr[lev][row + 1] - T.row_ptr[lev][row];
+        for (int q = 0; q < nb; ++q, ++it) {
+          const int st = it % S, ab = it & 1;
+          if (!mbar_wait(&full_bar[st], (uint32_t)((it / S) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 5);
+            break;
           }
+          if (it >= 2 && !mbar_wait(&free_bar[ab], (uint32_t)(((it >> 1) - 1) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 6);
+            break;
+          }
+          if (*abort_v) break;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t a0 = base + st * G::STAGE, a1 = a0 + G::A_BYTES;
+          const uint32_t b0 = a0 + G::A2, b1 = b0 + G::B_BYTES;
+          const uint32_t d_hh = tmem + (uint32_t)(64 * ab), d_cr = d_hh + 32;
+#pragma unroll
+          for (int pass = 0; pass < 3; ++pass) {
+            uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
+            uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
+            const uint32_t dd = pass == 0 ? d_hh : d_cr;
+#pragma unroll
+            for (int ks = 0; ks < G::KP / 16; ++ks) {
+              mma_f16(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
+              ad += 16;  // next K step: two core matrices = 256 bytes
+              bd += 16;
+            }
+          }
+          mma_commit(&done_bar[st]);
         }
-        mma_commit(&done_bar[st]);
       }
     }
   } else {
     // ---- epilogue warps 2-5: tensor-memory lanes 32 (warp % 4) .. +31 ----
-    float sum[32], comp[32];
-#pragma unroll
-    for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    const float* ainv = T.ainv[lev];
-    const float* binv = T.binv[lev];
-    bool ok = true;
-    for (int it = 0; it < nblk; ++it) {
-      const int st = it % S, ab = it & 1, k = kb + it;
-      int got = 1;
-      if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
-      got = __shfl_sync(0xffffffffu, got, 0);
-      if (!got) {
-        if (lane == 0) {
-          *abort_v = 1;
-          atomicExch(err, 7);
-        }
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      float hh[32], cr[32];
-      tmem_ld32(lane_base + (uint32_t)(64 * ab), hh);
-      tmem_ld32(lane_base + (uint32_t)(64 * ab + 32), cr);
-      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&free_bar[ab]);
-      const float sa = __ldg(&ainv[k]);
-      const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 b4 = __ldg(&sb[q]);
-        neumaier(sum[4 * q + 0], comp[4 * q + 0], (hh[4 * q + 0] + cr[4 * q + 0]) * (sa * b4.x));
-        neumaier(sum[4 * q + 1], comp[4 * q + 1], (hh[4 * q + 1] + cr[4 * q + 1]) * (sa * b4.y));
-        neumaier(sum[4 * q + 2], comp[4 * q + 2], (hh[4 * q + 2] + cr[4 * q + 2]) * (sa * b4.z));
-        neumaier(sum[4 * q + 3], comp[4 * q + 3], (hh[4 * q + 3] + cr[4 * q + 3]) * (sa * b4.w));
-      }
-    }
     const int m = (warp & 3) * 32 + lane;
-    if (ok && m < NP2) {
-      float* zo = z + ((long)row * NP2 + m) * nrhs;
+    int it = 0;
+    bool ok = true;
+    for (int wi = blockIdx.x; wi < nwork && ok; wi += gridDim.x) {
+      const int lev = work[wi].x, row = work[wi].y;
+      const int kb = T.row_ptr[lev][row], ke = T.row_ptr[lev][row + 1];
+      const int* col = T.col[lev];
+      const float* ainv = T.ainv[lev];
+      const float* binv = T.binv[lev];
+      float sum[32], comp[32];
 #pragma unroll
-      for (int n = 0; n < 32; ++n)
-        if (n < nrhs) zo[n] = sum[n] + comp[n];
+      for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
+      for (int k = kb; k < ke; ++k, ++it) {
+        const int st = it % S, ab = it & 1;
+        int got = 1;
+        if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (!got) {
+          if (lane == 0) {
+            *abort_v = 1;
+            atomicExch(err, 7);
+          }
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        float hh[32], cr[32];
+        tmem_ld32(lane_base + (uint32_t)(64 * ab), hh);
+        tmem_ld32(lane_base + (uint32_t)(64 * ab + 32), cr);
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&free_bar[ab]);
+        const float sa = __ldg(&ainv[k]);
+        const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float4 b4 = __ldg(&sb[q]);
+          neumaier(sum[4 * q + 0], comp[4 * q + 0], (hh[4 * q + 0] + cr[4 * q + 0]) * (sa * b4.x));
+          neumaier(sum[4 * q + 1], comp[4 * q + 1], (hh[4 * q + 1] + cr[4 * q + 1]) * (sa * b4.y));
+          neumaier(sum[4 * q + 2], comp[4 * q + 2], (hh[4 * q + 2] + cr[4 * q + 2]) * (sa * b4.z));
+          neumaier(sum[4 * q + 3], comp[4 * q + 3], (hh[4 * q + 3] + cr[4 * q + 3]) * (sa * b4.w));
+        }
+      }
+      if (ok && m < NP2) {  // rows without blocks come out as zeros
+        float* zo = T.z[lev] + ((long)row * NP2 + m) * nrhs;
+#pragma unroll
+        for (int n = 0; n < 32; ++n)
+          if (n < nrhs) zo[n] = sum[n] + comp[n];
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -1043,6 +781,11 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
                            cudaStream_t s) {
   if (nwork == 0) return cudaSuccess;
   if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
+  // one persistent CTA per SM (the shared-memory plan allows one)
+  int dev = 0, nsm = 0;
+  cudaError_t ea = cudaGetDevice(&dev);
+  if (ea == cudaSuccess) ea = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (ea != cudaSuccess) return ea;
   switch (np2) {
 #define BG_T(N)                                                                                             \
   case N: {                                                                                                 \
@@ -1050,7 +793,7 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
     static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
     cudaError_t e = cudaFuncSetAttribute(k_far_h16<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e != cudaSuccess) return e;                                                                         \
-    k_far_h16<N><<<nwork, kStoredThreads, smem, s>>>(T, work, nrhs, err);                                   \
+    k_far_h16<N><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err);            \
     return cudaGetLastError();                                                                              \
   }
     BG_H16_SHAPES(BG_T)

@@ -75,28 +75,11 @@ struct FarTcLevels {
   const float* y[kMaxFarLevels];
   float* z[kMaxFarLevels];
 };
-// Stored-tile far field, per level: the low-rank blocks' split tiles (a),
-// the split right-hand-side tiles of every cluster (b, rebuilt per product
-// from y), the product's output (z) and the cluster count (ncl)
-struct FarTcTiles {
-  const int* row_ptr[kMaxFarLevels];
-  const int* col[kMaxFarLevels];
-  const unsigned char* a[kMaxFarLevels];
-  unsigned char* b[kMaxFarLevels];
-  const float* y[kMaxFarLevels];
-  float* z[kMaxFarLevels];
-  int ncl[kMaxFarLevels];
-};
-size_t far_tc_atile_bytes(int np2);  // per low-rank block (0: shape not supported)
-size_t far_tc_btile_bytes(int np2);  // per cluster
-cudaError_t launch_build_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, cudaStream_t s);
-cudaError_t launch_build_btiles(const FarTcTiles& T, int nlev, int np2, int nrhs, cudaStream_t s);
-// every row of every level in work; err as for launch_far_tc
-cudaError_t launch_far_tc_stored(const FarTcTiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                                 cudaStream_t s);
-// FP16 stored-tile far field: as FarTcTiles plus the inverse block scales
-// (ainv, one per low-rank block) and inverse column scales (binv, 32 per
-// cluster, written by launch_build_h16_btiles)
+// Stored-tile far field, per level: the low-rank blocks' scaled FP16 hi/lo
+// tiles (a) and their inverse scales (ainv, one per block), the right-hand-side
+// tiles of every cluster (b) and inverse column scales (binv, 32 per cluster),
+// both rebuilt per product from y by launch_build_h16_btiles, the product's
+// output (z) and the cluster count (ncl)
 struct FarH16Tiles {
   const int* row_ptr[kMaxFarLevels];
   const int* col[kMaxFarLevels];

@@ -42,11 +42,11 @@ METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed p
 FP64_ITERS_C2 = 253
 # FP32 FMA throughput of one GB300 measured with an FMA-chain probe (TFLOP/s)
 FP32_FMA_TFLOPS = 75.0
-# DRAM bytes (read + write) per low-rank block of k_far_tc_stored, from one ncu
-# capture of the same kernel on the M=4 sphere (1.1413 GB for 17 616 blocks,
-# 64 785 bytes per block against 61 952 bytes of A tiles; the rest is the
-# right-hand-side tiles and the output)
-FAR_TILE_DRAM_BYTES_PER_BLOCK = 1.1413e9 / 17616
+# DRAM bytes (read + write) per low-rank block of k_far_h16, from one ncu
+# capture of the same kernel on the M=4 sphere (619.7 MB for 17 616 blocks:
+# 35 178 bytes per block against 33 792 bytes of operand tiles; the rest is
+# right-hand-side tiles missing L2 and the output)
+FAR_TILE_DRAM_BYTES_PER_BLOCK = 619.68e6 / 17616
 INNER_DESC = {"mixed": "inner GMRES(FP64 near, FP32 fused far)", "fp32": "inner GMRES(FP32 near, FP32 fused far)"}
 
 
