@@ -197,7 +197,7 @@ class H2Matrix:
                                                   prec, 0))
         return Y[:, 0].copy() if squeeze else Y
 
-    def solve(self, b, tol=1e-8, restart=200, max_iter=3000, inner="mixed", inner_tol=1e-5, max_refinements=12):
+    def solve(self, b, tol=1e-8, restart=200, max_iter=3000, inner="fp32", inner_tol=2e-3, max_refinements=12):
         """GMRES with FP64 iterative refinement; returns (x, stats dict)."""
         p = SolveParams()
         _lib.load().bg_solve_params_default(ctypes.byref(p))

@@ -63,8 +63,8 @@ void bg_solve_params_default(bg_solve_params* p) {
   p->tol = 1e-8;
   p->restart = 200;
   p->max_iter = 2000;
-  p->inner_precision = BG_PREC_MIXED;
-  p->inner_tol = 1e-5;
+  p->inner_precision = BG_PREC_FP32;
+  p->inner_tol = 2e-3;
   p->max_refinements = 12;
 }
 

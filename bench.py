@@ -10,7 +10,7 @@ reference) and reused by every solve.
 
 value:  solves/s = right-hand sides solved to 1e-8 per second: FP64 flexible
         GMRES over the FP64 H2 matrix, preconditioned by an inner GMRES (tol
-        1e-2) on a low-precision operator (--inner fp32: FP32 near field and
+        2e-3) on a low-precision operator (--inner fp32: FP32 near field and
         FP32 on-the-fly far field, default; --inner mixed: FP64 near field),
         operands in HBM. Every solve meets 1e-8 in the FP64 residual.
 e2e:    the same through the public C ABI with host (pinned) buffers, the
@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 GEO = os.path.join(ROOT, "tests", "golden", "geo", "sphere.dat")
 M, P, NP, NRHS = 5, 2, 9, 32
 TOL = 1e-8
+INNER_TOL = 2e-3  # relative tolerance of each inner (preconditioning) solve; the library default
 METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed precision)"
 # FP64 GMRES iterations of this workload (restart 200), used by the CPU model
 FP64_ITERS_C2 = 253
@@ -55,7 +56,7 @@ def workload_config(extra=None):
            "elements": 6144, "dofs": 6936, "refinement": M, "degree": P, "n_p": NP, "eta": 1.6, "nrhs": NRHS,
            "tol": TOL, "rhs": "point sources |x0|~U[1.5,3], seed 3",
            "l2": "flush: 256 MiB buffer written between timed steps; operator data (near field 175 MB) > L2",
-           "solver": "FGMRES(FP64 H2) preconditioned by an inner GMRES(1e-2) on a low-precision operator"}
+           "solver": "FGMRES(FP64 H2) preconditioned by an inner GMRES(2e-3) on a low-precision operator"}
     if extra:
         cfg.update(extra)
     return cfg
@@ -197,7 +198,7 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def solve(inner, b):
-        return A.solve(b, tol=TOL, inner=inner, inner_tol=1e-2, restart=200, max_refinements=12)
+        return A.solve(b, tol=TOL, inner=inner, inner_tol=INNER_TOL, restart=200, max_refinements=12)
 
     # FP64 GPU path (reference solution for the accuracy report), outside the timed region
     x64, st64 = solve("fp64", b_dev_t)
@@ -408,7 +409,7 @@ def run_profile_case(args):
         print(json.dumps({"profile": "matvec", "precision": args.precision, "M": m, "N": op.N, "products": 5}))
     else:
         b = op.load_vector(0, rhs_points())
-        _, st = A.solve(b, tol=TOL, inner=args.inner, inner_tol=1e-2, restart=200, max_refinements=12)
+        _, st = A.solve(b, tol=TOL, inner=args.inner, inner_tol=INNER_TOL, restart=200, max_refinements=12)
         print(json.dumps({"profile": "solve", "inner": args.inner, "N": op.N, "stats": st}))
 
 

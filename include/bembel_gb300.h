@@ -42,8 +42,10 @@ typedef enum { BG_LAPLACE_SL = 0, BG_HELMHOLTZ_SL = 1, BG_MAXWELL_SL = 2 } bg_op
 /* Arithmetic of a product. BG_PREC_FP64 applies the FP64 H2 matrix (stored
  * near and far field, the reference's H2Matrix). BG_PREC_MIXED keeps the
  * near-field product, T and the vectors in FP64 and evaluates the far field in
- * FP32: couplings generated on the fly inside the fused product (nothing
- * stored), moments and transfers in FP32. BG_PREC_FP32 also applies the near
+ * FP32 on the tensor cores: from couplings split into scaled FP16 high and low
+ * parts at assembly (22 bits kept; real operators with the FP64 far field
+ * stored), else from couplings generated on the fly; moments and transfers in
+ * FP32. BG_PREC_FP32 also applies the near
  * field in FP32 (an FP32 copy of the assembled FP64 blocks); T and the input and
  * output vectors stay FP64. FP32 is meant for the inner operator of the solver,
  * whose outer FP64 iteration removes its rounding. */
@@ -68,8 +70,8 @@ typedef struct {
   double tol;            /* target ||b - A x|| / ||b|| per column */
   int restart;           /* Krylov restart length */
   int max_iter;          /* total inner iterations, all refinement steps */
-  int inner_precision;   /* bg_precision of the inner (correction) operator */
-  double inner_tol;      /* relative tolerance of each inner solve */
+  int inner_precision;   /* bg_precision of the inner (correction) operator; default BG_PREC_FP32 */
+  double inner_tol;      /* relative tolerance of each inner solve; default 2e-3 */
   int max_refinements;   /* outer FP64 residual steps */
 } bg_solve_params;
 
