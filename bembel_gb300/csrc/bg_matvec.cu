@@ -515,9 +515,114 @@ __global__ void __launch_bounds__(256) k_tgemm(const T* __restrict__ AT, int ld,
   }
 }
 
+// Few batch items (coarse FMM levels): one CTA of up to 1024 threads per item
+// and 32 columns stages all of op(A)^T and B at once, then splits K across
+// ksplit thread groups; partial tiles are added in a fixed order, so the result
+// does not depend on scheduling.
+template <bool ACC>
+__global__ void __launch_bounds__(1024) k_tgemm_small(const float* __restrict__ AT, int ld, int Mo, int Ki,
+                                                      const float* __restrict__ B, long bstride, float* __restrict__ C,
+                                                      long cstride, int kk, int vec_b, int ksplit) {
+  constexpr int RT = 3, CT = 4, NCOL = 32;
+  extern __shared__ __align__(16) float smg[];
+  float* As = smg;                     // [Ki][ld]
+  float* Bs = As + (size_t)Ki * ld;    // [Ki][NCOL]
+  float* red = Bs + (size_t)Ki * NCOL; // [ksplit - 1][ntiles][RT * CT]
+  const int b = blockIdx.x, cbase = NCOL * blockIdx.y, tid = threadIdx.x;
+  const int ncol = min(NCOL, kk - cbase);
+  const float* Bb = B + (long)b * bstride + cbase;
+  for (int o = 4 * tid; o < Ki * ld; o += 4 * blockDim.x) cp_async16(As + o, AT + o);
+  if (vec_b) {
+    const int per_row = ncol / 4;
+    for (int t = tid; t < Ki * per_row; t += blockDim.x) {
+      const int q = t / per_row, v = t - q * per_row;
+      cp_async16(Bs + q * NCOL + 4 * v, Bb + (long)q * kk + 4 * v);
+    }
+  } else {
+    for (int t = tid; t < Ki * ncol; t += blockDim.x) {
+      const int q = t / ncol, c = t - q * ncol;
+      Bs[q * NCOL + c] = Bb[(long)q * kk + c];
+    }
+  }
+  if (ncol < NCOL)
+    for (int t = tid; t < Ki * NCOL; t += blockDim.x)
+      if (t % NCOL >= ncol) Bs[t] = 0.0f;
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int rtiles = (Mo + RT - 1) / RT, ctiles = (ncol + CT - 1) / CT, ntiles = rtiles * ctiles;
+  const int tile = tid % ntiles, kq = tid / ntiles;
+  const bool active = kq < ksplit;
+  float acc[RT][CT];
+#pragma unroll
+  for (int r = 0; r < RT; ++r)
+#pragma unroll
+    for (int c = 0; c < CT; ++c) acc[r][c] = 0.0f;
+  const int i0 = (tile / ctiles) * RT, c0 = (tile % ctiles) * CT;
+  if (active) {
+    const int q0 = (int)((long)kq * Ki / ksplit), q1 = (int)((long)(kq + 1) * Ki / ksplit);
+    for (int q = q0; q < q1; ++q) {
+      float a[RT], bv[CT];
+#pragma unroll
+      for (int r = 0; r < RT; ++r) a[r] = As[q * ld + i0 + r];
+      load4(Bs + q * NCOL + c0, bv);
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[r][c] = fmaf(a[r], bv[c], acc[r][c]);
+    }
+    if (kq > 0) {
+      float* rp = red + ((size_t)(kq - 1) * ntiles + tile) * (RT * CT);
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) rp[r * CT + c] = acc[r][c];
+    }
+  }
+  __syncthreads();
+  if (active && kq == 0) {
+    for (int g = 1; g < ksplit; ++g) {
+      const float* rp = red + ((size_t)(g - 1) * ntiles + tile) * (RT * CT);
+#pragma unroll
+      for (int r = 0; r < RT; ++r)
+#pragma unroll
+        for (int c = 0; c < CT; ++c) acc[r][c] += rp[r * CT + c];
+    }
+    float* Cb = C + (long)b * cstride + cbase;
+#pragma unroll
+    for (int r = 0; r < RT; ++r)
+#pragma unroll
+      for (int c = 0; c < CT; ++c)
+        if (i0 + r < Mo && c0 + c < ncol) {
+          float* o = Cb + (long)(i0 + r) * kk + c0 + c;
+          *o = ACC ? *o + acc[r][c] : acc[r][c];
+        }
+  }
+}
+
 template <typename T>
 static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, T* C, long cstride, int nbatch, int kk,
                            cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    // coarse levels: fewer CTAs than SMs -> whole-operand staging and split K
+    const long ctas = (long)nbatch * ((kk + 31) / 32);
+    const int ntiles = ((A.Mo + 2) / 3) * 8;
+    if (nbatch > 0 && ctas <= 152 && ntiles <= 1024 && A.ld % 4 == 0 && A.ld >= (A.Mo + 2) / 3 * 3) {
+      const int ksplit = std::max(1, std::min(8, 1024 / ntiles));
+      const int threads = std::min(1024, (ntiles * ksplit + 31) / 32 * 32);
+      const size_t smem = ((size_t)A.Ki * A.ld + (size_t)A.Ki * 32 + (size_t)(ksplit - 1) * ntiles * 12) * 4;
+      if (smem <= 200 * 1024) {
+        const int vec_b = (kk % 4) == 0 && (bstride % 4) == 0 && (reinterpret_cast<uintptr_t>(B) % 16) == 0;
+        auto kf = acc ? k_tgemm_small<true> : k_tgemm_small<false>;
+        cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kf<<<dim3(nbatch, (kk + 31) / 32), threads, smem, s>>>(reinterpret_cast<const float*>(A.at), A.ld, A.Mo, A.Ki,
+                                                                reinterpret_cast<const float*>(B), bstride,
+                                                                reinterpret_cast<float*>(C), cstride, kk, vec_b, ksplit);
+        return cudaGetLastError();
+      }
+    }
+  }
   if (nbatch == 0) return cudaSuccess;
   const int rtiles = (A.Mo + 2) / 3;
   if (rtiles * 8 > 4 * 256 || A.ld < rtiles * 3 || A.ld % 4 != 0) return cudaErrorInvalidValue;
@@ -958,8 +1063,79 @@ cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// FP32 block-sparse product with register tiles: thread t owns rows
+// 4 (t / (nrhs/4)) .. +3 and right-hand sides 4 (t % (nrhs/4)) .. +3, so every
+// block column costs two 16-byte shared loads for 16 FMAs. Blocks and x panels
+// are staged with cp.async, double-buffered. Needs B % 4 == 0, nrhs % 4 == 0
+// and a 16-byte block stride.
+__global__ void __launch_bounds__(128) k_bsr32_tile(const int* __restrict__ row_ptr, const int* __restrict__ col,
+                                                    const float* __restrict__ blocks, long bstride, int B,
+                                                    const float* __restrict__ x, float* __restrict__ y, int nrhs,
+                                                    int accumulate) {
+  extern __shared__ __align__(16) float sm32[];
+  const int fsz = B * B, xsz = B * nrhs;
+  float* st[2] = {sm32, sm32 + fsz + xsz};
+  const int row = blockIdx.x, t = threadIdx.x;
+  const int cq = nrhs >> 2;
+  const int i0 = 4 * (t / cq), c0 = 4 * (t % cq);
+  const bool active = t < (B >> 2) * cq;
+  float acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.0f;
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  auto issue = [&](int k, float* dst) {
+    const float* F = blocks + (long)k * bstride;
+    for (int e = 4 * t; e < fsz; e += 4 * blockDim.x) cp_async16(dst + e, F + e);
+    const float* xs = x + (long)col[k] * xsz;
+    for (int e = 4 * t; e < xsz; e += 4 * blockDim.x) cp_async16(dst + fsz + e, xs + e);
+    cp_async_commit();
+  };
+  if (kb < ke) issue(kb, st[0]);
+  for (int k = kb; k < ke; ++k) {
+    const int sb = (k - kb) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // block k staged; everyone is done with block k-1
+    if (k + 1 < ke) issue(k + 1, st[sb ^ 1]);
+    if (active) {
+      const float* F = st[sb];
+      const float* xs = st[sb] + fsz;
+#pragma unroll 4
+      for (int j = 0; j < B; ++j) {
+        const float4 f = *reinterpret_cast<const float4*>(F + j * B + i0);
+        const float4 v = *reinterpret_cast<const float4*>(xs + j * nrhs + c0);
+        const float fr[4] = {f.x, f.y, f.z, f.w}, xv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(fr[r], xv[c], acc[r][c]);
+      }
+    }
+  }
+  if (active) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float* yo = y + ((long)row * B + i0 + r) * nrhs + c0;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) yo[c] = accumulate ? yo[c] + acc[r][c] : acc[r][c];
+    }
+  }
+}
+
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
                             int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (!cplx && nrows > 0 && B % 4 == 0 && nrhs % 4 == 0 && bstride % 4 == 0 && (B / 4) * (nrhs / 4) <= 128) {
+    const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float);
+    if (smem <= 100 * 1024) {
+      const int threads = (((B / 4) * (nrhs / 4)) + 31) / 32 * 32;
+      cudaError_t e = cudaFuncSetAttribute(k_bsr32_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k_bsr32_tile<<<nrows, threads, smem, s>>>(row_ptr, col, static_cast<const float*>(blocks), bstride, B,
+                                                static_cast<const float*>(x), static_cast<float*>(y), nrhs, accumulate);
+      return cudaGetLastError();
+    }
+  }
   if (cplx)
     return bsr_pipe_typed<cf>(row_ptr, col, (const cf*)blocks, bstride, nrows, B, (const cf*)x, (cf*)y, nrhs, accumulate, s);
   return bsr_pipe_typed<float>(row_ptr, col, (const float*)blocks, bstride, nrows, B, (const float*)x, (float*)y,
