@@ -203,7 +203,7 @@ struct Counters {
 // every column's residual estimate is below tol * ||b_c||.
 template <typename S>
 bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inner_tol, int inner_max, const void* b,
-                 void* x, double tol, int max_iter, Counters* cnt, std::vector<double>* relres) {
+                 void* x, double tol, int max_iter, Counters* cnt, std::vector<double>* relres, int gs_passes = 2) {
   const bool low = prec != BG_PREC_FP64;
   typedef HostS<S> H;
   bg_operator* op = K.op;
@@ -256,7 +256,8 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
         e = cudaMemsetAsync(zdst, 0, nk * sizeof(S), s);
         if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
         Counters ic;
-        if ((st = fgmres<S>(*inner, inner_prec, nullptr, 0, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr)) !=
+        // the inner solve only preconditions (tolerance ~1e-3): one Gram-Schmidt pass
+        if ((st = fgmres<S>(*inner, inner_prec, nullptr, 0, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr, 1)) !=
             BG_OK)
           return st;
         cnt->mixed_mv += ic.mixed_mv;
@@ -265,12 +266,13 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
       }
       if ((st = apply_operator(op, k, prec, zj, K.w.p)) != BG_OK) return st;
       ++(low ? cnt->mixed_mv : cnt->fp64_mv);
-      // classical Gram-Schmidt, two passes, and the norm, all on the device;
+      // classical Gram-Schmidt (gs_passes passes: two for the outer and the plain
+      // FP64 solve, one for the inner preconditioning solve) and the norm, on the device;
       // one copy brings the Hessenberg column back
       S* h1 = K.hdev.as<S>();
       S* h2 = h1 + (size_t)(m + 1) * k;
       S* h3 = h2 + (size_t)(m + 1) * k;
-      for (int pass = 0; pass < 2; ++pass) {
+      for (int pass = 0; pass < gs_passes; ++pass) {
         S* hp = pass == 0 ? h1 : h2;
         // split the rows over enough CTAs to fill the GPU
         const int nch = std::max(1, std::min(64, (4 * 152 + j) / (j + 1)));
@@ -310,7 +312,8 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
       });
       std::vector<H> hp1((size_t)(j + 1) * k), hp2((size_t)(j + 1) * k), hp3(k);
       e = cudaMemcpyAsync(hp1.data(), h1, hp1.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(hp2.data(), h2, hp2.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && gs_passes > 1)
+        e = cudaMemcpyAsync(hp2.data(), h2, hp2.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaMemcpyAsync(hp3.data(), h3, hp3.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
       if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres orthogonalisation");
