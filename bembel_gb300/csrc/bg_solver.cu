@@ -196,8 +196,8 @@ struct Counters {
 };
 
 // Right-preconditioned restarted (F)GMRES for A x = b on row-major FP64 work
-// vectors, x updated in place from its current value. A is the FP64 operator
-// (mixed = false) or the mixed one. With a preconditioner (inner != nullptr)
+// vectors; x must be zero on entry and is updated in place. A is the operator
+// of precision prec. With a preconditioner (inner != nullptr)
 // z_j = M^-1 v_j is an inner GMRES solve on the low-precision operator and the
 // directions z_j are kept (flexible GMRES); otherwise z_j = v_j. Stops when
 // every column's residual estimate is below tol * ||b_c||.
@@ -220,14 +220,21 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
   std::vector<H> hcol((size_t)(m + 1) * k);
   std::vector<double> inv(k), beta;
   int it = 0;
+  bool first_cycle = true;
   while (true) {
-    // true residual r = b - A x
-    if ((st = apply_operator(op, k, prec, x, r.p)) != BG_OK) return st;
-    ++(low ? cnt->mixed_mv : cnt->fp64_mv);
-    timed_launch(op->ctx, KC_KRYLOV, [&] {
-      k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(b), nk, r.as<S>());
-      return cudaGetLastError();
-    });
+    // true residual r = b - A x (x is zero on entry, so the first one is b)
+    if (first_cycle) {
+      e = cudaMemcpyAsync(r.p, b, nk * sizeof(S), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
+      first_cycle = false;
+    } else {
+      if ((st = apply_operator(op, k, prec, x, r.p)) != BG_OK) return st;
+      ++(low ? cnt->mixed_mv : cnt->fp64_mv);
+      timed_launch(op->ctx, KC_KRYLOV, [&] {
+        k_residual<S><<<nblk(nk), 256, 0, s>>>(static_cast<const S*>(b), nk, r.as<S>());
+        return cudaGetLastError();
+      });
+    }
     if ((st = col_norms<S>(K, r.p, &beta)) != BG_OK) return st;
     bool done = true;
     for (int c = 0; c < k; ++c)
