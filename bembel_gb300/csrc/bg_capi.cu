@@ -108,6 +108,11 @@ bg_status bg_profile_enable(bg_context* ctx, int enable) {
   ctx->profiling = enable != 0;
   return BG_OK;
 }
+bg_status bg_profile_classes(bg_context* ctx, unsigned mask) {
+  if (!ctx) return BG_INVALID_ARG;
+  ctx->profile_mask = mask;
+  return BG_OK;
+}
 bg_status bg_profile_read(bg_context* ctx, double* ms8, long* launches8) {
   if (!ctx || !ms8 || !launches8) return BG_INVALID_ARG;
   if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context");

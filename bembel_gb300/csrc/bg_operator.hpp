@@ -68,6 +68,7 @@ struct bg_context {
   size_t pinned_bytes = 0;
   // kernel-class timing with CUDA events on `stream` (bg_profile)
   bool profiling = false;
+  unsigned profile_mask = 0xFFu;  // kernel classes bracketed with events while profiling
   long launches = 0;
   std::vector<cudaEvent_t> event_pool;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[8];
@@ -95,7 +96,7 @@ template <typename F>
 cudaError_t timed_launch(bg_context* ctx, int cls, F&& f) {
   ++ctx->launches;
   ++ctx->class_launches[cls];
-  if (!ctx->profiling) return f();
+  if (!ctx->profiling || !(ctx->profile_mask & (1u << cls))) return f();
   cudaEvent_t a = ctx->get_event(), b = ctx->get_event();
   cudaEventRecord(a, ctx->stream);
   cudaError_t e = f();
@@ -174,7 +175,12 @@ struct bg_operator {
   std::vector<DevBuf*> w_btiles;  // per level: FP16 hi/lo right-hand-side tiles of every cluster
   std::vector<DevBuf*> w_binv;    // per level: inverse column scales of those tiles (32 per cluster)
 
+  // solver workspaces kept between bg_solve calls (owned by the solver)
+  void* solver_ws = nullptr;
+  void (*solver_ws_free)(void*) = nullptr;
+
   ~bg_operator() {
+    if (solver_ws && solver_ws_free) solver_ws_free(solver_ws);
     for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv, &d_mom64, &d_mom32, &w_y,
                    &w_z, &w_ydf, &w_btiles, &w_binv})
       for (auto b : *v) delete b;

@@ -150,7 +150,21 @@ struct Krylov {
   bg_operator* op;
   int N, k, m;
   bool flexible;          // store the preconditioned directions Z
-  DevBuf V, Z, w, hdev, inv, ydev, part;
+  DevBuf V, Z, w, hdev, inv, ydev, part, r;
+  size_t hpin_bytes = 0;
+  // two pinned slots for the Hessenberg column of an Arnoldi step (h1, h2,
+  // norm), each with an event, so the host reads step j while step j+1 runs
+  void* hpin = nullptr;
+  size_t slot_bytes = 0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  Krylov() {}
+  Krylov(const Krylov&) = delete;
+  Krylov& operator=(const Krylov&) = delete;
+  ~Krylov() {
+    if (hpin) cudaFreeHost(hpin);
+    for (auto& x : ev)
+      if (x) cudaEventDestroy(x);
+  }
   bg_status init(bg_operator* o, int kk, int mm, bool flex, size_t sb) {
     op = o;
     N = o->N;
@@ -165,9 +179,37 @@ struct Krylov {
     if (e == cudaSuccess) e = part.alloc((size_t)(m + 1) * 64 * k * sb);
     if (e == cudaSuccess) e = inv.alloc(k * sizeof(double));
     if (e == cudaSuccess) e = ydev.alloc((size_t)(m + 1) * k * sb);
+    if (e == cudaSuccess) e = r.alloc(nk * sb);
+    // buffers are kept between solves and grown only when needed
+    slot_bytes = (size_t)(2 * (m + 1) + 1) * k * sb;
+    if (e == cudaSuccess && 2 * slot_bytes > hpin_bytes) {
+      if (hpin) cudaFreeHost(hpin);
+      hpin = nullptr;
+      hpin_bytes = 0;
+      e = cudaMallocHost(&hpin, 2 * slot_bytes);
+      if (e == cudaSuccess) hpin_bytes = 2 * slot_bytes;
+    }
+    for (auto& x : ev)
+      if (e == cudaSuccess && !x) e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
     return cuda_status(o->ctx, e, "solver workspace");
   }
 };
+
+// Solver workspaces of an operator, kept between bg_solve calls so that a
+// solve allocates nothing once the sizes have been seen (and no cudaFree
+// synchronises the device inside a solve)
+struct SolverWS {
+  Krylov plain, outer, inner;
+  DevBuf bw, xw, bu, xu;
+};
+void free_solver_ws(void* p) { delete static_cast<SolverWS*>(p); }
+SolverWS* get_ws(bg_operator* op) {
+  if (!op->solver_ws) {
+    op->solver_ws = new SolverWS();
+    op->solver_ws_free = free_solver_ws;
+  }
+  return static_cast<SolverWS*>(op->solver_ws);
+}
 
 template <typename S>
 using HostS = typename std::conditional<std::is_same<S, double>::value, double, std::complex<double>>::type;
@@ -213,9 +255,8 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
   std::vector<double> bn;
   bg_status st = col_norms<S>(K, b, &bn);
   if (st != BG_OK) return st;
-  DevBuf r;
-  cudaError_t e = r.alloc(nk * sizeof(S));
-  if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
+  DevBuf& r = K.r;
+  cudaError_t e = cudaSuccess;
   std::vector<H> Hm((size_t)(m + 1) * m * k), g((size_t)(m + 1) * k), cs((size_t)m * k), sn((size_t)m * k);
   std::vector<H> hcol((size_t)(m + 1) * k);
   std::vector<double> inv(k), beta;
@@ -254,76 +295,91 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
     std::fill(Hm.begin(), Hm.end(), H(0));
     std::fill(g.begin(), g.end(), H(0));
     for (int c = 0; c < k; ++c) g[c] = beta[c];
-    int j = 0;
-    for (; j < m && it < max_iter; ++j, ++it) {
-      S* vj = K.V.as<S>() + (long)j * vstride;
-      const S* zj = vj;
-      if (inner) {
-        S* zdst = K.Z.as<S>() + (long)j * vstride;
-        e = cudaMemsetAsync(zdst, 0, nk * sizeof(S), s);
-        if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
-        Counters ic;
-        // the inner solve only preconditions (tolerance ~1e-3): one Gram-Schmidt pass
-        if ((st = fgmres<S>(*inner, inner_prec, nullptr, 0, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr, 1)) !=
-            BG_OK)
-          return st;
-        cnt->mixed_mv += ic.mixed_mv;
-        cnt->inner_it += ic.outer_it;
-        zj = zdst;
-      }
-      if ((st = apply_operator(op, k, prec, zj, K.w.p)) != BG_OK) return st;
-      ++(low ? cnt->mixed_mv : cnt->fp64_mv);
-      // classical Gram-Schmidt (gs_passes passes: two for the outer and the plain
-      // FP64 solve, one for the inner preconditioning solve) and the norm, on the device;
-      // one copy brings the Hessenberg column back
-      S* h1 = K.hdev.as<S>();
-      S* h2 = h1 + (size_t)(m + 1) * k;
-      S* h3 = h2 + (size_t)(m + 1) * k;
-      for (int pass = 0; pass < gs_passes; ++pass) {
-        S* hp = pass == 0 ? h1 : h2;
-        // split the rows over enough CTAs to fill the GPU
-        const int nch = std::max(1, std::min(64, (4 * 152 + j) / (j + 1)));
-        const int rows_per = (N + nch - 1) / nch;
+    // Arnoldi steps with the host one step behind (without an inner solve):
+    // step jj+1 is launched (it needs only device data) before the host reads
+    // step jj's Hessenberg column from its pinned slot, so the GPU does not wait
+    // for the host. A step launched after the last needed one is wasted,
+    // nothing else; its pinned slot is the other one of the two.
+    const int it0 = it;
+    auto launch_step = [&](int jj) -> bg_status {
+        S* vj = K.V.as<S>() + (long)jj * vstride;
+        const S* zj = vj;
+        if (inner) {
+          S* zdst = K.Z.as<S>() + (long)jj * vstride;
+          e = cudaMemsetAsync(zdst, 0, nk * sizeof(S), s);
+          if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres");
+          Counters ic;
+          // the inner solve only preconditions (tolerance ~1e-3): one Gram-Schmidt pass
+          if ((st = fgmres<S>(*inner, inner_prec, nullptr, 0, 0, 0, vj, zdst, inner_tol, inner_max, &ic, nullptr, 1)) !=
+              BG_OK)
+            return st;
+          cnt->mixed_mv += ic.mixed_mv;
+          cnt->inner_it += ic.outer_it;
+          zj = zdst;
+        }
+        if ((st = apply_operator(op, k, prec, zj, K.w.p)) != BG_OK) return st;
+        ++(low ? cnt->mixed_mv : cnt->fp64_mv);
+        // classical Gram-Schmidt (gs_passes passes: two for the outer and the plain
+        // FP64 solve, one for the inner preconditioning solve) and the norm, on the device;
+        // one copy brings the Hessenberg column back
+        S* h1 = K.hdev.as<S>();
+        S* h2 = h1 + (size_t)(m + 1) * k;
+        S* h3 = h2 + (size_t)(m + 1) * k;
+        for (int pass = 0; pass < gs_passes; ++pass) {
+          S* hp = pass == 0 ? h1 : h2;
+          // split the rows over enough CTAs to fill the GPU
+          const int nch = std::max(1, std::min(64, (4 * 152 + jj) / (jj + 1)));
+          const int rows_per = (N + nch - 1) / nch;
+          timed_launch(op->ctx, KC_KRYLOV, [&] {
+            k_mdot_part<S><<<dim3(jj + 1, nch), 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, rows_per,
+                                                            K.part.as<S>());
+            return cudaGetLastError();
+          });
+          timed_launch(op->ctx, KC_KRYLOV, [&] {
+            k_reduce_parts<S><<<((jj + 1) * k + 255) / 256, 256, 0, s>>>(K.part.as<S>(), jj + 1, nch, k, hp);
+            return cudaGetLastError();
+          });
+          timed_launch(op->ctx, KC_KRYLOV, [&] {
+            k_vupdate<S><<<nblk(nk), 256, 0, s>>>(K.V.as<S>(), vstride, jj + 1, hp, N, k, K.w.as<S>());
+            return cudaGetLastError();
+          });
+        }
+        {
+          const int nch = 64, rows_per = (N + nch - 1) / nch;
+          timed_launch(op->ctx, KC_KRYLOV, [&] {
+            k_mdot_part<S><<<dim3(1, nch), 256, 0, s>>>(K.w.as<S>(), 0, K.w.as<S>(), N, k, rows_per, K.part.as<S>());
+            return cudaGetLastError();
+          });
+          timed_launch(op->ctx, KC_KRYLOV, [&] {
+            k_reduce_parts<S><<<1, 256, 0, s>>>(K.part.as<S>(), 1, nch, k, h3);
+            return cudaGetLastError();
+          });
+        }
         timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_mdot_part<S><<<dim3(j + 1, nch), 256, 0, s>>>(K.V.as<S>(), vstride, K.w.as<S>(), N, k, rows_per,
-                                                          K.part.as<S>());
+          k_inv_norm<S><<<1, 64, 0, s>>>(h3, k, K.inv.as<double>());
           return cudaGetLastError();
         });
         timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_reduce_parts<S><<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.part.as<S>(), j + 1, nch, k, hp);
+          k_vscale<S><<<nblk(nk), 256, 0, s>>>(K.w.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>() + (long)(jj + 1) * vstride);
           return cudaGetLastError();
         });
-        timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_vupdate<S><<<nblk(nk), 256, 0, s>>>(K.V.as<S>(), vstride, j + 1, hp, N, k, K.w.as<S>());
-          return cudaGetLastError();
-        });
-      }
-      {
-        const int nch = 64, rows_per = (N + nch - 1) / nch;
-        timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_mdot_part<S><<<dim3(1, nch), 256, 0, s>>>(K.w.as<S>(), 0, K.w.as<S>(), N, k, rows_per, K.part.as<S>());
-          return cudaGetLastError();
-        });
-        timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_reduce_parts<S><<<1, 256, 0, s>>>(K.part.as<S>(), 1, nch, k, h3);
-          return cudaGetLastError();
-        });
-      }
-      timed_launch(op->ctx, KC_KRYLOV, [&] {
-        k_inv_norm<S><<<1, 64, 0, s>>>(h3, k, K.inv.as<double>());
-        return cudaGetLastError();
-      });
-      timed_launch(op->ctx, KC_KRYLOV, [&] {
-        k_vscale<S><<<nblk(nk), 256, 0, s>>>(K.w.as<S>(), K.inv.as<double>(), N, k, K.V.as<S>() + (long)(j + 1) * vstride);
-        return cudaGetLastError();
-      });
-      std::vector<H> hp1((size_t)(j + 1) * k), hp2((size_t)(j + 1) * k), hp3(k);
-      e = cudaMemcpyAsync(hp1.data(), h1, hp1.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
+      unsigned char* slot = static_cast<unsigned char*>(K.hpin) + (jj & 1) * K.slot_bytes;
+      e = cudaMemcpyAsync(slot, h1, (size_t)(jj + 1) * k * sizeof(S), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess && gs_passes > 1)
-        e = cudaMemcpyAsync(hp2.data(), h2, hp2.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(hp3.data(), h3, hp3.size() * sizeof(S), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) return cuda_status(op->ctx, e, "gmres orthogonalisation");
+        e = cudaMemcpyAsync(slot + (size_t)(m + 1) * k * sizeof(S), h2, (size_t)(jj + 1) * k * sizeof(S),
+                            cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot + (size_t)2 * (m + 1) * k * sizeof(S), h3, k * sizeof(S), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaEventRecord(K.ev[jj & 1], s);
+      return cuda_status(op->ctx, e, "gmres orthogonalisation");
+    };
+    auto process_column = [&](int j, bool* all_done_out) -> bg_status {
+      cudaError_t ee = cudaEventSynchronize(K.ev[j & 1]);
+      if (ee != cudaSuccess) return cuda_status(op->ctx, ee, "gmres orthogonalisation");
+      const H* slot = reinterpret_cast<const H*>(static_cast<unsigned char*>(K.hpin) + (j & 1) * K.slot_bytes);
+      std::vector<H> hp1(slot, slot + (size_t)(j + 1) * k), hp2((size_t)(j + 1) * k, H(0)), hp3(k);
+      if (gs_passes > 1) std::copy(slot + (size_t)(m + 1) * k, slot + (size_t)(m + 1) * k + (size_t)(j + 1) * k, hp2.begin());
+      std::copy(slot + (size_t)2 * (m + 1) * k, slot + (size_t)2 * (m + 1) * k + k, hp3.begin());
       for (size_t q = 0; q < hp1.size(); ++q) hcol[q] = hp1[q] + hp2[q];
       std::vector<double> hn(k);
       for (int c = 0; c < k; ++c) hn[c] = std::sqrt(std::abs(hp3[c]));
@@ -354,12 +410,32 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
         g[(size_t)j * k + c] = cc * gj;
         if (std::abs(g[(size_t)(j + 1) * k + c]) > tol * bn[c] && hn[c] > 0) all_done = false;
       }
-      if (all_done) {
-        ++j;
-        ++it;
-        break;
+      *all_done_out = all_done;
+      return BG_OK;
+    };
+    auto can_launch = [&](int q) { return q < m && it0 + q < max_iter; };
+    // a flexible step contains an inner solve: too costly to launch speculatively
+    const bool speculate = inner == nullptr;
+    int launched = 0, j = 0;
+    if (can_launch(0)) {
+      if ((st = launch_step(0)) != BG_OK) return st;
+      launched = 1;
+    }
+    while (j < launched) {
+      if (speculate && can_launch(launched)) {
+        if ((st = launch_step(launched)) != BG_OK) return st;
+        ++launched;
+      }
+      bool all_done = false;
+      if ((st = process_column(j, &all_done)) != BG_OK) return st;
+      ++j;
+      if (all_done) break;
+      if (!speculate && can_launch(launched)) {
+        if ((st = launch_step(launched)) != BG_OK) return st;
+        ++launched;
       }
     }
+    it = it0 + j;
     // y = R^-1 g per column; x += [V or Z] y
     std::vector<H> y((size_t)j * k, H(0));
     for (int c = 0; c < k; ++c) {
@@ -395,13 +471,14 @@ bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, cons
   std::vector<double> relres;
   bg_status st;
   if (!mixed) {
-    Krylov K;
+    Krylov& K = get_ws(op)->plain;
     if ((st = K.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
     st = fgmres<S>(K, BG_PREC_FP64, nullptr, 0, 0, 0, bdof, xdof, prm.tol, prm.max_iter, &cnt, &relres);
     cnt.inner_it = cnt.outer_it;
   } else {
     // outer FP64 flexible GMRES; each direction is an inner mixed GMRES solve
-    Krylov outer, inner;
+    Krylov& outer = get_ws(op)->outer;
+    Krylov& inner = get_ws(op)->inner;
     const int mo = std::max(2, prm.max_refinements);
     if ((st = outer.init(op, k, mo, true, sizeof(S))) != BG_OK) return st;
     if ((st = inner.init(op, k, std::max(2, prm.restart), false, sizeof(S))) != BG_OK) return st;
@@ -446,7 +523,9 @@ extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs,
     bg_status st = ensure_work(op, k);
     if (st != BG_OK) return st;
     const long nk = (long)op->N * k;
-    DevBuf bw, xw, bu;
+    DevBuf& bw = get_ws(op)->bw;
+    DevBuf& xw = get_ws(op)->xw;
+    DevBuf& bu = get_ws(op)->bu;
     cudaError_t e = bw.alloc(nk * usz);
     if (e == cudaSuccess) e = xw.alloc(nk * usz);
     const void* bsrc = static_cast<const char*>(b) + (size_t)c0 * op->N * usz;
@@ -471,7 +550,7 @@ extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs,
     total.final_relres = std::max(total.final_relres, part.final_relres);
     const double one[2] = {1, 0}, zero2[2] = {0, 0};
     void* xdst = static_cast<char*>(x) + (size_t)c0 * op->N * usz;
-    DevBuf xu;
+    DevBuf& xu = get_ws(op)->xu;
     void* xd = xdst;
     if (!on_device) {
       if ((e = xu.alloc(nk * usz)) != cudaSuccess) return cuda_status(op->ctx, e, "solve staging");

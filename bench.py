@@ -212,6 +212,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
         times, stats = [], None
         if profile:
+            # inside the timed region only the dominant kernel class is bracketed
+            # with events (one pair per product); launches are counted for all
+            L.bg_profile_classes(ctx.h, 1 << CLASSES.index("far_fused_fp32"))
             L.bg_profile_enable(ctx.h, 1)
             _read_profile(L, ctx)  # reset counters
         for _ in range(steps):
@@ -231,11 +234,22 @@ def run_gpu(args):
             dist.barrier()
         return np.array(times), x, stats, prof
 
+    def class_breakdown(inner, b):
+        """Device time per kernel class of one untimed solve, every class bracketed."""
+        L.bg_profile_classes(ctx.h, 0xFF)
+        L.bg_profile_enable(ctx.h, 1)
+        _read_profile(L, ctx)
+        solve(inner, b)
+        prof = _read_profile(L, ctx)
+        L.bg_profile_enable(ctx.h, 0)
+        return prof
+
     inner = args.inner
     other = "mixed" if inner == "fp32" else "fp32"
     clocks = ClockSampler(local)
     with clocks:
         t_mixed, xm, stm, prof = timed_steps(inner, b_dev_t, args.steps, args.warmup, profile=True)
+    breakdown = class_breakdown(inner, b_dev_t)
     t_fp64, _, _, _ = timed_steps("fp64", b_dev_t, max(1, min(2, args.steps)), 1)
     t_other, _, st_other, _ = timed_steps(other, b_dev_t, max(1, min(2, args.steps)), 1)
     # end to end: host pinned b, host x, copies inside the step
@@ -303,7 +317,9 @@ def run_gpu(args):
             "matvec": {"fp64_products_per_s_32rhs": mv64, "mixed_products_per_s_32rhs": mvmx,
                        "fp32_products_per_s_32rhs": mv32, "fp64_matvec_per_s": mv64 * NRHS,
                        "mixed_matvec_per_s": mvmx * NRHS, "fp32_matvec_per_s": mv32 * NRHS},
-            "assembly_s": asm, "kernel_ms": prof["ms"] if prof else None}
+            "assembly_s": asm,
+            "kernel_ms_per_solve": {k: round(v, 3) for k, v in breakdown["ms"].items()},
+            "kernel_launches_per_solve": breakdown["launches"]}
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k in ("value", "unit", "cores", "kind",
                                                                                "sample")}

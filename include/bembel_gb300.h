@@ -101,6 +101,10 @@ bg_status bg_context_get_stream(bg_context* ctx, void** stream);
  * read, then resets them. */
 bg_status bg_profile_enable(bg_context* ctx, int enable);
 bg_status bg_profile_read(bg_context* ctx, double* ms8, long* launches8);
+/* Kernel classes (bit c for class c, in the order above) that bg_profile_enable
+ * brackets with events; default all. Timing only the classes of interest keeps
+ * the event overhead out of a measured region. Launch counts cover all. */
+bg_status bg_profile_classes(bg_context* ctx, unsigned mask);
 
 /* Geometry(const std::string&) with LoadGeometryFileDAT
  * (Geometry/Geometry.hpp:89-102, Geometry/GeometryIO.hpp:25-122). */
