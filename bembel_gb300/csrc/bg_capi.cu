@@ -151,6 +151,49 @@ bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** 
   *out = g;
   return BG_OK;
 }
+bg_status bg_geometry_from_bezier(bg_context* ctx, int npatch, const int* px, const int* py, const double* data,
+                                  bg_geometry** out) {
+  if (!ctx || !out || npatch <= 0 || !px || !py || !data || ctx->closing) return BG_INVALID_ARG;
+  *out = nullptr;
+  bg_geometry* g = new (std::nothrow) bg_geometry();
+  if (!g) return BG_OOM;
+  long off = 0;
+  for (int p = 0; p < npatch; ++p) {
+    if (px[p] < 1 || py[p] < 1 || px[p] > 16 || py[p] > 16) {
+      delete g;
+      return set_error(ctx, BG_INVALID_ARG, "patch " + std::to_string(p) + ": control points per direction out of 1..16");
+    }
+    PatchData P;
+    P.px = px[p];
+    P.py = py[p];
+    P.cp.assign(data + off, data + off + 4L * px[p] * py[p]);
+    off += 4L * px[p] * py[p];
+    for (int c = 0; c < px[p] * py[p]; ++c)
+      if (!(P.cp[4 * c + 3] > 0.0) || !std::isfinite(P.cp[4 * c]) || !std::isfinite(P.cp[4 * c + 1]) ||
+          !std::isfinite(P.cp[4 * c + 2])) {
+        delete g;
+        return set_error(ctx, BG_INVALID_ARG, "patch " + std::to_string(p) + ": non-finite point or weight <= 0");
+      }
+    g->g.patches.push_back(std::move(P));
+  }
+  g->ctx = ctx;
+  context_retain(ctx);
+  *out = g;
+  return BG_OK;
+}
+bg_status bg_geometry_patch_data(const bg_geometry* g, int patch, int* px, int* py, double* data) {
+  if (!g || !px || !py || patch < 0 || patch >= (int)g->g.patches.size()) return BG_INVALID_ARG;
+  const PatchData& P = g->g.patches[patch];
+  *px = P.px;
+  *py = P.py;
+  if (data) std::copy(P.cp.begin(), P.cp.end(), data);
+  return BG_OK;
+}
+bg_status bg_geometry_num_patches(const bg_geometry* g, int* n) {
+  if (!g || !n) return BG_INVALID_ARG;
+  *n = (int)g->g.patches.size();
+  return BG_OK;
+}
 bg_status bg_geometry_destroy(bg_geometry* g) {
   if (!g) return BG_INVALID_ARG;
   bg_context* ctx = g->ctx;

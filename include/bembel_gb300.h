@@ -110,6 +110,18 @@ bg_status bg_profile_classes(bg_context* ctx, unsigned mask);
  * (Geometry/Geometry.hpp:89-102, Geometry/GeometryIO.hpp:25-122). */
 bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** out);
 bg_status bg_geometry_destroy(bg_geometry* g);
+/* Geometry(const PatchVector&) (Geometry/Geometry.hpp:60-63) from Bezier
+ * patches already in memory, so an existing Bembel::Geometry can be handed
+ * over without a file: patch p has px[p] x py[p] control points (degree + 1 per
+ * direction) in the layout of Patch::data_ for a patch without interior knots
+ * (Patch.hpp:371): data[4 (px_i py[p] + iy) + k], k = x w, y w, z w, w;
+ * the patches are concatenated. */
+bg_status bg_geometry_from_bezier(bg_context* ctx, int npatch, const int* px, const int* py, const double* data,
+                                  bg_geometry** out);
+bg_status bg_geometry_num_patches(const bg_geometry* g, int* n);
+/* copy patch p's control data out in the layout above (data may be NULL to
+ * query px, py only; else 4 px py doubles) */
+bg_status bg_geometry_patch_data(const bg_geometry* g, int patch, int* px, int* py, double* data);
 /* Patch::updateSurfacePoint at patch coordinates (Geometry/Patch.hpp:294-365);
  * out12 = [s, t, 1, x(3), dx(3), dy(3)]. Host evaluation. */
 bg_status bg_geometry_surface_point(const bg_geometry* g, int patch, double s, double t, double* out12);
