@@ -289,9 +289,11 @@ class DiscreteOperator:
 
     # -- load vectors / potentials (DiscreteLinearForm, DiscretePotential) --
     def load_vector(self, kind, params):
-        """Dirichlet-trace load vectors for analytic data: kind 0 point source
-        1/(4 pi r), 1 Helmholtz point source, 2 plane wave; params (nrhs, 3)."""
-        prm = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, 3))
+        """Load vectors for analytic data. Dirichlet trace: kind 0 point source
+        1/(4 pi r), 1 Helmholtz point source, 2 plane wave; params (nrhs, 3).
+        Maxwell (tangential trace): kind 3 Hertz dipole; params (nrhs, 6) =
+        position, moment."""
+        prm = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, 6 if kind == 3 else 3))
         k = prm.shape[0]
         out = np.zeros((self.N, k), dtype=np.complex128 if self.is_complex else np.float64, order="F")
         self.ctx.check(_lib.load().bg_load_vector(self.h, kind, _dp(prm), k, out.ctypes.data_as(ctypes.c_void_p), 0))

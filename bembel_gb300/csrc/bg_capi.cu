@@ -2,7 +2,9 @@
 // context, geometry and operator lifecycle, device tables, assembly and the
 // batched H2 matvec.
 #include <algorithm>
+#include <array>
 #include <chrono>
+#include <complex>
 #include <cstring>
 #include <map>
 #include <new>
@@ -247,21 +249,23 @@ static void build_segments(bg_operator* op) {
   // far levels
   op->far.clear();
   op->far.resize(op->leaf_level + 1);
+  // Maxwell far blocks are one scalar kernel matrix per cluster pair
+  const int vdf = op->maxwell() ? 1 : vd;
   std::vector<std::vector<std::vector<std::pair<int, int>>>> rows(op->leaf_level + 1);
-  for (int l = 0; l <= op->leaf_level; ++l) rows[l].resize(vd * op->nclusters(l));
+  for (int l = 0; l <= op->leaf_level; ++l) rows[l].resize(vdf * op->nclusters(l));
   std::vector<int> pos(op->leaf_level + 1, 0);
   int li = 0;
   for (size_t k = 0; k < pt.leaf_list.size(); k += 4, ++li)
     if (pt.leaf_list[k] == 1) {
       const int l = pt.leaf_list[k + 1], c1 = pt.leaf_list[k + 2], c2 = pt.leaf_list[k + 3];
       const int ncl = op->nclusters(l);
-      for (int rc = 0; rc < vd; ++rc)
-        for (int cc = 0; cc < vd; ++cc) rows[l][rc * ncl + c1].push_back({cc * ncl + c2, (li << 4) | (rc * vd + cc)});
+      for (int rc = 0; rc < vdf; ++rc)
+        for (int cc = 0; cc < vdf; ++cc) rows[l][rc * ncl + c1].push_back({cc * ncl + c2, (li << 4) | (rc * vd + cc)});
     }
   for (int l = 0; l <= op->leaf_level; ++l) {
     BsrSegment& s = op->far[l];
-    s.B = op->R;
-    s.nrows = vd * op->nclusters(l);
+    s.B = op->maxwell() ? op->np * op->np : op->R;
+    s.nrows = vdf * op->nclusters(l);
     s.row_ptr.assign(1, 0);
     for (auto& r : rows[l]) {
       std::stable_sort(r.begin(), r.end());
@@ -504,6 +508,41 @@ extern "C" bg_status bg_operator_transform(const bg_operator* op, int* ptr, int*
   return BG_OK;
 }
 
+// The (rc, cc) block of a Maxwell low-rank leaf in the reference layout
+// (interpolateKernel, H2Multipole.hpp:336-375, with the 4 x 4 coupling of
+// Maxwell/SingleLayerOperator.hpp:90-120): [K o (t_rc . t_cc), 0; 0, -K / kappa^2]
+// over the np^2 points, rebuilt from the stored kernel matrix K and the tangents.
+static bg_status maxwell_far_block(const bg_operator* op, long leaf, long k, int rc, int cc, double* out) {
+  const int l = op->part.leaf_list[4 * leaf + 1], c1 = op->part.leaf_list[4 * leaf + 2],
+            c2 = op->part.leaf_list[4 * leaf + 3];
+  const int np2 = op->np * op->np, R = 2 * np2;
+  std::vector<double> K(2 * (size_t)np2 * np2), t1(6 * (size_t)np2), t2(6 * (size_t)np2);
+  cudaSetDevice(op->ctx->device);
+  cudaError_t e = cudaMemcpy(K.data(), static_cast<const char*>(op->d_far64[l]->p) + k * op->block_stride(np2) * 16,
+                             K.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t1.data(), op->d_tan64[l]->as<double>() + 6L * c1 * np2, t1.size() * sizeof(double),
+                   cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(t2.data(), op->d_tan64[l]->as<double>() + 6L * c2 * np2, t2.size() * sizeof(double),
+                   cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "copy leaf block");
+  const std::complex<double> kap(op->kre, op->kim), mk2 = -1.0 / (kap * kap);
+  std::fill(out, out + 2 * (size_t)R * R, 0.0);
+  for (int j = 0; j < np2; ++j)
+    for (int i = 0; i < np2; ++i) {
+      const std::complex<double> kv(K[2 * ((size_t)j * np2 + i)], K[2 * ((size_t)j * np2 + i) + 1]);
+      const double* ti = &t1[6 * i + 3 * rc];
+      const double* tj = &t2[6 * j + 3 * cc];
+      const std::complex<double> a = kv * (ti[0] * tj[0] + ti[1] * tj[1] + ti[2] * tj[2]), d = kv * mk2;
+      out[2 * ((size_t)j * R + i)] = a.real();
+      out[2 * ((size_t)j * R + i) + 1] = a.imag();
+      out[2 * ((size_t)(np2 + j) * R + np2 + i)] = d.real();
+      out[2 * ((size_t)(np2 + j) * R + np2 + i) + 1] = d.imag();
+    }
+  return BG_OK;
+}
+
 extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, int rc, int cc, double* out) {
   if (!op || !out || leaf < 0 || 4 * leaf >= (long)op->part.leaf_list.size() || rc < 0 || cc < 0 || rc >= op->vd ||
       cc >= op->vd)
@@ -521,10 +560,12 @@ extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, in
     seg = &op->far[l];
     data = op->d_far64[l];
   }
+  const bool mw_far = cls != 2 && op->maxwell();
   long k = -1;
   for (size_t i = 0; i < seg->leaf.size(); ++i)
-    if (seg->leaf[i] == leaf && seg->comp[i] == rc * op->vd + cc) k = (long)i;
+    if (seg->leaf[i] == leaf && (mw_far || seg->comp[i] == rc * op->vd + cc)) k = (long)i;
   if (k < 0) return set_error(op->ctx, BG_INVALID_ARG, "leaf not found");
+  if (mw_far) return maxwell_far_block(op, leaf, k, rc, cc, out);
   const size_t sb = op->scalar_bytes(false);
   const size_t bytes = (size_t)seg->B * seg->B * sb;
   const size_t stride = (size_t)op->block_stride(seg->B) * sb;
@@ -556,6 +597,8 @@ static bg_status assemble_far(bg_operator* op) {
       op->d_far_df.push_back(new DevBuf());
       op->d_far_atiles.push_back(new DevBuf());
       op->d_far_ainv.push_back(new DevBuf());
+      op->d_tan64.push_back(new DevBuf());
+      op->d_tan32.push_back(new DevBuf());
     }
     const int ncl = op->nclusters(l);
     std::vector<double> cen(4 * (size_t)ncl);
@@ -564,11 +607,16 @@ static bg_status assemble_far(bg_operator* op) {
     BG_CHECK(op->d_centres[l]->upload(cen, s), "cluster centres");
     BG_CHECK(op->d_pts64[l]->alloc((size_t)ncl * np2 * sizeof(d4)), "cluster points");
     BG_CHECK(op->d_pts32[l]->alloc((size_t)ncl * np2 * sizeof(float4)), "cluster points");
+    if (op->maxwell()) {
+      BG_CHECK(op->d_tan64[l]->alloc((size_t)ncl * np2 * 6 * sizeof(double)), "cluster tangents");
+      BG_CHECK(op->d_tan32[l]->alloc((size_t)ncl * np2 * 6 * sizeof(float)), "cluster tangents");
+    }
     BG_CHECK(timed_launch(op->ctx, KC_ASSEMBLY, [&] { return launch_cluster_points(op->G, pt, l, ncl, op->d_cheb.as<double>(), op->np, op->d_centres[l]->as<d4>(),
-                                   op->d_pts64[l]->as<d4>(), op->d_pts32[l]->as<float4>(), s); }),
+                                   op->d_pts64[l]->as<d4>(), op->d_pts32[l]->as<float4>(),
+                                   op->maxwell() ? op->d_tan64[l]->as<double>() : nullptr,
+                                   op->maxwell() ? op->d_tan32[l]->as<float>() : nullptr, s); }),
              "cluster points");
     if (!op->store_far || op->far[l].col.empty()) continue;
-    if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "stored far field of vector operators");
     const BsrSegment& f = op->far[l];
     std::vector<int2> pairs(f.col.size());
     for (int r = 0; r < f.nrows; ++r)
@@ -602,7 +650,123 @@ static bg_status assemble_far(bg_operator* op) {
   return BG_OK;
 }
 
+// Dense leaves of the Maxwell operator: every element pair fills its four
+// component blocks at once (H2Matrix.hpp:195-205 scatters them per component).
+static bg_status assemble_near_mw(bg_operator* op) {
+  cudaStream_t s = op->ctx->stream;
+  const BsrSegment& D = op->dense;
+  const int B = D.B, p2 = op->p2, P = op->P;
+  const int ecl = B / p2;
+  const int ncl = D.nrows / 2;
+  const long bstride = op->block_stride(B);
+  BG_CHECK(op->d_dense64.alloc((size_t)D.col.size() * bstride * 16), "near-field storage");
+  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, (size_t)D.col.size() * bstride * 16, s), "near-field storage");
+  // block index of every (leaf, component pair)
+  std::map<int, std::array<long, 4>> where;
+  for (size_t k = 0; k < D.col.size(); ++k) {
+    auto it = where.find(D.leaf[k]);
+    if (it == where.end()) it = where.emplace(D.leaf[k], std::array<long, 4>{-1, -1, -1, -1}).first;
+    it->second[D.comp[k]] = (long)k;
+  }
+  std::map<int, std::vector<NearPairV>> regular;
+  std::map<std::pair<int, int>, std::vector<NearPairV>> singular;
+  long npairs = 0;
+  for (int r = 0; r < ncl; ++r)
+    for (int k = D.row_ptr[r]; k < D.row_ptr[r + 1]; ++k) {
+      if (D.comp[k] != 0) continue;
+      const std::array<long, 4>& kk = where[D.leaf[k]];
+      if (kk[0] < 0 || kk[1] < 0 || kk[2] < 0 || kk[3] < 0)
+        return set_error(op->ctx, BG_DEVICE_ERROR, "incomplete component blocks of a dense leaf");
+      const int c1 = r, c2 = D.col[k];
+      for (int b = 0; b < ecl; ++b)
+        for (int a = 0; a < ecl; ++a) {
+          const int e1 = c1 * ecl + a, e2 = c2 * ecl + b;
+          PairClass pc = classify_pair(op->mesh, e1, e2, op->P);
+          NearPairV np;
+          np.e1 = e1;
+          np.e2 = e2;
+          np.rot = (pc.rot1 & 15) | ((pc.rot2 & 15) << 4);
+          np.pad = 0;
+          for (int c = 0; c < 4; ++c) np.dst[c] = (long long)kk[c] * bstride + (long long)(b * p2) * B + a * p2;
+          if (pc.cs == 0) regular[pc.deg].push_back(np);
+          else singular[{pc.cs, pc.deg}].push_back(np);
+          ++npairs;
+        }
+    }
+  op->near_pairs = npairs;
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  const double h = 1.0 / double(1 << op->M);
+  ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), h};
+  // idiv = -1 / (kappa^2 h^2) (Maxwell/SingleLayerOperator.hpp:71-76)
+  const std::complex<double> kap(op->kre, op->kim), idv = -1.0 / (kap * kap * h * h);
+  const cd idiv{idv.real(), idv.imag()};
+  cd* out = op->d_dense64.as<cd>();
+  std::vector<DevBuf*> keep;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(s);
+    for (auto b : keep) delete b;
+  };
+  bg_status st = BG_OK;
+  for (auto& kv : regular) {
+    const int deg = kv.first, n1 = deg + 1, Q = n1 * n1;
+    const Rule1D& gr = gauss_rule(n1);
+    // phi, d/ds phi, d/dt phi at the Q points ([3][Q][p2])
+    std::vector<double> basis3((size_t)3 * Q * p2);
+    for (int q = 0; q < Q; ++q) {
+      double bs[8], bt[8], ds[8], dt[8];
+      const double u = gr.x[q / n1], v = gr.x[q % n1];
+      bernstein(P, u, bs);
+      bernstein(P, v, bt);
+      bernstein_der(P, u, ds);
+      bernstein_der(P, v, dt);
+      for (int iy = 0; iy <= P; ++iy)
+        for (int ix = 0; ix <= P; ++ix) {
+          const size_t o = (size_t)q * p2 + iy * (P + 1) + ix;
+          basis3[o] = bs[ix] * bt[iy];
+          basis3[(size_t)Q * p2 + o] = ds[ix] * bt[iy];
+          basis3[(size_t)2 * Q * p2 + o] = bs[ix] * dt[iy];
+        }
+    }
+    DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dtab = new DevBuf(), *dbas = new DevBuf(), *dpairs = new DevBuf();
+    keep.insert(keep.end(), {dgx, dgw, dtab, dbas, dpairs});
+    cudaError_t e = dgx->upload(gr.x, s);
+    if (e == cudaSuccess) e = dgw->upload(gr.w, s);
+    if (e == cudaSuccess) e = dbas->upload(basis3, s);
+    if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
+    if (e == cudaSuccess) e = dtab->alloc((size_t)op->ne * Q * sizeof(MwPt));
+    if (e == cudaSuccess)
+      e = launch_quad_table_mw(op->G, pt, et, op->ne, dgx->as<double>(), dgw->as<double>(), n1, dtab->as<MwPt>(), s);
+    if (e == cudaSuccess)
+      e = launch_near_regular_mw(P, dpairs->as<NearPairV>(), (int)kv.second.size(), dtab->as<MwPt>(), n1,
+                                 dbas->as<double>(), op->kre, op->kim, idiv, out, B, s);
+    if ((st = cuda_status(op->ctx, e, "near-field regular pairs (Maxwell)")) != BG_OK) {
+      cleanup();
+      return st;
+    }
+  }
+  for (auto& kv : singular) {
+    const int cs = kv.first.first, deg = kv.first.second, n1 = deg + 1;
+    const Rule1D& gr = gauss_rule(n1);
+    DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dpairs = new DevBuf();
+    keep.insert(keep.end(), {dgx, dgw, dpairs});
+    cudaError_t e = dgx->upload(gr.x, s);
+    if (e == cudaSuccess) e = dgw->upload(gr.w, s);
+    if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
+    if (e == cudaSuccess)
+      e = launch_near_duffy_mw(op->G, P, cs, pt, et, dpairs->as<NearPairV>(), (int)kv.second.size(),
+                               dgx->as<double>(), dgw->as<double>(), n1, op->kre, op->kim, idiv, out, B, s);
+    if ((st = cuda_status(op->ctx, e, "near-field singular pairs (Maxwell)")) != BG_OK) {
+      cleanup();
+      return st;
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  cleanup();
+  return cuda_status(op->ctx, e, "near-field assembly");
+}
+
 static bg_status assemble_near(bg_operator* op) {
+  if (op->maxwell()) return assemble_near_mw(op);
   cudaStream_t s = op->ctx->stream;
   const BsrSegment& D = op->dense;
   const int B = D.B, p2 = op->p2;
@@ -695,7 +859,10 @@ static bg_status assemble_near(bg_operator* op) {
 extern "C" bg_status bg_operator_assemble(bg_operator* op) {
   if (!op) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
-  if (op->kind == BG_MAXWELL_SL) return set_error(op->ctx, BG_UNSUPPORTED, "Maxwell assembly is not available yet");
+  if (op->maxwell() && (op->P < 1 || op->P > 3))
+    return set_error(op->ctx, BG_UNSUPPORTED, "the Maxwell operator needs a polynomial degree in [1, 3]");
+  if (op->maxwell() && op->kre == 0.0 && op->kim == 0.0)
+    return set_error(op->ctx, BG_INVALID_ARG, "the Maxwell operator needs a nonzero wavenumber");
   cudaSetDevice(op->ctx->device);
   op->assembled = false;
   auto t0 = std::chrono::steady_clock::now();
@@ -738,6 +905,8 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     op->w_ydf.push_back(new DevBuf());
     op->w_btiles.push_back(new DevBuf());
     op->w_binv.push_back(new DevBuf());
+    op->w_yv.push_back(new DevBuf());
+    op->w_zv.push_back(new DevBuf());
   }
   for (int l = 0; l <= op->leaf_level; ++l) {
     const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
@@ -745,6 +914,11 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
     if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
     const size_t tb = far_h16_btile_bytes(op->np * op->np);
+    if (op->maxwell()) {
+      const size_t nv = (size_t)op->nclusters(l) * op->np * op->np * 4 * std::min(nrhs, (int)bg_operator::kMwRhsChunk) * sb;
+      BG_CHECK(op->w_yv[l]->alloc(nv), "work vectors");
+      BG_CHECK(op->w_zv[l]->alloc(nv), "work vectors");
+    }
     if (!op->cplx && tb > 0) {
       BG_CHECK(op->w_btiles[l]->alloc(tb * op->nclusters(l)), "work vectors");
       BG_CHECK(op->w_binv[l]->alloc(sizeof(float) * 32 * op->nclusters(l)), "work vectors");
@@ -852,7 +1026,36 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     for (int l = 0; l <= op->leaf_level && !tc; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
-        BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)f.nrows * f.B * nrhs * sfar, s), "far field");
+        BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sfar, s),
+                 "far field");
+        continue;
+      }
+      if (op->maxwell()) {
+        // tangential and divergence parts through the scalar kernel matrices,
+        // kMwRhsChunk right-hand sides (4 kernel columns each) at a time
+        if (!mixed && !op->store_far)
+          return set_error(op->ctx, BG_UNSUPPORTED, "the FP64 product needs the stored far field");
+        const int ncl = op->nclusters(l);
+        const void* tan = mixed ? (const void*)op->d_tan32[l]->p : (const void*)op->d_tan64[l]->p;
+        const std::complex<double> kap(op->kre, op->kim), mk2 = -1.0 / (kap * kap);
+        for (int r0 = 0; r0 < nrhs; r0 += bg_operator::kMwRhsChunk) {
+          const int nr = std::min((int)bg_operator::kMwRhsChunk, nrhs - r0);
+          BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_mw_far_in(Sfar, ncl, np2, op->w_y[l]->p, nrhs, r0, nr,
+                                                                          tan, op->w_yv[l]->p, s); }),
+                   "Maxwell far-field columns");
+          if (mixed)
+            BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_fused(true, op->d_pts32[l]->as<float4>(), op->d_centres[l]->as<d4>(),
+                                      f.d_row_ptr.as<int>(), f.d_col.as<int>(), f.nrows, np2, (float)op->kre, (float)op->kim,
+                                      op->w_yv[l]->p, op->w_zv[l]->p, 4 * nr, s); }),
+                     "far-field product (FP32 fused, Maxwell)");
+          else
+            BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(true, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
+                                  op->block_stride(f.B), f.nrows, f.B, op->w_yv[l]->p, op->w_zv[l]->p, 4 * nr, 0, s); }),
+                     "far-field product (Maxwell)");
+          BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_mw_far_out(Sfar, ncl, np2, op->w_zv[l]->p, nrhs, r0, nr, tan,
+                                                                           mk2.real(), mk2.imag(), op->w_z[l]->p, s); }),
+                   "Maxwell far-field columns");
+        }
         continue;
       }
       if (mixed) {

@@ -175,6 +175,24 @@ __device__ inline void tensor_basis(double s, double t, double* phi) {
     for (int ix = 0; ix <= P; ++ix) phi[iy * (P + 1) + ix] = bs[ix] * bt[iy];
 }
 
+// tensor Bernstein basis and its two partial derivatives in the element
+// coordinates (Basis.hpp:170-200 uses them for the divergence of the
+// div-conforming Maxwell basis); same local index as tensor_basis
+template <int P>
+__device__ inline void tensor_basis_grad(double s, double t, double* phi, double* phx, double* phy) {
+  double bs[P + 1], dbs[P + 1], bt[P + 1], dbt[P + 1];
+  bern_der<P + 1>(P, s, bs, dbs);
+  bern_der<P + 1>(P, t, bt, dbt);
+#pragma unroll
+  for (int iy = 0; iy <= P; ++iy)
+#pragma unroll
+    for (int ix = 0; ix <= P; ++ix) {
+      phi[iy * (P + 1) + ix] = bs[ix] * bt[iy];
+      phx[iy * (P + 1) + ix] = dbs[ix] * bt[iy];
+      phy[iy * (P + 1) + ix] = bs[ix] * dbt[iy];
+    }
+}
+
 // the DuffyTrick rotation tau (DuffyTrick/tau.hpp:26-42)
 __device__ inline void tau(double x, double y, int c, double* o) {
   if (c == 1) { o[0] = 1 - y; o[1] = x; }

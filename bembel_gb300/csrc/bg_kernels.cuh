@@ -16,6 +16,20 @@ struct NearPair {
   long long dst;
 };
 
+// element pair of a dense leaf of the Maxwell operator: one destination per
+// component pair (rc, cc) at dst[2 * rc + cc]
+struct NearPairV {
+  int e1, e2, rot, pad;
+  long long dst[4];
+};
+
+// a Gauss point of the Maxwell quadrature tables: surface point, the two
+// tangents of the patch parametrisation and the weight h * w (no surface
+// measure: the vector basis carries the Jacobian)
+struct MwPt {
+  double x[3], dx[3], dy[3], w;
+};
+
 struct ElementTable {
   const int* patch;    // per element
   const double* llc;   // 2 per element
@@ -34,10 +48,36 @@ cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable&
                               const NearPair* pairs, int npairs, const double* gx, const double* gw, int n1,
                               double kre, double kim, void* out, int B, cudaStream_t s);
 
+// Maxwell single layer (Maxwell/SingleLayerOperator.hpp:44-88): the four
+// component blocks of every element pair, idiv = -1 / (kappa^2 h^2)
+cudaError_t launch_quad_table_mw(int G, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                                 const double* gw, int n1, MwPt* out, cudaStream_t s);
+cudaError_t launch_near_regular_mw(int P, const NearPairV* pairs, int npairs, const MwPt* tab, int n1,
+                                   const double* basis3, double kre, double kim, cd idiv, cd* out, int B,
+                                   cudaStream_t s);
+cudaError_t launch_near_duffy_mw(int G, int P, int cs, const PatchTable& pt, const ElementTable& et,
+                                 const NearPairV* pairs, int npairs, const double* gx, const double* gw, int n1,
+                                 double kre, double kim, cd idiv, cd* out, int B, cudaStream_t s);
+
 // ---- far field ----
 // interpolation points of every cluster of a level: x, y, z, |dx x dy| (FP64 and FP32)
+// With tan64 set (Maxwell) the weight is 1 and the two tangents dx, dy of every
+// point go to tan64 (6 doubles) and tan32 (6 floats).
 cudaError_t launch_cluster_points(int G, const PatchTable& pt, int level, int nclusters, const double* cheb, int np,
-                                  const d4* centres, d4* out64, float4* out32, cudaStream_t s);
+                                  const d4* centres, d4* out64, float4* out32, double* tan64, float* tan32,
+                                  cudaStream_t s);
+// Maxwell far field through the scalar kernel matrix K of each cluster pair
+// (Maxwell/SingleLayerOperator.hpp:90-120 couples the tangential parts by
+// k t_rc(x).t_cc(y) and the divergence parts by -k / kappa^2):
+// mw_far_in forms, per cluster point j and right-hand side r of the chunk
+// [r0, r0 + nr), the four columns v_q = sum_cc t_cc,q(y_j) Yphi_cc (q < 3) and
+// v_3 = sum_cc Ydiv_cc from the component-major moments Y ([cc][cluster][2 np2][nrhs]),
+// into Yv ([cluster][np2][4 nr]); mw_far_out maps Zv = K Yv back to
+// Z ([rc][cluster][2 np2][nrhs]): Zphi_rc = sum_q t_rc,q(x_i) Zv_q, Zdiv_rc = m Zv_3.
+cudaError_t launch_mw_far_in(int S, int ncl, int np2, const void* y, int nrhs, int r0, int nr, const void* tan,
+                             void* yv, cudaStream_t s);
+cudaError_t launch_mw_far_out(int S, int ncl, int np2, const void* zv, int nrhs, int r0, int nr, const void* tan,
+                              double mre, double mim, void* z, cudaStream_t s);
 // F blocks (B x B, column-major) for the listed cluster pairs of one level
 // block k written at out + k * bstride scalars
 cudaError_t launch_far_assemble(bool cplx, const d4* pts, const int2* pairs, int nblocks, int B, long bstride,

@@ -371,4 +371,405 @@ cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable&
   }
 }
 
+// ---------------------------------------------------------------------------
+// Maxwell single layer (Maxwell/SingleLayerOperator.hpp:44-88 with
+// SuperSpace::addScaledVectorBasisInteraction, SuperSpace.hpp:236-258, and
+// Div_Phi_times_Div_Phi_, Basis.hpp:170-200). Per point pair, with
+// c = k(x, y) w_x w_y and t_0 = dx, t_1 = dy the patch tangents, block
+// (rc, cc) of the element pair gains
+//   c (t_rc(x) . t_cc(y)) phi_a(x) phi_b(y) + c idiv D_rc phi_a(x) D_cc phi_b(y)
+// where D_0, D_1 are the element-coordinate derivatives and
+// idiv = -1 / (kappa^2 h^2).
+
+template <int G>
+__global__ void k_quad_table_mw(PatchTable pt, ElementTable et, int ne, const double* __restrict__ gx,
+                                const double* __restrict__ gw, int n1, MwPt* __restrict__ out) {
+  const int Q = n1 * n1;
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)ne * Q) return;
+  const int e = (int)(idx / Q), q = (int)(idx % Q);
+  const double u = gx[q / n1], v = gx[q % n1], w = gw[q / n1] * gw[q % n1];
+  const double h = et.h;
+  MwPt p;
+  surface_frame<G>(pt, et.patch[e], et.llc[2 * e] + h * u, et.llc[2 * e + 1] + h * v, p.x, p.dx, p.dy);
+  p.w = h * w;
+  out[idx] = p;
+}
+
+cudaError_t launch_quad_table_mw(int G, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                                 const double* gw, int n1, MwPt* out, cudaStream_t s) {
+  const long n = (long)ne * n1 * n1;
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  switch (G) {
+    case 2: k_quad_table_mw<2><<<grid, 128, 0, s>>>(pt, et, ne, gx, gw, n1, out); break;
+    case 3: k_quad_table_mw<3><<<grid, 128, 0, s>>>(pt, et, ne, gx, gw, n1, out); break;
+    case 4: k_quad_table_mw<4><<<grid, 128, 0, s>>>(pt, et, ne, gx, gw, n1, out); break;
+    case 5: k_quad_table_mw<5><<<grid, 128, 0, s>>>(pt, et, ne, gx, gw, n1, out); break;
+    case 6: k_quad_table_mw<6><<<grid, 128, 0, s>>>(pt, et, ne, gx, gw, n1, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// Regular pairs, one CTA per pair, the tensor rule factorised as in
+// k_near_regular. The Gauss points i of e1 go in chunks of kMwChunk:
+//  A) Kt[i][j] = k(x_i, y_j) w_i w_j for the chunk;
+//  B) thread (i, cc, m) sums W[i][cc][m][b] = sum_j Kt[i][j] f_m(y_j) g_b(y_j)
+//     with (f_m, g) = (t_cc,m, phi) for m < 3 and (idiv, D_cc phi) for m = 3;
+//  C) thread per entry (rc, cc, a, b) adds
+//     sum_i phi_a(x_i) t_rc(x_i) . W[i][cc][0..2][b] + D_rc phi_a(x_i) W[i][cc][3][b].
+// basis3 holds phi, D_0 phi, D_1 phi at the Q points ([3][Q][P2]).
+constexpr int kMwChunk = 16;
+
+template <int P>
+__global__ void __launch_bounds__(128) k_near_regular_mw(const NearPairV* __restrict__ pairs,
+                                                         const MwPt* __restrict__ tab, int n1,
+                                                         const double* __restrict__ basis3, double kre, double kim,
+                                                         cd idiv, cd* __restrict__ out, int B) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  constexpr int NB = P2 * P2;
+  constexpr int NE = 4 * NB;
+  constexpr int PER = (NE + 127) / 128;
+  const int Q = n1 * n1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cd* Kt = reinterpret_cast<cd*>(smem_raw);  // [kMwChunk][Q]
+  cd* Ws = Kt + kMwChunk * Q;                // [kMwChunk][2][4][P2]
+  MwPt* ys = reinterpret_cast<MwPt*>(Ws + kMwChunk * 8 * P2);
+  MwPt* xs = ys + Q;  // [kMwChunk]
+  double* U = reinterpret_cast<double*>(xs + kMwChunk);
+  const NearPairV pr = pairs[blockIdx.x];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < Q; q += blockDim.x) ys[q] = tab[(long)pr.e2 * Q + q];
+  for (int k = tid; k < 3 * Q * P2; k += blockDim.x) U[k] = basis3[k];
+  cd acc[PER];
+#pragma unroll
+  for (int m = 0; m < PER; ++m) acc[m] = zero<cd>();
+  for (int i0 = 0; i0 < Q; i0 += kMwChunk) {
+    const int ic = min(kMwChunk, Q - i0);
+    __syncthreads();
+    if (tid < ic) xs[tid] = tab[(long)pr.e1 * Q + i0 + tid];
+    __syncthreads();
+    for (int e = tid; e < ic * Q; e += blockDim.x) {
+      const int ii = e / Q, j = e % Q;
+      const double d0 = xs[ii].x[0] - ys[j].x[0], d1 = xs[ii].x[1] - ys[j].x[1], d2 = xs[ii].x[2] - ys[j].x[2];
+      const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
+      Kt[e] = kernel_val<cd>(r2, kre, kim) * (xs[ii].w * ys[j].w);
+    }
+    __syncthreads();
+    for (int t = tid; t < ic * 8; t += blockDim.x) {
+      const int ii = t >> 3, cc = (t >> 2) & 1, m = t & 3;
+      const double* g = m < 3 ? U : U + (1 + cc) * Q * P2;
+      cd w[P2];
+#pragma unroll
+      for (int b = 0; b < P2; ++b) w[b] = zero<cd>();
+      for (int j = 0; j < Q; ++j) {
+        const double f = m < 3 ? (cc == 0 ? ys[j].dx[m] : ys[j].dy[m]) : 1.0;
+        const cd kk = Kt[ii * Q + j] * f;
+#pragma unroll
+        for (int b = 0; b < P2; ++b) w[b] = fmac(w[b], kk, g[j * P2 + b]);
+      }
+      cd* o = Ws + (ii * 8 + cc * 4 + m) * P2;
+#pragma unroll
+      for (int b = 0; b < P2; ++b) o[b] = m < 3 ? w[b] : w[b] * idiv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < PER; ++m) {
+      const int e = tid + 128 * m;
+      if (e < NE) {
+        const int comp = e / NB, wi = e % NB;
+        const int a = wi % P2, b = wi / P2, rc = comp >> 1, cc = comp & 1;
+        const double* Da = U + (1 + rc) * Q * P2;
+        cd v = acc[m];
+        for (int ii = 0; ii < ic; ++ii) {
+          const int i = i0 + ii;
+          const double* t = rc == 0 ? xs[ii].dx : xs[ii].dy;
+          const cd* wv = Ws + (ii * 8 + cc * 4) * P2 + b;
+          cd tv = wv[0] * t[0];
+          tv = fmac(tv, t[1], wv[P2]);
+          tv = fmac(tv, t[2], wv[2 * P2]);
+          v = fmac(v, U[i * P2 + a], tv);
+          v = fmac(v, Da[i * P2 + a], wv[3 * P2]);
+        }
+        acc[m] = v;
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < PER; ++m) {
+    const int e = tid + 128 * m;
+    if (e < NE) {
+      const int comp = e / NB, wi = e % NB;
+      const int a = wi % P2, b = wi / P2;
+      out[pr.dst[comp] + (long)b * B + a] = acc[m];
+    }
+  }
+}
+
+template <int P>
+static size_t regular_mw_smem(int Q) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  return (size_t)kMwChunk * Q * sizeof(cd) + (size_t)kMwChunk * 8 * P2 * sizeof(cd) + (size_t)Q * sizeof(MwPt) +
+         (size_t)kMwChunk * sizeof(MwPt) + (size_t)3 * Q * P2 * sizeof(double);
+}
+
+template <int P>
+static cudaError_t run_regular_mw(const NearPairV* pairs, int npairs, const MwPt* tab, int n1, const double* basis3,
+                                  double kre, double kim, cd idiv, cd* out, int B, cudaStream_t s) {
+  const size_t smem = regular_mw_smem<P>(n1 * n1);
+  if (smem > 220 * 1024) return cudaErrorInvalidConfiguration;
+  auto kfn = k_near_regular_mw<P>;
+  cudaError_t err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  if (npairs == 0) return cudaSuccess;
+  kfn<<<npairs, 128, smem, s>>>(pairs, tab, n1, basis3, kre, kim, idiv, out, B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_near_regular_mw(int P, const NearPairV* pairs, int npairs, const MwPt* tab, int n1,
+                                   const double* basis3, double kre, double kim, cd idiv, cd* out, int B,
+                                   cudaStream_t s) {
+  switch (P) {
+    case 1: return run_regular_mw<1>(pairs, npairs, tab, n1, basis3, kre, kim, idiv, out, B, s);
+    case 2: return run_regular_mw<2>(pairs, npairs, tab, n1, basis3, kre, kim, idiv, out, B, s);
+    case 3: return run_regular_mw<3>(pairs, npairs, tab, n1, basis3, kre, kim, idiv, out, B, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+
+// Singular pairs of the Maxwell operator: the quadratures of k_near_duffy, with
+// the samples of a warp staged as c = k w_x w_y, c idiv, the four tangent
+// products T[rc][cc] = t_rc(x) . t_cc(y) and (phi, D_0 phi, D_1 phi) at both
+// points; each lane accumulates its share of the 4 p^4 entries.
+template <int G, int P>
+__device__ inline void eval_point_mw(const PatchTable& pt, int patch, double l0, double l1, double h, double u,
+                                     double v, double w, MwPt* pe, double* phi3) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  surface_frame<G>(pt, patch, l0 + h * u, l1 + h * v, pe->x, pe->dx, pe->dy);
+  pe->w = w;
+  tensor_basis_grad<P>(u, v, phi3, phi3 + P2, phi3 + 2 * P2);
+}
+
+template <int P>
+struct MwWarpLayout {
+  static constexpr int P2 = (P + 1) * (P + 1);
+  // per warp, in doubles: sc, sd (32 complex each), st (32 x 4), sa, sb
+  // (32 x 3 P2 each), vp (4 points), vphi (4 x 3 P2)
+  static constexpr int SC = 0, SD = 64, ST = 128, SA = 256, SB = SA + 32 * 3 * P2, VP = SB + 32 * 3 * P2,
+                       VPHI = VP + 4 * 10, WORDS = VPHI + 4 * 3 * P2;
+};
+
+template <int G, int P, int CS>
+__global__ void __launch_bounds__(128) k_near_duffy_mw(PatchTable pt, ElementTable et,
+                                                       const NearPairV* __restrict__ pairs,
+                                                       const double* __restrict__ gx, const double* __restrict__ gw,
+                                                       int n1, double kre, double kim, cd idiv, cd* __restrict__ out,
+                                                       int B) {
+  using L = MwWarpLayout<P>;
+  constexpr int P2 = L::P2;
+  constexpr int NB = P2 * P2;
+  constexpr int NE = 4 * NB;
+  constexpr int PER = (NE + 31) / 32;
+  constexpr int NW = 4;
+  extern __shared__ __align__(16) double dsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* wb = dsm + warp * L::WORDS;
+  cd* sc = reinterpret_cast<cd*>(wb + L::SC);
+  cd* sd = reinterpret_cast<cd*>(wb + L::SD);
+  double* st = wb + L::ST;
+  double* sa = wb + L::SA;
+  double* sb = wb + L::SB;
+  MwPt* vp = reinterpret_cast<MwPt*>(wb + L::VP);
+  double* vphi = wb + L::VPHI;
+  const NearPairV pr = pairs[blockIdx.x];
+  const int rot1 = pr.rot & 15, rot2 = pr.rot >> 4;
+  const int p1 = et.patch[pr.e1], p2 = et.patch[pr.e2];
+  const double a0 = et.llc[2 * pr.e1], a1 = et.llc[2 * pr.e1 + 1];
+  const double b0 = et.llc[2 * pr.e2], b1 = et.llc[2 * pr.e2 + 1];
+  const double h = et.h;
+  const int Q = n1 * n1;
+  cd acc[PER];
+#pragma unroll
+  for (int m = 0; m < PER; ++m) acc[m] = zero<cd>();
+  for (int i = warp; i < Q; i += NW) {
+    const double x0 = gx[i / n1], x1 = gx[i % n1], wi = gw[i / n1] * gw[i % n1];
+    double w = 0;
+    if (CS == 2) w = h * h * wi * x0 * (1 - x0) * (1 - x0 * x1);
+    if (CS == 3) w = h * h * wi * x1 * x1;
+    if (CS == 4) {
+      w = h * h * wi * (x0 * x0 * x0);
+      const double y1 = x1 * x0;
+      if (lane < 4) {
+        double uv[2];
+        const int r = (lane < 2) ? rot1 : rot2;
+        if (lane == 0 || lane == 2) tau(x0, y1, r, uv); else tau(y1, x0, r, uv);
+        if (lane < 2) eval_point_mw<G, P>(pt, p1, a0, a1, h, uv[0], uv[1], w, &vp[lane], vphi + lane * 3 * P2);
+        else eval_point_mw<G, P>(pt, p2, b0, b1, h, uv[0], uv[1], w, &vp[lane], vphi + lane * 3 * P2);
+      }
+      __syncwarp();
+    }
+    for (int jj = 0; jj < Q; jj += 32) {
+      const int j = jj + lane;
+      const bool valid = j < Q;
+      const double e0 = valid ? gx[j / n1] : 0.5, e1 = valid ? gx[j % n1] : 0.5;
+      const double wj = valid ? gw[j / n1] * gw[j % n1] : 0.0;
+      constexpr int NK = CS == 2 ? 4 : (CS == 3 ? 6 : 4);
+#pragma unroll 1
+      for (int k = 0; k < NK; ++k) {
+        MwPt A, Bp;
+        double* pa = sa + lane * 3 * P2;
+        double* pb = sb + lane * 3 * P2;
+        if (CS == 2) {
+          // integrate2.hpp:41-60
+          const double t1 = e0 * (1 - x0), t2 = e1 * (1 - x0 * x1);
+          const double t3 = e0 * (1 - x0) + x0, t4 = e1 * (1 - x0 * x1) + x0 * x1;
+          double u1, v1, u2, v2;
+          if (k == 0) { u1 = t1; v1 = t2; u2 = t3; v2 = t4; }
+          else if (k == 1) { u1 = t1; v1 = t4; u2 = t3; v2 = t2; }
+          else if (k == 2) { u1 = t2; v1 = t1; u2 = t4; v2 = t3; }
+          else { u1 = t2; v1 = t3; u2 = t4; v2 = t1; }
+          eval_point_mw<G, P>(pt, p1, a0, a1, h, u1, v1, w, &A, pa);
+          eval_point_mw<G, P>(pt, p1, a0, a1, h, u2, v2, wj, &Bp, pb);
+        } else if (CS == 3) {
+          // integrate3.hpp:45-76
+          const double f0 = x1 * e0, f1 = x1 * e1;
+          const double t1 = x0 * (1 - x1), t2 = (1 - x0) * (1 - x1);
+          const double t3 = x0 * (1 - f0), t4 = (1 - x0) * (1 - f0);
+          double ua, va, ub, vb, wbb;
+          if (k == 0) { ua = t1; va = f0; ub = t2; vb = f1; wbb = wj * (1 - x1); }
+          else if (k == 1) { ua = 1 - t1; va = f0; ub = 1 - t2; vb = f1; wbb = wj * (1 - x1); }
+          else if (k == 2) { ua = t3; va = x1; ub = t4; vb = f1; wbb = wj * (1 - f0); }
+          else if (k == 3) { ua = 1 - t3; va = x1; ub = 1 - t4; vb = f1; wbb = wj * (1 - f0); }
+          else if (k == 4) { ua = t4; va = f1; ub = t3; vb = x1; wbb = wj * (1 - f0); }
+          else { ua = 1 - t4; va = f1; ub = 1 - t3; vb = x1; wbb = wj * (1 - f0); }
+          double uv1[2], uv2[2];
+          tau(ua, va, rot1, uv1);
+          tau(ub, vb, rot2, uv2);
+          eval_point_mw<G, P>(pt, p1, a0, a1, h, uv1[0], uv1[1], w, &A, pa);
+          eval_point_mw<G, P>(pt, p2, b0, b1, h, uv2[0], uv2[1], wbb, &Bp, pb);
+        } else {
+          // integrate4.hpp:49-58: (qp1,qp5), (qp2,qp5), (qp6,qp3), (qp6,qp4)
+          double uv[2];
+          if (k < 2) {
+            tau(x0 * e0, x0 * e1, rot2, uv);
+            eval_point_mw<G, P>(pt, p2, b0, b1, h, uv[0], uv[1], wj, &Bp, pb);
+            A = vp[k];
+#pragma unroll
+            for (int t = 0; t < 3 * P2; ++t) pa[t] = vphi[k * 3 * P2 + t];
+          } else {
+            tau(x0 * e0, x0 * e1, rot1, uv);
+            eval_point_mw<G, P>(pt, p1, a0, a1, h, uv[0], uv[1], wj, &A, pa);
+            Bp = vp[k];
+#pragma unroll
+            for (int t = 0; t < 3 * P2; ++t) pb[t] = vphi[k * 3 * P2 + t];
+          }
+        }
+        const double d0 = A.x[0] - Bp.x[0], d1 = A.x[1] - Bp.x[1], d2 = A.x[2] - Bp.x[2];
+        const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
+        cd c = kernel_val<cd>(r2, kre, kim) * (A.w * Bp.w);
+        if (!valid) c = zero<cd>();
+        sc[lane] = c;
+        sd[lane] = c * idiv;
+        double* tl = st + 4 * lane;
+        const double* ta[2] = {A.dx, A.dy};
+        const double* tb[2] = {Bp.dx, Bp.dy};
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+            tl[2 * r + q] = fma(ta[r][0], tb[q][0], fma(ta[r][1], tb[q][1], ta[r][2] * tb[q][2]));
+        __syncwarp();
+        for (int smp = 0; smp < 32; ++smp) {
+          const cd cs = sc[smp], ds = sd[smp];
+          const double* T = st + 4 * smp;
+          const double* fa = sa + smp * 3 * P2;
+          const double* fb = sb + smp * 3 * P2;
+#pragma unroll
+          for (int m = 0; m < PER; ++m) {
+            const int e = lane + 32 * m;
+            if (e < NE) {
+              const int comp = e / NB, wi = e % NB;
+              const int a = wi % P2, b = wi / P2, rc = comp >> 1, cc = comp & 1;
+              double v = T[comp] * fa[a] * fb[b];
+              double dv = fa[(1 + rc) * P2 + a] * fb[(1 + cc) * P2 + b];
+              if (CS == 2) {
+                // integrand(qp2, qp1) of the identical-element rule
+                v = fma(T[2 * cc + rc] * fb[a], fa[b], v);
+                dv = fma(fb[(1 + rc) * P2 + a], fa[(1 + cc) * P2 + b], dv);
+              }
+              acc[m] = fmac(fmac(acc[m], cs, v), ds, dv);
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (CS == 4) __syncwarp();
+  }
+  // reduce the warps' accumulators through the staging memory
+  static_assert(NE * 2 <= L::WORDS, "reduction buffer too small");
+  __syncthreads();
+  cd* red = reinterpret_cast<cd*>(dsm);
+  const int stride = L::WORDS / 2;
+#pragma unroll
+  for (int m = 0; m < PER; ++m) {
+    const int e = lane + 32 * m;
+    if (e < NE) red[warp * stride + e] = acc[m];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    cd v = red[e];
+#pragma unroll
+    for (int w2 = 1; w2 < NW; ++w2) v = v + red[w2 * stride + e];
+    const int comp = e / NB, wi = e % NB;
+    const int a = wi % P2, b = wi / P2;
+    out[pr.dst[comp] + (long)b * B + a] = v;
+  }
+}
+
+template <int G, int P>
+static cudaError_t run_duffy_mw(int cs, const PatchTable& pt, const ElementTable& et, const NearPairV* pairs,
+                                int npairs, const double* gx, const double* gw, int n1, double kre, double kim,
+                                cd idiv, cd* out, int B, cudaStream_t s) {
+  const size_t smem = 4 * MwWarpLayout<P>::WORDS * sizeof(double);
+#define BG_DMW(CSV)                                                                                      \
+  {                                                                                                      \
+    auto kfn = k_near_duffy_mw<G, P, CSV>;                                                               \
+    cudaError_t err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (err != cudaSuccess) return err;                                                                  \
+    if (npairs == 0) return cudaSuccess;                                                                 \
+    kfn<<<npairs, 128, smem, s>>>(pt, et, pairs, gx, gw, n1, kre, kim, idiv, out, B);                    \
+    return cudaGetLastError();                                                                           \
+  }
+  if (cs == 2) BG_DMW(2)
+  if (cs == 3) BG_DMW(3)
+  if (cs == 4) BG_DMW(4)
+#undef BG_DMW
+  return cudaErrorInvalidValue;
+}
+
+template <int G>
+static cudaError_t duffy_mw_p(int P, int cs, const PatchTable& pt, const ElementTable& et, const NearPairV* pairs,
+                              int npairs, const double* gx, const double* gw, int n1, double kre, double kim, cd idiv,
+                              cd* out, int B, cudaStream_t s) {
+  switch (P) {
+    case 1: return run_duffy_mw<G, 1>(cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    case 2: return run_duffy_mw<G, 2>(cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    case 3: return run_duffy_mw<G, 3>(cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_near_duffy_mw(int G, int P, int cs, const PatchTable& pt, const ElementTable& et,
+                                 const NearPairV* pairs, int npairs, const double* gx, const double* gw, int n1,
+                                 double kre, double kim, cd idiv, cd* out, int B, cudaStream_t s) {
+  switch (G) {
+    case 2: return duffy_mw_p<2>(P, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    case 3: return duffy_mw_p<3>(P, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    case 5: return duffy_mw_p<5>(P, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, idiv, out, B, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace bg

@@ -146,6 +146,7 @@ struct bg_operator {
   DevBuf d_T_ptr, d_T_idx, d_T_val, d_Tt_ptr, d_Tt_idx, d_Tt_val;
   DevBuf d_cheb;
   std::vector<DevBuf*> d_pts64, d_pts32, d_centres;  // per level
+  std::vector<DevBuf*> d_tan64, d_tan32;             // per level, Maxwell: tangents dx, dy of every point
   DevBuf d_dense64;                       // dense blocks (FP64)
   DevBuf d_dense32;                       // FP32 copy of the dense blocks (BG_PREC_FP32)
   std::vector<DevBuf*> d_far64;           // per level
@@ -172,6 +173,7 @@ struct bg_operator {
   DevBuf w_xdof, w_xss, w_yss, w_ydof, w_xss32, w_yss32;
   std::vector<DevBuf*> w_y, w_z;  // per level
   std::vector<DevBuf*> w_ydf;     // per level: FP32 (hi, lo) split of w_y for the double-float product
+  std::vector<DevBuf*> w_yv, w_zv;  // per level, Maxwell: the four kernel columns per right-hand side
   std::vector<DevBuf*> w_btiles;  // per level: FP16 hi/lo right-hand-side tiles of every cluster
   std::vector<DevBuf*> w_binv;    // per level: inverse column scales of those tiles (32 per cluster)
 
@@ -181,8 +183,8 @@ struct bg_operator {
 
   ~bg_operator() {
     if (solver_ws && solver_ws_free) solver_ws_free(solver_ws);
-    for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv, &d_mom64, &d_mom32, &w_y,
-                   &w_z, &w_ydf, &w_btiles, &w_binv})
+    for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_tan64, &d_tan32, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv,
+                   &d_mom64, &d_mom32, &w_y, &w_z, &w_ydf, &w_btiles, &w_binv, &w_yv, &w_zv})
       for (auto b : *v) delete b;
   }
   size_t scalar_bytes(bool fp32) const { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }
@@ -192,6 +194,10 @@ struct bg_operator {
   // FP32 blocks: stride a multiple of 16 bytes
   long block_stride32(int B) const { return cplx ? ((long)B * B + 1) / 2 * 2 : ((long)B * B + 3) / 4 * 4; }
   int stype(bool fp32) const { return (fp32 ? 2 : 0) + (cplx ? 1 : 0); }
+  // Maxwell: the far field is stored as the scalar kernel matrix of each
+  // cluster pair (np^2 x np^2) and applied to kMwRhsChunk right-hand sides at a time
+  bool maxwell() const { return vd == 2; }
+  static constexpr int kMwRhsChunk = 8;
   int nclusters(int level) const { return level < 0 ? 1 : mesh.npatch << (2 * level); }
 };
 

@@ -76,6 +76,102 @@ __global__ void k_load(PatchTable pt, ElementTable et, int ne, const double* __r
   }
 }
 
+// Maxwell excitation: the field of a Hertz dipole (examples/Data.hpp:73-90),
+// prm = position (3), moment (3), and its tangential part integrated against
+// the two tangent directions of the vector basis
+// (LinearForm/RotatedTangentialTrace.hpp:30-87): per Gauss point with weight
+// h w, t = (f - (f.n) n) h w, then dx.t phi_a into component 0 and dy.t phi_a
+// into component 1 of the superspace vector.
+__device__ inline void dipole_field(const double* prm, const double* x, double kre, double kim, cd* f) {
+  const double c0 = x[0] - prm[0], c1 = x[1] - prm[1], c2 = x[2] - prm[2];
+  const double r2 = c0 * c0 + c1 * c1 + c2 * c2;
+  const double ir = rsqrt_nr(r2), r = r2 * ir;
+  const double n[3] = {c0 * ir, c1 * ir, c2 * ir};
+  const double* len = prm + 3;
+  // (n x len) x n and 3 n (n.len) - len
+  const double nl[3] = {n[1] * len[2] - n[2] * len[1], n[2] * len[0] - n[0] * len[2], n[0] * len[1] - n[1] * len[0]};
+  const double ncl[3] = {nl[1] * n[2] - nl[2] * n[1], nl[2] * n[0] - nl[0] * n[2], nl[0] * n[1] - nl[1] * n[0]};
+  const double ndl = n[0] * len[0] + n[1] * len[1] + n[2] * len[2];
+  // exp(-i kappa r) with kappa = kre + i kim
+  double sn, cs;
+  sincos(kre * r, &sn, &cs);
+  const double a = kim != 0.0 ? exp(kim * r) : 1.0;
+  const cd ex{cs * a, -sn * a};
+  // ec = (1/r^3 + i kappa / r^2) exp(-i kappa r), fk = kappa^2 exp(-i kappa r) / r
+  const cd ec = cd{ir * ir * ir - kim * ir * ir, kre * ir * ir} * ex;
+  const cd fk = cd{kre * kre - kim * kim, 2 * kre * kim} * ex * ir;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) f[k] = fk * ncl[k] + ec * (3 * n[k] * ndl - len[k]);
+}
+
+template <int G, int P>
+__global__ void k_load_mw(PatchTable pt, ElementTable et, int ne, const double* __restrict__ gx,
+                          const double* __restrict__ gw, int n1, const double* __restrict__ prm, int k, double kre,
+                          double kim, cd* __restrict__ out) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)ne * k) return;
+  const int e = (int)(t / k), c = (int)(t % k);
+  const double h = et.h;
+  cd acc0[P2], acc1[P2];
+#pragma unroll
+  for (int a = 0; a < P2; ++a) acc0[a] = acc1[a] = zero<cd>();
+  for (int q = 0; q < n1 * n1; ++q) {
+    const double u = gx[q / n1], v = gx[q % n1], w = h * gw[q / n1] * gw[q % n1];
+    double x[3], dx[3], dy[3], phi[P2];
+    surface_frame<G>(pt, et.patch[e], et.llc[2 * e] + h * u, et.llc[2 * e + 1] + h * v, x, dx, dy);
+    double n[3] = {dx[1] * dy[2] - dx[2] * dy[1], dx[2] * dy[0] - dx[0] * dy[2], dx[0] * dy[1] - dx[1] * dy[0]};
+    const double in = rsqrt_nr(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] *= in;
+    n[1] *= in;
+    n[2] *= in;
+    cd f[3];
+    dipole_field(prm + 6 * c, x, kre, kim, f);
+    const cd fd = f[0] * n[0] + f[1] * n[1] + f[2] * n[2];
+    cd tc[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) tc[m] = (f[m] - fd * n[m]) * w;
+    const cd cx = tc[0] * dx[0] + tc[1] * dx[1] + tc[2] * dx[2];
+    const cd cy = tc[0] * dy[0] + tc[1] * dy[1] + tc[2] * dy[2];
+    tensor_basis<P>(u, v, phi);
+#pragma unroll
+    for (int a = 0; a < P2; ++a) {
+      acc0[a] = fmac(acc0[a], cx, phi[a]);
+      acc1[a] = fmac(acc1[a], cy, phi[a]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < P2; ++a) {
+    out[((long)e * P2 + a) * k + c] = acc0[a];
+    out[((long)(ne + e) * P2 + a) * k + c] = acc1[a];
+  }
+}
+
+template <int G>
+cudaError_t load_mw_p(int P, const PatchTable& pt, const ElementTable& et, int ne, const double* gx, const double* gw,
+                      int n1, const double* prm, int k, double kre, double kim, cd* out, cudaStream_t s) {
+  const unsigned g = (unsigned)(((long)ne * k + 127) / 128);
+  switch (P) {
+    case 1: k_load_mw<G, 1><<<g, 128, 0, s>>>(pt, et, ne, gx, gw, n1, prm, k, kre, kim, out); break;
+    case 2: k_load_mw<G, 2><<<g, 128, 0, s>>>(pt, et, ne, gx, gw, n1, prm, k, kre, kim, out); break;
+    case 3: k_load_mw<G, 3><<<g, 128, 0, s>>>(pt, et, ne, gx, gw, n1, prm, k, kre, kim, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+cudaError_t launch_load_mw(int G, int P, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
+                           const double* gw, int n1, const double* prm, int k, double kre, double kim, cd* out,
+                           cudaStream_t s) {
+  switch (G) {
+    case 2: return load_mw_p<2>(P, pt, et, ne, gx, gw, n1, prm, k, kre, kim, out, s);
+    case 3: return load_mw_p<3>(P, pt, et, ne, gx, gw, n1, prm, k, kre, kim, out, s);
+    case 4: return load_mw_p<4>(P, pt, et, ne, gx, gw, n1, prm, k, kre, kim, out, s);
+    case 5: return load_mw_p<5>(P, pt, et, ne, gx, gw, n1, prm, k, kre, kim, out, s);
+    case 6: return load_mw_p<6>(P, pt, et, ne, gx, gw, n1, prm, k, kre, kim, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 // CTA per evaluation point: threads over (element, Gauss point) sum
 // k(x, y_q) c_q rho(y_q) with c_q = h w |J| and rho = sum_a coef phi_a (the
 // 1/h of FunctionEvaluatorEval and the h^2 of the weight leave h).
@@ -196,9 +292,11 @@ cudaError_t launch_potential(int P, bool cplx, const d4* tab, int ne, int Q, con
 }  // namespace
 
 extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device) {
-  if (!op || !prm || !out || nrhs <= 0 || kind < 0 || kind > 2) return BG_INVALID_ARG;
+  if (!op || !prm || !out || nrhs <= 0 || kind < 0 || kind > 3) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: load vectors need a GPU");
-  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "load vectors of vector operators");
+  if ((op->vd == 2) != (kind == 3))
+    return set_error(op->ctx, BG_INVALID_ARG, "the Maxwell operator takes dipole data (kind 3) and only it");
+  const int npr = kind == 3 ? 6 : 3;  // parameters per right-hand side
   if (!op->cplx && kind != 0) return set_error(op->ctx, BG_INVALID_ARG, "complex data for a real operator");
   cudaSetDevice(op->ctx->device);
   cudaStream_t s = op->ctx->stream;
@@ -211,11 +309,14 @@ extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm
     bg_status st = ensure_work(op, k);
     if (st != BG_OK) return st;
     DevBuf gx, gw, dp, dout;
-    std::vector<double> p(prm + 3 * c0, prm + 3 * (c0 + k));
+    std::vector<double> p(prm + npr * c0, prm + npr * (c0 + k));
     cudaError_t e = gx.upload(gr.x, s);
     if (e == cudaSuccess) e = gw.upload(gr.w, s);
     if (e == cudaSuccess) e = dp.upload(p, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && kind == 3)
+      e = launch_load_mw(op->G, op->P, pt, et, op->ne, gx.as<double>(), gw.as<double>(), op->P + 2, dp.as<double>(),
+                         k, op->kre, op->kim, op->w_yss.as<cd>(), s);
+    else if (e == cudaSuccess)
       e = launch_load(op->G, op->P, op->cplx, pt, et, op->ne, gx.as<double>(), gw.as<double>(), op->P + 2, kind,
                       dp.as<double>(), k, op->kre, op->kim, op->w_yss.as<double>(), s);
     if (e == cudaSuccess)

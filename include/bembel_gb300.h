@@ -169,6 +169,7 @@ bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy,
  * (held on every GPU that loads it until the process exits). An operator whose
  * intermediates do not fit is rejected with BG_INVALID_ARG and a message giving
  * the bytes it would need (sphere, M = 5, P = 2, n_p = 9 needs about 4 MB).
+ * Laplace and Helmholtz operators only (Maxwell: BG_UNSUPPORTED).
  * All calls on a device share that array, so calls that overlap on the GPU
  * (other threads, other contexts, other streams) race and give wrong results.
  * The first call on each device looks up the array's device address; make it
@@ -180,6 +181,10 @@ bg_status bg_matvec_noalloc(bg_operator* op, const void* x, void* y, int precisi
  *   kind 0: u(x) = 1/(4 pi |x - x0|), prm = x0 (3 doubles per column)
  *   kind 1: u(x) = exp(-i k |x - x0|)/(4 pi |x - x0|), prm = x0 (3 per column)
  *   kind 2: plane wave u(x) = exp(-i k d.x), prm = d (3 per column)
+ * and, for the Maxwell operator only, DiscreteLinearForm<RotatedTangentialTrace<cplx>, Op>
+ * (LinearForm/RotatedTangentialTrace.hpp:30-87) of
+ *   kind 3: the field of a Hertz dipole (examples/Data.hpp:73-90), prm = position,
+ *           moment (6 doubles per column).
  * Output: nrhs load vectors (N x nrhs, column-major, ld = N), host or device. */
 bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device);
 

@@ -23,9 +23,9 @@ def ctx():
 
 def _pair(ctx, oracle, geo, M, P, kind, kappa=0.0, np_=6):
     import bembel_gb300 as bg
-    ops = {0: bg.LaplaceSingleLayerOperator, 1: bg.HelmholtzSingleLayerOperator}
+    ops = {0: bg.LaplaceSingleLayerOperator, 1: bg.HelmholtzSingleLayerOperator, 2: bg.MaxwellSingleLayerOperator}
     lin = ops[kind]()
-    if kind == 1:
+    if kind in (1, 2):
         lin.set_wavenumber(kappa)
     d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(geo, ctx), M, P), lin, n_p=np_)
     d.compute()
@@ -110,3 +110,59 @@ def test_solve_reaches_tolerance(ctx, oracle, inner):
     for c in range(3):
         r = b[:, c] - o.matvec(x[:, c])
         assert np.linalg.norm(r) / np.linalg.norm(b[:, c]) < 2e-8
+
+
+# Maxwell single layer (div-conforming vector basis, kappa = 2 as in the EFIE
+# workload): all four component blocks of every leaf, the product, the dipole
+# excitation and a solve.
+MW_CASES = [(SPHERE, 2, 1, 2.0, 6), (SPHERE, 2, 2, 2.0, 6), (TORUS, 1, 2, 1.5, 6)]
+MW_FP32_TOL = 1e-4  # the divergence part carries 1/(kappa h)^2: FP32 far field and transforms
+
+
+@pytest.mark.parametrize("geo,M,P,kappa,np_", MW_CASES)
+def test_maxwell_leaf_blocks(ctx, oracle, geo, M, P, kappa, np_):
+    d, o = _pair(ctx, oracle, geo, M, P, 2, kappa, np_)
+    worst = 0.0
+    for li in range(len(o.leaves())):
+        for rc in range(2):
+            for cc in range(2):
+                a = d.leaf_block(li, rc, cc)
+                b = o.leaf_matrix(li, rc, cc)
+                worst = max(worst, np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    assert worst < FP64_TOL, worst
+
+
+@pytest.mark.parametrize("geo,M,P,kappa,np_", MW_CASES)
+def test_maxwell_matvec(ctx, oracle, geo, M, P, kappa, np_):
+    d, o = _pair(ctx, oracle, geo, M, P, 2, kappa, np_)
+    rng = np.random.default_rng(11)
+    A = d.get_discrete_operator()
+    for nrhs in (1, 3, 11):  # 11 crosses the 8-column chunk of the far field
+        x = rng.uniform(-1, 1, (d.N, nrhs)) + 1j * rng.uniform(-1, 1, (d.N, nrhs))
+        ref = o.matvec(x)
+        y64 = A.matvec(x)
+        assert np.linalg.norm(y64 - ref) / np.linalg.norm(ref) < FP64_TOL
+        for prec in ("mixed", "fp32"):
+            y = A.matvec(x, precision=prec)
+            assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < MW_FP32_TOL, prec
+
+
+def test_maxwell_dipole_load_vector(ctx, oracle):
+    d, o = _pair(ctx, oracle, SPHERE, 2, 2, 2, 2.0, 6)
+    prm = np.array([[0.0, 0.1, 2.5, 0.3, -0.2, 0.9], [1.5, -1.8, 0.7, 1.0, 0.0, 0.0]])
+    got = d.load_vector(3, prm)
+    for c in range(prm.shape[0]):
+        ref = o.load_vector(3, prm[c])
+        assert np.linalg.norm(got[:, c] - ref) / np.linalg.norm(ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("inner", ["fp64", "fp32"])
+def test_maxwell_solve(ctx, oracle, inner):
+    d, o = _pair(ctx, oracle, SPHERE, 2, 2, 2, 2.0, 6)
+    prm = np.array([[0.0, 0.1, 2.5, 0.3, -0.2, 0.9], [1.5, -1.8, 0.7, 1.0, 0.0, 0.0]])
+    b = d.load_vector(3, prm)
+    x, st = d.get_discrete_operator().solve(b, tol=1e-8, inner=inner)
+    assert st["converged"]
+    for c in range(2):
+        r = b[:, c] - o.matvec(x[:, c:c + 1])[:, 0]
+        assert np.linalg.norm(r) / np.linalg.norm(b[:, c]) < 1e-7
