@@ -353,9 +353,24 @@ static bg_status upload_tables(bg_operator* op) {
     if ((st = build(4 * np2, np2, [&](int i, int q) { return tr[(size_t)q * 4 * np2 + i]; }, &op->tm[0].tr_b,
                     &op->tm[1].tr_b, &op->tm[0].a_tr_b, &op->tm[1].a_tr_b)) != BG_OK)
       return st;
+    if (op->maxwell()) {
+      // channel blocks: phi (rows 0..np2-1 of either component's matrix),
+      // d/ds phi (component 0) and d/dt phi (component 1), rows np2..2 np2-1
+      const double* sub[3] = {mom[0].data(), mom[0].data() + (size_t)np2 * Bq, mom[1].data() + (size_t)np2 * Bq};
+      for (int c = 0; c < 3; ++c) {
+        const double* m = sub[c];
+        if ((st = build(np2, Bq, [&](int i, int q) { return m[(size_t)i * Bq + q]; }, &op->tm[0].mw_f[c],
+                        &op->tm[1].mw_f[c], &op->tm[0].a_mw_f[c], &op->tm[1].a_mw_f[c])) != BG_OK)
+          return st;
+        if ((st = build(Bq, np2, [&](int i, int q) { return m[(size_t)q * Bq + i]; }, &op->tm[0].mw_b[c],
+                        &op->tm[1].mw_b[c], &op->tm[0].a_mw_b[c], &op->tm[1].a_mw_b[c])) != BG_OK)
+          return st;
+      }
+    }
     // every output row tile count within the kernel's 4 x 256 tiles of 3 x 4
     auto fits = [&](int Mo) { return (Mo + 2) / 3 * 8 <= 4 * 256; };
-    op->use_tgemm = op->nc == 1 && mom.size() <= 2 && fits(R) && fits(Bq) && fits(np2) && fits(4 * np2);
+    op->use_tgemm = (op->maxwell() || (op->nc == 1 && mom.size() <= 2 && fits(R))) && fits(Bq) && fits(np2) &&
+                    fits(4 * np2);
   }
   {
     // every row of every far-field level, rows with more blocks first so the
@@ -967,9 +982,40 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     }
     const int Ll = op->leaf_level;
     const bg_operator::TransformMats& tm = op->tm[mixed ? 1 : 0];
-    for (int c = 0; c < op->vd; ++c) {
+    // Maxwell moment blocks phi, d/ds phi, d/dt phi (np2 x Bq, row-major) for the generic path
+    const size_t rsz = mixed ? sizeof(float) : sizeof(double);
+    auto mw_mom = [&](int c) -> const void* {
+      const char* base = static_cast<const char*>(mixed ? op->d_mom32[c == 2 ? 1 : 0]->p : op->d_mom64[c == 2 ? 1 : 0]->p);
+      return base + (c == 0 ? 0 : (size_t)np2 * op->Bq * rsz);
+    };
+    const char* xc0 = static_cast<const char*>(xfar);
+    const char* xc1 = xc0 + comp_ss * nrhs * sfar;
+    if (op->maxwell()) {
+      // three channels: tangential part of each component, divergence of both
+      const size_t chl = (size_t)op->nleaf_cl * np2 * nrhs * sfar;
+      char* yl = static_cast<char*>(op->w_y[Ll]->p);
+      const char* xin[4] = {xc0, xc1, xc0, xc1};
+      char* yout[4] = {yl, yl + chl, yl + 2 * chl, yl + 2 * chl};
+      const int blk[4] = {0, 0, 1, 2};
+      for (int t = 0; t < 4; ++t)
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm
+                              ? launch_tgemm(Sfar, t == 3, tm.a_mw_f[blk[t]], xin[t], op->Bq, yout[t], np2, op->nleaf_cl, nrhs, s)
+                              : launch_moment_fwd_acc(Sfar, t == 3, mw_mom(blk[t]), np2, op->Bq, op->nleaf_cl, xin[t],
+                                                      yout[t], nrhs, s); }),
+                 "forward moments");
+      for (int l = Ll - 1; l >= 0; --l) {
+        const int nb = 3 * op->nclusters(l);
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, op->w_y[l + 1]->p, 4L * np2, op->w_y[l]->p, np2, nb, nrhs, s)
+                                        : launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, 1, nb,
+                                                              op->w_y[l + 1]->p, op->w_y[l]->p, nrhs, s); }),
+                 "forward transfer");
+      }
+    }
+    for (int c = 0; c < op->vd && !op->maxwell(); ++c) {
       const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
-      const char* xc = static_cast<const char*>(xfar) + c * comp_ss * nrhs * sfar;
+      const char* xc = c == 0 ? xc0 : xc1;
       char* yl = static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
       BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
                  return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_mom_f[c], xc, op->Bq, yl, op->R, op->nleaf_cl, nrhs, s)
@@ -1080,7 +1126,31 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                    "far-field product");
       }
     }
-    for (int c = 0; c < op->vd; ++c) {
+    if (op->maxwell()) {
+      for (int l = 0; l < Ll; ++l) {
+        const int nb = 3 * op->nclusters(l);
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, op->w_z[l]->p, np2, op->w_z[l + 1]->p, 4L * np2, nb, nrhs, s)
+                                        : launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, 1, nb,
+                                                              op->w_z[l]->p, op->w_z[l + 1]->p, nrhs, s); }),
+                 "backward transfer");
+      }
+      // y_0 += phi^T Zphi_0 + (d/ds phi)^T Zdiv,  y_1 += phi^T Zphi_1 + (d/dt phi)^T Zdiv
+      const size_t chl = (size_t)op->nleaf_cl * np2 * nrhs * sfar;
+      const char* zl = static_cast<const char*>(op->w_z[Ll]->p);
+      char* yc0 = static_cast<char*>(yfar);
+      char* yc1 = yc0 + comp_ss * nrhs * sfar;
+      const char* zin[4] = {zl, zl + 2 * chl, zl + chl, zl + 2 * chl};
+      char* yout[4] = {yc0, yc0, yc1, yc1};
+      const int blk[4] = {0, 1, 0, 2};
+      for (int t = 0; t < 4; ++t)
+        BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
+                   return op->use_tgemm
+                              ? launch_tgemm(Sfar, true, tm.a_mw_b[blk[t]], zin[t], np2, yout[t], op->Bq, op->nleaf_cl, nrhs, s)
+                              : launch_moment_bwd(Sfar, mw_mom(blk[t]), np2, op->Bq, op->nleaf_cl, zin[t], yout[t], nrhs, s); }),
+                 "backward moments");
+    }
+    for (int c = 0; c < op->vd && !op->maxwell(); ++c) {
       for (int l = 0; l < Ll; ++l) {
         const int ncl = op->nclusters(l);
         const char* zpa = static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;

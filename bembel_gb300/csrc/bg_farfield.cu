@@ -111,8 +111,8 @@ cudaError_t launch_far_assemble(bool cplx, const d4* pts, const int2* pairs, int
 
 // ---------------------------------------------------------------------------
 // Maxwell far field around the scalar kernel product. One thread per
-// (cluster, point, right-hand side of the chunk); R = 2 np2 rows per cluster
-// and component in Y and Z (tangential part first, then the divergence part).
+// (cluster, point, right-hand side of the chunk); the three channels of Y and
+// Z are [channel][cluster][np2][nrhs].
 template <typename S, typename R>
 __global__ void k_mw_far_in(int ncl, int np2, const S* __restrict__ y, int nrhs, int r0, int nr,
                             const R* __restrict__ tan, S* __restrict__ yv) {
@@ -120,16 +120,14 @@ __global__ void k_mw_far_in(int ncl, int np2, const S* __restrict__ y, int nrhs,
   if (idx >= (long)ncl * np2 * nr) return;
   const int r = (int)(idx % nr);
   const long cj = idx / nr;  // cluster * np2 + j
-  const int c = (int)(cj / np2), j = (int)(cj % np2);
-  const long comp = (long)ncl * 2 * np2 * nrhs;  // one component of Y
-  const long row = ((long)c * 2 * np2 + j) * nrhs + r0 + r;
-  const S p0 = y[row], p1 = y[comp + row];
-  const S d0 = y[row + (long)np2 * nrhs], d1 = y[comp + row + (long)np2 * nrhs];
+  const long ch = (long)ncl * np2 * nrhs;  // one channel
+  const long row = cj * nrhs + r0 + r;
+  const S p0 = y[row], p1 = y[ch + row], dv = y[2 * ch + row];
   const R* t = tan + 6 * cj;
   S* o = yv + cj * 4 * nr + r;
 #pragma unroll
   for (int q = 0; q < 3; ++q) o[q * nr] = p0 * t[q] + p1 * t[3 + q];
-  o[3 * nr] = d0 + d1;
+  o[3 * nr] = dv;
 }
 
 template <typename S, typename R>
@@ -139,16 +137,14 @@ __global__ void k_mw_far_out(int ncl, int np2, const S* __restrict__ zv, int nrh
   if (idx >= (long)ncl * np2 * nr) return;
   const int r = (int)(idx % nr);
   const long ci = idx / nr;
-  const int c = (int)(ci / np2), i = (int)(ci % np2);
-  const long comp = (long)ncl * 2 * np2 * nrhs;
-  const long row = ((long)c * 2 * np2 + i) * nrhs + r0 + r;
+  const long ch = (long)ncl * np2 * nrhs;
+  const long row = ci * nrhs + r0 + r;
   const R* t = tan + 6 * ci;
   const S* v = zv + ci * 4 * nr + r;
-  const S v0 = v[0], v1 = v[nr], v2 = v[2 * nr], dv = v[3 * nr] * m;
+  const S v0 = v[0], v1 = v[nr], v2 = v[2 * nr];
   z[row] = v0 * t[0] + v1 * t[1] + v2 * t[2];
-  z[comp + row] = v0 * t[3] + v1 * t[4] + v2 * t[5];
-  z[row + (long)np2 * nrhs] = dv;
-  z[comp + row + (long)np2 * nrhs] = dv;
+  z[ch + row] = v0 * t[3] + v1 * t[4] + v2 * t[5];
+  z[2 * ch + row] = v[3 * nr] * m;
 }
 
 cudaError_t launch_mw_far_in(int S, int ncl, int np2, const void* y, int nrhs, int r0, int nr, const void* tan,

@@ -68,12 +68,15 @@ cudaError_t launch_cluster_points(int G, const PatchTable& pt, int level, int nc
                                   cudaStream_t s);
 // Maxwell far field through the scalar kernel matrix K of each cluster pair
 // (Maxwell/SingleLayerOperator.hpp:90-120 couples the tangential parts by
-// k t_rc(x).t_cc(y) and the divergence parts by -k / kappa^2):
-// mw_far_in forms, per cluster point j and right-hand side r of the chunk
-// [r0, r0 + nr), the four columns v_q = sum_cc t_cc,q(y_j) Yphi_cc (q < 3) and
-// v_3 = sum_cc Ydiv_cc from the component-major moments Y ([cc][cluster][2 np2][nrhs]),
-// into Yv ([cluster][np2][4 nr]); mw_far_out maps Zv = K Yv back to
-// Z ([rc][cluster][2 np2][nrhs]): Zphi_rc = sum_q t_rc,q(x_i) Zv_q, Zdiv_rc = m Zv_3.
+// k t_rc(x).t_cc(y) and the divergence parts by -k / kappa^2). The moments of
+// a level are three channels, each [cluster][np2][nrhs]: Yphi_0, Yphi_1 (the
+// tangential parts of the two components) and Ydiv (the divergence parts of
+// both components summed; the transfers are linear, so the sum is formed at
+// the leaves). mw_far_in forms, per cluster point j and right-hand side r of
+// the chunk [r0, r0 + nr), the four columns v_q = sum_cc t_cc,q(y_j) Yphi_cc
+// (q < 3) and v_3 = Ydiv into Yv ([cluster][np2][4 nr]); mw_far_out maps
+// Zv = K Yv back to the channels of Z: Zphi_rc = sum_q t_rc,q(x_i) Zv_q and
+// Zdiv = m Zv_3 (shared by both row components).
 cudaError_t launch_mw_far_in(int S, int ncl, int np2, const void* y, int nrhs, int r0, int nr, const void* tan,
                              void* yv, cudaStream_t s);
 cudaError_t launch_mw_far_out(int S, int ncl, int np2, const void* zv, int nrhs, int r0, int nr, const void* tan,
@@ -93,6 +96,9 @@ cudaError_t launch_bsr(int S, const int* row_ptr, const int* col, const void* bl
 // block k starts at blocks + k * bstride scalars (bstride * sizeof >= 16 B multiple)
 cudaError_t launch_bsr_fp64(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
                             int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
+// as launch_moment_fwd, adding to y when acc is set
+cudaError_t launch_moment_fwd_acc(int S, bool acc, const void* mom, int R, int Bq, int nclusters, const void* xss,
+                                  void* y, int nrhs, cudaStream_t s);
 cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int nclusters, const void* xss, void* y, int nrhs,
                               cudaStream_t s);
 cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int nclusters, const void* z, void* yss, int nrhs,

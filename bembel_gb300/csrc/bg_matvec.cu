@@ -1171,6 +1171,14 @@ static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void
   kf<<<ncl, 256, smem, s>>>((const typename RealOf<S>::T*)mom, R, Bq, (const S*)xss, (S*)y, nrhs);
   return cudaGetLastError();
 }
+cudaError_t launch_moment_fwd_acc(int S, bool acc, const void* mom, int R, int Bq, int ncl, const void* xss, void* y,
+                                  int nrhs, cudaStream_t s) {
+  const int kk = (S & 1) ? 2 * nrhs : nrhs;
+  if (S < 2) return bgemm<double>(false, acc, (const double*)mom, R, Bq, (const double*)xss, (long)Bq * kk, (double*)y,
+                                  (long)R * kk, ncl, kk, s);
+  return bgemm<float>(false, acc, (const float*)mom, R, Bq, (const float*)xss, (long)Bq * kk, (float*)y, (long)R * kk,
+                      ncl, kk, s);
+}
 cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int ncl, const void* xss, void* y, int nrhs,
                               cudaStream_t s) {
   // Y[c] (R x k) = Mom (R x Bq) X[c] (Bq x k); complex vectors as 2k real columns

@@ -158,9 +158,11 @@ struct bg_operator {
   DevBuf d_tr64, d_tr32;
   // FMM matrices transposed and padded for launch_tgemm, per precision
   // (0 FP64, 1 FP32): moments forward/backward per component, transfers
+  // Maxwell: the np^2 x Bq moment blocks phi, d/ds phi, d/dt phi of the
+  // three transform channels (forward and backward)
   struct TransformMats {
-    DevBuf mom_f[2], mom_b[2], tr_f, tr_b;
-    bg::TGemmA a_mom_f[2], a_mom_b[2], a_tr_f, a_tr_b;
+    DevBuf mom_f[2], mom_b[2], tr_f, tr_b, mw_f[3], mw_b[3];
+    bg::TGemmA a_mom_f[2], a_mom_b[2], a_tr_f, a_tr_b, a_mw_f[3], a_mw_b[3];
   };
   TransformMats tm[2];
   bool use_tgemm = false;

@@ -393,6 +393,111 @@ def _roofline(op, prof, stats, steps):
     return base
 
 
+def run_maxwell(args):
+    """Side workload (not the headline line): the Maxwell single layer (EFIE)
+    on the sphere, M = 4, P = 2, n_p = 9, kappa = 2, with 8 right-hand sides
+    from Hertz dipoles at distance 2.5 with seeded random orientations (seed 6),
+    excitation = tangential trace. Reports batched solves/s to 1e-8 with the
+    FP32 inner operator and with the plain FP64 path, H2 products/s, the
+    assembly time and the mixed-vs-FP64 solution difference."""
+    import torch
+    import bembel_gb300 as bg
+    from bembel_gb300 import _lib
+    L = _lib.load()
+    ctx = bg.Context(0)
+    sp = ctypes_void_p()
+    L.bg_context_get_stream(ctx.h, ctypes_byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", 0))
+    m, p, n_p, k, nrhs = 4, 2, 9, 2.0, 8
+    t0 = time.time()
+    lin = bg.MaxwellSingleLayerOperator()
+    lin.set_wavenumber(k)
+    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, p), lin, n_p=n_p)
+    op.compute()
+    asm = op.assembly_times()
+    asm["wall_s"] = time.time() - t0
+    A = op.get_discrete_operator()
+    rng = np.random.default_rng(6)
+    pos = rng.normal(size=(nrhs, 3))
+    pos = 2.5 * pos / np.linalg.norm(pos, axis=1, keepdims=True)
+    mom = rng.normal(size=(nrhs, 3))
+    mom = mom / np.linalg.norm(mom, axis=1, keepdims=True)
+    b_host = op.load_vector(3, np.hstack([pos, mom]))
+    b = torch.from_numpy(np.ascontiguousarray(b_host.T)).cuda().t()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def timed(inner, steps, warmup):
+        for _ in range(warmup):
+            A.solve(b, tol=TOL, inner=inner, inner_tol=INNER_TOL, restart=200, max_refinements=12)
+        ts, x, st = [], None, None
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = ev(), ev()
+            e0.record(stream)
+            x, st = A.solve(b, tol=TOL, inner=inner, inner_tol=INNER_TOL, restart=200, max_refinements=12)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return np.array(ts), x, st
+
+    clocks = ClockSampler(0)
+    with clocks:
+        t_mx, xm, stm = timed("fp32", args.steps, args.warmup)
+    t_64, x64, st64 = timed("fp64", max(1, min(2, args.steps)), 1)
+
+    def mv_rate(prec, reps=5):
+        x = torch.randn(op.N, nrhs, dtype=torch.complex128, device="cuda")
+        for _ in range(2):
+            A.matvec(x, precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(reps):
+            A.matvec(x, precision=prec)
+        e1.record(stream)
+        e1.synchronize()
+        return reps / (e0.elapsed_time(e1) * 1e-3)
+
+    def breakdown(fn):
+        L.bg_profile_classes(ctx.h, 0xFF)
+        L.bg_profile_enable(ctx.h, 1)
+        _read_profile(L, ctx)
+        fn()
+        prof = _read_profile(L, ctx)
+        L.bg_profile_enable(ctx.h, 0)
+        return {"ms": {kk: round(v, 3) for kk, v in prof["ms"].items() if v}, "launches":
+                {kk: v for kk, v in prof["launches"].items() if v}}
+
+    xq = torch.randn(op.N, nrhs, dtype=torch.complex128, device="cuda")
+    per_product = {prec: breakdown(lambda: A.matvec(xq, precision=prec)) for prec in ("fp64", "fp32")}
+    per_solve = breakdown(lambda: A.solve(b, tol=TOL, inner="fp32", inner_tol=INNER_TOL, restart=200,
+                                          max_refinements=12))
+    xm_np, x64_np = xm.cpu().numpy(), x64.cpu().numpy()
+    info = op.info()
+    line = {"workload": "maxwell_sl_h2_sphere_M4_P2_np9_kappa2_8rhs", "metric": "solves/s (8-RHS batched Maxwell "
+            "SL H2 solves to rel.err 1e-8)", "unit": "solves/s", "value": nrhs / (float(np.mean(t_mx)) * 1e-3),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(t_mx)),
+            "dtype": "c128+c64", "data": "synthetic (seeded Hertz dipoles at distance 2.5, sphere.dat)",
+            "config": {"elements": int(info[2]), "dofs": op.N, "refinement": m, "degree": p, "n_p": n_p,
+                       "kappa": k, "nrhs": nrhs, "tol": TOL, "dense_leaves": int(info[3]),
+                       "lowrank_leaves": int(info[4]), "far_field_bytes": int(info[13]),
+                       "near_field_bytes": int(info[14]),
+                       "l2": "flush: 256 MiB buffer written between timed steps"},
+            "fp64_path": {"solves_per_s": nrhs / (float(np.mean(t_64)) * 1e-3), "ms_per_step": float(np.mean(t_64)),
+                          "iterations": st64["iterations"]},
+            "solver": {kk: stm[kk] for kk in ("iterations", "refinements", "fp64_matvecs", "low_matvecs",
+                                             "final_relres")},
+            "accuracy": {"mixed_vs_fp64_solution": float(np.max(np.linalg.norm(xm_np - x64_np, axis=0) /
+                                                                np.linalg.norm(x64_np, axis=0))),
+                         "fp64_final_relres": st64["final_relres"]},
+            "matvec": {"fp64_products_per_s_8rhs": mv_rate("fp64"), "fp32_products_per_s_8rhs": mv_rate("fp32")},
+            "assembly_s": asm, "clocks": clocks.summary(),
+            "kernel_ms_per_product": per_product, "kernel_ms_per_solve": per_solve}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_void_p():
     import ctypes
     return ctypes.c_void_p()
@@ -443,8 +548,12 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
                     help="product precision of --profile matvec")
     ap.add_argument("--profile-m", type=int, default=None, help="refinement level of --profile cases (default 5)")
+    ap.add_argument("--workload", default="laplace", choices=["laplace", "maxwell"],
+                    help="laplace: the headline line; maxwell: the EFIE side workload")
     args = ap.parse_args()
-    if args.profile:
+    if args.workload == "maxwell" and args.impl == "gb300" and not args.profile:
+        run_maxwell(args)
+    elif args.profile:
         run_profile_case(args)
     elif args.impl == "reference":
         run_reference(args)
