@@ -643,7 +643,18 @@ static bg_status assemble_far(bg_operator* op) {
     BG_CHECK(timed_launch(op->ctx, KC_ASSEMBLY, [&] { return launch_far_assemble(op->cplx, op->d_pts64[l]->as<d4>(), dp.as<int2>(), (int)pairs.size(), f.B,
                                  op->block_stride(f.B), op->kre, op->kim, op->d_far64[l]->p, s); }),
              "far-field assembly");
-    if (!op->cplx) {
+    if (op->cplx) {
+      // scaled FP16 hi / lo tiles of Re and Im for the complex tensor-core product
+      const size_t tb = far_h16c_atile_bytes(np2);
+      if (tb > 0) {
+        BG_CHECK(op->d_far_atiles[l]->alloc(tb * f.col.size()), "far field tiles");
+        BG_CHECK(op->d_far_ainv[l]->alloc(sizeof(float) * f.col.size()), "far field tiles");
+        BG_CHECK(launch_build_h16c_atiles(np2, op->d_far64[l]->p, op->block_stride(f.B), (long)f.col.size(),
+                                          op->d_far_atiles[l]->p, op->d_far_ainv[l]->as<float>(), s),
+                 "far-field tiles");
+        ++tiled_levels;
+      }
+    } else {
       // (hi, lo) FP32 pairs of the same blocks for the double-float FP64 product
       BG_CHECK(op->d_far_df[l]->alloc(bytes), "far field storage");
       BG_CHECK(launch_split_df(op->d_far64[l]->p, (long)f.col.size() * op->block_stride(f.B), op->d_far_df[l]->p, s),
@@ -928,13 +939,13 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
     if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
-    const size_t tb = far_h16_btile_bytes(op->np * op->np);
+    const size_t tb = op->cplx ? far_h16c_btile_bytes(op->np * op->np) : far_h16_btile_bytes(op->np * op->np);
     if (op->maxwell()) {
       const size_t nv = (size_t)op->nclusters(l) * op->np * op->np * 4 * std::min(nrhs, (int)bg_operator::kMwRhsChunk) * sb;
       BG_CHECK(op->w_yv[l]->alloc(nv), "work vectors");
       BG_CHECK(op->w_zv[l]->alloc(nv), "work vectors");
     }
-    if (!op->cplx && tb > 0) {
+    if (tb > 0) {
       BG_CHECK(op->w_btiles[l]->alloc(tb * op->nclusters(l)), "work vectors");
       BG_CHECK(op->w_binv[l]->alloc(sizeof(float) * 32 * op->nclusters(l)), "work vectors");
     }
@@ -1034,6 +1045,7 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
     }
     const bool tc = mixed && op->vd == 1 && op->nc == 1 && op->leaf_level < kMaxFarLevels &&
                     far_tc_supported(op->cplx, np2, nrhs);
+    const bool tcc = mixed && op->cplx && op->far_tiles && op->leaf_level < kMaxFarLevels;
     if (tc && op->far_tiles) {
       // stored FP16 tiles streamed by TMA bulk copies; all levels in one
       // launch, which writes every row of Z
@@ -1054,6 +1066,52 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
       BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->d_far_work.as<int2>(), op->n_far_work,
                                                                        np2, nrhs, op->d_err.as<int>(), s); }),
                "far-field product (stored FP16 tiles, tensor cores)");
+    } else if (tcc) {
+      // complex kernel: stored FP16 tiles of Re K and Im K, 16 complex columns
+      // per launch, all levels per launch (every row of Z written). Maxwell
+      // applies K to the four kernel columns of every right-hand side.
+      FarH16Tiles T{};
+      for (int l = 0; l <= op->leaf_level; ++l) {
+        T.row_ptr[l] = op->far[l].d_row_ptr.as<int>();
+        T.col[l] = op->far[l].d_col.as<int>();
+        T.a[l] = static_cast<const unsigned char*>(op->d_far_atiles[l]->p);
+        T.ainv[l] = op->d_far_ainv[l]->as<float>();
+        T.b[l] = static_cast<unsigned char*>(op->w_btiles[l]->p);
+        T.binv[l] = op->w_binv[l]->as<float>();
+        T.y[l] = static_cast<const float*>(op->maxwell() ? op->w_yv[l]->p : op->w_y[l]->p);
+        T.z[l] = static_cast<float*>(op->maxwell() ? op->w_zv[l]->p : op->w_z[l]->p);
+        T.ncl[l] = op->nclusters(l);
+      }
+      const int nlev = op->leaf_level + 1;
+      auto product = [&](int ld, int c0, int nc) -> bg_status {
+        BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16c_btiles(T, nlev, np2, ld, c0, nc, s); }),
+                 "right-hand-side tiles");
+        BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16c(T, op->d_far_work.as<int2>(), op->n_far_work,
+                                                                           np2, ld, c0, nc, op->d_err.as<int>(), s); }),
+                 "far-field product (stored complex FP16 tiles, tensor cores)");
+        return BG_OK;
+      };
+      bg_status st;
+      if (!op->maxwell()) {
+        for (int c0 = 0; c0 < nrhs; c0 += 16)
+          if ((st = product(nrhs, c0, std::min(16, nrhs - c0))) != BG_OK) return st;
+      } else {
+        const std::complex<double> kap(op->kre, op->kim), mk2 = -1.0 / (kap * kap);
+        for (int r0 = 0; r0 < nrhs; r0 += bg_operator::kMwRhsChunk) {
+          const int nr = std::min((int)bg_operator::kMwRhsChunk, nrhs - r0);
+          for (int l = 0; l <= op->leaf_level; ++l)
+            BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_mw_far_in(Sfar, op->nclusters(l), np2, op->w_y[l]->p, nrhs,
+                                                                            r0, nr, op->d_tan32[l]->p, op->w_yv[l]->p, s); }),
+                     "Maxwell far-field columns");
+          for (int c0 = 0; c0 < 4 * nr; c0 += 16)
+            if ((st = product(4 * nr, c0, std::min(16, 4 * nr - c0))) != BG_OK) return st;
+          for (int l = 0; l <= op->leaf_level; ++l)
+            BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_mw_far_out(Sfar, op->nclusters(l), np2, op->w_zv[l]->p, nrhs,
+                                                                             r0, nr, op->d_tan32[l]->p, mk2.real(),
+                                                                             mk2.imag(), op->w_z[l]->p, s); }),
+                     "Maxwell far-field columns");
+        }
+      }
     } else if (tc) {
       // all levels in one tensor-core launch; it writes every row of Z
       FarTcLevels L{};
@@ -1069,7 +1127,7 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                                                                       op->d_err.as<int>(), s); }),
                "far-field product (tensor cores)");
     }
-    for (int l = 0; l <= op->leaf_level && !tc; ++l) {
+    for (int l = 0; l <= op->leaf_level && !tc && !tcc; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
         BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sfar, s),

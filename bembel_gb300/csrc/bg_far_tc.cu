@@ -802,6 +802,361 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
   }
 }
 
+// ---------------------------------------------------------------------------
+// Complex stored-tile variant (Helmholtz and Maxwell kernels exp(-i k r)/(4 pi r)).
+// A block K = Kr + i Ki is stored as four FP16 tiles [Kr hi][Kr lo][Ki hi][Ki lo]
+// under one power-of-two scale; the right-hand sides of a cluster (up to 16
+// complex columns) as one real tile pair of 32 columns [Re Y | Im Y], each
+// column with its own scale. Per block the MMA warp forms P = Kr [Re Y | Im Y]
+// and Q = Ki [Re Y | Im Y] (hi*hi and hi*lo + lo*hi each, so four FP32
+// accumulators of 32 columns, two buffers: 256 tensor-memory columns), and the
+// epilogue folds Re Z = P_re - Q_im, Im Z = P_im + Q_re into compensated sums.
+// Two shared-memory stages (a stage holds 80 KB at n_p = 9, 105 KB at 10).
+constexpr int kH16CStages = 2;
+constexpr int kNC = 16;                // complex columns per launch
+constexpr uint32_t kTmemColsC = 256;
+
+template <int NP2>
+struct H16CShape {
+  using R = H16Shape<NP2>;
+  static constexpr uint32_t SBO = R::SBO, A_BYTES = R::A_BYTES, B_BYTES = R::B_BYTES;
+  static constexpr uint32_t A4 = 4 * A_BYTES, B2 = 2 * B_BYTES;
+  static constexpr uint32_t STAGE = A4 + B2;
+  static constexpr uint32_t TILES = kH16CStages * STAGE;
+  // an M = 128 operand read starting at the last A tile of the last stage
+  static constexpr uint32_t NEED = (kH16CStages - 1) * STAGE + 3 * A_BYTES + 16 * SBO;
+  static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
+};
+
+template <int NP2>
+__global__ void __launch_bounds__(kStoredThreads, 1)
+    k_far_h16c(FarH16Tiles T, const int2* __restrict__ work, int nwork, int ldz, int z0, int nc,
+               int* __restrict__ err) {
+  using G = H16CShape<NP2>;
+  constexpr int S = kH16CStages;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full_bar[S], done_bar[S], free_bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemColsC));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < S; ++b) {
+      mbar_init(&full_bar[b], 1);
+      mbar_init(&done_bar[b], 1);
+    }
+    mbar_init(&free_bar[0], 4);
+    mbar_init(&free_bar[1], 4);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ---- producer: 4 coupling tiles + 2 right-hand-side tiles per block ----
+    if (lane == 0) {
+      int it = 0;
+      for (int wi = blockIdx.x; wi < nwork && !*abort_v; wi += gridDim.x) {
+        const int lev = work[wi].x, row = work[wi].y;
+        const int kb = T.row_ptr[lev][row], ke = T.row_ptr[lev][row + 1];
+        const int* col = T.col[lev];
+        for (int k = kb; k < ke; ++k, ++it) {
+          const int st = it % S;
+          if (it >= S && !mbar_wait(&done_bar[st], (uint32_t)((it / S - 1) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 14);
+            break;
+          }
+          if (*abort_v) break;
+          unsigned char* sm = smem + st * G::STAGE;
+          const unsigned char* ga = T.a[lev] + (size_t)k * G::A4;
+          const unsigned char* gb = T.b[lev] + (size_t)col[k] * G::B2;
+          mbar_expect_tx(&full_bar[st], G::STAGE);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) bulk_g2s(sm + q * G::A_BYTES, ga + q * G::A_BYTES, G::A_BYTES, &full_bar[st]);
+          bulk_g2s(sm + G::A4, gb, G::B_BYTES, &full_bar[st]);
+          bulk_g2s(sm + G::A4 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_f16(128, kN);
+      const uint32_t base = smem_u32(smem);
+      int it = 0;
+      for (int wi = blockIdx.x; wi < nwork && !*abort_v; wi += gridDim.x) {
+        const int lev = work[wi].x, row = work[wi].y;
+        const int nb = T.row_ptr[lev][row + 1] - T.row_ptr[lev][row];
+        for (int q = 0; q < nb; ++q, ++it) {
+          const int st = it % S, ab = it & 1;
+          if (!mbar_wait(&full_bar[st], (uint32_t)((it / S) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 15);
+            break;
+          }
+          if (it >= 2 && !mbar_wait(&free_bar[ab], (uint32_t)(((it >> 1) - 1) & 1))) {
+            *abort_v = 1;
+            atomicExch(err, 16);
+            break;
+          }
+          if (*abort_v) break;
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t a0 = base + st * G::STAGE;
+          const uint32_t b0 = a0 + G::A4, b1 = b0 + G::B_BYTES;
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {  // 0: Kr -> P, 1: Ki -> Q
+            const uint32_t ahi = a0 + (2 * part) * G::A_BYTES, alo = ahi + G::A_BYTES;
+            const uint32_t d_hh = tmem + (uint32_t)(128 * ab + 64 * part), d_cr = d_hh + 32;
+#pragma unroll
+            for (int pass = 0; pass < 3; ++pass) {
+              uint64_t ad = umma_desc(pass == 2 ? alo : ahi, 128, G::SBO);
+              uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
+              const uint32_t dd = pass == 0 ? d_hh : d_cr;
+#pragma unroll
+              for (int ks = 0; ks < H16Shape<NP2>::KP / 16; ++ks) {
+                mma_f16(dd, ad, bd, idesc, (pass == 2 || ks != 0) ? 1u : 0u);
+                ad += 16;
+                bd += 16;
+              }
+            }
+          }
+          mma_commit(&done_bar[st]);
+        }
+      }
+    }
+  } else {
+    // ---- epilogue warps 2-5: tensor-memory lanes 32 (warp % 4) .. +31 ----
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const int m = (warp & 3) * 32 + lane;
+    int it = 0;
+    bool ok = true;
+    for (int wi = blockIdx.x; wi < nwork && ok; wi += gridDim.x) {
+      const int lev = work[wi].x, row = work[wi].y;
+      const int kb = T.row_ptr[lev][row], ke = T.row_ptr[lev][row + 1];
+      const int* col = T.col[lev];
+      const float* ainv = T.ainv[lev];
+      const float* binv = T.binv[lev];
+      float sre[kNC], cre[kNC], sim[kNC], cim[kNC];
+#pragma unroll
+      for (int n = 0; n < kNC; ++n) sre[n] = cre[n] = sim[n] = cim[n] = 0.0f;
+      for (int k = kb; k < ke; ++k, ++it) {
+        const int st = it % S, ab = it & 1;
+        int got = 1;
+        if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
+        got = __shfl_sync(0xffffffffu, got, 0);
+        if (!got) {
+          if (lane == 0) {
+            *abort_v = 1;
+            atomicExch(err, 17);
+          }
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const float sa = __ldg(&ainv[k]);
+        const float* sb = binv + (long)col[k] * kN;
+        float p[32];
+        {
+          float hh[32], cr[32];
+          tmem_ld32(lane_base + (uint32_t)(128 * ab), hh);
+          tmem_ld32(lane_base + (uint32_t)(128 * ab + 32), cr);
+#pragma unroll
+          for (int n = 0; n < 32; ++n) p[n] = (hh[n] + cr[n]) * (sa * __ldg(&sb[n]));
+        }
+        float hh[32], cr[32];
+        tmem_ld32(lane_base + (uint32_t)(128 * ab + 64), hh);
+        tmem_ld32(lane_base + (uint32_t)(128 * ab + 96), cr);
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&free_bar[ab]);
+#pragma unroll
+        for (int n = 0; n < kNC; ++n) {
+          const float q_re = (hh[n] + cr[n]) * (sa * __ldg(&sb[n]));
+          const float q_im = (hh[kNC + n] + cr[kNC + n]) * (sa * __ldg(&sb[kNC + n]));
+          neumaier(sre[n], cre[n], p[n] - q_im);
+          neumaier(sim[n], cim[n], p[kNC + n] + q_re);
+        }
+      }
+      if (ok && m < NP2) {
+        float2* zo = reinterpret_cast<float2*>(T.z[lev]) + ((long)row * NP2 + m) * ldz + z0;
+#pragma unroll
+        for (int n = 0; n < kNC; ++n)
+          if (n < nc) zo[n] = make_float2(sre[n] + cre[n], sim[n] + cim[n]);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemColsC));
+}
+
+// Complex A tiles: one scale per block from the largest |Re| or |Im|.
+template <int NP2>
+__global__ void __launch_bounds__(256) k_build_h16c_atiles(const double2* __restrict__ F, long bstride,
+                                                           __half* __restrict__ tiles, float* __restrict__ ainv) {
+  using G = H16Shape<NP2>;
+  constexpr int AH = G::A_BYTES / 2;
+  __shared__ float red[8];
+  const long b = blockIdx.x;
+  const double2* Fb = F + b * bstride;
+  float mx = 0.0f;
+  for (int e = threadIdx.x; e < NP2 * NP2; e += blockDim.x) {
+    const double2 v = Fb[e];
+    mx = fmaxf(mx, fmaxf((float)fabs(v.x), (float)fabs(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) mx = fmaxf(mx, red[i]);
+  const float sa = h16_scale(mx * 1.0000001f);
+  __half* out = tiles + b * 4 * AH;
+  for (int e = threadIdx.x; e < AH; e += blockDim.x) {
+    const int cm = e >> 6, r = (e >> 3) & 7, c = e & 7;
+    const int m = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + c;
+    double2 v = make_double2(0.0, 0.0);
+    if (m < NP2 && k < NP2) v = Fb[(long)k * NP2 + m];
+    const double vr = v.x * (double)sa, vi = v.y * (double)sa;
+    const __half hr = __double2half(vr), hi = __double2half(vi);
+    out[e] = hr;
+    out[AH + e] = __double2half(vr - (double)__half2float(hr));
+    out[2 * AH + e] = hi;
+    out[3 * AH + e] = __double2half(vi - (double)__half2float(hi));
+  }
+  if (threadIdx.x == 0) ainv[b] = 1.0f / sa;
+}
+
+// Complex B tiles of every cluster of every level: real columns n < 16 hold
+// Re Y[:, y0 + n], columns 16 + n hold Im Y[:, y0 + n] (n < nc; others zero).
+// Y rows have ldy complex entries.
+template <int NP2>
+__global__ void __launch_bounds__(256) k_build_h16c_btiles(FarH16Tiles T, int nlev, int ldy, int y0, int nc) {
+  using G = H16Shape<NP2>;
+  constexpr int BH = G::B_BYTES / 2;
+  __shared__ float cmax[8][kN];
+  __shared__ float scale[kN];
+  int c = blockIdx.x, lev = 0;
+  while (lev + 1 < nlev && c >= T.ncl[lev]) c -= T.ncl[lev++];
+  const float2* y = reinterpret_cast<const float2*>(T.y[lev]) + (long)c * NP2 * ldy + y0;
+  auto val = [&](int k, int n) -> float {
+    const int j = n & (kNC - 1);
+    if (j >= nc || k >= NP2) return 0.0f;
+    const float2 v = y[(long)k * ldy + j];
+    return n < kNC ? v.x : v.y;
+  };
+  {
+    const int n = threadIdx.x & 31, q = threadIdx.x >> 5;
+    float mx = 0.0f;
+    for (int k = q; k < NP2; k += 8) mx = fmaxf(mx, fabsf(val(k, n)));
+    cmax[q][n] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    float mx = 0.0f;
+    for (int q = 0; q < 8; ++q) mx = fmaxf(mx, cmax[q][threadIdx.x]);
+    const float sb = h16_scale(mx * 1.0000001f);
+    scale[threadIdx.x] = sb;
+    T.binv[lev][(long)c * kN + threadIdx.x] = 1.0f / sb;
+  }
+  __syncthreads();
+  __half* out = reinterpret_cast<__half*>(T.b[lev]) + (long)c * 2 * BH;
+  for (int e = threadIdx.x; e < BH; e += blockDim.x) {
+    const int cm = e >> 6, r = (e >> 3) & 7, cc = e & 7;
+    const int n = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + cc;
+    const float v = val(k, n) * scale[n];
+    const __half h = __float2half_rn(v);
+    out[e] = h;
+    out[BH + e] = __float2half_rn(v - __half2float(h));
+  }
+}
+
+#define BG_H16C_SHAPES(X) X(4) X(9) X(16) X(25) X(36) X(49) X(64) X(81) X(100)
+
+size_t far_h16c_atile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return H16CShape<N>::A4;
+    BG_H16C_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+size_t far_h16c_btile_bytes(int np2) {
+  switch (np2) {
+#define BG_T(N) \
+  case N: return H16CShape<N>::B2;
+    BG_H16C_SHAPES(BG_T)
+#undef BG_T
+    default: return 0;
+  }
+}
+
+cudaError_t launch_build_h16c_atiles(int np2, const void* F, long bstride, long nblocks, void* tiles, float* ainv,
+                                     cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  switch (np2) {
+#define BG_T(N)                                                                                          \
+  case N:                                                                                                \
+    k_build_h16c_atiles<N><<<(unsigned)nblocks, 256, 0, s>>>(static_cast<const double2*>(F), bstride,    \
+                                                             static_cast<__half*>(tiles), ainv);         \
+    break;
+    BG_H16C_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_h16c_btiles(const FarH16Tiles& T, int nlev, int np2, int ldy, int y0, int nc,
+                                     cudaStream_t s) {
+  if (nlev < 1 || nlev > kMaxFarLevels || nc < 1 || nc > kNC || y0 < 0 || y0 + nc > ldy) return cudaErrorInvalidValue;
+  int ncl_total = 0;
+  for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
+  if (ncl_total == 0) return cudaSuccess;
+  switch (np2) {
+#define BG_T(N) \
+  case N: k_build_h16c_btiles<N><<<ncl_total, 256, 0, s>>>(T, nlev, ldy, y0, nc); break;
+    BG_H16C_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_far_h16c(const FarH16Tiles& T, const int2* work, int nwork, int np2, int ldz, int z0, int nc,
+                            int* err, cudaStream_t s) {
+  if (nwork == 0) return cudaSuccess;
+  if (far_h16c_atile_bytes(np2) == 0 || nc < 1 || nc > kNC || z0 < 0 || z0 + nc > ldz) return cudaErrorInvalidValue;
+  int dev = 0, nsm = 0;
+  cudaError_t ea = cudaGetDevice(&dev);
+  if (ea == cudaSuccess) ea = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (ea != cudaSuccess) return ea;
+  switch (np2) {
+#define BG_T(N)                                                                                              \
+  case N: {                                                                                                  \
+    constexpr uint32_t smem = H16CShape<N>::SMEM;                                                            \
+    static_assert(smem <= 220 * 1024, "complex FP16 far field: shared memory plan too large");               \
+    cudaError_t e = cudaFuncSetAttribute(k_far_h16c<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e;                                                                          \
+    k_far_h16c<N><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, ldz, z0, nc, err);     \
+    return cudaGetLastError();                                                                               \
+  }
+    BG_H16C_SHAPES(BG_T)
+#undef BG_T
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 bool far_tc_supported(bool cplx, int np2, int nrhs) {
   const bool shape = np2 == 4 || np2 == 9 || np2 == 16 || np2 == 25 || np2 == 36 || np2 == 49 || np2 == 64 || np2 == 81;
   return !cplx && shape && nrhs >= 1 && nrhs <= kN;

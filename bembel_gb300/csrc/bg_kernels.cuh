@@ -146,6 +146,19 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
                            cudaStream_t s);
 // real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32
 bool far_tc_supported(bool cplx, int np2, int nrhs);
+// Complex kernels (Helmholtz, Maxwell): a holds [Re hi][Re lo][Im hi][Im lo]
+// per block (built from complex FP64 blocks), b a real tile pair of 32 columns
+// per cluster ([Re Y | Im Y] of up to 16 complex columns y0 .. y0 + nc - 1 of
+// rows with ldy entries); the product writes columns z0 .. z0 + nc - 1 of z
+// (rows of ldz complex entries). n_p^2 in {4, 9, ..., 81, 100}.
+size_t far_h16c_atile_bytes(int np2);  // per low-rank block (0: shape not supported)
+size_t far_h16c_btile_bytes(int np2);  // per cluster
+cudaError_t launch_build_h16c_atiles(int np2, const void* F, long bstride, long nblocks, void* tiles, float* ainv,
+                                     cudaStream_t s);
+cudaError_t launch_build_h16c_btiles(const FarH16Tiles& T, int nlev, int np2, int ldy, int y0, int nc,
+                                     cudaStream_t s);
+cudaError_t launch_far_h16c(const FarH16Tiles& T, const int2* work, int nwork, int np2, int ldz, int z0, int nc,
+                            int* err, cudaStream_t s);
 
 // work: (level, row) per CTA, every row of every level in L exactly once;
 // err: set to a nonzero code if a bounded wait of the kernel ran out
