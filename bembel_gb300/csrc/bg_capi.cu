@@ -644,6 +644,12 @@ static bg_status assemble_far(bg_operator* op) {
                                  op->block_stride(f.B), op->kre, op->kim, op->d_far64[l]->p, s); }),
              "far-field assembly");
     if (op->cplx) {
+      // double-float pairs of Re and Im for the complex FP64 product
+      const long sdf = ((long)f.B * f.B + 1) / 2 * 2;
+      BG_CHECK(op->d_far_df[l]->alloc(2 * f.col.size() * sdf * sizeof(float2)), "far field storage");
+      BG_CHECK(launch_split_df_cplx_blocks(op->d_far64[l]->p, op->block_stride(f.B), (long)f.B * f.B, (long)f.col.size(),
+                                           sdf, op->d_far_df[l]->p, s),
+               "far-field split");
       // scaled FP16 hi / lo tiles of Re and Im for the complex tensor-core product
       const size_t tb = far_h16c_atile_bytes(np2);
       if (tb > 0) {
@@ -938,7 +944,9 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
     const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sb;
     BG_CHECK(op->w_y[l]->alloc(n), "work vectors");
     BG_CHECK(op->w_z[l]->alloc(n), "work vectors");
-    if (!op->cplx) BG_CHECK(op->w_ydf[l]->alloc(n), "work vectors");
+    // double-float split of y (complex: 16 columns at a time)
+    BG_CHECK(op->w_ydf[l]->alloc(op->cplx ? (size_t)op->nclusters(l) * op->np * op->np * 32 * sizeof(float2) : n),
+             "work vectors");
     const size_t tb = op->cplx ? far_h16c_btile_bytes(op->np * op->np) : far_h16_btile_bytes(op->np * op->np);
     if (op->maxwell()) {
       const size_t nv = (size_t)op->nclusters(l) * op->np * op->np * 4 * std::min(nrhs, (int)bg_operator::kMwRhsChunk) * sb;
@@ -1127,6 +1135,29 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                                                                       op->d_err.as<int>(), s); }),
                "far-field product (tensor cores)");
     }
+    // complex FP64 far product of level l on the double-float pipes: z (rows
+    // of ld complex entries) = K y, 16 columns per pass, Kr split(y) + Ki split(i y)
+    auto far64_cplx = [&](int l, const void* y, int ld, void* z) -> bg_status {
+      const BsrSegment& f = op->far[l];
+      const long sdf = ((long)f.B * f.B + 1) / 2 * 2;
+      const float2* kr = op->d_far_df[l]->as<float2>();
+      const float2* ki = kr + (long)f.col.size() * sdf;
+      const long rows = (long)op->nclusters(l) * f.B;
+      for (int c0 = 0; c0 < ld; c0 += 16) {
+        const int nc = std::min(16, ld - c0);
+        for (int part = 0; part < 2; ++part) {
+          BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df_cols(y, rows, ld, c0, nc, part,
+                                                                                  op->w_ydf[l]->p, s); }),
+                   "far-field split of Y");
+          BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_df_cols(f.d_row_ptr.as<int>(), f.d_col.as<int>(),
+                                                                            part ? ki : kr, sdf, f.nrows, f.B,
+                                                                            op->w_ydf[l]->p, z, 2 * nc, 2 * ld,
+                                                                            2 * c0, part, s); }),
+                   "far-field product (complex double-float)");
+        }
+      }
+      return BG_OK;
+    };
     for (int l = 0; l <= op->leaf_level && !tc && !tcc; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
@@ -1152,7 +1183,10 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                                       f.d_row_ptr.as<int>(), f.d_col.as<int>(), f.nrows, np2, (float)op->kre, (float)op->kim,
                                       op->w_yv[l]->p, op->w_zv[l]->p, 4 * nr, s); }),
                      "far-field product (FP32 fused, Maxwell)");
-          else
+          else if (op->d_far_df[l]->p) {
+            bg_status st = far64_cplx(l, op->w_yv[l]->p, 4 * nr, op->w_zv[l]->p);
+            if (st != BG_OK) return st;
+          } else
             BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(true, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
                                   op->block_stride(f.B), f.nrows, f.B, op->w_yv[l]->p, op->w_zv[l]->p, 4 * nr, 0, s); }),
                      "far-field product (Maxwell)");
@@ -1170,7 +1204,10 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
                  "far-field product (FP32 fused)");
       } else {
         if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "the FP64 product needs the stored far field");
-        if (!op->cplx && op->d_far_df[l]->p) {
+        if (op->cplx && op->d_far_df[l]->p) {
+          bg_status st = far64_cplx(l, op->w_y[l]->p, nrhs, op->w_z[l]->p);
+          if (st != BG_OK) return st;
+        } else if (!op->cplx && op->d_far_df[l]->p) {
           BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df(op->w_y[l]->p, (long)op->nclusters(l) * op->R * nrhs,
                                                                          op->w_ydf[l]->p, s); }),
                    "far-field split of Y");

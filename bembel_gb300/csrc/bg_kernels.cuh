@@ -177,6 +177,16 @@ cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks
                           const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
 // out[t] = (hi, lo) of in[t] (FP64), t < n
 cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s);
+// as launch_bsr_df, writing columns y0 .. y0 + nrhs - 1 of y rows of ldy entries
+cudaError_t launch_bsr_df_cols(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
+                               const void* x, void* y, int nrhs, int ldy, int y0, int accumulate, cudaStream_t s);
+// Complex double-float product, Re y + i Im y = Kr split(x) + Ki split(i x) with
+// complex columns seen as interleaved real pairs: the column split of x (times
+// 1 or times i) and the split of complex blocks into Kr pairs followed by Ki pairs
+cudaError_t launch_split_df_cols(const void* in, long rows, int ld, int c0, int nc, int times_i, void* out,
+                                 cudaStream_t s);
+cudaError_t launch_split_df_cplx_blocks(const void* in, long sin, long B2, long nblocks, long sout, void* out,
+                                        cudaStream_t s);
 // op(A) of an FMM transform, stored transposed: AT[q][i], q < Ki, i < ld
 // (ld a multiple of 4, at least Mo rounded up to 3, zero beyond Mo)
 struct TGemmA {

@@ -936,7 +936,7 @@ template <int NCOL, bool FULL>
 __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr, const int* __restrict__ col,
                                                 const float2* __restrict__ blocks, long bstride, int B,
                                                 const float2* __restrict__ x, double* __restrict__ y, int nrhs,
-                                                int accumulate) {
+                                                int ldy, int y0, int accumulate) {
   extern __shared__ __align__(16) float2 xsm[];  // [2][B * nrhs]
   const int row = blockIdx.x, t = threadIdx.x;
   const int i = t % B, cg = t / B, c0 = cg * NCOL;
@@ -999,7 +999,7 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
     }
   }
   if (active) {
-    double* yo = y + ((long)row * B + i) * nrhs;
+    double* yo = y + ((long)row * B + i) * ldy + y0;
 #pragma unroll
     for (int c = 0; c < NCOL; ++c)
       if (FULL || c0 + c < nrhs) {
@@ -1011,7 +1011,12 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
 
 cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
                           const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  return launch_bsr_df_cols(row_ptr, col, blocks, bstride, nrows, B, x, y, nrhs, nrhs, 0, accumulate, s);
+}
+cudaError_t launch_bsr_df_cols(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
+                               const void* x, void* y, int nrhs, int ldy, int y0, int accumulate, cudaStream_t s) {
   if (nrows == 0) return cudaSuccess;
+  if (y0 < 0 || y0 + nrhs > ldy) return cudaErrorInvalidValue;
   int ncol = nrhs <= 1 ? 1 : (nrhs <= 2 ? 2 : (nrhs <= 4 ? 4 : 8));
   int groups = (nrhs + ncol - 1) / ncol;
   while (B * groups > 352) {
@@ -1031,7 +1036,7 @@ cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks
     auto kf = k_bsr_df<NC, FU>;                                                                             \
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
     if (e != cudaSuccess) return e;                                                                         \
-    kf<<<nrows, threads, smem, s>>>(row_ptr, col, bl, bstride, B, xx, yy, nrhs, accumulate);                \
+    kf<<<nrows, threads, smem, s>>>(row_ptr, col, bl, bstride, B, xx, yy, nrhs, ldy, y0, accumulate);      \
     return cudaGetLastError();                                                                              \
   }
   BG_DF(1, true)
@@ -1055,6 +1060,49 @@ __global__ void k_split_df(const double* __restrict__ in, long n, float2* __rest
   const double v = in[t];
   const float h = (float)v;
   out[t] = make_float2(h, (float)(v - (double)h));
+}
+// complex columns c0 .. c0 + nc - 1 of rows of ld complex entries, times 1 or
+// times i, as interleaved (re, im) double-float pairs: out[(r nc + c) 2 + {0, 1}]
+__global__ void k_split_df_cols(const double2* __restrict__ in, long rows, int ld, int c0, int nc, int times_i,
+                                float2* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= rows * nc) return;
+  const long r = t / nc;
+  const int c = (int)(t % nc);
+  const double2 v = in[r * ld + c0 + c];
+  const double re = times_i ? -v.y : v.x, im = times_i ? v.x : v.y;
+  const float hr = (float)re, hi = (float)im;
+  out[2 * t] = make_float2(hr, (float)(re - (double)hr));
+  out[2 * t + 1] = make_float2(hi, (float)(im - (double)hi));
+}
+cudaError_t launch_split_df_cols(const void* in, long rows, int ld, int c0, int nc, int times_i, void* out,
+                                 cudaStream_t s) {
+  const long n = rows * nc;
+  if (n == 0) return cudaSuccess;
+  if (c0 < 0 || nc < 1 || c0 + nc > ld) return cudaErrorInvalidValue;
+  k_split_df_cols<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const double2*>(in), rows, ld, c0, nc,
+                                                                times_i, static_cast<float2*>(out));
+  return cudaGetLastError();
+}
+// complex FP64 blocks -> double-float pairs of the real parts (out) and of the
+// imaginary parts (out + nblocks * sout); sout pairs between blocks
+__global__ void k_split_df_cplx_blocks(const double2* __restrict__ in, long sin, long B2, long nblocks, long sout,
+                                       float2* __restrict__ out) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nblocks * B2) return;
+  const long b = t / B2, e = t % B2;
+  const double2 v = in[b * sin + e];
+  const float hr = (float)v.x, hi = (float)v.y;
+  out[b * sout + e] = make_float2(hr, (float)(v.x - (double)hr));
+  out[(nblocks + b) * sout + e] = make_float2(hi, (float)(v.y - (double)hi));
+}
+cudaError_t launch_split_df_cplx_blocks(const void* in, long sin, long B2, long nblocks, long sout, void* out,
+                                        cudaStream_t s) {
+  const long n = nblocks * B2;
+  if (n == 0) return cudaSuccess;
+  k_split_df_cplx_blocks<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const double2*>(in), sin, B2,
+                                                                       nblocks, sout, static_cast<float2*>(out));
+  return cudaGetLastError();
 }
 cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
