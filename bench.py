@@ -328,6 +328,18 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def class_breakdown(L, ctx, fn):
+    """Device time and launches per kernel class of fn(), every class bracketed."""
+    L.bg_profile_classes(ctx.h, 0xFF)
+    L.bg_profile_enable(ctx.h, 1)
+    _read_profile(L, ctx)
+    fn()
+    prof = _read_profile(L, ctx)
+    L.bg_profile_enable(ctx.h, 0)
+    return {"ms": {k: round(v, 3) for k, v in prof["ms"].items() if v},
+            "launches": {k: v for k, v in prof["launches"].items() if v}}
+
+
 CLASSES = ["near_fp64", "far_fp64", "far_fused_fp32", "transforms", "t_apply", "krylov", "other", "assembly"]
 
 
@@ -498,6 +510,92 @@ def run_maxwell(args):
     print(json.dumps(line), flush=True)
 
 
+def run_helmholtz(args):
+    """Side workload (not the headline line): the Helmholtz single layer on the
+    16-patch torus (R = 2, r = 0.5), M = 4, P = 2, n_p = 10, swept over seeded
+    wavenumbers kappa ~ U[0.5, 6] (seed 4) with 64 plane-wave right-hand sides
+    exp(-i kappa d.x), d uniform on the sphere (seed 5). Per wavenumber: the
+    operator is re-assembled (near field, couplings, tensor-core tiles) and
+    the 64 systems are solved to 1e-8 with the FP32 inner operator; the first
+    wavenumber is also solved on the plain FP64 path. --kappas bounds how many
+    of the 16 wavenumbers run."""
+    import torch
+    import bembel_gb300 as bg
+    from bembel_gb300 import _lib
+    L = _lib.load()
+    ctx = bg.Context(0)
+    sp = ctypes_void_p()
+    L.bg_context_get_stream(ctx.h, ctypes_byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", 0))
+    geo = os.path.join(ROOT, "tests", "golden", "geo", "torus.dat")
+    m, p, n_p, nrhs = 4, 2, 10, 64
+    kappas = np.random.default_rng(4).uniform(0.5, 6.0, 16)[:max(1, min(16, args.kappas))]
+    d = np.random.default_rng(5).normal(size=(nrhs, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    lin = bg.HelmholtzSingleLayerOperator()
+    op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(geo, ctx), m, p), lin, n_p=n_p)
+    A = op.get_discrete_operator()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1) * 1e-3
+
+    per = []
+    clocks = ClockSampler(0)
+    t_all = time.time()
+    with clocks:
+        for i, k in enumerate(kappas):
+            lin.set_wavenumber(float(k))
+            t0 = time.time()
+            op.compute()
+            torch.cuda.synchronize()
+            t_asm = time.time() - t0
+            b = torch.from_numpy(np.ascontiguousarray(op.load_vector(2, d).T)).cuda().t()
+            (x, st), t_solve = timed(lambda: A.solve(b, tol=TOL, inner="fp32", inner_tol=INNER_TOL, restart=200,
+                                                     max_refinements=12))
+            rec = {"kappa": float(k), "assembly_s": t_asm, "solve_s": t_solve, "iterations": st["iterations"],
+                   "fp64_matvecs": st["fp64_matvecs"], "final_relres": st["final_relres"]}
+            if i == 0:
+                if not args.no_fp64:
+                    (x64, st64), t64 = timed(lambda: A.solve(b, tol=TOL, inner="fp64", restart=200,
+                                                             max_refinements=12))
+                    rec.update({"fp64_solve_s": t64, "fp64_iterations": st64["iterations"],
+                                "mixed_vs_fp64_solution": float(np.max(
+                                    np.linalg.norm((x - x64).cpu().numpy(), axis=0) /
+                                    np.linalg.norm(x64.cpu().numpy(), axis=0)))})
+                xq = torch.randn(op.N, nrhs, dtype=torch.complex128, device="cuda")
+                for prec in ("fp64", "fp32"):  # warm-up
+                    A.matvec(xq, precision=prec)
+                _, tm64 = timed(lambda: A.matvec(xq, precision="fp64"))
+                _, tm32 = timed(lambda: A.matvec(xq, precision="fp32"))
+                rec.update({"fp64_product_ms_64rhs": tm64 * 1e3, "fp32_product_ms_64rhs": tm32 * 1e3,
+                            "kernel_ms_per_product": {prec: class_breakdown(L, ctx, lambda: A.matvec(xq, precision=prec))
+                                                      for prec in ("fp64", "fp32")}})
+            per.append(rec)
+    wall = time.time() - t_all
+    solve_s = sum(r["solve_s"] for r in per)
+    asm_s = sum(r["assembly_s"] for r in per)
+    info = op.info()
+    line = {"workload": "helmholtz_sl_h2_torus_M4_P2_np10_64rhs_kappa_sweep",
+            "metric": "solves/s (64 plane waves per wavenumber, Helmholtz SL H2 solves to rel.err 1e-8)",
+            "unit": "solves/s", "value": nrhs * len(per) / solve_s,
+            "value_with_assembly": nrhs * len(per) / (solve_s + asm_s), "kappas": len(per), "wall_s": wall,
+            "fp64_path": ({"solves_per_s": nrhs / per[0]["fp64_solve_s"], "iterations": per[0]["fp64_iterations"]}
+                          if "fp64_solve_s" in per[0] else None),
+            "dtype": "c128+c64", "data": "synthetic (seeded wavenumbers and plane-wave directions, torus.dat)",
+            "config": {"elements": int(info[2]), "dofs": op.N, "refinement": m, "degree": p, "n_p": n_p, "nrhs": nrhs,
+                       "tol": TOL, "dense_leaves": int(info[3]), "lowrank_leaves": int(info[4]),
+                       "far_field_bytes": int(info[13]), "near_field_bytes": int(info[14])},
+            "per_kappa": per, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_void_p():
     import ctypes
     return ctypes.c_void_p()
@@ -548,11 +646,15 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
                     help="product precision of --profile matvec")
     ap.add_argument("--profile-m", type=int, default=None, help="refinement level of --profile cases (default 5)")
-    ap.add_argument("--workload", default="laplace", choices=["laplace", "maxwell"],
-                    help="laplace: the headline line; maxwell: the EFIE side workload")
+    ap.add_argument("--workload", default="laplace", choices=["laplace", "maxwell", "helmholtz"],
+                    help="laplace: the headline line; maxwell / helmholtz: side workloads")
+    ap.add_argument("--kappas", type=int, default=4, help="wavenumbers of the helmholtz sweep (of 16)")
+    ap.add_argument("--no-fp64", action="store_true", help="helmholtz: skip the plain FP64 solve")
     args = ap.parse_args()
     if args.workload == "maxwell" and args.impl == "gb300" and not args.profile:
         run_maxwell(args)
+    elif args.workload == "helmholtz" and args.impl == "gb300" and not args.profile:
+        run_helmholtz(args)
     elif args.profile:
         run_profile_case(args)
     elif args.impl == "reference":
