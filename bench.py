@@ -616,6 +616,20 @@ def run_profile_case(args):
     ctx = bg.Context(0)
     store = True  # the tensor-core far field streams tiles built from the stored FP64 blocks
     m = args.profile_m if args.profile_m is not None else M
+    if args.workload == "maxwell":
+        # EFIE on the sphere, P = 2, n_p = 9, kappa = 2, 8 right-hand sides
+        lin = bg.MaxwellSingleLayerOperator()
+        lin.set_wavenumber(2.0)
+        op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, P), lin, n_p=NP)
+        op.compute()
+        A = op.get_discrete_operator()
+        x = torch.randn(op.N, 8, dtype=torch.complex128, device="cuda")
+        for _ in range(5):
+            A.matvec(x, precision=args.precision)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "matvec", "workload": "maxwell", "precision": args.precision, "M": m, "N": op.N,
+                          "products": 5}))
+        return
     op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
                              store_fp64_far=store)
     op.compute()
