@@ -24,7 +24,7 @@ from . import _lib
 from ._lib import BembelError, H2Params, SolveParams, SolveStats
 
 __all__ = ["Context", "Geometry", "AnsatzSpace", "LaplaceSingleLayerOperator", "HelmholtzSingleLayerOperator",
-           "MaxwellSingleLayerOperator", "DiscreteOperator", "H2Matrix", "BembelError", "default_context"]
+           "MaxwellSingleLayerOperator", "DiscreteOperator", "H2Matrix", "Server", "BembelError", "default_context"]
 
 _default_ctx = None
 
@@ -343,3 +343,80 @@ class DiscreteOperator:
         buf = np.zeros(n * n, dtype=dt)
         self.ctx.check(_lib.load().bg_operator_leaf_block(self.h, leaf, rc, cc, _dp(buf.view(np.float64))))
         return buf.reshape((n, n), order="F")
+
+
+class Server:
+    """Serving loop of the library (bg_server_*): worker threads, each with
+    its own stream on the context's GPU, solve queued requests, batching
+    requests for the same operator; assembled operators are cached per
+    (geometry, kind, M, P, wavenumber), sharded over the workers and admitted
+    by device memory (least recently used evicted).
+
+        srv = Server(ctx, hbm_budget_bytes=200e9, workers=4)
+        g = srv.add_geometry(Geometry("sphere.dat", ctx))
+        t = srv.submit(g, "laplace", M=4, P=2, data_kind=0, data=x0)  # x0: (nrhs, 3)
+        x, info = srv.wait(t)                                          # x: (N, nrhs)
+    """
+
+    KINDS = {"laplace": _lib.LAPLACE_SL, "helmholtz": _lib.HELMHOLTZ_SL, "maxwell": _lib.MAXWELL_SL}
+
+    def __init__(self, ctx, hbm_budget_bytes, workers=1):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        ctx.check(_lib.load().bg_server_create(ctx.h, int(hbm_budget_bytes), int(workers), ctypes.byref(h)))
+        self.h = h
+        self._geos = []
+        self._pending = {}
+
+    def add_geometry(self, geometry):
+        idx = ctypes.c_int()
+        self.ctx.check(_lib.load().bg_server_add_geometry(self.h, geometry.h, ctypes.byref(idx)))
+        n = ctypes.c_int()
+        self.ctx.check(_lib.load().bg_geometry_num_patches(geometry.h, ctypes.byref(n)))
+        self._geos.append((geometry, n.value))
+        return idx.value
+
+    def submit(self, geometry, kind, M, P, data_kind, data, kappa=0.0, tol=1e-8, inner="fp32"):
+        op_kind = self.KINDS[kind] if isinstance(kind, str) else int(kind)
+        data = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1, 6 if data_kind == 3 else 3))
+        nrhs = data.shape[0]
+        vd = 2 if op_kind == _lib.MAXWELL_SL else 1
+        bound = vd * self._geos[geometry][1] * (2 ** M + P) ** 2  # dimension before gluing >= N
+        cplx = op_kind != _lib.LAPLACE_SL
+        x = np.zeros(bound * nrhs, dtype=np.complex128 if cplx else np.float64)
+        k = complex(kappa)
+        req = _lib.Request(geometry, op_kind, M, P, k.real, k.imag, data_kind, nrhs,
+                           data.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), tol, _lib.PRECISIONS[inner],
+                           x.ctypes.data_as(ctypes.c_void_p), bound * nrhs)
+        t = ctypes.c_long()
+        self.ctx.check(_lib.load().bg_server_submit(self.h, ctypes.byref(req), ctypes.byref(t)))
+        self._pending[t.value] = (x, nrhs)
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        """(x of shape (N, nrhs) or None on failure, result dict)."""
+        r = _lib.RequestResult()
+        self.ctx.check(_lib.load().bg_server_wait(self.h, ticket, float(timeout), ctypes.byref(r)))
+        x, nrhs = self._pending.pop(ticket)
+        info = {"status": r.status, "N": r.N, "t_submit": r.t_submit, "t_start": r.t_start, "t_done": r.t_done,
+                "cache_hit": bool(r.cache_hit), "batch_nrhs": r.batch_nrhs,
+                "stats": {k: getattr(r.stats, k) for k, _ in SolveStats._fields_},
+                "error": r.error.decode(errors="replace")}
+        ok = r.status in (_lib.BG_OK, _lib.BG_NOT_CONVERGED)
+        return (x[:r.N * nrhs].reshape((r.N, nrhs), order="F") if ok else None), info
+
+    def stats(self):
+        st = _lib.ServerStats()
+        self.ctx.check(_lib.load().bg_server_stats_get(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().bg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -34,6 +34,26 @@ class SolveStats(ctypes.Structure):
                 ("low_matvecs", ctypes.c_int), ("final_relres", ctypes.c_double)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("geometry", ctypes.c_int), ("op_kind", ctypes.c_int), ("M", ctypes.c_int), ("P", ctypes.c_int),
+                ("kre", ctypes.c_double), ("kim", ctypes.c_double), ("data_kind", ctypes.c_int),
+                ("nrhs", ctypes.c_int), ("data", ctypes.POINTER(ctypes.c_double)), ("tol", ctypes.c_double),
+                ("inner_precision", ctypes.c_int), ("x", ctypes.c_void_p), ("x_capacity", ctypes.c_long)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("N", ctypes.c_int), ("t_submit", ctypes.c_double),
+                ("t_start", ctypes.c_double), ("t_done", ctypes.c_double), ("cache_hit", ctypes.c_int),
+                ("batch_nrhs", ctypes.c_int), ("stats", SolveStats), ("error", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_long), ("completed", ctypes.c_long), ("failed", ctypes.c_long),
+                ("batches", ctypes.c_long), ("cache_hits", ctypes.c_long), ("cache_misses", ctypes.c_long),
+                ("evictions", ctypes.c_long), ("bytes_in_use", ctypes.c_size_t), ("bytes_budget", ctypes.c_size_t),
+                ("assembly_s", ctypes.c_double), ("solve_s", ctypes.c_double), ("cached_operators", ctypes.c_int)]
+
+
 class BembelError(RuntimeError):
     def __init__(self, status, message):
         name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
@@ -82,6 +102,14 @@ def load(build_if_missing=True):
         "bg_operator_leaves": (I, [P, ip]),
         "bg_operator_transform": (I, [P, ip, ip, dp]),
         "bg_operator_leaf_block": (I, [P, Lg, I, I, dp]),
+        "bg_operator_memory": (I, [P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+        "bg_geometry_num_patches": (I, [P, ip]),
+        "bg_server_create": (I, [P, ctypes.c_size_t, I, PP]),
+        "bg_server_destroy": (I, [P]),
+        "bg_server_add_geometry": (I, [P, P, ip]),
+        "bg_server_submit": (I, [P, ctypes.POINTER(Request), lp]),
+        "bg_server_wait": (I, [P, Lg, D, ctypes.POINTER(RequestResult)]),
+        "bg_server_stats_get": (I, [P, ctypes.POINTER(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

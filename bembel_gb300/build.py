@@ -55,7 +55,7 @@ def build(force=False, verbose=False):
         jobs.append([nvcc] + ARCH + common + ["-lineinfo", "-diag-suppress", "1444", "-c", src, "-o", obj])
     for src in cpp:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
-        jobs.append([nvcc] + common + ["-c", src, "-o", obj])
+        jobs.append([nvcc] + common + ["-Xcompiler", "-pthread", "-c", src, "-o", obj])
 
     def run(cmd):
         if verbose:
@@ -68,7 +68,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 2))) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"]
+    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static", "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -490,6 +490,50 @@ extern "C" bg_status bg_operator_info(const bg_operator* op, long* info) {
   std::memcpy(info, v, sizeof(v));
   return BG_OK;
 }
+extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated, size_t* estimate) {
+  if (!op || !allocated || !estimate) return BG_INVALID_ARG;
+  size_t a = 0;
+  for (const DevBuf* b : {&op->d_patch_meta, &op->d_patch_cp, &op->d_el_patch, &op->d_el_llc, &op->d_T_ptr,
+                          &op->d_T_idx, &op->d_T_val, &op->d_Tt_ptr, &op->d_Tt_idx, &op->d_Tt_val, &op->d_cheb,
+                          &op->d_dense64, &op->d_dense32, &op->d_tr64, &op->d_tr32, &op->d_far_work, &op->d_err,
+                          &op->w_xdof, &op->w_xss, &op->w_yss, &op->w_ydof, &op->w_xss32, &op->w_yss32,
+                          &op->dense.d_row_ptr, &op->dense.d_col})
+    a += b->bytes;
+  for (const auto* v : {&op->d_pts64, &op->d_pts32, &op->d_centres, &op->d_tan64, &op->d_tan32, &op->d_far64,
+                        &op->d_far_df, &op->d_far_atiles, &op->d_far_ainv, &op->d_mom64, &op->d_mom32, &op->w_y,
+                        &op->w_z, &op->w_ydf, &op->w_yv, &op->w_zv, &op->w_btiles, &op->w_binv})
+    for (const DevBuf* b : *v) a += b->bytes;
+  for (const auto& tm : op->tm)
+    for (const DevBuf* b : {&tm.mom_f[0], &tm.mom_f[1], &tm.mom_b[0], &tm.mom_b[1], &tm.tr_f, &tm.tr_b, &tm.mw_f[0],
+                            &tm.mw_f[1], &tm.mw_f[2], &tm.mw_b[0], &tm.mw_b[1], &tm.mw_b[2]})
+      a += b->bytes;
+  for (const auto& f : op->far) a += f.d_row_ptr.bytes + f.d_col.bytes;
+  if (op->solver_ws && op->solver_ws_bytes) a += op->solver_ws_bytes(op->solver_ws);
+  *allocated = a;
+  // stored fields once assembled
+  const size_t sb = op->scalar_bytes(false);
+  const int np2 = op->np * op->np;
+  size_t e = (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * sb +
+             (size_t)op->dense.col.size() * op->block_stride32(op->dense.B) * sb / 2;
+  for (int l = 0; l <= op->leaf_level && l < (int)op->far.size(); ++l) {
+    const size_t nb = op->far[l].col.size();
+    const size_t ncl = (size_t)op->nclusters(l);
+    e += ncl * np2 * (sizeof(d4) + sizeof(float4) + (op->maxwell() ? 6 * (sizeof(double) + sizeof(float)) : 0));
+    if (!op->store_far) continue;
+    e += nb * op->block_stride(op->far[l].B) * sb;                 // FP64 couplings
+    e += nb * op->block_stride(op->far[l].B) * 8 * (op->cplx ? 2 : 1);  // double-float pairs
+    e += nb * (op->cplx ? far_h16c_atile_bytes(np2) : far_h16_atile_bytes(np2)) + nb * sizeof(float);
+  }
+  // work vectors and solver workspaces for 32 right-hand sides: superspace and
+  // level vectors, and three Krylov bases (restart 200) of N x 32
+  const size_t k = 32;
+  size_t lev = 0;
+  for (int l = 0; l <= op->leaf_level; ++l) lev += (size_t)op->vd * op->nclusters(l) * op->R;
+  e += 8 * (size_t)op->S * k * sb + 4 * lev * k * sb + 3 * 202 * (size_t)op->N * k * sb;
+  *estimate = std::max(e, a);
+  return BG_OK;
+}
+
 extern "C" bg_status bg_operator_assembly_times(const bg_operator* op, double* t3) {
   if (!op || !t3) return BG_INVALID_ARG;
   t3[0] = op->t_near;

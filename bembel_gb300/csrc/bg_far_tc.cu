@@ -405,7 +405,7 @@ template <int NP2>
 static cudaError_t launch_np(const FarTcLevels& L, const int2* work, int nwork, int nrhs, int* err, cudaStream_t s) {
   constexpr uint32_t smem = TcShape<NP2>::TOTAL;
   static_assert(smem <= 227 * 1024, "tensor-core far field: shared memory plan too large");
-  cudaError_t e = cudaFuncSetAttribute(k_far_tc<NP2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = smem_limit(k_far_tc<NP2>, smem);
   if (e != cudaSuccess) return e;
   k_far_tc<NP2><<<nwork, kThreads, smem, s>>>(L, work, nrhs, err);
   return cudaGetLastError();
@@ -791,7 +791,7 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
   case N: {                                                                                                 \
     constexpr uint32_t smem = H16Shape<N>::SMEM;                                                            \
     static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
-    cudaError_t e = cudaFuncSetAttribute(k_far_h16<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaError_t e = smem_limit(k_far_h16<N>, smem); \
     if (e != cudaSuccess) return e;                                                                         \
     k_far_h16<N><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err);            \
     return cudaGetLastError();                                                                              \
@@ -1146,7 +1146,7 @@ cudaError_t launch_far_h16c(const FarH16Tiles& T, const int2* work, int nwork, i
   case N: {                                                                                                  \
     constexpr uint32_t smem = H16CShape<N>::SMEM;                                                            \
     static_assert(smem <= 220 * 1024, "complex FP16 far field: shared memory plan too large");               \
-    cudaError_t e = cudaFuncSetAttribute(k_far_h16c<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaError_t e = smem_limit(k_far_h16c<N>, smem); \
     if (e != cudaSuccess) return e;                                                                          \
     k_far_h16c<N><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, ldz, z0, nc, err);     \
     return cudaGetLastError();                                                                               \

@@ -9,6 +9,17 @@
 
 namespace bg {
 
+// Raise the dynamic shared-memory limit of a kernel to at least bytes. The
+// limit is one value per kernel for the whole process and launches from
+// several host threads (the serving workers) may use different sizes, so it
+// only ever grows: lowering it between another thread's call and launch would
+// make that launch fail.
+cudaError_t raise_smem_limit(const void* func, size_t bytes);
+template <typename K>
+inline cudaError_t smem_limit(K* func, size_t bytes) {
+  return raise_smem_limit(reinterpret_cast<const void*>(func), bytes);
+}
+
 // element pair of a dense leaf: output block position dst (scalars) inside
 // the dense-block pool; rot packs rot1 | rot2 << 4
 struct NearPair {

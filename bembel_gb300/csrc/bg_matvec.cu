@@ -11,9 +11,24 @@
 #include <algorithm>
 #include <type_traits>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "bg_kernels.cuh"
 
 namespace bg {
+
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> limit;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = limit[func];
+  if (bytes <= cur) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 
 template <typename S> struct RealOf;
 template <> struct RealOf<double> { typedef double T; };
@@ -379,7 +394,7 @@ static cudaError_t bgemm(bool ta, bool acc, const T* A, int Mo, int Ki, const T*
 #define BG_GEMM(TA_, AC_, ST_)                                                                             \
     {                                                                                                      \
       auto kf = k_bgemm<T, TA_, AC_, ST_, 3, 4>;                                                           \
-      cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);    \
+      cudaError_t e = smem_limit(kf, smem);    \
       if (e != cudaSuccess) return e;                                                                      \
       kf<<<grid, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, nbatch, kk);                           \
       return cudaGetLastError();                                                                           \
@@ -395,7 +410,7 @@ static cudaError_t bgemm(bool ta, bool acc, const T* A, int Mo, int Ki, const T*
 #define BG_KC(TA_, AC_)                                                                                    \
   {                                                                                                        \
     auto kf = k_bgemm_kc<T, TA_, AC_, RT, CT, KC>;                                                         \
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);      \
+    cudaError_t e = smem_limit(kf, smem);      \
     if (e != cudaSuccess) return e;                                                                        \
     kf<<<nbatch, 256, smem, s>>>(A, Mo, Ki, B, bstride, C, cstride, kk);                                   \
     return cudaGetLastError();                                                                             \
@@ -614,7 +629,7 @@ static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, 
       if (smem <= 200 * 1024) {
         const int vec_b = (kk % 4) == 0 && (bstride % 4) == 0 && (reinterpret_cast<uintptr_t>(B) % 16) == 0;
         auto kf = acc ? k_tgemm_small<true> : k_tgemm_small<false>;
-        cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = smem_limit(kf, smem);
         if (e != cudaSuccess) return e;
         kf<<<dim3(nbatch, (kk + 31) / 32), threads, smem, s>>>(reinterpret_cast<const float*>(A.at), A.ld, A.Mo, A.Ki,
                                                                 reinterpret_cast<const float*>(B), bstride,
@@ -631,7 +646,7 @@ static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, 
                     (reinterpret_cast<uintptr_t>(B) % 16) == 0;
   const dim3 grid(nbatch, (kk + 31) / 32);
   auto kf = acc ? k_tgemm<T, true> : k_tgemm<T, false>;
-  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = smem_limit(kf, smem);
   if (e != cudaSuccess) return e;
   kf<<<grid, 256, smem, s>>>(static_cast<const T*>(A.at), A.ld, A.Mo, A.Ki, B, bstride, C, cstride, kk, vec_b);
   return cudaGetLastError();
@@ -851,7 +866,7 @@ static cudaError_t bsr_typed(const int* row_ptr, const int* col, const S* blocks
 #define BG_BSR(NRV)                                                                                          \
   {                                                                                                          \
     auto kf = k_bsr<S, NRV>;                                                                                 \
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
+    cudaError_t e = smem_limit(kf, smem);        \
     if (e != cudaSuccess) return e;                                                                          \
     kf<<<nrows, bs, smem, s>>>(row_ptr, col, blocks, B, x, y, nrhs, accumulate);                             \
     return cudaGetLastError();                                                                               \
@@ -899,7 +914,7 @@ static cudaError_t bsr_pipe_typed(const int* row_ptr, const int* col, const S* b
 #define BG_PIPE(NC)                                                                                         \
   if (ncol == NC) {                                                                                         \
     auto kf = k_bsr_pipe<S, NC>;                                                                            \
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+    cudaError_t e = smem_limit(kf, smem);       \
     if (e != cudaSuccess) return e;                                                                         \
     kf<<<nrows, threads, smem, s>>>(row_ptr, col, blocks, bstride, B, x, y, nrhs, accumulate);              \
     return cudaGetLastError();                                                                              \
@@ -1034,7 +1049,7 @@ cudaError_t launch_bsr_df_cols(const int* row_ptr, const int* col, const void* b
 #define BG_DF(NC, FU)                                                                                       \
   if (ncol == NC && full == FU) {                                                                           \
     auto kf = k_bsr_df<NC, FU>;                                                                             \
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+    cudaError_t e = smem_limit(kf, smem);       \
     if (e != cudaSuccess) return e;                                                                         \
     kf<<<nrows, threads, smem, s>>>(row_ptr, col, bl, bstride, B, xx, yy, nrhs, ldy, y0, accumulate);      \
     return cudaGetLastError();                                                                              \
@@ -1177,7 +1192,7 @@ cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const
     const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float);
     if (smem <= 100 * 1024) {
       const int threads = (((B / 4) * (nrhs / 4)) + 31) / 32 * 32;
-      cudaError_t e = cudaFuncSetAttribute(k_bsr32_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = smem_limit(k_bsr32_tile, smem);
       if (e != cudaSuccess) return e;
       k_bsr32_tile<<<nrows, threads, smem, s>>>(row_ptr, col, static_cast<const float*>(blocks), bstride, B,
                                                 static_cast<const float*>(x), static_cast<float*>(y), nrhs, accumulate);
@@ -1214,7 +1229,7 @@ static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void
   if (ncl == 0) return cudaSuccess;
   const size_t smem = (size_t)Bq * nrhs * sizeof(S);
   auto kf = k_moment_fwd<S>;
-  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = smem_limit(kf, smem);
   if (e != cudaSuccess) return e;
   kf<<<ncl, 256, smem, s>>>((const typename RealOf<S>::T*)mom, R, Bq, (const S*)xss, (S*)y, nrhs);
   return cudaGetLastError();
@@ -1248,7 +1263,7 @@ static cudaError_t mom_bwd_t(const void* mom, int R, int Bq, int ncl, const void
   if (ncl == 0) return cudaSuccess;
   const size_t smem = (size_t)R * nrhs * sizeof(S);
   auto kf = k_moment_bwd<S>;
-  cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = smem_limit(kf, smem);
   if (e != cudaSuccess) return e;
   kf<<<ncl, 256, smem, s>>>((const typename RealOf<S>::T*)mom, R, Bq, (const S*)z, (S*)yss, nrhs);
   return cudaGetLastError();
@@ -1319,7 +1334,7 @@ static cudaError_t far_fused_t(const float4* pts, const d4* centres, const int* 
 #define BG_FF(NCV)                                                                                          \
   {                                                                                                         \
     auto kf = k_far_fused<CPLX, NP2, NCV>;                                                                  \
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);       \
+    cudaError_t e = smem_limit(kf, smem);       \
     if (e != cudaSuccess) return e;                                                                         \
     kf<<<nrows, 128, smem, s>>>(pts, centres, row_ptr, col, kre, kim, y, z, nrhs);                          \
     return cudaGetLastError();                                                                              \

@@ -123,7 +123,7 @@ static cudaError_t run_regular(const NearPair* pairs, int npairs, const d4* tab,
   size_t smem = Q * sizeof(d4) + Q * P2 * sizeof(double) + Q * sizeof(double) + Q * P2 * sizeof(S);
   if (smem > 200 * 1024) return cudaErrorInvalidConfiguration;
   auto kfn = k_near_regular<P, S>;
-  cudaError_t err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = smem_limit(kfn, smem);
   if (err != cudaSuccess) return err;
   if (npairs == 0) return cudaSuccess;
   kfn<<<npairs, 128, smem, s>>>(pairs, tab, n1, basis, kre, kim, out, B);
@@ -519,7 +519,7 @@ static cudaError_t run_regular_mw(const NearPairV* pairs, int npairs, const MwPt
   const size_t smem = regular_mw_smem<P>(n1 * n1);
   if (smem > 220 * 1024) return cudaErrorInvalidConfiguration;
   auto kfn = k_near_regular_mw<P>;
-  cudaError_t err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = smem_limit(kfn, smem);
   if (err != cudaSuccess) return err;
   if (npairs == 0) return cudaSuccess;
   kfn<<<npairs, 128, smem, s>>>(pairs, tab, n1, basis3, kre, kim, idiv, out, B);
@@ -736,7 +736,7 @@ static cudaError_t run_duffy_mw(int cs, const PatchTable& pt, const ElementTable
 #define BG_DMW(CSV)                                                                                      \
   {                                                                                                      \
     auto kfn = k_near_duffy_mw<G, P, CSV>;                                                               \
-    cudaError_t err = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    cudaError_t err = smem_limit(kfn, smem); \
     if (err != cudaSuccess) return err;                                                                  \
     if (npairs == 0) return cudaSuccess;                                                                 \
     kfn<<<npairs, 128, smem, s>>>(pt, et, pairs, gx, gw, n1, kre, kim, idiv, out, B);                    \

@@ -182,6 +182,7 @@ struct bg_operator {
   // solver workspaces kept between bg_solve calls (owned by the solver)
   void* solver_ws = nullptr;
   void (*solver_ws_free)(void*) = nullptr;
+  size_t (*solver_ws_bytes)(const void*) = nullptr;
 
   ~bg_operator() {
     if (solver_ws && solver_ws_free) solver_ws_free(solver_ws);

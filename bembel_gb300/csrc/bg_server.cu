@@ -1,0 +1,377 @@
+// Serving loop over the C ABI: a request queue drained by one worker thread
+// on the context's GPU, batching of requests that share an operator, and a
+// cache of assembled operators with admission by device memory.
+//
+// The reference has no serving layer (its examples assemble once and solve
+// once); this file is the runtime around the operator for a stream of solves
+// on different geometries, refinement levels, degrees and wavenumbers.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <list>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "bg_operator.hpp"
+
+namespace {
+
+struct OpKey {
+  int geo, kind, M, P;
+  double kre, kim;
+  bool operator<(const OpKey& o) const {
+    return std::tie(geo, kind, M, P, kre, kim) < std::tie(o.geo, o.kind, o.M, o.P, o.kre, o.kim);
+  }
+  bool operator==(const OpKey& o) const {
+    return geo == o.geo && kind == o.kind && M == o.M && P == o.P && kre == o.kre && kim == o.kim;
+  }
+};
+
+struct CacheEntry {
+  OpKey key;
+  bg_operator* op;
+  size_t bytes;  // admitted footprint (estimate at admission, raised to the measured one after use)
+};
+
+struct Job {
+  long ticket;
+  bg_request req;
+  std::vector<double> data;  // copy of the data parameters
+  double t_submit;
+};
+
+OpKey key_of(const bg_request& r) {
+  const bool wave = r.op_kind != BG_LAPLACE_SL;
+  return OpKey{r.geometry, r.op_kind, r.M, r.P, wave ? r.kre : 0.0, wave ? r.kim : 0.0};
+}
+
+// requests that can share one batched solve
+bool batchable(const bg_request& a, const bg_request& b) {
+  return key_of(a) == key_of(b) && a.data_kind == b.data_kind && a.tol == b.tol &&
+         a.inner_precision == b.inner_precision;
+}
+
+}  // namespace
+
+// One worker: its own context (stream, pinned staging) on the server's GPU,
+// its own operator cache and its share of the memory budget. Operators are
+// sharded over the workers by key, so an operator only ever runs on the
+// stream of the context that created it.
+struct Worker {
+  int id = 0;
+  bg_context* ctx = nullptr;
+  size_t budget = 0;
+  std::list<CacheEntry> cache;  // front: most recently used
+  size_t in_use = 0;
+  DevBuf b_dev, x_dev;
+  std::thread th;
+};
+
+struct bg_server {
+  bg_context* ctx = nullptr;
+  size_t budget = 0;
+  std::vector<const bg_geometry*> geos;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job> queue;
+  std::map<long, bg_request_result> done;
+  long next_ticket = 1;
+  bool stop = false;
+  bg_server_stats st{};
+  std::chrono::steady_clock::time_point t0;
+  std::vector<Worker*> workers;
+
+  double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+
+  int shard(const OpKey& k) const {
+    size_t h = std::hash<int>()(k.geo) * 1000003u ^ std::hash<int>()(k.kind * 131 + k.M * 17 + k.P);
+    h = h * 1000003u ^ std::hash<double>()(k.kre) ^ (std::hash<double>()(k.kim) << 1);
+    return (int)(h % workers.size());
+  }
+
+  void update_usage() {  // caller holds mu
+    size_t u = 0;
+    int n = 0;
+    for (const Worker* w : workers) {
+      u += w->in_use;
+      n += (int)w->cache.size();
+    }
+    st.bytes_in_use = u;
+    st.cached_operators = n;
+  }
+
+  void evict_back(Worker& w) {
+    CacheEntry& e = w.cache.back();
+    bg_operator_destroy(e.op);
+    std::lock_guard<std::mutex> lk(mu);
+    w.in_use -= e.bytes;
+    w.cache.pop_back();
+    ++st.evictions;
+    update_usage();
+  }
+
+  // operator of key k, assembled; nullptr and *status on failure
+  bg_operator* acquire(Worker& w, const OpKey& k, bool* hit, bg_status* status) {
+    for (auto it = w.cache.begin(); it != w.cache.end(); ++it)
+      if (it->key == k) {
+        std::lock_guard<std::mutex> lk(mu);
+        w.cache.splice(w.cache.begin(), w.cache, it);
+        *hit = true;
+        return w.cache.front().op;
+      }
+    *hit = false;
+    if (k.geo < 0 || k.geo >= (int)geos.size()) {
+      *status = BG_INVALID_ARG;
+      return nullptr;
+    }
+    bg_h2_params prm;
+    bg_h2_params_default(&prm);
+    bg_operator* op = nullptr;
+    bg_status s = bg_operator_create(w.ctx, geos[k.geo], k.M, k.P, k.kind, &prm, &op);
+    if (s == BG_OK && k.kind != BG_LAPLACE_SL) s = bg_operator_set_wavenumber(op, k.kre, k.kim);
+    size_t alloc = 0, est = 0;
+    if (s == BG_OK) s = bg_operator_memory(op, &alloc, &est);
+    if (s == BG_OK && est > w.budget) s = BG_OOM;
+    if (s != BG_OK) {
+      if (op) bg_operator_destroy(op);
+      *status = s;
+      return nullptr;
+    }
+    while (!w.cache.empty() && w.in_use + est > w.budget) evict_back(w);
+    const double t = now();
+    s = bg_operator_assemble(op);
+    std::lock_guard<std::mutex> lk(mu);
+    st.assembly_s += now() - t;
+    if (s != BG_OK) {
+      bg_operator_destroy(op);
+      *status = s;
+      return nullptr;
+    }
+    w.cache.push_front(CacheEntry{k, op, est});
+    w.in_use += est;
+    update_usage();
+    return op;
+  }
+
+  void finish(Worker& w, std::vector<Job>& batch, bg_status status, int N, double t_start, bool hit, int tot,
+              const bg_solve_stats& stats) {
+    const double t_done = now();
+    std::string msg;
+    if (status != BG_OK && status != BG_NOT_CONVERGED) {
+      const char* m = bg_last_error_string(w.ctx);
+      msg = m ? m : "";
+      if (msg.empty()) msg = "status " + std::to_string((int)status);
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Job& j : batch) {
+      bg_request_result r{};
+      r.status = status;
+      r.N = N;
+      r.t_submit = j.t_submit;
+      r.t_start = t_start;
+      r.t_done = t_done;
+      r.cache_hit = hit ? 1 : 0;
+      r.batch_nrhs = tot;
+      r.stats = stats;
+      std::strncpy(r.error, msg.c_str(), sizeof(r.error) - 1);
+      done[j.ticket] = r;
+      ++(status == BG_OK || status == BG_NOT_CONVERGED ? st.completed : st.failed);
+    }
+    ++st.batches;
+    if (status == BG_OK || status == BG_NOT_CONVERGED) (hit ? st.cache_hits : st.cache_misses)++;
+    update_usage();
+    cv_done.notify_all();
+  }
+
+  void process(Worker& w, std::vector<Job>& batch) {
+    const double t_start = now();
+    bool hit = false;
+    bg_status status = BG_OK;
+    bg_solve_stats stats{};
+    bg_operator* op = acquire(w, key_of(batch[0].req), &hit, &status);
+    if (!op) {
+      finish(w, batch, status, 0, t_start, hit, 0, stats);
+      return;
+    }
+    const int N = op->N;
+    const size_t usz = op->cplx ? 16 : 8;
+    int tot = 0;
+    for (const Job& j : batch) tot += j.req.nrhs;
+    cudaError_t e = w.b_dev.alloc((size_t)N * tot * usz);
+    if (e == cudaSuccess) e = w.x_dev.alloc((size_t)N * tot * usz);
+    if (e != cudaSuccess) {
+      finish(w, batch, BG_OOM, N, t_start, hit, tot, stats);
+      return;
+    }
+    for (const Job& j : batch)
+      if (j.req.x_capacity < (long)N * j.req.nrhs) status = BG_INVALID_ARG;
+    long off = 0;
+    for (size_t i = 0; i < batch.size() && status == BG_OK; ++i) {
+      status = bg_load_vector(op, batch[i].req.data_kind, batch[i].data.data(), batch[i].req.nrhs,
+                              static_cast<char*>(w.b_dev.p) + off * N * usz, 1);
+      off += batch[i].req.nrhs;
+    }
+    const double ts = now();
+    if (status == BG_OK) {
+      bg_solve_params sp;
+      bg_solve_params_default(&sp);
+      sp.tol = batch[0].req.tol;
+      sp.inner_precision = batch[0].req.inner_precision;
+      status = bg_solve(op, w.b_dev.p, w.x_dev.p, tot, &sp, &stats, 1);
+    }
+    off = 0;
+    for (size_t i = 0; i < batch.size() && (status == BG_OK || status == BG_NOT_CONVERGED); ++i) {
+      e = cudaMemcpyAsync(batch[i].req.x, static_cast<char*>(w.x_dev.p) + off * N * usz,
+                          (size_t)N * batch[i].req.nrhs * usz, cudaMemcpyDeviceToHost, w.ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(w.ctx->stream);
+      if (e != cudaSuccess) status = BG_DEVICE_ERROR;
+      off += batch[i].req.nrhs;
+    }
+    // raise the admitted footprint to what the operator holds after a solve
+    size_t alloc = 0, est = 0;
+    const bool measured = bg_operator_memory(op, &alloc, &est) == BG_OK;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      st.solve_s += now() - ts;
+      if (measured && alloc > w.cache.front().bytes) {
+        w.in_use += alloc - w.cache.front().bytes;
+        w.cache.front().bytes = alloc;
+      }
+    }
+    finish(w, batch, status, N, t_start, hit, tot, stats);
+  }
+
+  void run(Worker& w) {
+    cudaSetDevice(w.ctx->device);
+    for (;;) {
+      std::vector<Job> batch;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        auto mine = [&] {
+          for (auto it = queue.begin(); it != queue.end(); ++it)
+            if (shard(key_of(it->req)) == w.id) return it;
+          return queue.end();
+        };
+        cv_work.wait(lk, [&] { return stop || mine() != queue.end(); });
+        auto first = mine();
+        if (first == queue.end()) break;  // stopping and nothing left for this worker
+        batch.push_back(std::move(*first));
+        queue.erase(first);
+        int tot = batch[0].req.nrhs;
+        for (auto it = queue.begin(); it != queue.end();) {
+          if (batchable(it->req, batch[0].req) && tot + it->req.nrhs <= 32) {
+            tot += it->req.nrhs;
+            batch.push_back(std::move(*it));
+            it = queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      }
+      process(w, batch);
+    }
+    while (!w.cache.empty()) evict_back(w);
+  }
+};
+
+extern "C" {
+
+bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers, bg_server** out) {
+  if (!ctx || !out || hbm_budget_bytes == 0 || workers < 1 || workers > 16) return BG_INVALID_ARG;
+  if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context: the server needs a GPU");
+  bg_server* s = new bg_server();
+  s->ctx = ctx;
+  s->budget = hbm_budget_bytes;
+  s->st.bytes_budget = hbm_budget_bytes;
+  s->t0 = std::chrono::steady_clock::now();
+  for (int i = 0; i < workers; ++i) {
+    Worker* w = new Worker();
+    w->id = i;
+    w->budget = hbm_budget_bytes / workers;
+    bg_status st = bg_context_create(ctx->device, &w->ctx);
+    if (st != BG_OK) {
+      delete w;
+      bg_server_destroy(s);
+      return set_error(ctx, st, "server worker context");
+    }
+    s->workers.push_back(w);
+  }
+  for (Worker* w : s->workers) w->th = std::thread([s, w] { s->run(*w); });
+  *out = s;
+  return BG_OK;
+}
+
+bg_status bg_server_destroy(bg_server* srv) {
+  if (!srv) return BG_INVALID_ARG;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stop = true;
+  }
+  srv->cv_work.notify_all();
+  for (Worker* w : srv->workers) {
+    if (w->th.joinable()) w->th.join();
+    w->b_dev.release();
+    w->x_dev.release();
+    if (w->ctx) bg_context_destroy(w->ctx);
+    delete w;
+  }
+  delete srv;
+  return BG_OK;
+}
+
+bg_status bg_server_add_geometry(bg_server* srv, const bg_geometry* g, int* index) {
+  if (!srv || !g || !index) return BG_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  srv->geos.push_back(g);
+  *index = (int)srv->geos.size() - 1;
+  return BG_OK;
+}
+
+bg_status bg_server_submit(bg_server* srv, const bg_request* req, long* ticket) {
+  if (!srv || !req || !ticket || !req->data || !req->x || req->nrhs < 1 || req->nrhs > 32 || !(req->tol > 0.0))
+    return BG_INVALID_ARG;
+  const int npr = req->data_kind == 3 ? 6 : 3;
+  Job j;
+  j.req = *req;
+  j.data.assign(req->data, req->data + (size_t)npr * req->nrhs);
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->stop) return BG_CANCELLED;
+    if (req->geometry < 0 || req->geometry >= (int)srv->geos.size()) return BG_INVALID_ARG;
+    j.ticket = srv->next_ticket++;
+    j.t_submit = srv->now();
+    *ticket = j.ticket;
+    ++srv->st.submitted;
+    srv->queue.push_back(std::move(j));
+  }
+  srv->cv_work.notify_all();  // the worker of this request's shard may be any of them
+  return BG_OK;
+}
+
+bg_status bg_server_wait(bg_server* srv, long ticket, double timeout_s, bg_request_result* out) {
+  if (!srv || !out) return BG_INVALID_ARG;
+  std::unique_lock<std::mutex> lk(srv->mu);
+  auto ready = [&] { return srv->done.count(ticket) != 0; };
+  if (timeout_s < 0) {
+    srv->cv_done.wait(lk, ready);
+  } else if (!srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready)) {
+    return BG_TIMEOUT;
+  }
+  *out = srv->done[ticket];
+  srv->done.erase(ticket);
+  return BG_OK;
+}
+
+bg_status bg_server_stats_get(bg_server* srv, bg_server_stats* out) {
+  if (!srv || !out) return BG_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  *out = srv->st;
+  return BG_OK;
+}
+
+}  // extern "C"

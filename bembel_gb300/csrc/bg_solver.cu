@@ -203,10 +203,19 @@ struct SolverWS {
   DevBuf bw, xw, bu, xu;
 };
 void free_solver_ws(void* p) { delete static_cast<SolverWS*>(p); }
+size_t krylov_bytes(const Krylov& k) {
+  return k.V.bytes + k.Z.bytes + k.w.bytes + k.hdev.bytes + k.inv.bytes + k.ydev.bytes + k.part.bytes + k.r.bytes;
+}
+size_t solver_ws_bytes(const void* p) {
+  const SolverWS* w = static_cast<const SolverWS*>(p);
+  return krylov_bytes(w->plain) + krylov_bytes(w->outer) + krylov_bytes(w->inner) + w->bw.bytes + w->xw.bytes +
+         w->bu.bytes + w->xu.bytes;
+}
 SolverWS* get_ws(bg_operator* op) {
   if (!op->solver_ws) {
     op->solver_ws = new SolverWS();
     op->solver_ws_free = free_solver_ws;
+    op->solver_ws_bytes = solver_ws_bytes;
   }
   return static_cast<SolverWS*>(op->solver_ws);
 }

@@ -596,6 +596,94 @@ def run_helmholtz(args):
     print(json.dumps(line), flush=True)
 
 
+def serving_stream(n, max_level, seed=7):
+    """Seeded request stream: Poisson arrivals (mean 200/s), sphere or torus,
+    refinement 2^M with M uniform in {2..max_level}, P in {1, 2}, Laplace or
+    Helmholtz with kappa ~ U[0.5, 8] snapped to 8 bucket centres, 1-32
+    right-hand sides (point sources outside the surface, or plane waves)."""
+    rng = np.random.default_rng(seed)
+    centres = 0.5 + 7.5 * (np.arange(8) + 0.5) / 8
+    t, out = 0.0, []
+    for _ in range(n):
+        t += rng.exponential(1.0 / 200.0)
+        geo = int(rng.integers(2))
+        m = int(rng.integers(2, max_level + 1))
+        p = int(rng.integers(1, 3))
+        helm = bool(rng.integers(2))
+        k = float(centres[np.argmin(np.abs(centres - rng.uniform(0.5, 8.0)))]) if helm else 0.0
+        nrhs = int(rng.integers(1, 33))
+        d = rng.normal(size=(nrhs, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        if helm:
+            data, dk = d, 2
+        else:
+            r = rng.uniform(1.5, 3.0, (nrhs, 1)) if geo == 0 else rng.uniform(3.0, 4.5, (nrhs, 1))
+            data, dk = d * r, 0
+        out.append({"t": t, "geo": geo, "M": m, "P": p, "kind": "helmholtz" if helm else "laplace", "kappa": k,
+                    "data_kind": dk, "data": data})
+    return out
+
+
+def run_serving(args):
+    """Side workload (not the headline line): the serving loop (bg_server) on a
+    seeded Poisson stream of Laplace / Helmholtz solve requests. Pass 1 starts
+    with an empty operator cache, pass 2 replays the stream with the cache as
+    pass 1 left it (mixed inner operator), pass 3 replays the first requests on
+    the plain FP64 path. Latency = completion - submission; throughput = solved
+    right-hand sides per second of the pass."""
+    import torch
+    import bembel_gb300 as bg
+    ctx = bg.Context(0)
+    free, total = torch.cuda.mem_get_info()
+    budget = int(min(200e9, 0.8 * free))
+    srv = bg.Server(ctx, budget, workers=args.workers)
+    geos = [srv.add_geometry(bg.Geometry(GEO, ctx)),
+            srv.add_geometry(bg.Geometry(os.path.join(ROOT, "tests", "golden", "geo", "torus.dat"), ctx))]
+    stream = serving_stream(args.requests, args.max_level)
+
+    def one_pass(reqs, inner):
+        t0 = time.time()
+        tickets = []
+        for r in reqs:
+            dt = r["t"] - (time.time() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(srv.submit(geos[r["geo"]], r["kind"], r["M"], r["P"], r["data_kind"], r["data"],
+                                      kappa=r["kappa"], tol=TOL, inner=inner))
+        res = [srv.wait(t)[1] for t in tickets]
+        lat = np.array([x["t_done"] - x["t_submit"] for x in res])
+        span = max(x["t_done"] for x in res) - min(x["t_submit"] for x in res)
+        nr = sum(r["data"].shape[0] for r in reqs)
+        ok = sum(1 for x in res if x["status"] in (0, 7))
+        return {"requests": len(reqs), "ok": ok, "rhs": nr, "span_s": span, "solves_per_s": nr / span,
+                "requests_per_s": len(reqs) / span, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                "p99_ms": 1e3 * float(np.percentile(lat, 99)), "cache_hits": sum(x["cache_hit"] for x in res),
+                "max_final_relres": max(x["stats"]["final_relres"] for x in res)}
+
+    clocks = ClockSampler(0)
+    with clocks:
+        cold = one_pass(stream, "fp32")
+        s1 = srv.stats()
+        warm = one_pass(stream, "fp32")
+        k = min(len(stream), args.fp64_requests)
+        warm_k = one_pass(stream[:k], "fp32")
+        fp64 = one_pass(stream[:k], "fp64")
+    st = srv.stats()
+    srv.close()
+    keys = {(r["geo"], r["kind"], r["M"], r["P"], r["kappa"]) for r in stream}
+    line = {"workload": "serving_poisson200_laplace_helmholtz_sphere_torus",
+            "metric": "served solves/s and p50/p99 latency (rel.err 1e-8)", "unit": "solves/s",
+            "value": warm["solves_per_s"], "offered_requests_per_s": 200.0,
+            "config": {"requests": len(stream), "distinct_operators": len(keys), "levels": [2, args.max_level],
+                       "workers": args.workers,
+                       "degrees": [1, 2], "kappa_buckets": 8, "nrhs": [1, 32], "hbm_budget_bytes": budget,
+                       "note": "requests for one operator that wait together are solved as one batch"},
+            "cold_cache": cold, "warm_cache": warm,
+            "mixed_vs_fp64_same_requests": {"mixed": warm_k, "fp64": fp64},
+            "server": {"after_cold": s1, "final": st}, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_void_p():
     import ctypes
     return ctypes.c_void_p()
@@ -660,15 +748,21 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
                     help="product precision of --profile matvec")
     ap.add_argument("--profile-m", type=int, default=None, help="refinement level of --profile cases (default 5)")
-    ap.add_argument("--workload", default="laplace", choices=["laplace", "maxwell", "helmholtz"],
+    ap.add_argument("--workload", default="laplace", choices=["laplace", "maxwell", "helmholtz", "serving"],
                     help="laplace: the headline line; maxwell / helmholtz: side workloads")
     ap.add_argument("--kappas", type=int, default=4, help="wavenumbers of the helmholtz sweep (of 16)")
     ap.add_argument("--no-fp64", action="store_true", help="helmholtz: skip the plain FP64 solve")
+    ap.add_argument("--requests", type=int, default=100, help="serving: requests in the stream")
+    ap.add_argument("--max-level", type=int, default=4, help="serving: largest refinement level (2..6)")
+    ap.add_argument("--fp64-requests", type=int, default=30, help="serving: requests replayed on the FP64 path")
+    ap.add_argument("--workers", type=int, default=4, help="serving: worker streams of the server")
     args = ap.parse_args()
     if args.workload == "maxwell" and args.impl == "gb300" and not args.profile:
         run_maxwell(args)
     elif args.workload == "helmholtz" and args.impl == "gb300" and not args.profile:
         run_helmholtz(args)
+    elif args.workload == "serving" and args.impl == "gb300" and not args.profile:
+        run_serving(args)
     elif args.profile:
         run_profile_case(args)
     elif args.impl == "reference":

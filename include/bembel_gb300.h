@@ -199,6 +199,68 @@ bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_s
  * at npts points (3 doubles each) for nrhs densities rho (N x nrhs). */
 bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out);
 
+/* Device memory of an operator: *allocated = bytes it holds now (tables,
+ * assembled fields, work vectors, solver workspaces); *estimate = bytes it
+ * will hold once assembled and used for solves of up to 32 right-hand sides
+ * (computable before bg_operator_assemble; the serving loop admits by it). */
+bg_status bg_operator_memory(const bg_operator* op, size_t* allocated, size_t* estimate);
+
+/* ---- serving loop ----
+ * No counterpart in the reference (its examples assemble one operator and
+ * solve once). A server owns worker threads on the context's GPU, a queue of
+ * solve requests and a cache of assembled operators keyed by (geometry, kind,
+ * M, P, wavenumber). Requests for the same operator that are waiting together
+ * are solved as one multi-column batch (up to 32 right-hand sides). Admission
+ * is by device memory: an operator that is not cached is created only after
+ * least-recently-used operators have been evicted until its estimated
+ * footprint fits the server's budget; a request whose operator alone exceeds
+ * the budget fails with BG_OOM. Load vectors are assembled on the device from
+ * analytic data (bg_load_vector kinds), solutions are copied to host memory
+ * the caller keeps valid until the request is done. The context must not be
+ * used by other threads while a server runs on it. */
+typedef struct bg_server bg_server;
+typedef struct {
+  int geometry;          /* index returned by bg_server_add_geometry */
+  int op_kind;           /* bg_op_kind */
+  int M, P;
+  double kre, kim;       /* wavenumber (Helmholtz, Maxwell) */
+  int data_kind;         /* bg_load_vector kind */
+  int nrhs;              /* 1 .. 32 */
+  const double* data;    /* nrhs x 3 (kind 3: x 6) data parameters, copied at submit */
+  double tol;            /* relative residual per column */
+  int inner_precision;   /* bg_precision of the inner operator (BG_PREC_FP64: plain FP64 GMRES) */
+  void* x;               /* host, N x nrhs column-major (complex interleaved) */
+  long x_capacity;       /* scalars available at x */
+} bg_request;
+typedef struct {
+  int status;            /* bg_status of the solve */
+  int N;                 /* unknowns of the operator */
+  double t_submit, t_start, t_done;  /* seconds since the server started */
+  int cache_hit;         /* operator was cached when the request's batch started */
+  int batch_nrhs;        /* right-hand sides solved together with this request */
+  bg_solve_stats stats;
+  char error[160];       /* message of a failed request (empty on success) */
+} bg_request_result;
+typedef struct {
+  long submitted, completed, failed, batches;
+  long cache_hits, cache_misses, evictions;
+  size_t bytes_in_use, bytes_budget;
+  double assembly_s, solve_s;  /* worker time spent assembling / solving */
+  int cached_operators;
+} bg_server_stats;
+
+/* workers: 1 .. 16 worker threads, each with its own context (stream) on
+ * ctx's device and budget / workers bytes; operators are sharded over them by
+ * key, so solves on different operators overlap on the GPU */
+bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers, bg_server** out);
+/* stops the worker after the queue drains and frees every cached operator */
+bg_status bg_server_destroy(bg_server* srv);
+bg_status bg_server_add_geometry(bg_server* srv, const bg_geometry* g, int* index);
+bg_status bg_server_submit(bg_server* srv, const bg_request* req, long* ticket);
+/* blocks until the request is done (timeout_s < 0: no limit; BG_TIMEOUT when it runs out) */
+bg_status bg_server_wait(bg_server* srv, long ticket, double timeout_s, bg_request_result* out);
+bg_status bg_server_stats_get(bg_server* srv, bg_server_stats* out);
+
 /* ---- inspection entry points used by the parity tests ---- */
 /* per element id: patch, vertex ids[4]; and llc[2], ball midpoint[3], radius */
 bg_status bg_operator_elements(const bg_operator* op, int* ints5, double* dbl6);

@@ -81,3 +81,31 @@ def test_invalid_arguments(bg_host):
         bg.DiscreteOperator(bg.AnsatzSpace(g, 1, 7), bg.LaplaceSingleLayerOperator())
     with pytest.raises(bg.BembelError):
         bg.DiscreteOperator(bg.AnsatzSpace(g, 1, 1), bg.LaplaceSingleLayerOperator(), n_p=1)
+
+
+def test_memory_estimate_before_assembly(bg_host):
+    """The serving loop admits operators by this estimate; it is available
+    before assembly and covers the stored fields."""
+    import ctypes
+    from bembel_gb300 import _lib
+    bg, ctx = bg_host
+    g = bg.Geometry(SPHERE, ctx)
+    prev = 0
+    for M in (1, 2, 3):
+        d = bg.DiscreteOperator(bg.AnsatzSpace(g, M, 2), bg.LaplaceSingleLayerOperator())
+        a, e = ctypes.c_size_t(), ctypes.c_size_t()
+        ctx.check(_lib.load().bg_operator_memory(d.h, ctypes.byref(a), ctypes.byref(e)))
+        info = d.info()
+        assert a.value == 0  # nothing on a device
+        assert e.value >= int(info[13]) + int(info[14]) and e.value > prev
+        prev = e.value
+
+
+def test_host_only_context_refuses_server(bg_host):
+    import ctypes
+    from bembel_gb300 import _lib
+    bg, ctx = bg_host
+    h = ctypes.c_void_p()
+    assert _lib.load().bg_server_create(ctx.h, 1 << 30, 1, ctypes.byref(h)) == _lib.BG_UNSUPPORTED
+    assert _lib.load().bg_server_create(ctx.h, 0, 1, ctypes.byref(h)) == _lib.BG_INVALID_ARG
+    assert _lib.load().bg_server_create(ctx.h, 1 << 30, 0, ctypes.byref(h)) == _lib.BG_INVALID_ARG
