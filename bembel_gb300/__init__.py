@@ -300,12 +300,18 @@ class DiscreteOperator:
         return out
 
     def potential(self, rho, points):
+        """DiscretePotential::evaluate at points (npts, 3) for densities rho
+        (N, nrhs): (npts, nrhs); Maxwell: the field, (npts, 3, nrhs)."""
         rho = np.asfortranarray(np.asarray(rho, dtype=np.complex128 if self.is_complex else np.float64).reshape(self.N, -1))
         pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
-        out = np.zeros((pts.shape[0], rho.shape[1]), dtype=rho.dtype, order="F")
-        self.ctx.check(_lib.load().bg_potential(self.h, rho.ctypes.data_as(ctypes.c_void_p), rho.shape[1], _dp(pts),
+        k = rho.shape[1]
+        if self.lin_op.kind == _lib.MAXWELL_SL:
+            out = np.zeros((k, pts.shape[0], 3), dtype=np.complex128)
+        else:
+            out = np.zeros((pts.shape[0], k), dtype=rho.dtype, order="F")
+        self.ctx.check(_lib.load().bg_potential(self.h, rho.ctypes.data_as(ctypes.c_void_p), k, _dp(pts),
                                                 pts.shape[0], out.ctypes.data_as(ctypes.c_void_p)))
-        return out
+        return out.transpose(1, 2, 0) if self.lin_op.kind == _lib.MAXWELL_SL else out
 
     # -- inspection --
     def elements(self):

@@ -726,6 +726,29 @@ static bg_status assemble_far(bg_operator* op) {
   return BG_OK;
 }
 
+// phi, d/ds phi, d/dt phi of the degree-P tensor Bernstein basis at the
+// points of the n1 x n1 tensor rule gr, as [3][n1^2][(P+1)^2]
+std::vector<double> basis3_table(int P, const Rule1D& gr) {
+  const int n1 = (int)gr.x.size(), Q = n1 * n1, p2 = (P + 1) * (P + 1);
+  std::vector<double> basis3((size_t)3 * Q * p2);
+  for (int q = 0; q < Q; ++q) {
+    double bs[8], bt[8], ds[8], dt[8];
+    const double u = gr.x[q / n1], v = gr.x[q % n1];
+    bernstein(P, u, bs);
+    bernstein(P, v, bt);
+    bernstein_der(P, u, ds);
+    bernstein_der(P, v, dt);
+    for (int iy = 0; iy <= P; ++iy)
+      for (int ix = 0; ix <= P; ++ix) {
+        const size_t o = (size_t)q * p2 + iy * (P + 1) + ix;
+        basis3[o] = bs[ix] * bt[iy];
+        basis3[(size_t)Q * p2 + o] = ds[ix] * bt[iy];
+        basis3[(size_t)2 * Q * p2 + o] = bs[ix] * dt[iy];
+      }
+  }
+  return basis3;
+}
+
 // Dense leaves of the Maxwell operator: every element pair fills its four
 // component blocks at once (H2Matrix.hpp:195-205 scatters them per component).
 static bg_status assemble_near_mw(bg_operator* op) {
@@ -786,23 +809,7 @@ static bg_status assemble_near_mw(bg_operator* op) {
   for (auto& kv : regular) {
     const int deg = kv.first, n1 = deg + 1, Q = n1 * n1;
     const Rule1D& gr = gauss_rule(n1);
-    // phi, d/ds phi, d/dt phi at the Q points ([3][Q][p2])
-    std::vector<double> basis3((size_t)3 * Q * p2);
-    for (int q = 0; q < Q; ++q) {
-      double bs[8], bt[8], ds[8], dt[8];
-      const double u = gr.x[q / n1], v = gr.x[q % n1];
-      bernstein(P, u, bs);
-      bernstein(P, v, bt);
-      bernstein_der(P, u, ds);
-      bernstein_der(P, v, dt);
-      for (int iy = 0; iy <= P; ++iy)
-        for (int ix = 0; ix <= P; ++ix) {
-          const size_t o = (size_t)q * p2 + iy * (P + 1) + ix;
-          basis3[o] = bs[ix] * bt[iy];
-          basis3[(size_t)Q * p2 + o] = ds[ix] * bt[iy];
-          basis3[(size_t)2 * Q * p2 + o] = bs[ix] * dt[iy];
-        }
-    }
+    const std::vector<double> basis3 = basis3_table(P, gr);
     DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dtab = new DevBuf(), *dbas = new DevBuf(), *dpairs = new DevBuf();
     keep.insert(keep.end(), {dgx, dgw, dtab, dbas, dpairs});
     cudaError_t e = dgx->upload(gr.x, s);

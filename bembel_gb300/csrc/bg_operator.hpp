@@ -205,6 +205,7 @@ struct bg_operator {
 };
 
 bg_status set_error(bg_context* ctx, bg_status st, const std::string& msg);
+std::vector<double> basis3_table(int P, const bg::Rule1D& gr);
 // child bookkeeping: a context is released only after its last child
 void context_retain(bg_context* ctx);
 void context_release(bg_context* ctx);

@@ -7,6 +7,7 @@
 // bg_potential: DiscretePotential::evaluate (Potential/DiscretePotential.hpp:49-107)
 // for the Laplace / Helmholtz single layer potential.
 #include <algorithm>
+#include <complex>
 #include <vector>
 
 #include "bg_operator.hpp"
@@ -237,6 +238,87 @@ __global__ void k_potential(const d4* __restrict__ tab, int ne, int Q, const dou
   }
 }
 
+// Maxwell field (Maxwell/SingleLayerPotential.hpp:44-95 with the div-conforming
+// evaluator of AnsatzSpace/FunctionEvaluatorEval.hpp:39-83): CTA per evaluation
+// point x; threads over (element, Gauss point y) sum, with weight h^2 w,
+//   k(x, y) u(y) + grad_x k(x, y) div u(y) / kappa^2,
+// u = (c0 dx + c1 dy) / h, div u = (sum c0 d/ds phi + sum c1 d/dt phi) / h^2,
+// c0, c1 the superspace coefficients of the two components at the element.
+// tab holds x, dx, dy and h w per Gauss point; basis3 = [phi | d/ds phi | d/dt phi].
+// Output: 3 complex values per point and right-hand side, [rhs][point][xyz].
+template <int P>
+__global__ void __launch_bounds__(256) k_potential_mw(const MwPt* __restrict__ tab, int ne, int Q, double h,
+                                                      const double* __restrict__ basis3, const cd* __restrict__ coef,
+                                                      int k, const double* __restrict__ pts, double kre, double kim,
+                                                      cd inv_k2, cd* __restrict__ out) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  __shared__ double red[6][256];
+  const int p = blockIdx.x;
+  const double px = pts[3 * p], py = pts[3 * p + 1], pz = pts[3 * p + 2];
+  for (int c = 0; c < k; ++c) {
+    cd acc[3] = {zero<cd>(), zero<cd>(), zero<cd>()};
+    for (long t = threadIdx.x; t < (long)ne * Q; t += blockDim.x) {
+      const int e = (int)(t / Q), q = (int)(t % Q);
+      const MwPt y = tab[t];
+      cd t0 = zero<cd>(), t1 = zero<cd>(), dv = zero<cd>();
+#pragma unroll
+      for (int a = 0; a < P2; ++a) {
+        const cd a0 = coef[((long)e * P2 + a) * k + c], a1 = coef[((long)(ne + e) * P2 + a) * k + c];
+        t0 = fmac(t0, a0, basis3[q * P2 + a]);
+        t1 = fmac(t1, a1, basis3[q * P2 + a]);
+        dv = fmac(dv, a0, basis3[(Q + q) * P2 + a]);
+        dv = fmac(dv, a1, basis3[(2 * Q + q) * P2 + a]);
+      }
+      const double w = y.w * h;  // h^2 w
+      const double ih = 1.0 / h;
+      const double d0 = px - y.x[0], d1 = py - y.x[1], d2 = pz - y.x[2];
+      const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
+      const double ir = rsqrt_nr(r2), r = r2 * ir;
+      double sn, cs;
+      sincos(kre * r, &sn, &cs);
+      const double amp = (kim != 0.0 ? exp(kim * r) : 1.0) * kInv4Pi * ir;
+      const cd kv{cs * amp, -sn * amp};                      // exp(-i kappa r) / (4 pi r)
+      // grad_x: exp(-i kappa r) (-1 - i kappa r) / (4 pi r^3) (x - y), kappa = kre + i kim
+      const cd gk = kv * cd{-1.0 + kim * r, -kre * r} * (ir * ir);
+      const cd dq = dv * inv_k2 * (ih * ih);
+      const double dd[3] = {d0, d1, d2};
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const cd u = (t0 * y.dx[m] + t1 * y.dy[m]) * ih;
+        acc[m] = acc[m] + (kv * u + gk * dq * dd[m]) * w;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      red[2 * m][threadIdx.x] = acc[m].re;
+      red[2 * m + 1][threadIdx.x] = acc[m].im;
+    }
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s)
+#pragma unroll
+        for (int v = 0; v < 6; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) out[((long)c * gridDim.x + p) * 3 + m] = cd{red[2 * m][0], red[2 * m + 1][0]};
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_potential_mw(int P, const MwPt* tab, int ne, int Q, double h, const double* basis3,
+                                const cd* coef, int k, const double* pts, int npts, double kre, double kim, cd inv_k2,
+                                cd* out, cudaStream_t s) {
+  switch (P) {
+    case 1: k_potential_mw<1><<<npts, 256, 0, s>>>(tab, ne, Q, h, basis3, coef, k, pts, kre, kim, inv_k2, out); break;
+    case 2: k_potential_mw<2><<<npts, 256, 0, s>>>(tab, ne, Q, h, basis3, coef, k, pts, kre, kim, inv_k2, out); break;
+    case 3: k_potential_mw<3><<<npts, 256, 0, s>>>(tab, ne, Q, h, basis3, coef, k, pts, kre, kim, inv_k2, out); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 template <int G, int P>
 cudaError_t run_load(bool cplx, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
                      const double* gw, int n1, int kind, const double* prm, int k, double kre, double kim, double* out,
@@ -337,11 +419,57 @@ extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm
   return BG_OK;
 }
 
+// Maxwell: the field (3 complex values per point)
+static bg_status potential_mw(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out) {
+  cudaStream_t s = op->ctx->stream;
+  const int n1 = op->P + 2, Q = n1 * n1;
+  const Rule1D& gr = gauss_rule(n1);
+  const std::vector<double> basis3 = basis3_table(op->P, gr);
+  PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
+  const double h = 1.0 / double(1 << op->M);
+  ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), h};
+  const std::complex<double> kap(op->kre, op->kim), ik2 = 1.0 / (kap * kap);
+  DevBuf gx, gw, tab, dbas, dpts, drho, dout;
+  std::vector<double> P3(pts, pts + 3 * npts);
+  cudaError_t e = gx.upload(gr.x, s);
+  if (e == cudaSuccess) e = gw.upload(gr.w, s);
+  if (e == cudaSuccess) e = dbas.upload(basis3, s);
+  if (e == cudaSuccess) e = dpts.upload(P3, s);
+  if (e == cudaSuccess) e = tab.alloc((size_t)op->ne * Q * sizeof(MwPt));
+  if (e == cudaSuccess)
+    e = launch_quad_table_mw(op->G, pt, et, op->ne, gx.as<double>(), gw.as<double>(), n1, tab.as<MwPt>(), s);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "potential setup");
+  for (int c0 = 0; c0 < nrhs; c0 += 32) {
+    const int k = std::min(32, nrhs - c0);
+    bg_status st = ensure_work(op, k);
+    if (st != BG_OK) return st;
+    e = drho.alloc((size_t)op->N * k * 16);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(drho.p, static_cast<const char*>(rho) + (size_t)c0 * op->N * 16, (size_t)op->N * k * 16,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = launch_gather_in(1, 1, drho.p, op->N, op->N, k, op->w_xdof.p, s);
+    if (e == cudaSuccess)
+      e = launch_csr_apply(1, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S,
+                           op->w_xdof.p, op->w_xss.p, k, s);
+    if (e == cudaSuccess) e = dout.alloc((size_t)npts * 3 * k * 16);
+    if (e == cudaSuccess)
+      e = launch_potential_mw(op->P, tab.as<MwPt>(), op->ne, Q, h, dbas.as<double>(), op->w_xss.as<cd>(), k,
+                              dpts.as<double>(), npts, op->kre, op->kim, cd{ik2.real(), ik2.imag()},
+                              dout.as<cd>(), s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<char*>(out) + (size_t)c0 * npts * 3 * 16, dout.p, (size_t)npts * 3 * k * 16,
+                          cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(op->ctx, e, "potential");
+  }
+  return BG_OK;
+}
+
 extern "C" bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out) {
   if (!op || !rho || !pts || !out || nrhs <= 0 || npts <= 0) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: potentials need a GPU");
-  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "potentials of vector operators");
   cudaSetDevice(op->ctx->device);
+  if (op->maxwell()) return potential_mw(op, rho, nrhs, pts, npts, out);
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;
   const int n1 = op->P + 2, Q = n1 * n1, p2 = op->p2;

@@ -196,7 +196,10 @@ bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_s
                    bg_solve_stats* stats, int on_device);
 
 /* DiscretePotential<...SingleLayerPotential>::evaluate (Potential/DiscretePotential.hpp:49-107)
- * at npts points (3 doubles each) for nrhs densities rho (N x nrhs). */
+ * at npts points (3 doubles each) for nrhs densities rho (N x nrhs), host
+ * pointers. Laplace / Helmholtz: out is npts x nrhs (column-major). Maxwell
+ * (Maxwell/SingleLayerPotential.hpp:44-95): the field, 3 complex values per
+ * point, out[(c * npts + p) * 3 + xyz]. */
 bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out);
 
 /* Device memory of an operator: *allocated = bytes it holds now (tables,

@@ -268,11 +268,12 @@ class Problem:
         return out
 
     def potential(self, rho, pts):
+        """Single-layer potential at pts (npts, 3); Maxwell: the field, (npts, 3)."""
         rho = np.ascontiguousarray(rho, dtype=self.dtype)
         pts = np.ascontiguousarray(pts, dtype=np.float64)
-        out = np.zeros(pts.shape[0], dtype=self.dtype)
+        out = np.zeros(pts.shape[0] * (3 if self.kind == MAXWELL else 1), dtype=self.dtype)
         lib().orc_potential(self.h, _dp(rho.view(np.float64)), _dp(pts), pts.shape[0], _dp(out.view(np.float64)))
-        return out
+        return out.reshape(-1, 3) if self.kind == MAXWELL else out
 
     def gmres(self, b, tol=1e-10, restart=100, maxit=1000):
         b = np.ascontiguousarray(b, dtype=self.dtype)

@@ -285,6 +285,62 @@ void potential(Problem& p, const S* rho, const double* pts, int npts, S* out) {
   }
 }
 
+// DiscretePotential::evaluate with MaxwellSingleLayerPotential::evaluateIntegrand_impl
+// (Maxwell/SingleLayerPotential.hpp:44-95) and the div-conforming function
+// evaluator (AnsatzSpace/FunctionEvaluatorEval.hpp:39-83): per Gauss point
+// (GS[P+1], weight h^2 w), E(x) += w [k(x, y) u(y) + grad_x k(x, y) div u(y) / kappa^2]
+// with u = (c0 dx + c1 dy) / h, div u = (sum c0 phi_dx + sum c1 phi_dy) / h^2.
+void potential_mw(Problem& p, const cplx* rho, const double* pts, int npts, cplx* out) {
+  const int n = p.ss.p2(), ne = p.ss.ne();
+  std::vector<cplx> coef((size_t)p.S());
+  p.T.apply(rho, coef.data());
+  const cplx* c0 = coef.data();
+  const cplx* c1 = coef.data() + (size_t)n * ne;
+  const Cubature& Q = GS(p.ss.P + 1);
+  const cplx i1(0, 1), kap = p.op.kappa, kap2 = p.op.kappa2;
+  for (int i = 0; i < 3 * npts; ++i) out[i] = 0;
+#pragma omp parallel
+  {
+    std::vector<cplx> mine(3 * (size_t)npts, cplx(0));
+#pragma omp for schedule(static)
+    for (int e = 0; e < ne; ++e) {
+      const Node& el = p.ss.element(e);
+      SurfacePoint qp;
+      double b[64], bdx[64], bdy[64];
+      const double h = el.h();
+      for (int q = 0; q < Q.size(); ++q) {
+        p.ss.map2surface(el, Q.x0[q], Q.x1[q], h * h * Q.w[q], &qp);
+        p.ss.phiphi(qp.v[0], qp.v[1], b);
+        p.ss.phiphi_dx(qp.v[0], qp.v[1], bdx);
+        p.ss.phiphi_dy(qp.v[0], qp.v[1], bdy);
+        cplx t0 = 0, t1 = 0, dv = 0;
+        for (int k = 0; k < n; ++k) {
+          const cplx a0 = c0[(size_t)n * el.id + k], a1 = c1[(size_t)n * el.id + k];
+          t0 += a0 * b[k];
+          t1 += a1 * b[k];
+          dv += a0 * bdx[k] + a1 * bdy[k];
+        }
+        dv = dv / h / h;
+        const V3 dx = qp.dx(), dy = qp.dy(), y = qp.x();
+        const cplx u[3] = {(dx.x * t0 + dy.x * t1) / h, (dx.y * t0 + dy.y * t1) / h, (dx.z * t0 + dy.z * t1) / h};
+        const double w = qp.v[2];
+        for (int i = 0; i < npts; ++i) {
+          const V3 x(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+          const V3 c = x - y;
+          const double r = c.norm();
+          const cplx ex = std::exp(-i1 * kap * r);
+          const cplx k = ex / 4. / kPi / r;
+          const cplx g = ex * (-1. - i1 * kap * r) / 4. / kPi / (r * r * r);
+          const double cc[3] = {c.x, c.y, c.z};
+          for (int d = 0; d < 3; ++d) mine[3 * (size_t)i + d] += (k * u[d] + 1. / kap2 * (g * cc[d]) * dv) * w;
+        }
+      }
+    }
+#pragma omp critical
+    for (int i = 0; i < 3 * npts; ++i) out[i] += mine[i];
+  }
+}
+
 // DOF-level product y = A x for nrhs columns (column-major, leading dim N)
 template <typename S>
 void h2_matvec(Problem& p, const S* x, S* y, int nrhs) {
@@ -679,7 +735,9 @@ void orc_load_vector(void* h, int kind, const double* prm, double* out) {
 }
 void orc_potential(void* h, const double* rho, const double* pts, int npts, double* out) {
   Problem& p = *static_cast<Problem*>(h);
-  if (p.op.is_complex())
+  if (p.op.kind == kMaxwell)
+    potential_mw(p, reinterpret_cast<const cplx*>(rho), pts, npts, reinterpret_cast<cplx*>(out));
+  else if (p.op.is_complex())
     potential<cplx>(p, reinterpret_cast<const cplx*>(rho), pts, npts, reinterpret_cast<cplx*>(out));
   else
     potential<double>(p, rho, pts, npts, out);

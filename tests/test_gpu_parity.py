@@ -166,3 +166,35 @@ def test_maxwell_solve(ctx, oracle, inner):
     for c in range(2):
         r = b[:, c] - o.matvec(x[:, c:c + 1])[:, 0]
         assert np.linalg.norm(r) / np.linalg.norm(b[:, c]) < 1e-7
+
+
+def test_maxwell_potential(ctx, oracle):
+    d, o = _pair(ctx, oracle, SPHERE, 2, 2, 2, 2.0, 6)
+    rng = np.random.default_rng(13)
+    rho = rng.uniform(-1, 1, (d.N, 2)) + 1j * rng.uniform(-1, 1, (d.N, 2))
+    pts = np.r_[rng.uniform(-0.3, 0.3, (4, 3)), 2.0 * np.eye(3)]
+    got = d.potential(rho, pts)
+    for c in range(2):
+        ref = o.potential(rho[:, c], pts)
+        assert np.linalg.norm(got[:, :, c] - ref) / np.linalg.norm(ref) < FP64_TOL
+
+
+def test_maxwell_field_converges_on_gpu(ctx):
+    """examples/MaxwellSingleLayerH2.cpp:30-96 on the GPU path: dipole inside
+    the sphere, field at radius 2, rate >= 0.9 (2P + 1) for P = 1."""
+    import bembel_gb300 as bg
+    from test_oracle_pins import _dipole_field, _sphere_points
+    k, pos, mom = 2.0, np.array([0.2, 0.2, 0.2]), np.array([0.0, 0.1, 0.1])
+    grid = _sphere_points(2.0, 100)
+    ref = _dipole_field(grid, k, pos, mom)
+    errs = []
+    for M in (1, 2, 3):
+        lin = bg.MaxwellSingleLayerOperator()
+        lin.set_wavenumber(k)
+        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, 1), lin)
+        d.compute()
+        x, st = d.get_discrete_operator().solve(d.load_vector(3, np.r_[pos, mom]), tol=1e-10)
+        assert st["converged"]
+        errs.append(np.max(np.linalg.norm(d.potential(x, grid)[:, :, 0] - ref, axis=1)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(rates >= 0.9 * 3), (errs, rates)

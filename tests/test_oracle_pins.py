@@ -190,3 +190,38 @@ def test_laplace_convergence(oracle):
         errs.append(np.max(np.abs(p.potential(rho, pts) - ref)))
     rate = math.log2(errs[-2] / errs[-1])
     assert rate >= 0.9 * 3
+
+
+def _dipole_field(pt, k, pos, mom):
+    """examples/Data.hpp:73-90 (Hertz dipole), numpy restatement for the check."""
+    c = pt - pos
+    r = np.linalg.norm(c, axis=1, keepdims=True)
+    n = c / r
+    ex = np.exp(-1j * k * r)
+    ncl = np.cross(np.cross(n, mom), n)
+    hh = n * (3 * (n @ mom))[:, None] - mom
+    return k * k * ex / r * ncl + (1 / r ** 3 + 1j * k / r ** 2) * ex * hh
+
+
+def _sphere_points(radius, m):
+    i = np.arange(m) + 0.5
+    phi = np.arccos(1 - 2 * i / m)
+    th = np.pi * (1 + 5 ** 0.5) * i
+    return radius * np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1)
+
+
+def test_maxwell_field_converges(oracle):
+    """examples/MaxwellSingleLayerH2.cpp:30-96: a dipole at (0.2, 0.2, 0.2) with
+    moment (0, 0.1, 0.1) inside the sphere, kappa = 2, excitation its tangential
+    trace; the single-layer field at 100 points of radius 2 must match the
+    dipole field with rate >= 0.9 (2P + 1) over the refinement levels."""
+    k, pos, mom = 2.0, np.array([0.2, 0.2, 0.2]), np.array([0.0, 0.1, 0.1])
+    grid = _sphere_points(2.0, 100)
+    ref = _dipole_field(grid, k, pos, mom)
+    errs = []
+    for M in (0, 1, 2):
+        p = oracle.Problem(SPHERE, M, 1, oracle.MAXWELL, kappa=k, np_=9)
+        x, _ = p.gmres(p.load_vector(3, np.r_[pos, mom]), tol=1e-10, restart=500, maxit=5000)
+        errs.append(np.max(np.linalg.norm(p.potential(x, grid) - ref, axis=1)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert np.all(rates >= 0.9 * 3), (errs, rates)
