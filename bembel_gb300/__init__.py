@@ -65,12 +65,14 @@ def default_context():
 
 
 class Geometry:
-    """Geometry(filename): patches of a .dat file (Geometry/Geometry.hpp:89-102)."""
+    """Geometry(filename): patches of a .dat or .igs/.iges file (Geometry/Geometry.hpp:89-102)."""
 
     def __init__(self, filename, context=None):
         self.ctx = context or default_context()
         h = ctypes.c_void_p()
-        self.ctx.check(_lib.load().bg_geometry_load_dat(self.ctx.h, str(filename).encode(), ctypes.byref(h)))
+        igs = str(filename).lower().endswith((".igs", ".iges"))
+        load = _lib.load().bg_geometry_load_igs if igs else _lib.load().bg_geometry_load_dat
+        self.ctx.check(load(self.ctx.h, str(filename).encode(), ctypes.byref(h)))
         self.h = h
         self.filename = str(filename)
 

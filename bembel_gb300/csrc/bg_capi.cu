@@ -153,6 +153,21 @@ bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** 
   *out = g;
   return BG_OK;
 }
+bg_status bg_geometry_load_igs(bg_context* ctx, const char* path, bg_geometry** out) {
+  if (!ctx || !path || !out || ctx->closing) return BG_INVALID_ARG;
+  *out = nullptr;
+  bg_geometry* g = new (std::nothrow) bg_geometry();
+  if (!g) return BG_OOM;
+  std::string err;
+  if (!load_igs(path, &g->g, &err)) {
+    delete g;
+    return set_error(ctx, BG_INVALID_ARG, err);
+  }
+  g->ctx = ctx;
+  context_retain(ctx);
+  *out = g;
+  return BG_OK;
+}
 bg_status bg_geometry_from_bezier(bg_context* ctx, int npatch, const int* px, const int* py, const double* data,
                                   bg_geometry** out) {
   if (!ctx || !out || npatch <= 0 || !px || !py || !data || ctx->closing) return BG_INVALID_ARG;

@@ -2,6 +2,7 @@
 #include "bg_host.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <fstream>
 #include <map>
 #include <mutex>
@@ -79,6 +80,91 @@ bool load_dat(const std::string& path, Geometry* g, std::string* err) {
     for (int ix = 0; ix < nx; ++ix)
       for (int iy = 0; iy < ny; ++iy)
         for (int c = 0; c < 4; ++c) P.cp[4 * (ix * ny + iy) + c] = mat[c][iy * nx + ix];
+    g->patches.push_back(std::move(P));
+  }
+  return true;
+}
+
+bool load_igs(const std::string& path, Geometry* g, std::string* err) {
+  std::ifstream f(path);
+  if (!f) {
+    *err = "cannot open geometry file " + path;
+    return false;
+  }
+  std::vector<std::string> dir, par;
+  std::string line;
+  while (std::getline(f, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.size() < 73) continue;
+    if (line[72] == 'D') dir.push_back(line);
+    if (line[72] == 'P') par.push_back(line);
+  }
+  if (dir.empty() || dir.size() % 2) {
+    *err = "IGES file without a well-formed directory section: " + path;
+    return false;
+  }
+  auto field = [](const std::string& l, int k) {  // k-th 8-column field of a directory line
+    return std::atoi(l.substr(8 * k, 8).c_str());
+  };
+  g->patches.clear();
+  for (size_t e = 0; e < dir.size(); e += 2) {
+    const int type = field(dir[e], 0), first = field(dir[e], 1), count = field(dir[e + 1], 3);
+    if (type != 128) {
+      *err = "IGES entity " + std::to_string(type) + " is not a rational B-spline surface (128): " + path;
+      return false;
+    }
+    if (first < 1 || count < 1 || first - 1 + count > (int)par.size()) {
+      *err = "IGES parameter pointer out of range: " + path;
+      return false;
+    }
+    // parameter data: columns 1-64 of the entity's lines, ',' between values, ';' at the end
+    std::string data;
+    for (int k = first - 1; k < first - 1 + count; ++k) data += par[k].substr(0, 64);
+    std::vector<double> v;
+    std::string tok;
+    for (char c : data + ",") {
+      if (c == ',' || c == ';') {
+        if (!tok.empty()) {
+          for (char& t : tok)
+            if (t == 'D' || t == 'd') t = 'E';  // Fortran exponents
+          v.push_back(std::strtod(tok.c_str(), nullptr));
+        }
+        tok.clear();
+        if (c == ';') break;
+      } else if (c != ' ') {
+        tok += c;
+      }
+    }
+    if (v.size() < 10 || (int)v[0] != 128) {
+      *err = "malformed IGES entity 128 parameters: " + path;
+      return false;
+    }
+    const int K1 = (int)v[1], K2 = (int)v[2], M1 = (int)v[3], M2 = (int)v[4];
+    const int A = K1 + M1 + 1, B = K2 + M2 + 1, C = (K1 + 1) * (K2 + 1);  // knot counts - 1, points
+    if (K1 < 0 || K2 < 0 || M1 < 0 || M2 < 0 || v.size() < (size_t)(10 + A + 1 + B + 1 + 4 * C)) {
+      *err = "malformed IGES entity 128 parameters: " + path;
+      return false;
+    }
+    if (K1 != M1 || K2 != M2) {
+      *err = "patches with interior knots are not supported: " + path;
+      return false;
+    }
+    const double* W = v.data() + 10 + A + 1 + B + 1;
+    const double* X = W + C;
+    PatchData P;
+    P.px = K1 + 1;
+    P.py = K2 + 1;
+    P.cp.resize(4 * C);
+    for (int j = 0; j <= K2; ++j)
+      for (int i = 0; i <= K1; ++i) {
+        const int q = j * (K1 + 1) + i;  // IGES order: first index fastest
+        const double w = W[q];
+        double* c = &P.cp[4 * (i * P.py + j)];
+        c[0] = X[3 * q] * w;  // homogeneous coordinates, as in the .dat files
+        c[1] = X[3 * q + 1] * w;
+        c[2] = X[3 * q + 2] * w;
+        c[3] = w;
+      }
     g->patches.push_back(std::move(P));
   }
   return true;

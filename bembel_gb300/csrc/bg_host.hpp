@@ -27,6 +27,11 @@ struct Geometry {
 // Parse an Octave-NURBS .dat file (Geometry/GeometryIO.hpp:25-122). Patches
 // with interior knots are rejected (the H2 path uses Bezier patches).
 bool load_dat(const std::string& path, Geometry* g, std::string* err);
+// Parse the rational B-spline surfaces (entity 128) of an IGES file
+// (Geometry/GeometryIGS.hpp:25-151): fixed 80-column records, section letter
+// in column 73, two directory lines per entity, parameter data in columns
+// 1-64. Single-span (Bezier) surfaces only, like load_dat.
+bool load_igs(const std::string& path, Geometry* g, std::string* err);
 
 void bernstein(int p, double x, double* b);      // degree p, p+1 values
 void bernstein_der(int p, double x, double* b);  // derivative, p+1 values

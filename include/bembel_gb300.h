@@ -109,6 +109,10 @@ bg_status bg_profile_classes(bg_context* ctx, unsigned mask);
 /* Geometry(const std::string&) with LoadGeometryFileDAT
  * (Geometry/Geometry.hpp:89-102, Geometry/GeometryIO.hpp:25-122). */
 bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** out);
+/* Geometry(const std::string&) with LoadGeometryFileIGS (Geometry/GeometryIGS.hpp:25-151):
+ * the rational B-spline surfaces (entity 128) of an IGES file; single-span
+ * (Bezier) surfaces only, other entities and interior knots give BG_INVALID_ARG. */
+bg_status bg_geometry_load_igs(bg_context* ctx, const char* path, bg_geometry** out);
 bg_status bg_geometry_destroy(bg_geometry* g);
 /* Geometry(const PatchVector&) (Geometry/Geometry.hpp:60-63) from Bezier
  * patches already in memory, so an existing Bembel::Geometry can be handed

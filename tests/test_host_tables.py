@@ -109,3 +109,33 @@ def test_host_only_context_refuses_server(bg_host):
     assert _lib.load().bg_server_create(ctx.h, 1 << 30, 1, ctypes.byref(h)) == _lib.BG_UNSUPPORTED
     assert _lib.load().bg_server_create(ctx.h, 0, 1, ctypes.byref(h)) == _lib.BG_INVALID_ARG
     assert _lib.load().bg_server_create(ctx.h, 1 << 30, 0, ctypes.byref(h)) == _lib.BG_INVALID_ARG
+
+
+def test_igs_geometry_matches_dat(bg_host, tmp_path):
+    """LoadGeometryFileIGS (Geometry/GeometryIGS.hpp:25-151): the sphere written
+    as IGES entity 128 evaluates like the .dat sphere; other entities and
+    interior knots are refused."""
+    import sys
+    sys.path.insert(0, ROOT + "/tests/golden")
+    from igs_writer import read_dat, write_igs
+    bg, ctx = bg_host
+    patches = read_dat(SPHERE)
+    igs = str(tmp_path / "sphere.igs")
+    write_igs(patches, igs)
+    a, b = bg.Geometry(SPHERE, ctx), bg.Geometry(igs, ctx)
+    rng = np.random.default_rng(17)
+    for _ in range(60):
+        p, s, t = int(rng.integers(len(patches))), rng.uniform(), rng.uniform()
+        assert np.abs(a.surface_point(p, s, t)[3:] - b.surface_point(p, s, t)[3:]).max() < 1e-13
+    d1 = bg.DiscreteOperator(bg.AnsatzSpace(a, 2, 2), bg.LaplaceSingleLayerOperator())
+    d2 = bg.DiscreteOperator(bg.AnsatzSpace(b, 2, 2), bg.LaplaceSingleLayerOperator())
+    assert d1.N == d2.N and d1.n_lowrank == d2.n_lowrank
+    bad = str(tmp_path / "bad.igs")
+    write_igs(patches[:1], bad, entity=126)
+    with pytest.raises(bg.BembelError):
+        bg.Geometry(bad, ctx)
+    px, py = patches[0][0], patches[0][1]
+    write_igs(patches[:1], bad, knots=[([0.0] * px + [0.5] + [1.0] * px, [0.0] * py + [1.0] * py)])
+    with pytest.raises(bg.BembelError) as ei:
+        bg.Geometry(bad, ctx)
+    assert "interior knots" in str(ei.value)
