@@ -237,13 +237,15 @@ class H2Matrix:
 class DiscreteOperator:
     """DiscreteOperator<H2Matrix<S>, Op>(ansatz_space) (DiscreteOperator.hpp:107-145)."""
 
-    def __init__(self, ansatz_space, linear_operator, n_p=9, eta=1.6, min_cluster_level=1, store_fp64_far=True):
+    def __init__(self, ansatz_space, linear_operator, n_p=9, eta=1.6, min_cluster_level=1, store_fp64_far=True,
+                 keep_fp64_blocks=True):
         self.ansatz_space = ansatz_space
         self.lin_op = linear_operator
         self.ctx = ansatz_space.geometry.ctx
         prm = H2Params()
         _lib.load().bg_h2_params_default(ctypes.byref(prm))
         prm.n_p, prm.eta, prm.min_cluster_level, prm.store_fp64_far = n_p, eta, min_cluster_level, int(store_fp64_far)
+        prm.keep_fp64_blocks = int(keep_fp64_blocks)
         h = ctypes.c_void_p()
         self.ctx.check(_lib.load().bg_operator_create(self.ctx.h, ansatz_space.geometry.h,
                                                       ansatz_space.refinement_level, ansatz_space.polynomial_degree,

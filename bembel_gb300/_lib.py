@@ -20,7 +20,7 @@ PRECISIONS = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "fp32": PREC_FP32}
 
 class H2Params(ctypes.Structure):
     _fields_ = [("n_p", ctypes.c_int), ("eta", ctypes.c_double), ("min_cluster_level", ctypes.c_int),
-                ("store_fp64_far", ctypes.c_int)]
+                ("store_fp64_far", ctypes.c_int), ("keep_fp64_blocks", ctypes.c_int)]
 
 
 class SolveParams(ctypes.Structure):

@@ -59,6 +59,7 @@ void bg_h2_params_default(bg_h2_params* p) {
   p->eta = 1.6;
   p->min_cluster_level = 1;
   p->store_fp64_far = 1;
+  p->keep_fp64_blocks = 1;
 }
 void bg_solve_params_default(bg_solve_params* p) {
   if (!p) return;
@@ -429,6 +430,7 @@ extern "C" bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, i
   op->eta = prm.eta;
   op->mcl = prm.min_cluster_level;
   op->store_far = prm.store_fp64_far != 0;
+  op->keep_far64 = prm.keep_fp64_blocks != 0;
   op->cplx = op_kind != BG_LAPLACE_SL;
   op->vd = op_kind == BG_MAXWELL_SL ? 2 : 1;
   op->nc = op_kind == BG_MAXWELL_SL ? 2 : 1;
@@ -535,7 +537,7 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
     const size_t ncl = (size_t)op->nclusters(l);
     e += ncl * np2 * (sizeof(d4) + sizeof(float4) + (op->maxwell() ? 6 * (sizeof(double) + sizeof(float)) : 0));
     if (!op->store_far) continue;
-    e += nb * op->block_stride(op->far[l].B) * sb;                 // FP64 couplings
+    if (op->keep_far64) e += nb * op->block_stride(op->far[l].B) * sb;  // FP64 couplings
     e += nb * op->block_stride(op->far[l].B) * 8 * (op->cplx ? 2 : 1);  // double-float pairs
     e += nb * (op->cplx ? far_h16c_atile_bytes(np2) : far_h16_atile_bytes(np2)) + nb * sizeof(float);
   }
@@ -631,6 +633,8 @@ extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, in
   } else {
     if (!op->store_far) return set_error(op->ctx, BG_INVALID_ARG, "far field is not stored");
     const int l = op->part.leaf_list[4 * leaf + 1];
+    if (!op->d_far64[l]->p)
+      return set_error(op->ctx, BG_INVALID_ARG, "the FP64 coupling blocks were released after assembly");
     seg = &op->far[l];
     data = op->d_far64[l];
   }
@@ -736,6 +740,8 @@ static bg_status assemble_far(bg_operator* op) {
       }
     }
     BG_CHECK(cudaStreamSynchronize(s), "far-field assembly");
+    // the products read the double-float pairs and the tiles, not the FP64 blocks
+    if (!op->keep_far64 && op->d_far_df[l]->p) op->d_far64[l]->release();
   }
   op->far_tiles = tiled_levels == far_levels && op->leaf_level < kMaxFarLevels;
   return BG_OK;

@@ -154,6 +154,7 @@ struct bg_operator {
   std::vector<DevBuf*> d_far_atiles;      // per level: FP16 hi/lo tensor-core tiles of the low-rank blocks
   std::vector<DevBuf*> d_far_ainv;        // per level: inverse power-of-two scale of every tile
   bool far_tiles = false;                 // every far-field level has its tiles
+  bool keep_far64 = true;                 // keep d_far64 after assembly (else released)
   std::vector<DevBuf*> d_mom64, d_mom32;  // per vector component
   DevBuf d_tr64, d_tr32;
   // FMM matrices transposed and padded for launch_tgemm, per precision

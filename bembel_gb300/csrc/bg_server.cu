@@ -131,6 +131,7 @@ struct bg_server {
     }
     bg_h2_params prm;
     bg_h2_params_default(&prm);
+    prm.keep_fp64_blocks = 0;  // the cache holds only what the products read
     bg_operator* op = nullptr;
     bg_status s = bg_operator_create(w.ctx, geos[k.geo], k.M, k.P, k.kind, &prm, &op);
     if (s == BG_OK && k.kind != BG_LAPLACE_SL) s = bg_operator_set_wavenumber(op, k.kre, k.kim);

@@ -63,6 +63,10 @@ typedef struct {
   double eta;            /* admissibility constant */
   int min_cluster_level; /* leaf clusters hold 4^min_cluster_level elements */
   int store_fp64_far;    /* 1: assemble and store the FP64 far field */
+  int keep_fp64_blocks;  /* 1 (default): keep the FP64 coupling blocks after assembly (leaf-block
+                            inspection); 0: release them once their double-float pairs and
+                            tensor-core tiles are built, which the products use (about a third
+                            less device memory; the serving loop does this) */
 } bg_h2_params;
 
 /* Solve controls for bg_solve (GMRES with iterative refinement). */

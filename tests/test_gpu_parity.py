@@ -198,3 +198,25 @@ def test_maxwell_field_converges_on_gpu(ctx):
         errs.append(np.max(np.linalg.norm(d.potential(x, grid)[:, :, 0] - ref, axis=1)))
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert np.all(rates >= 0.9 * 3), (errs, rates)
+
+
+def test_released_fp64_blocks_keep_products(ctx, oracle):
+    """keep_fp64_blocks=False: the products read the double-float pairs and
+    tiles, so they still match; only the leaf inspection is refused."""
+    import bembel_gb300 as bg
+    for kind, k in ((0, 0.0), (1, 2.0)):
+        lin = bg.LaplaceSingleLayerOperator() if kind == 0 else bg.HelmholtzSingleLayerOperator()
+        if kind:
+            lin.set_wavenumber(k)
+        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 2, 1), lin, n_p=6, keep_fp64_blocks=False)
+        d.compute()
+        o = oracle.Problem(SPHERE, 2, 1, kind, kappa=k, np_=6)
+        rng = np.random.default_rng(3)
+        x = rng.uniform(-1, 1, (d.N, 3)) + (1j * rng.uniform(-1, 1, (d.N, 3)) if kind else 0)
+        ref = o.matvec(x)
+        A = d.get_discrete_operator()
+        assert np.linalg.norm(A.matvec(x) - ref) / np.linalg.norm(ref) < FP64_TOL
+        assert np.linalg.norm(A.matvec(x, precision="fp32") - ref) / np.linalg.norm(ref) < FP32_TOL
+        far = [i for i, l in enumerate(d.leaves()) if l[0] == 1][0]
+        with pytest.raises(bg.BembelError):
+            d.leaf_block(far)

@@ -66,7 +66,8 @@ def test_server_evicts_under_budget(ctx):
     # budget: room for the larger of two operators, not for both
     sizes = []
     for M in (2, 3):
-        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, 1), bg.LaplaceSingleLayerOperator())
+        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, 1), bg.LaplaceSingleLayerOperator(),
+                                keep_fp64_blocks=False)  # as the server caches them
         import ctypes
         a, e = ctypes.c_size_t(), ctypes.c_size_t()
         ctx.check(_lib.load().bg_operator_memory(d.h, ctypes.byref(a), ctypes.byref(e)))
