@@ -220,3 +220,17 @@ def test_released_fp64_blocks_keep_products(ctx, oracle):
         far = [i for i, l in enumerate(d.leaves()) if l[0] == 1][0]
         with pytest.raises(bg.BembelError):
             d.leaf_block(far)
+
+
+@pytest.mark.parametrize("np_,nrhs", [(10, 3), (6, 20)])
+def test_helmholtz_tile_shapes_and_chunks(ctx, oracle, np_, nrhs):
+    """Complex tensor-core far field at n_p = 10 (the torus sweep's tile shape)
+    and with more right-hand sides than one 16-column pass."""
+    d, o = _pair(ctx, oracle, SPHERE, 2, 1, 1, 3.0, np_)
+    rng = np.random.default_rng(19)
+    x = rng.uniform(-1, 1, (d.N, nrhs)) + 1j * rng.uniform(-1, 1, (d.N, nrhs))
+    ref = o.matvec(x)
+    A = d.get_discrete_operator()
+    assert np.linalg.norm(A.matvec(x) - ref) / np.linalg.norm(ref) < FP64_TOL
+    for prec in ("mixed", "fp32"):
+        assert np.linalg.norm(A.matvec(x, precision=prec) - ref) / np.linalg.norm(ref) < FP32_TOL, prec
