@@ -544,11 +544,10 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
           unsigned char* sm = smem + st * G::STAGE;
           const unsigned char* ga = atiles + (size_t)k * G::A2;
           const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
+          // hi and lo tiles are contiguous in global and shared memory: one copy each for A and B
           mbar_expect_tx(&full_bar[st], G::STAGE);
-          bulk_g2s(sm, ga, G::A_BYTES, &full_bar[st]);
-          bulk_g2s(sm + G::A_BYTES, ga + G::A_BYTES, G::A_BYTES, &full_bar[st]);
-          bulk_g2s(sm + G::A2, gb, G::B_BYTES, &full_bar[st]);
-          bulk_g2s(sm + G::A2 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
+          bulk_g2s(sm, ga, G::A2, &full_bar[st]);
+          bulk_g2s(sm + G::A2, gb, G::B2, &full_bar[st]);
         }
       }
     }
@@ -879,11 +878,10 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
           unsigned char* sm = smem + st * G::STAGE;
           const unsigned char* ga = T.a[lev] + (size_t)k * G::A4;
           const unsigned char* gb = T.b[lev] + (size_t)col[k] * G::B2;
+          // the four coupling tiles and the two right-hand-side tiles are contiguous: two copies
           mbar_expect_tx(&full_bar[st], G::STAGE);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) bulk_g2s(sm + q * G::A_BYTES, ga + q * G::A_BYTES, G::A_BYTES, &full_bar[st]);
-          bulk_g2s(sm + G::A4, gb, G::B_BYTES, &full_bar[st]);
-          bulk_g2s(sm + G::A4 + G::B_BYTES, gb + G::B_BYTES, G::B_BYTES, &full_bar[st]);
+          bulk_g2s(sm, ga, G::A4, &full_bar[st]);
+          bulk_g2s(sm + G::A4, gb, G::B2, &full_bar[st]);
         }
       }
     }
