@@ -1186,8 +1186,91 @@ __global__ void __launch_bounds__(128) k_bsr32_tile(const int* __restrict__ row_
   }
 }
 
+// Complex FP32 block-sparse product with register tiles: thread t owns RT rows
+// and 2 complex right-hand sides (columns 2 (t % (nrhs/2)) ..), so a block
+// column costs RT/2 + 1 16-byte shared loads for 2 RT complex multiply-adds.
+// Blocks and x panels staged with cp.async, double-buffered, as k_bsr32_tile.
+template <int RT>
+__global__ void __launch_bounds__(256) k_bsr32c_tile(const int* __restrict__ row_ptr, const int* __restrict__ col,
+                                                     const float2* __restrict__ blocks, long bstride, int B,
+                                                     const float2* __restrict__ x, float2* __restrict__ y, int nrhs,
+                                                     int accumulate) {
+  extern __shared__ __align__(16) float2 smc[];
+  const int fsz = B * B, xsz = B * nrhs;
+  float2* st[2] = {smc, smc + fsz + xsz};
+  const int row = blockIdx.x, t = threadIdx.x;
+  const int cq = nrhs >> 1;
+  const int i0 = RT * (t / cq), c0 = 2 * (t % cq);
+  const bool active = t < (B / RT) * cq;
+  float2 acc[RT][2];
+#pragma unroll
+  for (int r = 0; r < RT; ++r) acc[r][0] = acc[r][1] = make_float2(0.0f, 0.0f);
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  auto issue = [&](int k, float2* dst) {
+    const float2* F = blocks + (long)k * bstride;
+    for (int e = 2 * t; e < fsz; e += 2 * blockDim.x) cp_async16(dst + e, F + e);
+    const float2* xs = x + (long)col[k] * xsz;
+    for (int e = 2 * t; e < xsz; e += 2 * blockDim.x) cp_async16(dst + fsz + e, xs + e);
+    cp_async_commit();
+  };
+  if (kb < ke) issue(kb, st[0]);
+  for (int k = kb; k < ke; ++k) {
+    const int sb = (k - kb) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // block k staged; everyone is done with block k-1
+    if (k + 1 < ke) issue(k + 1, st[sb ^ 1]);
+    if (active) {
+      const float2* F = st[sb];
+      const float2* xs = st[sb] + fsz;
+#pragma unroll 4
+      for (int j = 0; j < B; ++j) {
+        float2 f[RT];
+#pragma unroll
+        for (int h = 0; h < RT / 2; ++h) {
+          const float4 q = *reinterpret_cast<const float4*>(F + j * B + i0 + 2 * h);
+          f[2 * h] = make_float2(q.x, q.y);
+          f[2 * h + 1] = make_float2(q.z, q.w);
+        }
+        const float4 v = *reinterpret_cast<const float4*>(xs + j * nrhs + c0);
+        const float2 xv[2] = {make_float2(v.x, v.y), make_float2(v.z, v.w)};
+#pragma unroll
+        for (int r = 0; r < RT; ++r)
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            acc[r][c].x = fmaf(f[r].x, xv[c].x, fmaf(-f[r].y, xv[c].y, acc[r][c].x));
+            acc[r][c].y = fmaf(f[r].x, xv[c].y, fmaf(f[r].y, xv[c].x, acc[r][c].y));
+          }
+      }
+    }
+  }
+  if (active) {
+#pragma unroll
+    for (int r = 0; r < RT; ++r) {
+      float2* yo = y + ((long)row * B + i0 + r) * nrhs + c0;
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        yo[c] = accumulate ? make_float2(yo[c].x + acc[r][c].x, yo[c].y + acc[r][c].y) : acc[r][c];
+    }
+  }
+}
+
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
                             int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
+  if (cplx && nrows > 0 && B % 2 == 0 && nrhs % 2 == 0 && bstride % 2 == 0 &&
+      (reinterpret_cast<uintptr_t>(blocks) % 16) == 0 && (reinterpret_cast<uintptr_t>(x) % 16) == 0) {
+    const int rt = (B % 4 == 0 && (B / 4) * (nrhs / 2) >= 64) ? 4 : 2;
+    const int nthr = (B / rt) * (nrhs / 2);
+    const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float2);
+    if (nthr <= 256 && smem <= 100 * 1024) {
+      const int threads = (nthr + 31) / 32 * 32;
+      auto kf = rt == 4 ? k_bsr32c_tile<4> : k_bsr32c_tile<2>;
+      cudaError_t e = smem_limit(kf, smem);
+      if (e != cudaSuccess) return e;
+      kf<<<nrows, threads, smem, s>>>(row_ptr, col, static_cast<const float2*>(blocks), bstride, B,
+                                      static_cast<const float2*>(x), static_cast<float2*>(y), nrhs, accumulate);
+      return cudaGetLastError();
+    }
+  }
   if (!cplx && nrows > 0 && B % 4 == 0 && nrhs % 4 == 0 && bstride % 4 == 0 && (B / 4) * (nrhs / 4) <= 128) {
     const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float);
     if (smem <= 100 * 1024) {
