@@ -383,8 +383,8 @@ static bg_status upload_tables(bg_operator* op) {
           return st;
       }
     }
-    // every output row tile count within the kernel's 4 x 256 tiles of 3 x 4
-    auto fits = [&](int Mo) { return (Mo + 2) / 3 * 8 <= 4 * 256; };
+    // every output row tile count within the kernel's 6 x 256 tiles of 3 x 4
+    auto fits = [&](int Mo) { return (Mo + 2) / 3 * 8 <= 6 * 256; };
     op->use_tgemm = (op->maxwell() || (op->nc == 1 && mom.size() <= 2 && fits(R))) && fits(Bq) && fits(np2) &&
                     fits(4 * np2);
   }

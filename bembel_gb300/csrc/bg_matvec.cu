@@ -439,11 +439,11 @@ __device__ __forceinline__ void load4(const T* p, T* v) {
   }
 }
 
-template <typename T, bool ACC>
+template <typename T, bool ACC, int MAXT>
 __global__ void __launch_bounds__(256) k_tgemm(const T* __restrict__ AT, int ld, int Mo, int Ki,
                                                const T* __restrict__ B, long bstride, T* __restrict__ C, long cstride,
                                                int kk, int vec_b) {
-  constexpr int KC = 16, RT = 3, CT = 4, NCOL = 32, MAXT = 4;
+  constexpr int KC = 16, RT = 3, CT = 4, NCOL = 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);  // [2][KC][ld]
   T* Bs = As + 2 * KC * ld;                // [2][KC][NCOL]
@@ -640,12 +640,14 @@ static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, 
   }
   if (nbatch == 0) return cudaSuccess;
   const int rtiles = (A.Mo + 2) / 3;
-  if (rtiles * 8 > 4 * 256 || A.ld < rtiles * 3 || A.ld % 4 != 0) return cudaErrorInvalidValue;
+  // up to 4 (or, for op(A) of up to 512 rows, 6) tiles of 3 x 4 per thread
+  if (rtiles * 8 > 6 * 256 || A.ld < rtiles * 3 || A.ld % 4 != 0) return cudaErrorInvalidValue;
   const size_t smem = (size_t)2 * 16 * (A.ld + 32) * sizeof(T);
   const int vec_b = (kk * sizeof(T)) % 16 == 0 && (bstride * sizeof(T)) % 16 == 0 &&
                     (reinterpret_cast<uintptr_t>(B) % 16) == 0;
   const dim3 grid(nbatch, (kk + 31) / 32);
-  auto kf = acc ? k_tgemm<T, true> : k_tgemm<T, false>;
+  const bool big = rtiles * 8 > 4 * 256;
+  auto kf = big ? (acc ? k_tgemm<T, true, 6> : k_tgemm<T, false, 6>) : (acc ? k_tgemm<T, true, 4> : k_tgemm<T, false, 4>);
   cudaError_t e = smem_limit(kf, smem);
   if (e != cudaSuccess) return e;
   kf<<<grid, 256, smem, s>>>(static_cast<const T*>(A.at), A.ld, A.Mo, A.Ki, B, bstride, C, cstride, kk, vec_b);
