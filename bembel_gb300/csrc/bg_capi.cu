@@ -1085,14 +1085,16 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
       // three channels: tangential part of each component, divergence of both
       const size_t chl = (size_t)op->nleaf_cl * np2 * nrhs * sfar;
       char* yl = static_cast<char*>(op->w_y[Ll]->p);
-      const char* xin[4] = {xc0, xc1, xc0, xc1};
-      char* yout[4] = {yl, yl + chl, yl + 2 * chl, yl + 2 * chl};
-      const int blk[4] = {0, 0, 1, 2};
-      for (int t = 0; t < 4; ++t)
+      // tangential channels of both components in one batch: the two components'
+      // leaf panels are consecutive in x (component-major) and so are the channels
+      const char* xin[3] = {xc0, xc0, xc1};
+      char* yout[3] = {yl, yl + 2 * chl, yl + 2 * chl};
+      const int blk[3] = {0, 1, 2}, nb[3] = {2 * op->nleaf_cl, op->nleaf_cl, op->nleaf_cl};
+      for (int t = 0; t < 3; ++t)
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
                    return op->use_tgemm
-                              ? launch_tgemm(Sfar, t == 3, tm.a_mw_f[blk[t]], xin[t], op->Bq, yout[t], np2, op->nleaf_cl, nrhs, s)
-                              : launch_moment_fwd_acc(Sfar, t == 3, mw_mom(blk[t]), np2, op->Bq, op->nleaf_cl, xin[t],
+                              ? launch_tgemm(Sfar, t == 2, tm.a_mw_f[blk[t]], xin[t], op->Bq, yout[t], np2, nb[t], nrhs, s)
+                              : launch_moment_fwd_acc(Sfar, t == 2, mw_mom(blk[t]), np2, op->Bq, nb[t], xin[t],
                                                       yout[t], nrhs, s); }),
                  "forward moments");
       for (int l = Ll - 1; l >= 0; --l) {
@@ -1307,14 +1309,14 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
       const char* zl = static_cast<const char*>(op->w_z[Ll]->p);
       char* yc0 = static_cast<char*>(yfar);
       char* yc1 = yc0 + comp_ss * nrhs * sfar;
-      const char* zin[4] = {zl, zl + 2 * chl, zl + chl, zl + 2 * chl};
-      char* yout[4] = {yc0, yc0, yc1, yc1};
-      const int blk[4] = {0, 1, 0, 2};
-      for (int t = 0; t < 4; ++t)
+      const char* zin[3] = {zl, zl + 2 * chl, zl + 2 * chl};
+      char* yout[3] = {yc0, yc0, yc1};
+      const int blk[3] = {0, 1, 2}, nb[3] = {2 * op->nleaf_cl, op->nleaf_cl, op->nleaf_cl};
+      for (int t = 0; t < 3; ++t)
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
                    return op->use_tgemm
-                              ? launch_tgemm(Sfar, true, tm.a_mw_b[blk[t]], zin[t], np2, yout[t], op->Bq, op->nleaf_cl, nrhs, s)
-                              : launch_moment_bwd(Sfar, mw_mom(blk[t]), np2, op->Bq, op->nleaf_cl, zin[t], yout[t], nrhs, s); }),
+                              ? launch_tgemm(Sfar, true, tm.a_mw_b[blk[t]], zin[t], np2, yout[t], op->Bq, nb[t], nrhs, s)
+                              : launch_moment_bwd(Sfar, mw_mom(blk[t]), np2, op->Bq, nb[t], zin[t], yout[t], nrhs, s); }),
                  "backward moments");
     }
     for (int c = 0; c < op->vd && !op->maxwell(); ++c) {
