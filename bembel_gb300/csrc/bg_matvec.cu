@@ -189,39 +189,6 @@ __global__ void k_bsr_pipe(const int* __restrict__ row_ptr, const int* __restric
   }
 }
 
-// Y[c][r][k] = sum_q Mom[r][q] X[c*Bq + q][k]
-template <typename S>
-__global__ void k_moment_fwd(const typename RealOf<S>::T* __restrict__ mom, int R, int Bq,
-                             const S* __restrict__ xss, S* __restrict__ y, int nrhs) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  S* xs = reinterpret_cast<S*>(smem_raw);
-  const int c = blockIdx.x;
-  for (int t = threadIdx.x; t < Bq * nrhs; t += blockDim.x) xs[t] = xss[(long)c * Bq * nrhs + t];
-  __syncthreads();
-  for (int t = threadIdx.x; t < R * nrhs; t += blockDim.x) {
-    const int r = t / nrhs, k = t % nrhs;
-    S acc = zero<S>();
-    for (int q = 0; q < Bq; ++q) acc = fmac(acc, xs[q * nrhs + k], mom[r * Bq + q]);
-    y[(long)c * R * nrhs + t] = acc;
-  }
-}
-// Yss[c*Bq + q][k] += sum_r Mom[r][q] Z[c][r][k]
-template <typename S>
-__global__ void k_moment_bwd(const typename RealOf<S>::T* __restrict__ mom, int R, int Bq, const S* __restrict__ z,
-                             S* __restrict__ yss, int nrhs) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  S* zs = reinterpret_cast<S*>(smem_raw);
-  const int c = blockIdx.x;
-  for (int t = threadIdx.x; t < R * nrhs; t += blockDim.x) zs[t] = z[(long)c * R * nrhs + t];
-  __syncthreads();
-  for (int t = threadIdx.x; t < Bq * nrhs; t += blockDim.x) {
-    const int q = t / nrhs, k = t % nrhs;
-    S acc = zero<S>();
-    for (int r = 0; r < R; ++r) acc = fmac(acc, zs[r * nrhs + k], mom[r * Bq + q]);
-    const long o = (long)c * Bq * nrhs + t;
-    yss[o] = add(yss[o], acc);
-  }
-}
 // parent[p][comp*np2 + r][k] = sum_{ch, q} T[r][ch*np2 + q] child[4p+ch][comp*np2 + q][k]
 template <typename S>
 __global__ void k_transfer_fwd(const typename RealOf<S>::T* __restrict__ T, int np2, int nc,
@@ -1309,16 +1276,6 @@ cudaError_t launch_convert_blocks(bool cplx, const void* in, long sin, void* out
   return cudaGetLastError();
 }
 
-template <typename S>
-static cudaError_t mom_fwd_t(const void* mom, int R, int Bq, int ncl, const void* xss, void* y, int nrhs, cudaStream_t s) {
-  if (ncl == 0) return cudaSuccess;
-  const size_t smem = (size_t)Bq * nrhs * sizeof(S);
-  auto kf = k_moment_fwd<S>;
-  cudaError_t e = smem_limit(kf, smem);
-  if (e != cudaSuccess) return e;
-  kf<<<ncl, 256, smem, s>>>((const typename RealOf<S>::T*)mom, R, Bq, (const S*)xss, (S*)y, nrhs);
-  return cudaGetLastError();
-}
 cudaError_t launch_moment_fwd_acc(int S, bool acc, const void* mom, int R, int Bq, int ncl, const void* xss, void* y,
                                   int nrhs, cudaStream_t s) {
   const int kk = (S & 1) ? 2 * nrhs : nrhs;
@@ -1335,23 +1292,6 @@ cudaError_t launch_moment_fwd(int S, const void* mom, int R, int Bq, int ncl, co
                                   (long)R * kk, ncl, kk, s);
   return bgemm<float>(false, false, (const float*)mom, R, Bq, (const float*)xss, (long)Bq * kk, (float*)y, (long)R * kk,
                       ncl, kk, s);
-  switch (S) {
-    case 0: return mom_fwd_t<double>(mom, R, Bq, ncl, xss, y, nrhs, s);
-    case 1: return mom_fwd_t<cd>(mom, R, Bq, ncl, xss, y, nrhs, s);
-    case 2: return mom_fwd_t<float>(mom, R, Bq, ncl, xss, y, nrhs, s);
-    case 3: return mom_fwd_t<cf>(mom, R, Bq, ncl, xss, y, nrhs, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-template <typename S>
-static cudaError_t mom_bwd_t(const void* mom, int R, int Bq, int ncl, const void* z, void* yss, int nrhs, cudaStream_t s) {
-  if (ncl == 0) return cudaSuccess;
-  const size_t smem = (size_t)R * nrhs * sizeof(S);
-  auto kf = k_moment_bwd<S>;
-  cudaError_t e = smem_limit(kf, smem);
-  if (e != cudaSuccess) return e;
-  kf<<<ncl, 256, smem, s>>>((const typename RealOf<S>::T*)mom, R, Bq, (const S*)z, (S*)yss, nrhs);
-  return cudaGetLastError();
 }
 cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int ncl, const void* z, void* yss, int nrhs,
                               cudaStream_t s) {
@@ -1361,13 +1301,6 @@ cudaError_t launch_moment_bwd(int S, const void* mom, int R, int Bq, int ncl, co
                                   (long)Bq * kk, ncl, kk, s);
   return bgemm<float>(true, true, (const float*)mom, Bq, R, (const float*)z, (long)R * kk, (float*)yss, (long)Bq * kk,
                       ncl, kk, s);
-  switch (S) {
-    case 0: return mom_bwd_t<double>(mom, R, Bq, ncl, z, yss, nrhs, s);
-    case 1: return mom_bwd_t<cd>(mom, R, Bq, ncl, z, yss, nrhs, s);
-    case 2: return mom_bwd_t<float>(mom, R, Bq, ncl, z, yss, nrhs, s);
-    case 3: return mom_bwd_t<cf>(mom, R, Bq, ncl, z, yss, nrhs, s);
-    default: return cudaErrorInvalidValue;
-  }
 }
 cudaError_t launch_transfer_fwd(int S, const void* T, int np2, int nc, int np_, const void* yc, void* yp, int nrhs,
                                 cudaStream_t s) {
