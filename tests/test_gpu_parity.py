@@ -234,3 +234,26 @@ def test_helmholtz_tile_shapes_and_chunks(ctx, oracle, np_, nrhs):
     assert np.linalg.norm(A.matvec(x) - ref) / np.linalg.norm(ref) < FP64_TOL
     for prec in ("mixed", "fp32"):
         assert np.linalg.norm(A.matvec(x, precision=prec) - ref) / np.linalg.norm(ref) < FP32_TOL, prec
+
+
+def test_helmholtz_field_converges_on_gpu(ctx):
+    """examples/HelmholtzSingleLayerH2.cpp:30-98 on the GPU path: source at the
+    origin, kappa = 2, potential at 100 points of radius 2, rate >= 0.9 (2P + 3), P = 0."""
+    import math
+    import bembel_gb300 as bg
+    from test_oracle_pins import _sphere_points
+    k = 2.0
+    grid = _sphere_points(2.0, 100)
+    r = np.linalg.norm(grid, axis=1)
+    ref = np.exp(-1j * k * r) / (4 * math.pi * r)
+    errs = []
+    for M in (1, 2, 3):
+        lin = bg.HelmholtzSingleLayerOperator()
+        lin.set_wavenumber(k)
+        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, 0), lin)
+        d.compute()
+        x, st = d.get_discrete_operator().solve(d.load_vector(1, np.zeros((1, 3))), tol=1e-10)
+        assert st["converged"]
+        errs.append(np.max(np.abs(d.potential(x, grid)[:, 0] - ref)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert rates[-1] >= 0.9 * 3, (errs, rates)

@@ -225,3 +225,21 @@ def test_maxwell_field_converges(oracle):
         errs.append(np.max(np.linalg.norm(p.potential(x, grid) - ref, axis=1)))
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert np.all(rates >= 0.9 * 3), (errs, rates)
+
+
+def test_helmholtz_convergence(oracle):
+    """examples/HelmholtzSingleLayerH2.cpp:30-98: kappa = 2, the fundamental
+    solution with its source at the origin (inside the sphere) as Dirichlet
+    data; the potential at 100 points of radius 2 converges at rate
+    >= 0.9 (2P + 3), here P = 0 over refinement levels 1..3."""
+    k = 2.0
+    grid = _sphere_points(2.0, 100)
+    r = np.linalg.norm(grid, axis=1)
+    ref = np.exp(-1j * k * r) / (4 * math.pi * r)
+    errs = []
+    for M in (1, 2, 3):
+        p = oracle.Problem(SPHERE, M, 0, oracle.HELMHOLTZ, kappa=k, np_=9)
+        rho, _ = p.gmres(p.load_vector(1, np.zeros(3)), tol=1e-12, restart=200, maxit=2000)
+        errs.append(np.max(np.abs(p.potential(rho, grid) - ref)))
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert rates[-1] >= 0.9 * 3, (errs, rates)
