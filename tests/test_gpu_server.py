@@ -99,3 +99,23 @@ def test_server_rejects_operator_above_budget(ctx):
     srv.close()
     assert x is None and info["status"] == _lib.BG_OOM
     assert st["failed"] == 1 and st["cached_operators"] == 0
+
+
+def test_server_results_alone_and_in_the_mix(ctx):
+    """Each request's solution is the same whether it is served alone or
+    together with the others (batched with same-operator requests, overlapped
+    with other operators' solves on other worker streams), within the solve
+    tolerance: both meet the 1e-8 residual and agree to 1e-5 relative."""
+    import bembel_gb300 as bg
+    cases = _cases()
+    srv = bg.Server(ctx, 50e9, workers=2)
+    gs = [srv.add_geometry(bg.Geometry(SPHERE, ctx)), srv.add_geometry(bg.Geometry(TORUS, ctx))]
+    alone = [srv.wait(srv.submit(gs[g], kind, M, P, dk, data, kappa=k), timeout=300)
+             for g, _, kind, M, P, k, dk, data in cases]
+    tickets = [srv.submit(gs[g], kind, M, P, dk, data, kappa=k) for g, _, kind, M, P, k, dk, data in cases]
+    mix = [srv.wait(t, timeout=300) for t in tickets]
+    srv.close()
+    for (x1, i1), (x2, i2) in zip(alone, mix):
+        assert i1["status"] == 0 and i2["status"] == 0
+        assert i1["stats"]["final_relres"] <= 1e-8 and i2["stats"]["final_relres"] <= 1e-8
+        assert np.linalg.norm(x2 - x1) / np.linalg.norm(x1) < 1e-5
