@@ -969,6 +969,7 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
     return set_error(op->ctx, BG_INVALID_ARG, "the Maxwell operator needs a nonzero wavenumber");
   cudaSetDevice(op->ctx->device);
   op->assembled = false;
+  op->drop_graphs();  // assembly may move the stored fields
   auto t0 = std::chrono::steady_clock::now();
   bg_status st = assemble_far(op);
   if (st != BG_OK) return st;
@@ -996,6 +997,7 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
 // ---------------------------------------------------------------------------
 bg_status ensure_work(bg_operator* op, int nrhs) {
   if (nrhs <= op->cap) return BG_OK;
+  op->drop_graphs();  // the buffers below move
   const size_t sb = op->scalar_bytes(false);  // FP64 sizes cover the FP32 path
   BG_CHECK(op->w_xdof.alloc((size_t)op->N * nrhs * sb), "work vectors");
   BG_CHECK(op->w_ydof.alloc((size_t)op->N * nrhs * sb), "work vectors");
@@ -1035,7 +1037,10 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
 }
 
 // One H2 product on row-major FP64 work vectors (H2DenseProduct.hpp:33-165).
-bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
+// The product between T x and T^T y: superspace x in w_xss to superspace y in
+// w_yss, only on the operator's own work buffers (so it can be captured as a
+// CUDA graph and replayed).
+static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
   cudaStream_t s = op->ctx->stream;
   const bool mixed = prec != BG_PREC_FP64;   // far field and transforms in FP32
   const bool near32 = prec == BG_PREC_FP32;  // near field in FP32 too
@@ -1043,9 +1048,6 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
   const size_t sfar = op->scalar_bytes(mixed);
   const int np2 = op->np * op->np;
   const long ss_n = (long)op->S * nrhs;
-  BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
-                            op->w_xss.p, nrhs, s); }),
-           "T x");
   bool any_far = false;
   for (const auto& f : op->far) any_far |= !f.col.empty();
   if (near32) {
@@ -1343,6 +1345,64 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
   }
   if (near32)
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(Sfar, S64, op->w_yss32.p, ss_n, op->w_yss.p, s); }), "y to FP64");
+  return BG_OK;
+}
+
+// One H2 product on row-major FP64 work vectors (H2DenseProduct.hpp:33-165).
+// Outside profiling runs the middle part is captured once per (nrhs,
+// precision) as a CUDA graph and replayed; growing the work vectors or
+// re-assembling the operator drops the graphs. A capture that fails falls back
+// to direct launches for this operator.
+bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
+  cudaStream_t s = op->ctx->stream;
+  const int S64 = op->stype(false);
+  BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
+                            op->w_xss.p, nrhs, s); }),
+           "T x");
+  bg_status st = BG_OK;
+  bg_context* ctx = op->ctx;
+  if (ctx->profiling || !op->use_graphs) {
+    st = apply_middle(op, nrhs, prec);
+  } else {
+    const long key = (long)nrhs * 4 + prec;
+    auto it = op->graphs.find(key);
+    if (it == op->graphs.end() && !op->graph_seen.count(key)) {
+      // first product of this shape: direct launches (they also raise the
+      // kernels' shared-memory limits, which a capture must not do)
+      op->graph_seen.insert(key);
+      st = apply_middle(op, nrhs, prec);
+    } else if (it == op->graphs.end()) {
+      // capture: count the launches the graph holds, per kernel class
+      const long l0 = ctx->launches;
+      long c0[8];
+      for (int c = 0; c < 8; ++c) c0[c] = ctx->class_launches[c];
+      cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      bg_status mst = e == cudaSuccess ? apply_middle(op, nrhs, prec) : BG_DEVICE_ERROR;
+      cudaGraph_t g = nullptr;
+      if (e == cudaSuccess) e = cudaStreamEndCapture(s, &g);
+      bg_operator::ProductGraph pg;
+      if (e == cudaSuccess && mst == BG_OK && g) e = cudaGraphInstantiate(&pg.exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();  // a failed capture leaves no sticky error
+      pg.launches = ctx->launches - l0;
+      for (int c = 0; c < 8; ++c) pg.class_launches[c] = ctx->class_launches[c] - c0[c];
+      ctx->launches = l0;
+      for (int c = 0; c < 8; ++c) ctx->class_launches[c] = c0[c];
+      if (e != cudaSuccess || mst != BG_OK || !pg.exec) {
+        if (pg.exec) cudaGraphExecDestroy(pg.exec);
+        op->use_graphs = false;
+        st = apply_middle(op, nrhs, prec);
+      } else {
+        it = op->graphs.emplace(key, pg).first;
+      }
+    }
+    if (op->use_graphs && it != op->graphs.end()) {
+      BG_CHECK(cudaGraphLaunch(it->second.exec, s), "H2 product (graph)");
+      ctx->launches += it->second.launches;
+      for (int c = 0; c < 8; ++c) ctx->class_launches[c] += it->second.class_launches[c];
+    }
+  }
+  if (st != BG_OK) return st;
   BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_Tt_ptr.as<int>(), op->d_Tt_idx.as<int>(), op->d_Tt_val.as<double>(), op->N,
                             op->w_yss.p, ydof, nrhs, s); }),
            "T^T y");

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -180,12 +182,29 @@ struct bg_operator {
   std::vector<DevBuf*> w_btiles;  // per level: FP16 hi/lo right-hand-side tiles of every cluster
   std::vector<DevBuf*> w_binv;    // per level: inverse column scales of those tiles (32 per cluster)
 
+  // CUDA graphs of the product's middle part, per (nrhs, precision)
+  struct ProductGraph {
+    cudaGraphExec_t exec = nullptr;
+    long launches = 0;
+    long class_launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  };
+  std::map<long, ProductGraph> graphs;
+  std::set<long> graph_seen;  // shapes run once directly (captured on the next product)
+  bool use_graphs = true;
+  void drop_graphs() {
+    for (auto& kv : graphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+    graph_seen.clear();
+  }
+
   // solver workspaces kept between bg_solve calls (owned by the solver)
   void* solver_ws = nullptr;
   void (*solver_ws_free)(void*) = nullptr;
   size_t (*solver_ws_bytes)(const void*) = nullptr;
 
   ~bg_operator() {
+    drop_graphs();
     if (solver_ws && solver_ws_free) solver_ws_free(solver_ws);
     for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_tan64, &d_tan32, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv,
                    &d_mom64, &d_mom32, &w_y, &w_z, &w_ydf, &w_btiles, &w_binv, &w_yv, &w_zv})
