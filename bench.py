@@ -166,6 +166,22 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+def aggregate_replicas(total_ms, dist=None, device="cuda"):
+    """Whole-job time of N independent replicas: the maximum over the ranks of
+    their timed totals (the job is as slow as its slowest replica)."""
+    if dist is None or dist.get_world_size() <= 1:
+        return total_ms
+    import torch
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(nrhs, steps, world, total_ms):
+    """solves/s of the whole job: every replica solves nrhs right-hand sides per step."""
+    return world * nrhs * steps / (total_ms * 1e-3)
+
+
 def run_gpu(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -271,12 +287,8 @@ def run_gpu(args):
         return reps / (e0.elapsed_time(e1) * 1e-3)
     mv64, mvmx, mv32 = mv_rate("fp64"), mv_rate("mixed"), mv_rate("fp32")
 
-    total_ms = float(t_mixed.sum())
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = world * NRHS * args.steps / (total_ms * 1e-3)
+    total_ms = aggregate_replicas(float(t_mixed.sum()), dist)
+    value = replica_value(NRHS, args.steps, world, total_ms)
     fp64_value = NRHS / (float(np.mean(t_fp64)) * 1e-3)
     e2e_value = NRHS / (float(np.mean(t_e2e)) * 1e-3)
 
