@@ -32,7 +32,7 @@ def _rank(rank, world, port, out):
 
 def test_replica_timing_is_max_over_ranks():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()  # no fork of this (threaded) process
     mp.spawn(_rank, args=(world, _port(), out), nprocs=world, join=True)
     for r in range(world):
         total, value = out[r]
