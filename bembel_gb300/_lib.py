@@ -104,6 +104,7 @@ def load(build_if_missing=True):
         "bg_operator_transform": (I, [P, ip, ip, dp]),
         "bg_operator_leaf_block": (I, [P, Lg, I, I, dp]),
         "bg_operator_memory": (I, [P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+        "bg_watchdog_selftest": (I, [P, ctypes.c_longlong]),
         "bg_geometry_num_patches": (I, [P, ip]),
         "bg_server_create": (I, [P, ctypes.c_size_t, I, PP]),
         "bg_server_destroy": (I, [P]),

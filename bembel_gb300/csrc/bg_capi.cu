@@ -507,6 +507,30 @@ extern "C" bg_status bg_operator_info(const bg_operator* op, long* info) {
   std::memcpy(info, v, sizeof(v));
   return BG_OK;
 }
+// bg_watchdog_selftest: CUDA errors are reported against the context
+#define WD_CHECK(expr, what)                                   \
+  do {                                                         \
+    bg_status _st = cuda_status(ctx, (expr), (what));          \
+    if (_st != BG_OK) return _st;                              \
+  } while (0)
+extern "C" bg_status bg_watchdog_selftest(bg_context* ctx, long long limit_cycles) {
+  if (!ctx || limit_cycles <= 0) return BG_INVALID_ARG;
+  if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context: the self-test needs a GPU");
+  cudaSetDevice(ctx->device);
+  DevBuf flag;
+  WD_CHECK(flag.alloc(sizeof(int)), "watchdog self-test");
+  WD_CHECK(cudaMemsetAsync(flag.p, 0, sizeof(int), ctx->stream), "watchdog self-test");
+  WD_CHECK(launch_wait_selftest(limit_cycles, flag.as<int>(), ctx->stream), "watchdog self-test");
+  int code = 0;
+  WD_CHECK(cudaMemcpyAsync(&code, flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "watchdog self-test");
+  WD_CHECK(cudaStreamSynchronize(ctx->stream), "watchdog self-test");
+  if (code != 0)
+    return set_error(ctx, BG_TIMEOUT, "watchdog self-test: the bounded device wait ran out (code " +
+                                           std::to_string(code) + ")");
+  return BG_OK;
+}
+#undef WD_CHECK
+
 extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated, size_t* estimate) {
   if (!op || !allocated || !estimate) return BG_INVALID_ARG;
   size_t a = 0;

@@ -1155,6 +1155,38 @@ cudaError_t launch_far_h16c(const FarH16Tiles& T, const int2* work, int nwork, i
   }
 }
 
+// ---------------------------------------------------------------------------
+// Watchdog self-test: one thread waits on an mbarrier that nothing completes,
+// with a wait bounded by `limit` clock cycles, the same bounded wait the
+// tensor-core kernels use; when it runs out the kernel records code 99 in the
+// error flag and returns normally.
+__global__ void k_wait_selftest(long long limit, int* __restrict__ err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    const uint32_t a = smem_u32(&bar);
+    const long long t0 = clock64();
+    bool done = false;
+    while (!done && clock64() - t0 <= limit) {
+      uint32_t d;
+      asm volatile(
+          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(d)
+          : "r"(a), "r"(0u)
+          : "memory");
+      done = d != 0;
+    }
+    if (!done) atomicExch(err, 99);
+  }
+}
+
+cudaError_t launch_wait_selftest(long long limit_cycles, int* err, cudaStream_t s) {
+  if (limit_cycles <= 0 || limit_cycles > 4000000000LL) return cudaErrorInvalidValue;
+  k_wait_selftest<<<1, 32, 0, s>>>(limit_cycles, err);
+  return cudaGetLastError();
+}
+
 bool far_tc_supported(bool cplx, int np2, int nrhs) {
   const bool shape = np2 == 4 || np2 == 9 || np2 == 16 || np2 == 25 || np2 == 36 || np2 == 49 || np2 == 64 || np2 == 81;
   return !cplx && shape && nrhs >= 1 && nrhs <= kN;

@@ -155,6 +155,8 @@ cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long
 cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s);
 cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
                            cudaStream_t s);
+// watchdog self-test: a bounded wait that cannot complete; sets *err = 99 when it runs out
+cudaError_t launch_wait_selftest(long long limit_cycles, int* err, cudaStream_t s);
 // real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32
 bool far_tc_supported(bool cplx, int np2, int nrhs);
 // Complex kernels (Helmholtz, Maxwell): a holds [Re hi][Re lo][Im hi][Im lo]

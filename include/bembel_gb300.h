@@ -216,6 +216,13 @@ bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double*
  * (computable before bg_operator_assemble; the serving loop admits by it). */
 bg_status bg_operator_memory(const bg_operator* op, size_t* allocated, size_t* estimate);
 
+/* Watchdog self-test (no reference counterpart): runs the bounded device wait
+ * that the tensor-core kernels use on an mbarrier that nothing completes,
+ * limited to limit_cycles SM clock cycles. Returns BG_TIMEOUT (the expected
+ * outcome: the wait ran out, the kernel reported it and returned) with the
+ * context still usable, BG_OK if the wait completed. */
+bg_status bg_watchdog_selftest(bg_context* ctx, long long limit_cycles);
+
 /* ---- serving loop ----
  * No counterpart in the reference (its examples assemble one operator and
  * solve once). A server owns worker threads on the context's GPU, a queue of

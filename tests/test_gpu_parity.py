@@ -257,3 +257,16 @@ def test_helmholtz_field_converges_on_gpu(ctx):
         errs.append(np.max(np.abs(d.potential(x, grid)[:, 0] - ref)))
     rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
     assert rates[-1] >= 0.9 * 3, (errs, rates)
+
+
+def test_watchdog_wait_runs_out_and_context_survives(ctx, oracle):
+    """Failure detection without a GPU fault: a bounded wait on an mbarrier
+    that nothing completes runs out (about 1 ms), the kernel reports it,
+    the call returns BG_TIMEOUT, and the context keeps working."""
+    from bembel_gb300 import _lib
+    assert _lib.load().bg_watchdog_selftest(ctx.h, 2_000_000) == _lib.BG_TIMEOUT
+    assert "ran out" in _lib.load().bg_last_error_string(ctx.h).decode()
+    d, o = _pair(ctx, oracle, SPHERE, 2, 1, 0)
+    x = np.random.default_rng(4).uniform(-1, 1, (d.N, 2))
+    ref = o.matvec(x)
+    assert np.linalg.norm(d.get_discrete_operator().matvec(x) - ref) / np.linalg.norm(ref) < FP64_TOL

@@ -139,3 +139,10 @@ def test_igs_geometry_matches_dat(bg_host, tmp_path):
     with pytest.raises(bg.BembelError) as ei:
         bg.Geometry(bad, ctx)
     assert "interior knots" in str(ei.value)
+
+
+def test_watchdog_selftest_needs_a_gpu(bg_host):
+    from bembel_gb300 import _lib
+    bg, ctx = bg_host
+    assert _lib.load().bg_watchdog_selftest(ctx.h, 1000) == _lib.BG_UNSUPPORTED
+    assert _lib.load().bg_watchdog_selftest(ctx.h, 0) == _lib.BG_INVALID_ARG
