@@ -140,6 +140,12 @@ def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
 
+def _prec_code(precision):
+    if precision not in _lib.PRECISIONS:
+        raise BembelError(_lib.BG_INVALID_ARG, "precision must be one of %s" % sorted(_lib.PRECISIONS))
+    return _lib.PRECISIONS[precision]
+
+
 class H2Matrix:
     """Device-resident H2 matrix; rows() == cols() == number of DOFs."""
 
@@ -316,6 +322,27 @@ class DiscreteOperator:
         self.ctx.check(_lib.load().bg_potential(self.h, rho.ctypes.data_as(ctypes.c_void_p), k, _dp(pts),
                                                 pts.shape[0], out.ctypes.data_as(ctypes.c_void_p)))
         return out.transpose(1, 2, 0) if self.lin_op.kind == _lib.MAXWELL_SL else out
+
+    # -- launch plans and the autotuner --
+    def set_plan(self, nrhs, precision="mixed", near_kernel=0, split_k_batches=-1, far_order=0):
+        """Kernel variants and schedules of products with nrhs right-hand
+        sides at precision (bg_launch_plan; {0, -1, 0} is the built-in plan)."""
+        p = _lib.LaunchPlan(near_kernel, split_k_batches, far_order)
+        self.ctx.check(_lib.load().bg_operator_set_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
+
+    def get_plan(self, nrhs, precision="mixed"):
+        p = _lib.LaunchPlan()
+        self.ctx.check(_lib.load().bg_operator_get_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
+        return {"near_kernel": p.near_kernel, "split_k_batches": p.split_k_batches, "far_order": p.far_order}
+
+    def autotune(self, nrhs, precision="mixed", reps=5):
+        """Time the product's kernel variants for nrhs right-hand sides at
+        precision on the GPU and keep the fastest plan (bg_operator_autotune)."""
+        r = _lib.TuneReport()
+        self.ctx.check(_lib.load().bg_operator_autotune(self.h, nrhs, _prec_code(precision), reps, ctypes.byref(r)))
+        return {"candidates": r.candidates, "builtin_ms": r.builtin_ms, "tuned_ms": r.tuned_ms,
+                "plan": {"near_kernel": r.plan.near_kernel, "split_k_batches": r.plan.split_k_batches,
+                         "far_order": r.plan.far_order}}
 
     # -- inspection --
     def elements(self):

@@ -34,6 +34,15 @@ class SolveStats(ctypes.Structure):
                 ("low_matvecs", ctypes.c_int), ("final_relres", ctypes.c_double)]
 
 
+class LaunchPlan(ctypes.Structure):
+    _fields_ = [("near_kernel", ctypes.c_int), ("split_k_batches", ctypes.c_int), ("far_order", ctypes.c_int)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("candidates", ctypes.c_int), ("builtin_ms", ctypes.c_double), ("tuned_ms", ctypes.c_double),
+                ("plan", LaunchPlan)]
+
+
 class Request(ctypes.Structure):
     _fields_ = [("geometry", ctypes.c_int), ("op_kind", ctypes.c_int), ("M", ctypes.c_int), ("P", ctypes.c_int),
                 ("kre", ctypes.c_double), ("kim", ctypes.c_double), ("data_kind", ctypes.c_int),
@@ -105,6 +114,9 @@ def load(build_if_missing=True):
         "bg_operator_leaf_block": (I, [P, Lg, I, I, dp]),
         "bg_operator_memory": (I, [P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
         "bg_watchdog_selftest": (I, [P, ctypes.c_longlong]),
+        "bg_operator_set_plan": (I, [P, I, I, ctypes.POINTER(LaunchPlan)]),
+        "bg_operator_get_plan": (I, [P, I, I, ctypes.POINTER(LaunchPlan)]),
+        "bg_operator_autotune": (I, [P, I, I, I, ctypes.POINTER(TuneReport)]),
         "bg_geometry_num_patches": (I, [P, ip]),
         "bg_server_create": (I, [P, ctypes.c_size_t, I, PP]),
         "bg_server_destroy": (I, [P]),

@@ -295,6 +295,41 @@ static void build_segments(bg_operator* op) {
   }
 }
 
+
+// Alternative orders of the heaviest-first far-field rows for a persistent
+// kernel whose CTA b takes list items b, b + G, b + 2G, ...: order 1 reverses
+// every second round of G items (serpentine); order 2 gives each round's
+// items, heaviest first, to the CTAs with the least work so far (work of a
+// row: its blocks + 1). Both only permute items within a round. Returns false
+// unless the result is a permutation of the rows.
+static bool far_row_order(const std::vector<std::pair<int, int2>>& sorted, int G, int order, std::vector<int2>* out) {
+  const size_t n = sorted.size();
+  std::vector<long> pos(n, -1);  // list position of sorted item i
+  std::vector<long> load(G, 0);
+  std::vector<int> cta(G);
+  for (size_t r0 = 0; r0 < n; r0 += G) {
+    const int m = (int)std::min<size_t>(G, n - r0);
+    for (int j = 0; j < m; ++j) cta[j] = j;
+    if (order == 1) {
+      if ((r0 / G) % 2 == 1) std::reverse(cta.begin(), cta.begin() + m);
+    } else {
+      std::stable_sort(cta.begin(), cta.begin() + m, [&](int a, int b) { return load[a] < load[b]; });
+    }
+    for (int j = 0; j < m; ++j) {
+      pos[r0 + j] = (long)r0 + cta[j];
+      load[cta[j]] += sorted[r0 + j].first + 1;
+    }
+  }
+  out->assign(n, make_int2(-1, -1));
+  std::vector<char> used(n, 0);
+  for (size_t i = 0; i < n; ++i) {
+    if (pos[i] < 0 || pos[i] >= (long)n || used[pos[i]]) return false;
+    used[pos[i]] = 1;
+    (*out)[pos[i]] = sorted[i].second;
+  }
+  return true;
+}
+
 static bg_status upload_tables(bg_operator* op) {
   cudaStream_t s = op->ctx->stream;
   std::vector<int> meta;
@@ -400,6 +435,17 @@ static bg_status upload_tables(bg_operator* op) {
     for (size_t i = 0; i < items.size(); ++i) work[i] = items[i].second;
     BG_CHECK(op->d_far_work.upload(work, s), "far-field work list");
     op->n_far_work = (int)work.size();
+    // alternative orders for the persistent far-field kernels (one CTA per SM)
+    int nsm = 0;
+    BG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, op->ctx->device), "device attributes");
+    for (int o = 0; o < 2; ++o) op->d_far_work_alt[o].release();
+    if (nsm > 0 && (long)items.size() > nsm)
+      for (int o = 1; o <= 2; ++o) {
+        std::vector<int2> alt;
+        if (!far_row_order(items, nsm, o, &alt))
+          return set_error(op->ctx, BG_DEVICE_ERROR, "far-field schedule is not a permutation of the rows");
+        BG_CHECK(op->d_far_work_alt[o - 1].upload(alt, s), "far-field work list");
+      }
   }
   BG_CHECK(op->d_err.alloc(sizeof(int)), "error flag");
   BG_CHECK(cudaMemsetAsync(op->d_err.p, 0, sizeof(int), s), "error flag");
@@ -1072,13 +1118,14 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
   const size_t sfar = op->scalar_bytes(mixed);
   const int np2 = op->np * op->np;
   const long ss_n = (long)op->S * nrhs;
+  const bg_launch_plan pl = op->plan_for(nrhs, prec);
   bool any_far = false;
   for (const auto& f : op->far) any_far |= !f.col.empty();
   if (near32) {
     // FP32 near field into the FP32 accumulator the far field adds to
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp32(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense32.p,
-                        op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss32.p, op->w_yss32.p, nrhs, 0, s); }),
+                        op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss32.p, op->w_yss32.p, nrhs, 0, s, pl.near_kernel); }),
              "near-field product (FP32)");
   } else {
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
@@ -1119,14 +1166,14 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       for (int t = 0; t < 3; ++t)
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
                    return op->use_tgemm
-                              ? launch_tgemm(Sfar, t == 2, tm.a_mw_f[blk[t]], xin[t], op->Bq, yout[t], np2, nb[t], nrhs, s)
+                              ? launch_tgemm(Sfar, t == 2, tm.a_mw_f[blk[t]], xin[t], op->Bq, yout[t], np2, nb[t], nrhs, s, pl.split_k_batches)
                               : launch_moment_fwd_acc(Sfar, t == 2, mw_mom(blk[t]), np2, op->Bq, nb[t], xin[t],
                                                       yout[t], nrhs, s); }),
                  "forward moments");
       for (int l = Ll - 1; l >= 0; --l) {
         const int nb = 3 * op->nclusters(l);
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, op->w_y[l + 1]->p, 4L * np2, op->w_y[l]->p, np2, nb, nrhs, s)
+                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, op->w_y[l + 1]->p, 4L * np2, op->w_y[l]->p, np2, nb, nrhs, s, pl.split_k_batches)
                                         : launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, 1, nb,
                                                               op->w_y[l + 1]->p, op->w_y[l]->p, nrhs, s); }),
                  "forward transfer");
@@ -1137,7 +1184,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       const char* xc = c == 0 ? xc0 : xc1;
       char* yl = static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
       BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                 return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_mom_f[c], xc, op->Bq, yl, op->R, op->nleaf_cl, nrhs, s)
+                 return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_mom_f[c], xc, op->Bq, yl, op->R, op->nleaf_cl, nrhs, s, pl.split_k_batches)
                                       : launch_moment_fwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl, xc, yl, nrhs, s); }),
                "forward moments");
       for (int l = Ll - 1; l >= 0; --l) {
@@ -1145,7 +1192,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
         const char* ych = static_cast<const char*>(op->w_y[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar;
         char* ypa = static_cast<char*>(op->w_y[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, ych, 4L * op->R, ypa, op->R, ncl, nrhs, s)
+                   return op->use_tgemm ? launch_tgemm(Sfar, false, tm.a_tr_f, ych, 4L * op->R, ypa, op->R, ncl, nrhs, s, pl.split_k_batches)
                                         : launch_transfer_fwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
                                                               ych, ypa, nrhs, s); }),
                  "forward transfer");
@@ -1171,7 +1218,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       }
       BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
                "right-hand-side tiles");
-      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->d_far_work.as<int2>(), op->n_far_work,
+      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->far_work(pl.far_order), op->n_far_work,
                                                                        np2, nrhs, op->d_err.as<int>(), s); }),
                "far-field product (stored FP16 tiles, tensor cores)");
     } else if (tcc) {
@@ -1194,7 +1241,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       auto product = [&](int ld, int c0, int nc) -> bg_status {
         BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16c_btiles(T, nlev, np2, ld, c0, nc, s); }),
                  "right-hand-side tiles");
-        BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16c(T, op->d_far_work.as<int2>(), op->n_far_work,
+        BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16c(T, op->far_work(pl.far_order), op->n_far_work,
                                                                            np2, ld, c0, nc, op->d_err.as<int>(), s); }),
                  "far-field product (stored complex FP16 tiles, tensor cores)");
         return BG_OK;
@@ -1231,7 +1278,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
         L.y[l] = static_cast<const float*>(op->w_y[l]->p);
         L.z[l] = static_cast<float*>(op->w_z[l]->p);
       }
-      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_tc(L, op->d_far_work.as<int2>(), op->n_far_work, np2, nrhs,
+      BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_tc(L, op->far_work(pl.far_order), op->n_far_work, np2, nrhs,
                                                                       op->d_err.as<int>(), s); }),
                "far-field product (tensor cores)");
     }
@@ -1325,7 +1372,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       for (int l = 0; l < Ll; ++l) {
         const int nb = 3 * op->nclusters(l);
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, op->w_z[l]->p, np2, op->w_z[l + 1]->p, 4L * np2, nb, nrhs, s)
+                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, op->w_z[l]->p, np2, op->w_z[l + 1]->p, 4L * np2, nb, nrhs, s, pl.split_k_batches)
                                         : launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, 1, nb,
                                                               op->w_z[l]->p, op->w_z[l + 1]->p, nrhs, s); }),
                  "backward transfer");
@@ -1341,7 +1388,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       for (int t = 0; t < 3; ++t)
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
                    return op->use_tgemm
-                              ? launch_tgemm(Sfar, true, tm.a_mw_b[blk[t]], zin[t], np2, yout[t], op->Bq, nb[t], nrhs, s)
+                              ? launch_tgemm(Sfar, true, tm.a_mw_b[blk[t]], zin[t], np2, yout[t], op->Bq, nb[t], nrhs, s, pl.split_k_batches)
                               : launch_moment_bwd(Sfar, mw_mom(blk[t]), np2, op->Bq, nb[t], zin[t], yout[t], nrhs, s); }),
                  "backward moments");
     }
@@ -1351,7 +1398,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
         const char* zpa = static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;
         char* zch = static_cast<char*>(op->w_z[l + 1]->p) + (size_t)c * 4 * ncl * op->R * nrhs * sfar;
         BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, zpa, op->R, zch, 4L * op->R, ncl, nrhs, s)
+                   return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_tr_b, zpa, op->R, zch, 4L * op->R, ncl, nrhs, s, pl.split_k_batches)
                                         : launch_transfer_bwd(Sfar, mixed ? op->d_tr32.p : op->d_tr64.p, np2, op->nc, ncl,
                                                               zpa, zch, nrhs, s); }),
                  "backward transfer");
@@ -1360,7 +1407,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       const char* zl = static_cast<const char*>(op->w_z[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
       char* yc = static_cast<char*>(yfar) + c * comp_ss * nrhs * sfar;
       BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] {
-                 return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_mom_b[c], zl, op->R, yc, op->Bq, op->nleaf_cl, nrhs, s)
+                 return op->use_tgemm ? launch_tgemm(Sfar, true, tm.a_mom_b[c], zl, op->R, yc, op->Bq, op->nleaf_cl, nrhs, s, pl.split_k_batches)
                                       : launch_moment_bwd(Sfar, mom, op->R, op->Bq, op->nleaf_cl, zl, yc, nrhs, s); }),
                "backward moments");
     }
@@ -1388,7 +1435,7 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
   if (ctx->profiling || !op->use_graphs) {
     st = apply_middle(op, nrhs, prec);
   } else {
-    const long key = (long)nrhs * 4 + prec;
+    const long key = bg_operator::plan_key(nrhs, prec);
     auto it = op->graphs.find(key);
     if (it == op->graphs.end() && !op->graph_seen.count(key)) {
       // first product of this shape: direct launches (they also raise the
@@ -1443,6 +1490,130 @@ bg_status check_device_flag(bg_operator* op) {
   BG_CHECK(cudaMemset(op->d_err.p, 0, sizeof(int)), "error flag");
   return set_error(op->ctx, BG_TIMEOUT,
                    "a bounded wait of the tensor-core far-field kernel ran out (code " + std::to_string(code) + ")");
+}
+
+static bool valid_precision(int p) { return p == BG_PREC_FP64 || p == BG_PREC_MIXED || p == BG_PREC_FP32; }
+
+extern "C" bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precision, const bg_launch_plan* plan) {
+  if (!op || !plan) return BG_INVALID_ARG;
+  if (nrhs < 1 || !valid_precision(precision))
+    return set_error(op->ctx, BG_INVALID_ARG, "launch plan: nrhs must be positive and the precision a bg_precision");
+  if (plan->near_kernel < 0 || plan->near_kernel > 3 || plan->split_k_batches < -1 ||
+      plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2)
+    return set_error(op->ctx, BG_INVALID_ARG, "launch plan: a field is out of range");
+  op->plans[bg_operator::plan_key(nrhs, precision)] = *plan;
+  op->drop_graphs();
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_get_plan(const bg_operator* op, int nrhs, int precision, bg_launch_plan* plan) {
+  if (!op || !plan || nrhs < 1 || !valid_precision(precision)) return BG_INVALID_ARG;
+  *plan = op->plan_for(nrhs, precision);
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precision, int reps, bg_tune_report* report) {
+  if (!op || !report) return BG_INVALID_ARG;
+  bg_context* ctx = op->ctx;
+  if (nrhs < 1 || !valid_precision(precision) || reps < 0 || reps > 1000)
+    return set_error(ctx, BG_INVALID_ARG, "autotune: nrhs must be positive, reps in [0, 1000]");
+  if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context: the autotuner needs a GPU");
+  if (!op->assembled) return set_error(ctx, BG_INVALID_ARG, "autotune: the operator is not assembled");
+  if (reps == 0) reps = 5;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  bg_status st = ensure_work(op, nrhs);
+  if (st != BG_OK) return st;
+  // seeded superspace input in [-1, 1) (a 64-bit linear congruential generator)
+  std::vector<double> x((size_t)op->S * nrhs * (op->cplx ? 2 : 1));
+  uint64_t z = 0x2545F4914F6CDD1DULL;
+  for (double& v : x) {
+    z = z * 6364136223846793005ULL + 1442695040888963407ULL;
+    v = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  }
+  BG_CHECK(cudaMemcpyAsync(op->w_xss.p, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice, s),
+           "autotune input");
+  BG_CHECK(cudaStreamSynchronize(s), "autotune input");
+  struct Events {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~Events() {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+    }
+  } ev;
+  BG_CHECK(cudaEventCreate(&ev.a), "autotune events");
+  BG_CHECK(cudaEventCreate(&ev.b), "autotune events");
+  const long key = bg_operator::plan_key(nrhs, precision);
+  // the plan in force before tuning, put back if tuning fails
+  const auto prev = op->plans.find(key);
+  const bool had_plan = prev != op->plans.end();
+  const bg_launch_plan saved = had_plan ? prev->second : bg_operator::builtin_plan();
+  auto restore = [&] {
+    if (had_plan) op->plans[key] = saved;
+    else op->plans.erase(key);
+  };
+  // mean time of one product middle under plan p (after one untimed product,
+  // which also raises the kernels' shared-memory limits)
+  auto time_plan = [&](const bg_launch_plan& p, double* ms) -> bg_status {
+    op->plans[key] = p;
+    bg_status r = apply_middle(op, nrhs, precision);
+    if (r != BG_OK) return r;
+    BG_CHECK(cudaEventRecord(ev.a, s), "autotune events");
+    for (int i = 0; i < reps; ++i)
+      if ((r = apply_middle(op, nrhs, precision)) != BG_OK) return r;
+    BG_CHECK(cudaEventRecord(ev.b, s), "autotune events");
+    BG_CHECK(cudaEventSynchronize(ev.b), "autotune events");
+    if ((r = check_device_flag(op)) != BG_OK) return r;
+    float t = 0.0f;
+    BG_CHECK(cudaEventElapsedTime(&t, ev.a, ev.b), "autotune events");
+    *ms = (double)t / reps;
+    return BG_OK;
+  };
+  bg_launch_plan cur = bg_operator::builtin_plan();
+  double cur_ms = 0.0;
+  int count = 1;
+  if ((st = time_plan(cur, &cur_ms)) != BG_OK) {
+    restore();
+    return st;
+  }
+  const double builtin_ms = cur_ms;
+  // one knob at a time; a change is kept when it is at least 2 % faster
+  auto sweep = [&](int bg_launch_plan::*field, const std::vector<int>& values) -> bg_status {
+    const int start = cur.*field;
+    for (int v : values) {
+      if (v == start) continue;
+      bg_launch_plan p = cur;
+      p.*field = v;
+      double ms = 0.0;
+      bg_status r = time_plan(p, &ms);
+      if (r != BG_OK) return r;
+      ++count;
+      if (ms < 0.98 * cur_ms) {
+        cur = p;
+        cur_ms = ms;
+      }
+    }
+    return BG_OK;
+  };
+  const bool mixed = precision != BG_PREC_FP64, near32 = precision == BG_PREC_FP32;
+  if (near32) {
+    std::vector<int> v = {1, 2};
+    if (op->cplx && op->dense.B % 4 == 0) v.push_back(3);
+    st = sweep(&bg_launch_plan::near_kernel, v);
+  }
+  if (st == BG_OK && mixed && op->use_tgemm) st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
+  if (st == BG_OK && mixed && op->d_far_work_alt[0].p) st = sweep(&bg_launch_plan::far_order, {1, 2});
+  if (st != BG_OK) {
+    restore();
+    return st;
+  }
+  op->plans[key] = cur;
+  op->drop_graphs();
+  report->candidates = count;
+  report->builtin_ms = builtin_ms;
+  report->tuned_ms = cur_ms;
+  report->plan = cur;
+  return BG_OK;
 }
 
 static bg_status stage_host(bg_context* ctx, DevBuf* buf, const void* host, long ld, long rows, int ncols, size_t esz,

@@ -207,12 +207,15 @@ struct TGemmA {
   int ld, Mo, Ki;
 };
 // C[b] (=, += if acc) op(A) B[b] for nbatch items; B[b] = B + b * bstride_rows
-// rows of the vector type S (bg stype), C likewise; nrhs columns
+// rows of the vector type S (bg stype), C likewise; nrhs columns. FP32
+// launches of at most split_k_batches CTAs (-1: 152) use the split-K kernel.
 cudaError_t launch_tgemm(int S, bool acc, const TGemmA& A, const void* B, long bstride_rows, void* C,
-                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s);
-// FP32 / complex-FP32 blocks; same layout rules as launch_bsr_fp64
+                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s, int split_k_batches = -1);
+// FP32 / complex-FP32 blocks; same layout rules as launch_bsr_fp64. variant
+// (bg_launch_plan::near_kernel): 0 built-in, 1 pipelined, 2 register tiles
+// (complex: 2 rows per thread), 3 complex tiles of 4 rows
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
-                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s, int variant = 0);
 // out[b*sout + e] = (FP32) in[b*sin + e], e < B2, b < nblocks
 cudaError_t launch_convert_blocks(bool cplx, const void* in, long sin, void* out, long sout, long B2, long nblocks,
                                   cudaStream_t s);

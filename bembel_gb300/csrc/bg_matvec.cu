@@ -584,12 +584,13 @@ __global__ void __launch_bounds__(1024) k_tgemm_small(const float* __restrict__ 
 
 template <typename T>
 static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, T* C, long cstride, int nbatch, int kk,
-                           cudaStream_t s) {
+                           cudaStream_t s, int split_k_batches) {
   if constexpr (sizeof(T) == 4) {
     // coarse levels: fewer CTAs than SMs -> whole-operand staging and split K
     const long ctas = (long)nbatch * ((kk + 31) / 32);
+    const long split_max = split_k_batches < 0 ? 152 : split_k_batches;
     const int ntiles = ((A.Mo + 2) / 3) * 8;
-    if (nbatch > 0 && ctas <= 152 && ntiles <= 1024 && A.ld % 4 == 0 && A.ld >= (A.Mo + 2) / 3 * 3) {
+    if (nbatch > 0 && ctas <= split_max && ntiles <= 1024 && A.ld % 4 == 0 && A.ld >= (A.Mo + 2) / 3 * 3) {
       const int ksplit = std::max(1, std::min(8, 1024 / ntiles));
       const int threads = std::min(1024, (ntiles * ksplit + 31) / 32 * 32);
       const size_t smem = ((size_t)A.Ki * A.ld + (size_t)A.Ki * 32 + (size_t)(ksplit - 1) * ntiles * 12) * 4;
@@ -622,14 +623,14 @@ static cudaError_t tgemm_t(bool acc, const TGemmA& A, const T* B, long bstride, 
 }
 
 cudaError_t launch_tgemm(int S, bool acc, const TGemmA& A, const void* B, long bstride_rows, void* C,
-                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s) {
+                         long cstride_rows, int nbatch, int nrhs, cudaStream_t s, int split_k_batches) {
   // complex vectors are real matrices with 2 nrhs columns
   const int kk = (S & 1) ? 2 * nrhs : nrhs;
   if (S < 2)
     return tgemm_t<double>(acc, A, static_cast<const double*>(B), bstride_rows * kk, static_cast<double*>(C),
-                           cstride_rows * kk, nbatch, kk, s);
+                           cstride_rows * kk, nbatch, kk, s, split_k_batches);
   return tgemm_t<float>(acc, A, static_cast<const float*>(B), bstride_rows * kk, static_cast<float*>(C),
-                        cstride_rows * kk, nbatch, kk, s);
+                        cstride_rows * kk, nbatch, kk, s, split_k_batches);
 }
 
 // Fused FP32 far field: the coupling F_ij = k(x_i, y_j) |J_i| |J_j| is
@@ -1224,10 +1225,12 @@ __global__ void __launch_bounds__(256) k_bsr32c_tile(const int* __restrict__ row
 }
 
 cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows,
-                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
-  if (cplx && nrows > 0 && B % 2 == 0 && nrhs % 2 == 0 && bstride % 2 == 0 &&
+                            int B, const void* x, void* y, int nrhs, int accumulate, cudaStream_t s, int variant) {
+  if (variant != 1 && cplx && nrows > 0 && B % 2 == 0 && nrhs % 2 == 0 && bstride % 2 == 0 &&
       (reinterpret_cast<uintptr_t>(blocks) % 16) == 0 && (reinterpret_cast<uintptr_t>(x) % 16) == 0) {
-    const int rt = (B % 4 == 0 && (B / 4) * (nrhs / 2) >= 64) ? 4 : 2;
+    int rt = (B % 4 == 0 && (B / 4) * (nrhs / 2) >= 64) ? 4 : 2;
+    if (variant == 2) rt = 2;
+    if (variant == 3 && B % 4 == 0) rt = 4;
     const int nthr = (B / rt) * (nrhs / 2);
     const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float2);
     if (nthr <= 256 && smem <= 100 * 1024) {
@@ -1240,7 +1243,8 @@ cudaError_t launch_bsr_fp32(bool cplx, const int* row_ptr, const int* col, const
       return cudaGetLastError();
     }
   }
-  if (!cplx && nrows > 0 && B % 4 == 0 && nrhs % 4 == 0 && bstride % 4 == 0 && (B / 4) * (nrhs / 4) <= 128) {
+  if (variant != 1 && !cplx && nrows > 0 && B % 4 == 0 && nrhs % 4 == 0 && bstride % 4 == 0 &&
+      (B / 4) * (nrhs / 4) <= 128) {
     const size_t smem = (size_t)2 * (B * B + B * nrhs) * sizeof(float);
     if (smem <= 100 * 1024) {
       const int threads = (((B / 4) * (nrhs / 4)) + 31) / 32 * 32;

@@ -169,9 +169,16 @@ struct bg_operator {
   };
   TransformMats tm[2];
   bool use_tgemm = false;
-  // tensor-core far field: (level, row) work list, heaviest rows first
+  // tensor-core far field: (level, row) work list, heaviest rows first, and
+  // the two alternative orders of bg_launch_plan::far_order (built only when
+  // there are more rows than persistent CTAs)
   DevBuf d_far_work;
+  DevBuf d_far_work_alt[2];
   int n_far_work = 0;
+  const int2* far_work(int order) const {
+    if ((order == 1 || order == 2) && d_far_work_alt[order - 1].p) return d_far_work_alt[order - 1].as<int2>();
+    return d_far_work.as<int2>();
+  }
   DevBuf d_err;  // int: nonzero after a bounded device wait ran out
   // work vectors (sized for the largest nrhs seen)
   int cap = 0;
@@ -196,6 +203,15 @@ struct bg_operator {
       if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     graphs.clear();
     graph_seen.clear();
+  }
+
+  // launch plans per (nrhs, precision), keyed as the graphs
+  std::map<long, bg_launch_plan> plans;
+  static long plan_key(int nrhs, int prec) { return (long)nrhs * 4 + prec; }
+  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0}; }
+  bg_launch_plan plan_for(int nrhs, int prec) const {
+    auto it = plans.find(plan_key(nrhs, prec));
+    return it == plans.end() ? builtin_plan() : it->second;
   }
 
   // solver workspaces kept between bg_solve calls (owned by the solver)

@@ -205,6 +205,11 @@ def run_gpu(args):
     op.compute()
     asm = op.assembly_times()
     asm["wall_s"] = time.time() - t0
+    # launch plans of the 32-column products: built-in, or timed by the
+    # library's autotuner (outside the timed region)
+    plans = {"launch_plans": "built-in"}
+    if args.autotune:
+        plans = {"launch_plans": {p: op.autotune(NRHS, p) for p in ("fp32", "mixed")}}
     A = op.get_discrete_operator()
     N = op.N
     x0 = rhs_points()
@@ -311,7 +316,7 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
             "data": "synthetic (seeded point sources, sphere.dat geometry)",
             "config": workload_config({"parallelism": "replicas x%d" % world if world > 1 else "single gpu",
-                                       "inner_operator": INNER_DESC[inner]}),
+                                       "inner_operator": INNER_DESC[inner], **plans}),
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(N * NRHS * 8),
                     "d2h_bytes_per_step": int(N * NRHS * 8)},
             "gpu_launches": int(prof["launches_total"]) if prof else None,
@@ -768,6 +773,8 @@ def main():
     ap.add_argument("--max-level", type=int, default=4, help="serving: largest refinement level (2..6)")
     ap.add_argument("--fp64-requests", type=int, default=30, help="serving: requests replayed on the FP64 path")
     ap.add_argument("--workers", type=int, default=4, help="serving: worker streams of the server")
+    ap.add_argument("--autotune", action="store_true",
+                    help="laplace: set the 32-column products' launch plans with the autotuner first")
     args = ap.parse_args()
     if args.workload == "maxwell" and args.impl == "gb300" and not args.profile:
         run_maxwell(args)

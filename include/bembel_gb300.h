@@ -223,6 +223,44 @@ bg_status bg_operator_memory(const bg_operator* op, size_t* allocated, size_t* e
  * context still usable, BG_OK if the wait completed. */
 bg_status bg_watchdog_selftest(bg_context* ctx, long long limit_cycles);
 
+/* ---- launch plans and the autotuner (no reference counterpart) ----
+ * A launch plan fixes the kernel variants and schedules of the H2 product for
+ * one (number of right-hand sides, precision). Products with no plan set use
+ * the built-in choices ({0, -1, 0}). The FP64 product has no choices. */
+typedef struct bg_launch_plan {
+  /* FP32 near field (BG_PREC_FP32): 0 built-in choice; 1 the pipelined block
+   * kernel; 2 register tiles (complex: 2 block rows per thread); 3 complex
+   * register tiles of 4 block rows. A variant the block shape does not allow
+   * falls back to the built-in choice. */
+  int near_kernel;
+  /* FP32 transforms: launches of at most this many CTAs (batch items x
+   * 32-column panels) use the split-K kernel; -1 built-in (152), 0 never. */
+  int split_k_batches;
+  /* order of the far-field rows over the persistent CTAs, which take items
+   * b, b + G, b + 2G, ...: 0 heaviest first; 1 heaviest first with every
+   * second round reversed; 2 heaviest first, each round's items to the CTAs
+   * with the least work so far. Results are identical for every order. */
+  int far_order;
+} bg_launch_plan;
+
+typedef struct bg_tune_report {
+  int candidates;        /* plans timed */
+  double builtin_ms;     /* product between T x and T^T y, built-in plan */
+  double tuned_ms;       /* the same with the chosen plan */
+  bg_launch_plan plan;   /* the chosen plan (now set on the operator) */
+} bg_tune_report;
+
+/* Set / read the plan of products with nrhs right-hand sides at precision.
+ * Setting a plan drops the operator's captured CUDA graphs. */
+bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precision, const bg_launch_plan* plan);
+bg_status bg_operator_get_plan(const bg_operator* op, int nrhs, int precision, bg_launch_plan* plan);
+
+/* Autotuner: times the product (between T x and T^T y) on seeded inputs with
+ * CUDA events, reps products per candidate (0: 5), one knob at a time from
+ * the built-in plan, keeps a change only when it is at least 2 % faster, and
+ * sets the chosen plan. Needs an assembled operator on a device context. */
+bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precision, int reps, bg_tune_report* report);
+
 /* ---- serving loop ----
  * No counterpart in the reference (its examples assemble one operator and
  * solve once). A server owns worker threads on the context's GPU, a queue of

@@ -146,3 +146,28 @@ def test_watchdog_selftest_needs_a_gpu(bg_host):
     bg, ctx = bg_host
     assert _lib.load().bg_watchdog_selftest(ctx.h, 1000) == _lib.BG_UNSUPPORTED
     assert _lib.load().bg_watchdog_selftest(ctx.h, 0) == _lib.BG_INVALID_ARG
+
+
+def test_launch_plans_round_trip_and_validation(bg_host):
+    """Launch plans are operator state keyed by (nrhs, precision): unset keys
+    read as the built-in plan, out-of-range fields are refused, and the
+    autotuner itself needs a device."""
+    from bembel_gb300 import BembelError, _lib
+    bg, ctx = bg_host
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 2, 2), bg.LaplaceSingleLayerOperator())
+    builtin = {"near_kernel": 0, "split_k_batches": -1, "far_order": 0}
+    assert d.get_plan(32, "mixed") == builtin
+    d.set_plan(32, "fp32", near_kernel=2, split_k_batches=608, far_order=2)
+    assert d.get_plan(32, "fp32") == {"near_kernel": 2, "split_k_batches": 608, "far_order": 2}
+    assert d.get_plan(32, "mixed") == builtin and d.get_plan(16, "fp32") == builtin
+    for bad in ({"near_kernel": 4}, {"near_kernel": -1}, {"split_k_batches": -2}, {"far_order": 3}):
+        with pytest.raises(BembelError):
+            d.set_plan(8, "mixed", **bad)
+    with pytest.raises(BembelError):
+        d.set_plan(0, "mixed")
+    with pytest.raises(BembelError):
+        d.get_plan(8, "fp16")
+    assert d.get_plan(8, "mixed") == builtin
+    with pytest.raises(BembelError) as e:
+        d.autotune(32, "mixed")
+    assert e.value.status == _lib.BG_UNSUPPORTED

@@ -10,7 +10,8 @@ must not change across calls once the first call on the device has looked up
 the fixed scratch array. An operator whose intermediate vectors exceed the
 16 MiB array is rejected with BG_INVALID_ARG and a message naming the size.
 
-This file is collected last on purpose; it must also pass alone.
+This file is collected after the other product tests on purpose; it must
+also pass alone.
 """
 import ctypes
 
