@@ -133,12 +133,6 @@ __global__ void k_residual(const S* __restrict__ b, long n, S* __restrict__ r) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) r[t] = sub(b[t], r[t]);
 }
-template <typename S>
-__global__ void k_axpy(S* __restrict__ x, const S* __restrict__ d, long n) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) x[t] = addv(x[t], d[t]);
-}
-
 inline unsigned nblk(long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
