@@ -69,6 +69,9 @@ def lib():
         L.orc_create_sampled.argtypes = [ctypes.c_char_p, I, I, I, D, D, I, D, I, I]
         L.orc_last_product_split.argtypes = [P, dp]
         L.orc_threads.restype = I
+        L.orc_projector_csr.argtypes = [P, lp, ip, ip, dp]
+        L.orc_bernstein.restype = D
+        L.orc_bernstein.argtypes = [I, dp, D, I]
         _lib = L
     return _lib
 
@@ -79,6 +82,12 @@ def _dp(a):
 
 def _ip(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def bernstein(p, coefs, x, der=False):
+    """sum_i coefs[i] B_{i,p}(x) (or its derivative) in the Bernstein basis."""
+    c = np.ascontiguousarray(np.asarray(coefs, dtype=np.float64)[:p + 1])
+    return lib().orc_bernstein(p, _dp(c), float(x), int(der))
 
 
 def transfer_matrices(np_):
@@ -160,6 +169,21 @@ class Problem:
         val = np.zeros(self.nnz)
         lib().orc_transform_csr(self.h, _ip(ptr), _ip(idx), _dp(val))
         return ptr, idx, val
+
+    def projector_dense(self):
+        """The Projector matrix before gluing (Projector.hpp:52-90)."""
+        dims = np.zeros(3, dtype=np.int64)
+        lp = ctypes.POINTER(ctypes.c_long)
+        lib().orc_projector_csr(self.h, dims.ctypes.data_as(lp), None, None, None)
+        rows, cols, nnz = (int(v) for v in dims)
+        ptr = np.zeros(rows + 1, dtype=np.int32)
+        idx = np.zeros(nnz, dtype=np.int32)
+        val = np.zeros(nnz)
+        lib().orc_projector_csr(self.h, dims.ctypes.data_as(lp), _ip(ptr), _ip(idx), _dp(val))
+        T = np.zeros((rows, cols))
+        for r in range(rows):
+            T[r, idx[ptr[r]:ptr[r + 1]]] += val[ptr[r]:ptr[r + 1]]
+        return T
 
     def transform_dense(self):
         ptr, idx, val = self.transform_csr()

@@ -489,6 +489,17 @@ void* orc_create(const char* geo, int M, int P, int kind, double kre, double kim
 }
 void orc_destroy(void* h) { delete static_cast<Problem*>(h); }
 
+// sum_i coefs[i] B_{i,p}(x) or its derivative in x (Spline/Bernstein.hpp,
+// Basis::ShapeFunctionHandler::evalCoef / evalDerCoef)
+double orc_bernstein(int p, const double* coefs, double x, int der) {
+  std::vector<double> b(p + 1);
+  if (der) bernstein_der_basis(p, x, b.data());
+  else bernstein_basis(p, x, b.data());
+  double r = 0;
+  for (int i = 0; i <= p; ++i) r += coefs[i] * b[i];
+  return r;
+}
+
 // As orc_create with assembly, but only every leaf_stride-th leaf of the block
 // partition is assembled (a bounded sample of the H2 matrix for CPU timing).
 void* orc_create_sampled(const char* geo, int M, int P, int kind, double kre, double kim, int np, double eta, int mcl,
@@ -529,6 +540,20 @@ void orc_transform_csr(void* h, int* ptr, int* idx, double* val) {
 }
 
 // per element: patch, level, id, llc0, llc1, vertices[4], mid[3], radius
+// the Projector matrix alone (no gluing): dims[0..2] = rows, cols, nnz; the
+// CSR arrays are written when ptr is not null
+void orc_projector_csr(void* h, long* dims, int* ptr, int* idx, double* val) {
+  Problem& p = *static_cast<Problem*>(h);
+  const Sparse P = projector_matrix(p.ss, p.op.kind == kDummy ? kLaplace : p.op.kind);
+  dims[0] = P.rows;
+  dims[1] = P.cols;
+  dims[2] = (long)P.val.size();
+  if (!ptr) return;
+  std::copy(P.ptr.begin(), P.ptr.end(), ptr);
+  std::copy(P.idx.begin(), P.idx.end(), idx);
+  std::copy(P.val.begin(), P.val.end(), val);
+}
+
 void orc_elements(void* h, int* ints, double* dbl) {
   Problem& p = *static_cast<Problem*>(h);
   for (int e = 0; e < p.ss.ne(); ++e) {

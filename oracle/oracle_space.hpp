@@ -279,8 +279,10 @@ inline Sparse glue_divconforming(const SuperSpace& ss, int rep, int pre_dofs) {
   return Sparse::from_triplets(pre_dofs, post, t);
 }
 
-// AnsatzSpace::init_AnsatzSpace (AnsatzSpace.hpp:102-111), knot repetition 1
-inline Sparse transformation_matrix(const SuperSpace& ss, int kind, int rep = 1) {
+// Projector::get_projection_matrix (Projector.hpp:52-90): the spline space of
+// every patch in the superspace, before any gluing; div-conforming: the two
+// components (degrees (P+1, P) and (P, P+1) per direction) stacked
+inline Sparse projector_matrix(const SuperSpace& ss, int kind, int rep = 1) {
   const int P = ss.P;
   if (kind != kMaxwell) {
     ProjInfo pi = local_projection(ss, P + 1, P + 1, rep);
@@ -290,7 +292,13 @@ inline Sparse transformation_matrix(const SuperSpace& ss, int kind, int rep = 1)
   ProjInfo b = local_projection(ss, P, P + 1, rep);
   std::vector<Triplet> t = a.t;
   for (auto x : b.t) t.push_back({x.r + a.num_dc_dof, x.c + a.num_c_dof, x.v});
-  Sparse proj = Sparse::from_triplets(a.num_dc_dof + b.num_dc_dof, a.num_c_dof + b.num_c_dof, t);
+  return Sparse::from_triplets(a.num_dc_dof + b.num_dc_dof, a.num_c_dof + b.num_c_dof, t);
+}
+
+// AnsatzSpace::init_AnsatzSpace (AnsatzSpace.hpp:102-111), knot repetition 1
+inline Sparse transformation_matrix(const SuperSpace& ss, int kind, int rep = 1) {
+  Sparse proj = projector_matrix(ss, kind, rep);
+  if (kind != kMaxwell) return proj;
   Sparse g = glue_divconforming(ss, rep, proj.cols);
   return proj.mul(g);
 }

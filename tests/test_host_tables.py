@@ -53,6 +53,22 @@ def test_tables_match_oracle(bg_host, oracle, geo, M, P):
     assert np.abs(a[2] - b[2]).max() < 1e-13
 
 
+@pytest.mark.parametrize("geo,M,P", [(SPHERE, 1, 1), (SPHERE, 2, 2), (TORUS, 1, 3), ("screen", 1, 2), ("screen", 2, 1)])
+def test_divconforming_transform_matches_oracle(bg_host, oracle, screen_path, geo, M, P):
+    """Maxwell's T = Projector * Glue (div-conforming gluing across patch
+    edges, boundary functions of an open surface dropped), against the oracle."""
+    bg, ctx = bg_host
+    geo = screen_path if geo == "screen" else geo
+    lin = bg.MaxwellSingleLayerOperator()
+    lin.set_wavenumber(1.0)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(geo, ctx), M, P), lin, n_p=4)
+    o = oracle.Problem(geo, M, P, oracle.MAXWELL, kappa=1.0, np_=4, assemble=False)
+    assert (d.N, d.S) == (o.N, o.S)
+    a, b = d.transform_csr(), o.transform_csr()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.abs(a[2] - b[2]).max() < 1e-13
+
+
 def test_surface_point_matches_oracle(bg_host, oracle):
     bg, ctx = bg_host
     g = bg.Geometry(SPHERE, ctx)

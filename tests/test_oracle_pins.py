@@ -169,6 +169,53 @@ def test_h2_vs_dense_maxwell(oracle):
     assert np.linalg.norm(p.matvec(a) - D @ a) < 1e-8 * max(1.0, np.linalg.norm(D @ a))
 
 
+EQ_POINTS = [0.1 * i for i in range(11)]  # tests/Test.hpp:35
+
+
+def test_bernstein_matches_de_boor(oracle):
+    """tests/test_Bernstein.cpp: sum_i c_i B_{i,p}(x) with c_i = (i + 1) / 21
+    equals de Boor's evaluation of the spline with the same coefficients on
+    the Bezier knot vector, p = 0..20 (derivatives p = 1..20), at the 11
+    equispaced points, to 1e-6 (coefficient_accuracy, tests/Test.hpp:39).
+    scipy's BSpline is the independent de Boor evaluation."""
+    BSpline = pytest.importorskip("scipy.interpolate").BSpline
+    maxp = 20
+    coefs = [(i + 1) / (maxp + 1) for i in range(maxp + 1)]
+    for p in range(maxp + 1):
+        spl = BSpline(np.r_[np.zeros(p + 1), np.ones(p + 1)], np.array(coefs[:p + 1]), p)
+        der = spl.derivative() if p >= 1 else None
+        for x in EQ_POINTS:
+            assert abs(oracle.bernstein(p, coefs, x) - float(spl(x))) < 1e-6
+            if der is not None:
+                assert abs(oracle.bernstein(p, coefs, x, der=True) - float(der(x))) < 1e-6
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("m", [0, 1, 2])
+def test_projector_counts_and_partition_of_unity(oracle, screen_path, p, m):
+    """tests/test_Projector.cpp on the unit-square screen with knot
+    repetition 1: the superspace has (p+1)^2 4^m functions per component; the
+    spline space (p + 2^m)^2 (scalar, discontinuous form) or
+    2 (p + 2^m)(p - 1 + 2^m) (div-conforming); T maps the all-ones
+    coefficients to all ones (partition of unity, 1e-6 there). On a single
+    patch the scalar T is this projector; the div-conforming T glues it and,
+    on the open screen, drops the functions whose normal component does not
+    vanish on the boundary."""
+    n = 1 << m
+    for kind, kappa, rows, cols in ((oracle.LAPLACE, 0.0, (p + 1) ** 2 * n * n, (p + n) ** 2),
+                                    (oracle.MAXWELL, 1.0, 2 * (p + 1) ** 2 * n * n, 2 * (p + n) * (p - 1 + n))):
+        pr = oracle.Problem(screen_path, m, p, kind, kappa=kappa, np_=4, assemble=False)
+        Pm = pr.projector_dense()
+        assert Pm.shape == (rows, cols)
+        assert np.max(np.abs(Pm @ np.ones(cols) - 1.0)) < 1e-12
+        if kind == oracle.LAPLACE:
+            assert np.array_equal(pr.transform_dense(), Pm)
+        else:
+            # each component loses the 2 (p - 1 + n) functions whose normal
+            # component is nonzero on one of its two boundary edges
+            assert pr.transform_dense().shape == (rows, cols - 4 * (p - 1 + n))
+
+
 def test_partition_counts(oracle):
     """Block partition of the sphere, M = 3 (eta = 1.6, min cluster level 1)."""
     p = oracle.Problem(SPHERE, 3, 1, oracle.LAPLACE, np_=6, assemble=False)
