@@ -1,6 +1,7 @@
-// Serving loop over the C ABI: a request queue drained by one worker thread
-// on the context's GPU, batching of requests that share an operator, and a
-// cache of assembled operators with admission by device memory.
+// Serving loop over the C ABI: a request queue drained by worker threads on
+// the context's GPU (each with its own context and stream), batching of
+// requests that share an operator, and per-worker caches of assembled
+// operators with admission by device memory.
 //
 // The reference has no serving layer (its examples assemble once and solve
 // once); this file is the runtime around the operator for a stream of solves
@@ -13,6 +14,9 @@
 #include <list>
 #include <map>
 #include <mutex>
+#include <new>
+#include <set>
+#include <system_error>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -79,7 +83,8 @@ struct bg_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Job> queue;
-  std::map<long, bg_request_result> done;
+  std::set<long> pending;                  // submitted, result not yet posted
+  std::map<long, bg_request_result> done;  // posted, not yet collected by bg_server_wait
   long next_ticket = 1;
   bool stop = false;
   bg_server_stats st{};
@@ -181,6 +186,7 @@ struct bg_server {
       r.stats = stats;
       std::strncpy(r.error, msg.c_str(), sizeof(r.error) - 1);
       done[j.ticket] = r;
+      pending.erase(j.ticket);
       ++(status == BG_OK || status == BG_NOT_CONVERGED ? st.completed : st.failed);
     }
     ++st.batches;
@@ -285,13 +291,18 @@ extern "C" {
 bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers, bg_server** out) {
   if (!ctx || !out || hbm_budget_bytes == 0 || workers < 1 || workers > 16) return BG_INVALID_ARG;
   if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context: the server needs a GPU");
-  bg_server* s = new bg_server();
+  bg_server* s = new (std::nothrow) bg_server();
+  if (!s) return BG_OOM;
   s->ctx = ctx;
   s->budget = hbm_budget_bytes;
   s->st.bytes_budget = hbm_budget_bytes;
   s->t0 = std::chrono::steady_clock::now();
   for (int i = 0; i < workers; ++i) {
-    Worker* w = new Worker();
+    Worker* w = new (std::nothrow) Worker();
+    if (!w) {
+      bg_server_destroy(s);
+      return BG_OOM;
+    }
     w->id = i;
     w->budget = hbm_budget_bytes / workers;
     bg_status st = bg_context_create(ctx->device, &w->ctx);
@@ -302,7 +313,12 @@ bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers
     }
     s->workers.push_back(w);
   }
-  for (Worker* w : s->workers) w->th = std::thread([s, w] { s->run(*w); });
+  try {
+    for (Worker* w : s->workers) w->th = std::thread([s, w] { s->run(*w); });
+  } catch (const std::system_error&) {
+    bg_server_destroy(s);  // joins the workers already started
+    return set_error(ctx, BG_OOM, "server worker threads could not be started");
+  }
   *out = s;
   return BG_OK;
 }
@@ -337,18 +353,21 @@ bg_status bg_server_submit(bg_server* srv, const bg_request* req, long* ticket) 
   if (!srv || !req || !ticket || !req->data || !req->x || req->nrhs < 1 || req->nrhs > 32 || !(req->tol > 0.0))
     return BG_INVALID_ARG;
   const int npr = req->data_kind == 3 ? 6 : 3;
-  Job j;
-  j.req = *req;
-  j.data.assign(req->data, req->data + (size_t)npr * req->nrhs);
-  {
+  try {
+    Job j;
+    j.req = *req;
+    j.data.assign(req->data, req->data + (size_t)npr * req->nrhs);
     std::lock_guard<std::mutex> lk(srv->mu);
     if (srv->stop) return BG_CANCELLED;
     if (req->geometry < 0 || req->geometry >= (int)srv->geos.size()) return BG_INVALID_ARG;
     j.ticket = srv->next_ticket++;
     j.t_submit = srv->now();
-    *ticket = j.ticket;
-    ++srv->st.submitted;
+    srv->pending.insert(j.ticket);
     srv->queue.push_back(std::move(j));
+    *ticket = srv->next_ticket - 1;
+    ++srv->st.submitted;
+  } catch (const std::bad_alloc&) {
+    return BG_OOM;
   }
   srv->cv_work.notify_all();  // the worker of this request's shard may be any of them
   return BG_OK;
@@ -357,6 +376,8 @@ bg_status bg_server_submit(bg_server* srv, const bg_request* req, long* ticket) 
 bg_status bg_server_wait(bg_server* srv, long ticket, double timeout_s, bg_request_result* out) {
   if (!srv || !out) return BG_INVALID_ARG;
   std::unique_lock<std::mutex> lk(srv->mu);
+  // a ticket never issued, or already collected, would never complete
+  if (!srv->pending.count(ticket) && !srv->done.count(ticket)) return BG_INVALID_ARG;
   auto ready = [&] { return srv->done.count(ticket) != 0; };
   if (timeout_s < 0) {
     srv->cv_done.wait(lk, ready);

@@ -309,11 +309,14 @@ typedef struct {
  * ctx's device and budget / workers bytes; operators are sharded over them by
  * key, so solves on different operators overlap on the GPU */
 bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers, bg_server** out);
-/* stops the worker after the queue drains and frees every cached operator */
+/* stops the workers after the queue drains and frees every cached operator;
+ * no other thread may be inside a bg_server_* call on srv meanwhile */
 bg_status bg_server_destroy(bg_server* srv);
 bg_status bg_server_add_geometry(bg_server* srv, const bg_geometry* g, int* index);
 bg_status bg_server_submit(bg_server* srv, const bg_request* req, long* ticket);
-/* blocks until the request is done (timeout_s < 0: no limit; BG_TIMEOUT when it runs out) */
+/* blocks until the request is done (timeout_s < 0: no limit; BG_TIMEOUT when
+ * it runs out) and collects its result; a ticket that was never issued or was
+ * already collected returns BG_INVALID_ARG */
 bg_status bg_server_wait(bg_server* srv, long ticket, double timeout_s, bg_request_result* out);
 bg_status bg_server_stats_get(bg_server* srv, bg_server_stats* out);
 

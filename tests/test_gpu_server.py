@@ -1,6 +1,8 @@
 """Serving loop (bg_server_*): requests on different operators, batching,
 eviction under a small memory budget and admission failure, checked by the
 FP64 residual of every served solution."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -49,6 +51,11 @@ def test_server_solves_and_batches(ctx):
     tickets = [srv.submit(gs[g], kind, M, P, dk, data, kappa=k) for g, _, kind, M, P, k, dk, data in cases]
     out = [srv.wait(t, timeout=300) for t in tickets]
     st = srv.stats()
+    # collected and never-issued tickets are refused instead of waiting forever
+    from bembel_gb300 import _lib
+    for t in (tickets[0], max(tickets) + 1000):
+        r = _lib.RequestResult()
+        assert _lib.load().bg_server_wait(srv.h, t, -1.0, ctypes.byref(r)) == _lib.BG_INVALID_ARG
     srv.close()
     assert st["completed"] == len(cases) and st["failed"] == 0, [(i["status"], i["error"]) for _, i in out]
     assert st["cache_misses"] == 3  # three distinct operators
