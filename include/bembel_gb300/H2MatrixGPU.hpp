@@ -172,6 +172,21 @@ class Operator {
     detail::check(bg_solve(h_.get(), b, x, nrhs, params, &st, on_device ? 1 : 0), ctx());
     return st;
   }
+  // launch plan of products with nrhs columns at precision; autotune() times
+  // the variants on the GPU and sets the fastest plan
+  void set_plan(int nrhs, int precision, const bg_launch_plan& plan) {
+    detail::check(bg_operator_set_plan(h_.get(), nrhs, precision, &plan), ctx());
+  }
+  bg_launch_plan plan(int nrhs, int precision) const {
+    bg_launch_plan p{};
+    detail::check(bg_operator_get_plan(h_.get(), nrhs, precision, &p), ctx());
+    return p;
+  }
+  bg_tune_report autotune(int nrhs, int precision, int reps = 0) {
+    bg_tune_report r{};
+    detail::check(bg_operator_autotune(h_.get(), nrhs, precision, reps, &r), ctx());
+    return r;
+  }
   bg_operator* get() const { return h_.get(); }
   bg_context* ctx() const { return geo_.context().get(); }
 

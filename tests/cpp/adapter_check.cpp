@@ -63,6 +63,18 @@ int main(int argc, char** argv) {
     threw = e.status() == BG_INVALID_ARG && std::string(e.what()).find("weight") != std::string::npos;
   }
   if (!threw) return fail("invalid weight not reported");
+  // launch plans are operator state: set, read back, refused when out of range
+  A.set_plan(32, BG_PREC_FP32, bg_launch_plan{2, 608, 1});
+  const bg_launch_plan lp = A.plan(32, BG_PREC_FP32);
+  if (lp.near_kernel != 2 || lp.split_k_batches != 608 || lp.far_order != 1) return fail("launch plan round trip");
+  if (A.plan(32, BG_PREC_MIXED).split_k_batches != -1) return fail("built-in plan");
+  threw = false;
+  try {
+    A.set_plan(32, BG_PREC_FP32, bg_launch_plan{0, -1, 3});
+  } catch (const Error& e) {
+    threw = e.status() == BG_INVALID_ARG;
+  }
+  if (!threw) return fail("invalid launch plan not reported");
   if (gpu) {
     Operator<double> B(h, 2, 1, BG_LAPLACE_SL);
     B.assemble();
