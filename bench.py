@@ -114,7 +114,7 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(threads=None):
+def cpu_sample(warmup=1, steps=None):
     """Time the CPU oracle's H2 product on a bounded sample of the workload.
 
     The oracle (a restatement of the reference's OpenMP algorithm) assembles
@@ -122,7 +122,8 @@ def cpu_sample(threads=None):
     right-hand side (the reference applies right-hand sides one at a time,
     H2DenseProduct.hpp:50) and the leaf-loop time is scaled by
     total/sampled matrix entries. A solve costs FP64_ITERS_C2 products of
-    NRHS right-hand sides."""
+    NRHS right-hand sides. warmup untimed products, then steps timed ones
+    (None: up to 20 within 20 s); the median is reported."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -130,10 +131,11 @@ def cpu_sample(threads=None):
     p = oracle.Problem(GEO, M, P, oracle.LAPLACE, np_=NP, leaf_stride=40)
     t_asm = time.time() - t0
     x = np.random.default_rng(0).uniform(-1, 1, p.N)
-    p.matvec(x)
+    for _ in range(max(0, warmup)):
+        p.matvec(x)
     reps = []
     t1 = time.time()
-    while len(reps) < 20 and time.time() - t1 < 20:
+    while (len(reps) < steps) if steps else (len(reps) < 20 and time.time() - t1 < 20):
         p.matvec(x)
         reps.append(p.last_product_split())
     r = np.median(np.array(reps), axis=0)
@@ -153,9 +155,11 @@ def run_reference(args):
     if rank != 0:
         return
     t0 = time.time()
-    base = cpu_sample()
-    line = {"metric": METRIC, "value": base["value"], "unit": "solves/s", "n_gpus": args.gpus, "steps": 1,
-            "warmup": 0, "ms_per_step": 1e3 * NRHS / base["value"], "higher_is_better": True, "scaling": "weak",
+    # each step: one sampled product, extrapolated to a 32-RHS solve
+    base = cpu_sample(warmup=args.warmup, steps=max(1, args.steps))
+    line = {"metric": METRIC, "value": base["value"], "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": max(1, args.steps), "warmup": args.warmup, "ms_per_step": 1e3 * NRHS / base["value"],
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded point sources on sphere.dat)",
             "impl": "reference", "config": workload_config({"parallelism": "cpu openmp"}),
             "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},

@@ -49,3 +49,24 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch, capsys):
         gpus, steps, warmup = 2, 1, 0
     bench.run_reference(Args())
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line():
+    """bench.py --impl reference: one JSON line with the arm's metric, the
+    steps and warm-up it was given, the CPU baseline it measured and an e2e
+    block without host-device copies (about 20 s on 8 cores)."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    j = json.loads(lines[0])
+    assert j["impl"] == "reference" and j["unit"] == "solves/s" and j["higher_is_better"] is True
+    assert j["steps"] == 2 and j["warmup"] == 1 and j["value"] > 0
+    assert j["cpu_baseline"]["value"] == j["value"] and j["cpu_baseline"]["cores"] >= 1
+    assert j["cpu_baseline"]["kind"] == "port" and j["cpu_baseline"]["sample"]
+    assert j["e2e"] == {"value": j["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert j["config"]["workload"] == "laplace_sl_h2_sphere_M5_P2_np9_32rhs"
