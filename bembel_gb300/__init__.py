@@ -140,6 +140,12 @@ def _is_torch(x):
     return type(x).__module__.startswith("torch")
 
 
+def _columns(a, n):
+    """a (a vector or an n x k block, k = 0 allowed) as n x k."""
+    size = a.numel() if _is_torch(a) else a.size
+    return a.reshape(n, size // n if n else 0)
+
+
 def _prec_code(precision):
     if precision not in _lib.PRECISIONS:
         raise BembelError(_lib.BG_INVALID_ARG, "precision must be one of %s" % sorted(_lib.PRECISIONS))
@@ -186,8 +192,8 @@ class H2Matrix:
         if _is_torch(x):
             import torch
             squeeze = x.dim() == 1
-            X = (x.reshape(N, -1)).t().contiguous()  # (nrhs, N): column-major N x nrhs
-            Y = torch.empty_like(X) if out is None else out.reshape(N, -1).t().contiguous()
+            X = (_columns(x, N)).t().contiguous()  # (nrhs, N): column-major N x nrhs
+            Y = torch.empty_like(X) if out is None else _columns(out, N).t().contiguous()
             on_dev = 1 if X.is_cuda else 0
             if not on_dev:
                 raise BembelError(_lib.BG_INVALID_ARG, "pass numpy arrays for host memory")
@@ -198,8 +204,8 @@ class H2Matrix:
             return Y.reshape(N) if squeeze else Y
         x = np.asarray(x, dtype=self.dtype)
         squeeze = x.ndim == 1
-        X = np.asfortranarray(x.reshape(N, -1))
-        Y = np.zeros_like(X, order="F") if out is None else np.asfortranarray(np.asarray(out, self.dtype).reshape(N, -1))
+        X = np.asfortranarray(_columns(x, N))
+        Y = np.zeros_like(X, order="F") if out is None else np.asfortranarray(_columns(np.asarray(out, self.dtype), N))
         self._dop.ctx.check(_lib.load().bg_matvec(self.h, X.ctypes.data_as(ctypes.c_void_p), N,
                                                   Y.ctypes.data_as(ctypes.c_void_p), N, X.shape[1], _dp(a), _dp(b),
                                                   prec, 0))
@@ -219,7 +225,7 @@ class H2Matrix:
         if _is_torch(b):
             import torch
             squeeze = b.dim() == 1
-            B = b.reshape(N, -1).t().contiguous()
+            B = _columns(b, N).t().contiguous()
             X = torch.empty_like(B) if B.is_cuda else torch.empty(B.shape, dtype=B.dtype, pin_memory=B.is_pinned())
             status = _lib.load().bg_solve(self.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
                                           B.shape[0], ctypes.byref(p), ctypes.byref(st), 1 if B.is_cuda else 0)
@@ -228,7 +234,7 @@ class H2Matrix:
         else:
             b = np.asarray(b, dtype=self.dtype)
             squeeze = b.ndim == 1
-            B = np.asfortranarray(b.reshape(N, -1))
+            B = np.asfortranarray(_columns(b, N))
             X = np.zeros_like(B, order="F")
             status = _lib.load().bg_solve(self.h, B.ctypes.data_as(ctypes.c_void_p), X.ctypes.data_as(ctypes.c_void_p),
                                           B.shape[1], ctypes.byref(p), ctypes.byref(st), 0)
@@ -312,7 +318,7 @@ class DiscreteOperator:
     def potential(self, rho, points):
         """DiscretePotential::evaluate at points (npts, 3) for densities rho
         (N, nrhs): (npts, nrhs); Maxwell: the field, (npts, 3, nrhs)."""
-        rho = np.asfortranarray(np.asarray(rho, dtype=np.complex128 if self.is_complex else np.float64).reshape(self.N, -1))
+        rho = np.asfortranarray(_columns(np.asarray(rho, dtype=np.complex128 if self.is_complex else np.float64), self.N))
         pts = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
         k = rho.shape[1]
         if self.lin_op.kind == _lib.MAXWELL_SL:

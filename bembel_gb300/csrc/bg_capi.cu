@@ -1627,7 +1627,9 @@ static bg_status stage_host(bg_context* ctx, DevBuf* buf, const void* host, long
 
 extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
                                const double* alpha, const double* beta, int precision, int on_device) {
-  if (!op || !x || !y || nrhs <= 0 || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
+  if (!op || nrhs < 0) return BG_INVALID_ARG;
+  if (nrhs == 0) return BG_OK;  // no columns: nothing to do (as Eigen's empty product)
+  if (!x || !y || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
   if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
   if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED && precision != BG_PREC_FP32)

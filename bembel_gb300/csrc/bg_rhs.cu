@@ -374,7 +374,9 @@ cudaError_t launch_potential(int P, bool cplx, const d4* tab, int ne, int Q, con
 }  // namespace
 
 extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device) {
-  if (!op || !prm || !out || nrhs <= 0 || kind < 0 || kind > 3) return BG_INVALID_ARG;
+  if (!op || nrhs < 0 || kind < 0 || kind > 3) return BG_INVALID_ARG;
+  if (nrhs == 0) return BG_OK;  // no columns
+  if (!prm || !out) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: load vectors need a GPU");
   if ((op->vd == 2) != (kind == 3))
     return set_error(op->ctx, BG_INVALID_ARG, "the Maxwell operator takes dipole data (kind 3) and only it");
@@ -466,7 +468,9 @@ static bg_status potential_mw(bg_operator* op, const void* rho, int nrhs, const 
 }
 
 extern "C" bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out) {
-  if (!op || !rho || !pts || !out || nrhs <= 0 || npts <= 0) return BG_INVALID_ARG;
+  if (!op || nrhs < 0 || npts < 0) return BG_INVALID_ARG;
+  if (nrhs == 0 || npts == 0) return BG_OK;  // nothing to evaluate
+  if (!rho || !pts || !out) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: potentials need a GPU");
   cudaSetDevice(op->ctx->device);
   if (op->maxwell()) return potential_mw(op, rho, nrhs, pts, npts, out);

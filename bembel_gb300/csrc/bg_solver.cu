@@ -507,7 +507,12 @@ bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, cons
 
 extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params* params,
                               bg_solve_stats* stats, int on_device) {
-  if (!op || !b || !x || nrhs <= 0) return BG_INVALID_ARG;
+  if (!op || nrhs < 0) return BG_INVALID_ARG;
+  if (nrhs == 0) {  // no right-hand sides: nothing to solve
+    if (stats) *stats = bg_solve_stats{};
+    return BG_OK;
+  }
+  if (!b || !x) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: solves need a GPU");
   if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
   bg_solve_params prm;

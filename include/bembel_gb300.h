@@ -159,7 +159,8 @@ bg_status bg_operator_assembly_times(const bg_operator* op, double* t3);
  *   Y = beta * Y + alpha * A X   for nrhs columns.
  * x, y are host pointers when on_device == 0 (staged through pinned buffers),
  * device pointers otherwise. alpha/beta are complex (re, im) pairs; for a real
- * operator their imaginary parts must be 0. precision: bg_precision. */
+ * operator their imaginary parts must be 0. precision: bg_precision.
+ * nrhs == 0 is an empty product: BG_OK, nothing read or written. */
 bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
                     const double* alpha, const double* beta, int precision, int on_device);
 
@@ -193,13 +194,15 @@ bg_status bg_matvec_noalloc(bg_operator* op, const void* x, void* y, int precisi
  * (LinearForm/RotatedTangentialTrace.hpp:30-87) of
  *   kind 3: the field of a Hertz dipole (examples/Data.hpp:73-90), prm = position,
  *           moment (6 doubles per column).
- * Output: nrhs load vectors (N x nrhs, column-major, ld = N), host or device. */
+ * Output: nrhs load vectors (N x nrhs, column-major, ld = N), host or device.
+ * nrhs == 0: BG_OK, nothing written. */
 bg_status bg_load_vector(bg_operator* op, int kind, const double* prm, int nrhs, void* out, int on_device);
 
 /* GMRES on the H2 operator with iterative refinement (replaces the Eigen
  * solvers called at examples/LaplaceSingleLayerH2.cpp:78-81 and
  * examples/HelmholtzSingleLayerH2.cpp:82-85). Residuals, the near field and the
- * Krylov basis are FP64; the inner correction operator is params->inner_precision. */
+ * Krylov basis are FP64; the inner correction operator is params->inner_precision.
+ * nrhs == 0: BG_OK with zeroed stats. */
 bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params* params,
                    bg_solve_stats* stats, int on_device);
 
@@ -207,7 +210,7 @@ bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_s
  * at npts points (3 doubles each) for nrhs densities rho (N x nrhs), host
  * pointers. Laplace / Helmholtz: out is npts x nrhs (column-major). Maxwell
  * (Maxwell/SingleLayerPotential.hpp:44-95): the field, 3 complex values per
- * point, out[(c * npts + p) * 3 + xyz]. */
+ * point, out[(c * npts + p) * 3 + xyz]. nrhs == 0 or npts == 0: BG_OK, nothing written. */
 bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, const double* pts, int npts, void* out);
 
 /* Device memory of an operator: *allocated = bytes it holds now (tables,

@@ -187,3 +187,19 @@ def test_launch_plans_round_trip_and_validation(bg_host):
     with pytest.raises(BembelError) as e:
         d.autotune(32, "mixed")
     assert e.value.status == _lib.BG_UNSUPPORTED
+
+
+def test_empty_inputs_are_no_ops(bg_host):
+    """Zero right-hand sides or zero points: empty results and no error,
+    before any device work (Eigen's products with empty operands are no-ops)."""
+    bg, ctx = bg_host
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 1, 1), bg.LaplaceSingleLayerOperator())
+    A = d.get_discrete_operator()
+    assert A.matvec(np.zeros((d.N, 0))).shape == (d.N, 0)
+    x, st = A.solve(np.zeros((d.N, 0)))
+    assert x.shape == (d.N, 0) and st["converged"] and st["iterations"] == 0
+    assert d.load_vector(0, np.zeros((0, 3))).shape == (d.N, 0)
+    assert d.potential(np.zeros((d.N, 0)), np.ones((4, 3))).shape == (4, 0)
+    assert d.potential(np.zeros((d.N, 2)), np.zeros((0, 3))).shape == (0, 2)
+    with pytest.raises(bg.BembelError):  # one column still needs a device
+        A.matvec(np.zeros(d.N))
