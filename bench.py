@@ -181,6 +181,12 @@ def aggregate_replicas(total_ms, dist=None, device="cuda"):
     return float(t.item())
 
 
+def col_rel_err(a, ref):
+    """Largest column-wise relative error ||a_c - ref_c|| / ||ref_c|| (numpy arrays, N x k)."""
+    a, ref = np.asarray(a).reshape(ref.shape[0], -1), np.asarray(ref).reshape(ref.shape[0], -1)
+    return float(np.max(np.linalg.norm(a - ref, axis=0) / np.linalg.norm(ref, axis=0)))
+
+
 def replica_value(nrhs, steps, world, total_ms):
     """solves/s of the whole job: every replica solves nrhs right-hand sides per step."""
     return world * nrhs * steps / (total_ms * 1e-3)
@@ -284,6 +290,7 @@ def run_gpu(args):
     # matvec throughput (32 RHS per product)
     def mv_rate(prec, reps=5):
         x = torch.randn(N, NRHS, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
         for _ in range(2):
             A.matvec(x, precision=prec)
         torch.cuda.synchronize()
@@ -295,6 +302,11 @@ def run_gpu(args):
         e1.synchronize()
         return reps / (e0.elapsed_time(e1) * 1e-3)
     mv64, mvmx, mv32 = mv_rate("fp64"), mv_rate("mixed"), mv_rate("fp32")
+    # product error of the low-precision operators against the FP64 product
+    xr = torch.randn(N, NRHS, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()  # the library reads xr on its own (non-blocking) stream
+    y_ref = A.matvec(xr, precision="fp64").cpu().numpy()
+    mv_err = {p: col_rel_err(A.matvec(xr, precision=p).cpu().numpy(), y_ref) for p in ("mixed", "fp32")}
 
     total_ms = aggregate_replicas(float(t_mixed.sum()), dist)
     value = replica_value(NRHS, args.steps, world, total_ms)
@@ -304,13 +316,14 @@ def run_gpu(args):
     # accuracy: mixed vs FP64 solution, and potential error vs the analytic point source
     xm_np = xm.cpu().numpy() if hasattr(xm, "cpu") else xm
     x64_np = x64.cpu().numpy() if hasattr(x64, "cpu") else x64
-    rel_vs_fp64 = float(np.max(np.linalg.norm(xm_np - x64_np, axis=0) / np.linalg.norm(x64_np, axis=0)))
+    rel_vs_fp64 = col_rel_err(xm_np, x64_np)
     rng = np.random.default_rng(2)
     pts = rng.normal(size=(100, 3))
     pts = pts / np.linalg.norm(pts, axis=1, keepdims=True) * (0.25 * rng.uniform(0, 1, (100, 1)) ** (1 / 3))
     pot = op.potential(xm_np, pts)
     ref = 1.0 / (4 * np.pi * np.linalg.norm(pts[:, None, :] - x0[None, :, :], axis=2))
     pot_err = float(np.max(np.abs(pot - ref)) / np.max(np.abs(ref)))
+    pot64_err = float(np.max(np.abs(op.potential(x64_np, pts) - ref)) / np.max(np.abs(ref)))
 
     if rank != 0:
         return
@@ -334,7 +347,8 @@ def run_gpu(args):
             "solver": {k: stm[k] for k in ("iterations", "refinements", "fp64_matvecs", "low_matvecs",
                                             "final_relres")},
             "accuracy": {"mixed_vs_fp64_solution": rel_vs_fp64, "potential_vs_analytic": pot_err,
-                         "fp64_final_relres": st64["final_relres"]},
+                         "fp64_potential_vs_analytic": pot64_err, "fp64_final_relres": st64["final_relres"],
+                         "mixed_matvec_vs_fp64": mv_err["mixed"], "fp32_matvec_vs_fp64": mv_err["fp32"]},
             "matvec": {"fp64_products_per_s_32rhs": mv64, "mixed_products_per_s_32rhs": mvmx,
                        "fp32_products_per_s_32rhs": mv32, "fp64_matvec_per_s": mv64 * NRHS,
                        "mixed_matvec_per_s": mvmx * NRHS, "fp32_matvec_per_s": mv32 * NRHS},

@@ -70,3 +70,15 @@ def test_reference_arm_json_line():
     assert j["cpu_baseline"]["kind"] == "port" and j["cpu_baseline"]["sample"]
     assert j["e2e"] == {"value": j["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert j["config"]["workload"] == "laplace_sl_h2_sphere_M5_P2_np9_32rhs"
+
+
+def test_bench_column_errors():
+    """The accuracy figures of the bench line: largest column-wise relative error."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    ref = np.array([[1.0, 0.0], [0.0, 2.0]])
+    a = np.array([[1.0, 0.0], [0.1, 2.0]])
+    assert abs(bench.col_rel_err(a, ref) - 0.1) < 1e-15
+    assert bench.col_rel_err(ref, ref) == 0.0
+    assert abs(bench.col_rel_err(np.array([2.0, 0.0]), np.array([1.0, 0.0])) - 1.0) < 1e-15
