@@ -233,14 +233,15 @@ inline Sparse glue_divconforming(const SuperSpace& ss, int rep, int pre_dofs) {
       for (int i = 0; i < sz; ++i) {
         int j = rev ? sz - 1 - i : i;
         DofId d;
-        d.dofs = {std::min(d1[i], d2[j]), std::max(d1[i], d2[j])};
+        d.dofs.push_back(std::min(d1[i], d2[j]));
+        d.dofs.push_back(std::max(d1[i], d2[j]));
         d.coef = coef;
         ids.push_back(d);
       }
     } else {
       for (int i = 0; i < sz; ++i) {
         DofId d;
-        d.dofs = {d1[i]};
+        d.dofs.push_back(d1[i]);
         ids.push_back(d);
       }
     }
