@@ -487,7 +487,6 @@ extern "C" bg_status bg_operator_create(bg_context* ctx, const bg_geometry* g, i
     delete op;
     return set_error(ctx, BG_UNSUPPORTED, "patch degree above 5 is not supported");
   }
-  if (op->G == 4 || op->G == 6) op->G = op->G;  // supported by the point kernels
   std::string err;
   if (!build_mesh(op->geo, M, &op->mesh, &err) || !build_transform(op->mesh, P, op->vd == 2, &op->T, &err)) {
     delete op;

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cmath>
 #include <fstream>
 #include <map>
 #include <mutex>
@@ -12,9 +13,21 @@
 namespace bg {
 
 // ---------------------------------------------------------------------------
-// .dat geometry files: 4 comment lines, a header line "2 3 npatch 0 0", then
-// per patch: "PATCH k", degrees, control point counts, two knot vectors and
-// the x, y, z, w matrices (rows = y, cols = x).
+// the next line as exactly n numbers; false when the line is missing or short
+static bool read_numbers(std::istream& f, size_t n, std::vector<double>* out) {
+  std::string line;
+  if (!std::getline(f, line)) return false;
+  std::istringstream is(line);
+  out->assign(n, 0.0);
+  for (double& v : *out)
+    if (!(is >> v)) return false;
+  return true;
+}
+
+// .dat geometry files (GeometryIO.hpp:25-122): 4 comment lines, a header line
+// "2 3 npatch 0 0", then per patch: "PATCH k", degrees, control point counts,
+// two knot vectors and the x, y, z, w matrices (rows = y, cols = x). Every row
+// must be complete, coordinates finite and weights positive.
 bool load_dat(const std::string& path, Geometry* g, std::string* err) {
   std::ifstream f(path);
   if (!f) {
@@ -35,37 +48,32 @@ bool load_dat(const std::string& path, Geometry* g, std::string* err) {
   }
   g->patches.clear();
   for (int p = 0; p < hdr[2]; ++p) {
-    int deg[2], ncp[2];
+    std::vector<double> deg, ncp;
     std::getline(f, line);  // PATCH k
-    std::getline(f, line);
-    { std::istringstream is(line); is >> deg[0] >> deg[1]; }
-    std::getline(f, line);
-    { std::istringstream is(line); is >> ncp[0] >> ncp[1]; }
-    if (!f || ncp[0] <= 0 || ncp[1] <= 0) {
-      *err = "malformed patch header in " + path;
+    if (!f || !read_numbers(f, 2, &deg) || !read_numbers(f, 2, &ncp) || deg[0] < 0 || deg[1] < 0 ||
+        deg[0] > 15 || deg[1] > 15 || ncp[0] < 1 || ncp[1] < 1 || ncp[0] > 16 || ncp[1] > 16) {
+      *err = "malformed patch header (degrees 0..15, control points 1..16 per direction) in " + path;
       return false;
     }
+    const int nx = (int)ncp[0], ny = (int)ncp[1];
     std::vector<double> knots[2];
     for (int d = 0; d < 2; ++d) {
-      std::getline(f, line);
-      std::istringstream is(line);
-      knots[d].resize(deg[d] + ncp[d] + 1);
-      for (double& k : knots[d]) is >> k;
+      if (!read_numbers(f, (size_t)deg[d] + (size_t)ncp[d] + 1, &knots[d])) {
+        *err = "malformed knot vector in " + path;
+        return false;
+      }
       for (double k : knots[d])
         if (k > 1e-6 && k < 1 - 1e-6) {
           *err = "patches with interior knots are not supported: " + path;
           return false;
         }
     }
-    const int nx = ncp[0], ny = ncp[1];
     std::vector<double> mat[4];
     for (int c = 0; c < 4; ++c) {
-      std::getline(f, line);
-      std::istringstream is(line);
-      mat[c].resize(nx * ny);
-      for (double& v : mat[c]) is >> v;
-      if (!is && !is.eof()) {
-        *err = "malformed control points in " + path;
+      bool ok = read_numbers(f, (size_t)nx * ny, &mat[c]);
+      for (double v : mat[c]) ok = ok && std::isfinite(v) && (c < 3 || v > 0.0);
+      if (!ok) {
+        *err = "malformed control points (missing values, or a weight that is not positive) in " + path;
         return false;
       }
     }
@@ -135,13 +143,16 @@ bool load_igs(const std::string& path, Geometry* g, std::string* err) {
         tok += c;
       }
     }
-    if (v.size() < 10 || (int)v[0] != 128) {
+    // upper indices and degrees in 0..15 (as for the .dat files), checked before any arithmetic on them
+    bool in_range = v.size() >= 10 && v[0] == 128.0;
+    for (int i = 1; i <= 4 && in_range; ++i) in_range = v[i] >= 0.0 && v[i] <= 15.0;
+    if (!in_range) {
       *err = "malformed IGES entity 128 parameters: " + path;
       return false;
     }
     const int K1 = (int)v[1], K2 = (int)v[2], M1 = (int)v[3], M2 = (int)v[4];
     const int A = K1 + M1 + 1, B = K2 + M2 + 1, C = (K1 + 1) * (K2 + 1);  // knot counts - 1, points
-    if (K1 < 0 || K2 < 0 || M1 < 0 || M2 < 0 || v.size() < (size_t)(10 + A + 1 + B + 1 + 4 * C)) {
+    if (v.size() < (size_t)(10 + A + 1 + B + 1 + 4 * C)) {
       *err = "malformed IGES entity 128 parameters: " + path;
       return false;
     }
@@ -151,6 +162,12 @@ bool load_igs(const std::string& path, Geometry* g, std::string* err) {
     }
     const double* W = v.data() + 10 + A + 1 + B + 1;
     const double* X = W + C;
+    for (int q = 0; q < C; ++q)
+      if (!(W[q] > 0.0) || !std::isfinite(W[q]) || !std::isfinite(X[3 * q]) || !std::isfinite(X[3 * q + 1]) ||
+          !std::isfinite(X[3 * q + 2])) {
+        *err = "IGES control point with a weight that is not positive, or not finite: " + path;
+        return false;
+      }
     PatchData P;
     P.px = K1 + 1;
     P.py = K2 + 1;

@@ -155,6 +155,14 @@ def test_igs_geometry_matches_dat(bg_host, tmp_path):
     with pytest.raises(bg.BembelError) as ei:
         bg.Geometry(bad, ctx)
     assert "interior knots" in str(ei.value)
+    # a control point with a negative weight is refused, as in the .dat reader
+    px, py, X, Y, Z, W = patches[0]
+    W = [-W[0]] + list(W[1:])
+    X, Y, Z = ([-v[0]] + list(v[1:]) for v in (X, Y, Z))
+    write_igs([(px, py, X, Y, Z, W)], bad)
+    with pytest.raises(bg.BembelError) as ei:
+        bg.Geometry(bad, ctx)
+    assert "weight" in str(ei.value)
 
 
 def test_watchdog_selftest_needs_a_gpu(bg_host):
@@ -203,3 +211,22 @@ def test_empty_inputs_are_no_ops(bg_host):
     assert d.potential(np.zeros((d.N, 2)), np.zeros((0, 3))).shape == (0, 2)
     with pytest.raises(bg.BembelError):  # one column still needs a device
         A.matvec(np.zeros(d.N))
+
+
+def test_dat_loader_refuses_incomplete_patches(bg_host, tmp_path):
+    """A .dat file cut inside its last patch, or with a zero weight, is an
+    error instead of a geometry that evaluates to inf / nan."""
+    bg, ctx = bg_host
+    lines = open(SPHERE).read().splitlines()
+    for cut in (len(lines) - 1, len(lines) - 3, len(lines) - 7):
+        p = tmp_path / ("cut%d.dat" % cut)
+        p.write_text("\n".join(lines[:cut]) + "\n")
+        with pytest.raises(bg.BembelError):
+            bg.Geometry(str(p), ctx)
+    w = list(lines)
+    w[-1] = " ".join(["0.0"] + w[-1].split()[1:])  # first weight of the last patch
+    p = tmp_path / "zero_weight.dat"
+    p.write_text("\n".join(w) + "\n")
+    with pytest.raises(bg.BembelError) as ei:
+        bg.Geometry(str(p), ctx)
+    assert "weight" in str(ei.value)
