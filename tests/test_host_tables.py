@@ -230,3 +230,53 @@ def test_dat_loader_refuses_incomplete_patches(bg_host, tmp_path):
     with pytest.raises(bg.BembelError) as ei:
         bg.Geometry(str(p), ctx)
     assert "weight" in str(ei.value)
+
+
+def test_abi_entry_points_refuse_null_arguments(bg_host):
+    """Every entry point declared in the header returns a status (no crash)
+    when called with null pointers and zero sizes: first with null handles,
+    then with valid host-only handles and everything else null or zero. Zero
+    right-hand sides are an empty call (BG_OK); everything else is refused."""
+    import ctypes
+    from bembel_gb300 import _lib
+    bg, ctx = bg_host
+    hdr = re.sub(r"/\*.*?\*/", "", open(ROOT + "/include/bembel_gb300.h").read(), flags=re.S)
+    decls = {name: [p.strip().replace(" ", "") for p in params.split(",")]
+             for name, params in re.findall(r"\b(bg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", hdr)}
+    assert len(decls) >= 40
+    g = bg.Geometry(SPHERE, ctx)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(g, 2, 1), bg.LaplaceSingleLayerOperator())
+    handles = {"bg_context*": ctx.h, "bg_operator*": d.h, "constbg_operator*": d.h, "bg_geometry*": g.h,
+               "constbg_geometry*": g.h}
+    L = _lib.load()
+    statuses = set(range(len(_lib.STATUS_NAMES)))
+    for name, params in sorted(decls.items()):
+        if name.endswith("_destroy") or name.endswith("_default") or name == "bg_last_error_string":
+            continue
+        for with_handles in (False, True):
+            args, types = [], []
+            for i, p in enumerate(params):
+                ptype = p.rsplit("*", 1)[0] + "*" if "*" in p else p
+                if i == 0 and with_handles and ptype in handles:
+                    args.append(ctypes.c_void_p(handles[ptype].value if hasattr(handles[ptype], "value")
+                                                else handles[ptype]))
+                    types.append(ctypes.c_void_p)
+                elif "*" in p:
+                    args.append(None)
+                    types.append(ctypes.c_void_p)
+                elif p.startswith("double"):
+                    args.append(0.0)
+                    types.append(ctypes.c_double)
+                else:
+                    args.append(0)
+                    types.append(ctypes.c_long if p.startswith(("long", "size_t")) else ctypes.c_int)
+            f = getattr(L, name)
+            saved = (f.argtypes, f.restype)
+            f.argtypes, f.restype = types, ctypes.c_int
+            try:
+                st = f(*args)
+            finally:
+                f.argtypes, f.restype = saved
+            assert st in statuses, (name, with_handles, st)
+            if not with_handles:
+                assert st == _lib.BG_INVALID_ARG, name
