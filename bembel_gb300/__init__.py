@@ -359,9 +359,12 @@ class DiscreteOperator:
         return ints, dbl
 
     def leaves(self):
-        out = np.zeros((self.n_dense + self.n_lowrank, 4), dtype=np.int32)
-        self.ctx.check(_lib.load().bg_operator_leaves(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
-        return out
+        # the partition is fixed when the operator is created: read it once
+        if getattr(self, "_leaves", None) is None:
+            out = np.zeros((self.n_dense + self.n_lowrank, 4), dtype=np.int32)
+            self.ctx.check(_lib.load().bg_operator_leaves(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+            self._leaves = out
+        return self._leaves.copy()
 
     def transform_csr(self):
         info = self.info()
@@ -375,7 +378,8 @@ class DiscreteOperator:
         return ptr, idx, val
 
     def leaf_block(self, leaf, rc=0, cc=0):
-        lv = self.leaves()[leaf]
+        self.leaves()
+        lv = self._leaves[leaf]
         info = self.info()
         p2 = (int(info[10]) + 1) ** 2
         if lv[0] == 2:

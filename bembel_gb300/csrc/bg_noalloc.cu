@@ -18,10 +18,22 @@
 //    calls that overlap on the GPU race and give wrong results;
 //  - the first call on a device looks the array's device address up
 //    (cudaGetSymbolAddress) and caches it; make that first call before any
-//    stream capture.
+//    stream capture. The cached address belongs to the device's primary
+//    context, the one the CUDA runtime uses: after cudaDeviceReset on that
+//    device it is stale, so do not call this entry point after a reset;
+//  - the call selects the operator's device for its duration and restores
+//    the caller's current device before it returns.
 // Nothing in the array needs to start at zero: every buffer carved from it is
 // fully written before it is read, and the FP32 accumulator of the mixed path
 // is cleared with cudaMemsetAsync on each call.
+//
+// The FP64 far field follows bg_matvec: real operators multiply the
+// double-float (hi, lo) copies of the couplings when they exist, complex ones
+// the split real and imaginary pairs, and only operators without those copies
+// read the FP64 blocks. Operators assembled with keep_fp64_blocks = 0 (as the
+// serving cache builds them) have released the FP64 blocks and always take
+// the double-float route; an operator holding neither is refused with
+// BG_UNSUPPORTED before any device work.
 #include <cstdint>
 #include <mutex>
 
@@ -61,6 +73,7 @@ size_t round256(size_t n) { return (n + 255) & ~size_t(255); }
 struct ScratchPlan {
   size_t xss = 0, yss = 0, xss32 = 0, yss32 = 0;
   std::vector<size_t> y, z;  // per FMM level
+  std::vector<size_t> ydf;   // per FMM level: double-float split of y (FP64 product on the pairs)
   size_t total = 0;
 };
 
@@ -91,6 +104,13 @@ ScratchPlan plan_scratch(const bg_operator* op, bool mixed) {
       const size_t n = (size_t)op->vd * op->nclusters(l) * op->R * fsb;
       sp.y.push_back(take(n));
       sp.z.push_back(take(n));
+      // one (hi, lo) float pair per real entry of y: one pair for a real
+      // coupling column, two (re, im) for a complex one
+      // (the size check runs before the assembled check, so the per-level
+      // buffers may not exist yet)
+      const bool df = !mixed && !op->far[l].col.empty() && l < (int)op->d_far_df.size() && op->d_far_df[l]->p;
+      const size_t ndf = df ? (size_t)op->nclusters(l) * op->R * (op->cplx ? 2 : 1) * sizeof(float2) : 0;
+      sp.ydf.push_back(ndf ? take(ndf) : 0);
     }
   }
   sp.total = off;
@@ -165,10 +185,28 @@ static bg_status product_in_scratch(bg_operator* op, bool mixed, const ScratchPl
                                   f.d_row_ptr.as<int>(), f.d_col.as<int>(), f.nrows, np2, (float)op->kre,
                                   (float)op->kim, Y(l), Z(l), 1, s),
                  "far-field product (FP32 fused)");
-      else
+      else if (op->d_far_df[l]->p && op->cplx) {
+        // Re K split(y) + Im K split(i y), the second pass accumulating
+        const long sdf = ((long)f.B * f.B + 1) / 2 * 2;
+        const float2* kr = op->d_far_df[l]->as<float2>();
+        const float2* ki = kr + (long)f.col.size() * sdf;
+        const long rows = (long)op->nclusters(l) * f.B;
+        for (int part = 0; part < 2; ++part) {
+          NA_CHECK(launch_split_df_cols(Y(l), rows, 1, 0, 1, part, base + sp.ydf[l], s), "far-field split of Y");
+          NA_CHECK(launch_bsr_df_cols(f.d_row_ptr.as<int>(), f.d_col.as<int>(), part ? ki : kr, sdf, f.nrows, f.B,
+                                      base + sp.ydf[l], Z(l), 2, 2, 0, part, s),
+                   "far-field product (complex double-float)");
+        }
+      } else if (op->d_far_df[l]->p) {
+        NA_CHECK(launch_split_df(Y(l), (long)op->nclusters(l) * op->R, base + sp.ydf[l], s), "far-field split of Y");
+        NA_CHECK(launch_bsr_df(f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far_df[l]->p, op->block_stride(f.B),
+                               f.nrows, f.B, base + sp.ydf[l], Z(l), 1, 0, s),
+                 "far-field product (double-float)");
+      } else {
         NA_CHECK(launch_bsr_fp64(op->cplx, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
                                  op->block_stride(f.B), f.nrows, f.B, Y(l), Z(l), 1, 0, s),
                  "far-field product");
+      }
     }
     for (int c = 0; c < op->vd; ++c) {
       for (int l = 0; l < Ll; ++l) {
@@ -210,11 +248,22 @@ extern "C" bg_status bg_matvec_noalloc(bg_operator* op, const void* x, void* y, 
   const uintptr_t align = op->cplx ? 16 : 8;
   if (reinterpret_cast<uintptr_t>(x) % align || reinterpret_cast<uintptr_t>(y) % align)
     return set_error(op->ctx, BG_INVALID_ARG, "bg_matvec_noalloc: x and y must be aligned to their scalar type");
+  if (!mixed && has_far(op))
+    for (int l = 0; l <= op->leaf_level; ++l)
+      if (!op->far[l].col.empty() && !op->d_far_df[l]->p && !op->d_far64[l]->p)
+        return set_error(op->ctx, BG_UNSUPPORTED,
+                         "bg_matvec_noalloc: the FP64 product needs the stored far field (FP64 blocks or their "
+                         "double-float copies); use bg_matvec");
+  int caller_device = -1;
+  NA_CHECK(cudaGetDevice(&caller_device), "current device");
   NA_CHECK(cudaSetDevice(op->ctx->device), "select device");
   void* scratch = nullptr;
-  NA_CHECK(scratch_address(op->ctx->device, &scratch), "scratch address (cudaGetSymbolAddress)");
-  bg_status st = product_in_scratch(op, mixed, sp, static_cast<char*>(scratch), x, y);
-  if (st != BG_OK) return st;
-  NA_CHECK(cudaStreamSynchronize(op->ctx->stream), "H2 matvec (no allocation)");
-  return BG_OK;
+  bg_status st = cuda_status(op->ctx, scratch_address(op->ctx->device, &scratch),
+                             "scratch address (cudaGetSymbolAddress)");
+  if (st == BG_OK) st = product_in_scratch(op, mixed, sp, static_cast<char*>(scratch), x, y);
+  if (st == BG_OK) st = cuda_status(op->ctx, cudaStreamSynchronize(op->ctx->stream), "H2 matvec (no allocation)");
+  // the caller's device comes back whatever happened above
+  const cudaError_t back = cudaSetDevice(caller_device);
+  if (st == BG_OK) st = cuda_status(op->ctx, back, "restore the caller's device");
+  return st;
 }

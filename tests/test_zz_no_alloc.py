@@ -40,12 +40,13 @@ def ctx():
     return bg.Context(0)
 
 
-def _operator(ctx, M, P, kind, kappa=0.0, np_=9, assemble=True):
+def _operator(ctx, M, P, kind, kappa=0.0, np_=9, assemble=True, keep_fp64_blocks=True):
     import bembel_gb300 as bg
     lin = bg.LaplaceSingleLayerOperator() if kind == 0 else bg.HelmholtzSingleLayerOperator()
     if kind == 1:
         lin.set_wavenumber(kappa)
-    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, P), lin, n_p=np_)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, P), lin, n_p=np_,
+                            keep_fp64_blocks=keep_fp64_blocks)
     if assemble:
         d.compute()
     return d
@@ -101,3 +102,26 @@ def test_noalloc_rejects_operators_beyond_scratch(ctx):
     assert st == _lib.BG_INVALID_ARG
     msg = _lib.load().bg_last_error_string(ctx.h).decode()
     assert "scratch" in msg and "16 MiB" in msg, msg
+
+
+@pytest.mark.parametrize("kind,kappa", [(0, 0.0), (1, 2.0)])
+def test_noalloc_fp64_without_fp64_blocks(ctx, kind, kappa):
+    """An operator assembled with keep_fp64_blocks=False (as the serving cache
+    builds them) has released its FP64 coupling blocks; the FP64 product then
+    runs on their double-float copies, as bg_matvec does."""
+    import torch
+    from bembel_gb300 import _lib
+    d = _operator(ctx, 3, 2, kind, kappa, keep_fp64_blocks=False)
+    A = d.get_discrete_operator()
+    rng = np.random.default_rng(12)
+    dtype = torch.complex128 if d.is_complex else torch.float64
+    y_dev = torch.empty(d.N, dtype=dtype, device="cuda:0")
+    for call in range(2):
+        x = rng.uniform(-1, 1, d.N)
+        if d.is_complex:
+            x = x + 1j * rng.uniform(-1, 1, d.N)
+        y = _noalloc(ctx, d, torch.from_numpy(x).to("cuda:0"), y_dev, _lib.PREC_FP64)
+        ref = A.matvec(x.reshape(-1, 1), precision="fp64").reshape(-1)
+        err = np.linalg.norm(y - ref) / np.linalg.norm(ref)
+        assert err < FP64_TOL, (call, err)
+
