@@ -35,7 +35,8 @@ class SolveStats(ctypes.Structure):
 
 
 class LaunchPlan(ctypes.Structure):
-    _fields_ = [("near_kernel", ctypes.c_int), ("split_k_batches", ctypes.c_int), ("far_order", ctypes.c_int)]
+    _fields_ = [("near_kernel", ctypes.c_int), ("split_k_batches", ctypes.c_int), ("far_order", ctypes.c_int),
+                ("transforms", ctypes.c_int)]
 
 
 class TuneReport(ctypes.Structure):

@@ -424,6 +424,52 @@ static bg_status upload_tables(bg_operator* op) {
                     fits(4 * np2);
   }
   {
+    // tensor-product factors of the transfer and moment matrices for the
+    // fused transforms (scalar operators with a transfer level); used only if
+    // they rebuild the assembled matrices to rounding
+    op->fmm_fused = false;
+    const int cr = std::min(op->mcl, op->M), np = op->np, np2 = np * np;
+    if (!op->maxwell() && op->vd == 1 && op->nc == 1 && op->leaf_level >= 1 && op->leaf_level < kMaxFarLevels &&
+        np <= kFmmMaxNp) {
+      std::vector<double> E = transfer_factors(np), ms, mt;
+      std::vector<int> cmap;
+      moment_factors(op->P, op->leaf_level, cr, np, &ms, &mt, &cmap);
+      const int w1 = (1 << cr) * (op->P + 1);
+      bool ok = w1 <= 16 && w1 * w1 == op->Bq && (int)cmap.size() == op->Bq && mom.size() == 1;
+      double dev = 0.0, big = 0.0;
+      static const int sx[4] = {0, 1, 1, 0}, sy[4] = {0, 0, 1, 1};
+      for (int k = 0; ok && k < 4; ++k)
+        for (int o = 0; o < np2; ++o)
+          for (int q = 0; q < np2; ++q) {
+            const double f = E[sx[k] * np2 + (q / np) * np + o / np] * E[sy[k] * np2 + (q % np) * np + o % np];
+            const double t = tr[(size_t)o * 4 * np2 + k * np2 + q];
+            dev = std::max(dev, std::fabs(f - t));
+            big = std::max(big, std::fabs(t));
+          }
+      double mdev = 0.0, mbig = 0.0;
+      for (int o = 0; ok && o < np2; ++o)
+        for (int q = 0; q < op->Bq; ++q) {
+          const int a = cmap[q] & 0xFF, b = cmap[q] >> 8;
+          const double f = ms[(o / np) * w1 + a] * mt[(o % np) * w1 + b];
+          const double t = mom[0][(size_t)o * op->Bq + q];
+          mdev = std::max(mdev, std::fabs(f - t));
+          mbig = std::max(mbig, std::fabs(t));
+        }
+      ok = ok && dev <= 1e-14 * big && mdev <= 1e-14 * mbig;
+      if (ok) {
+        std::vector<double> fac(E);
+        fac.insert(fac.end(), ms.begin(), ms.end());
+        fac.insert(fac.end(), mt.begin(), mt.end());
+        std::vector<float> f32(fac.begin(), fac.end());
+        BG_CHECK(op->d_fmm_fac64.upload(fac, s), "upload transforms");
+        BG_CHECK(op->d_fmm_fac32.upload(f32, s), "upload transforms");
+        BG_CHECK(op->d_fmm_cmap.upload(cmap, s), "upload transforms");
+        op->fmm_w1 = w1;
+        op->fmm_fused = true;
+      }
+    }
+  }
+  {
     // every row of every far-field level, rows with more blocks first so the
     // longest CTAs start in the first wave
     std::vector<std::pair<int, int2>> items;
@@ -581,8 +627,9 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
   size_t a = 0;
   for (const DevBuf* b : {&op->d_patch_meta, &op->d_patch_cp, &op->d_el_patch, &op->d_el_llc, &op->d_T_ptr,
                           &op->d_T_idx, &op->d_T_val, &op->d_Tt_ptr, &op->d_Tt_idx, &op->d_Tt_val, &op->d_cheb,
-                          &op->d_dense64, &op->d_dense32, &op->d_tr64, &op->d_tr32, &op->d_far_work, &op->d_err,
-                          &op->w_xdof, &op->w_xss, &op->w_yss, &op->w_ydof, &op->w_xss32, &op->w_yss32,
+                          &op->d_dense64, &op->d_dense32, &op->d_dense_df, &op->d_tr64, &op->d_tr32,
+                          &op->d_far_work, &op->d_err, &op->w_xdof, &op->w_xss, &op->w_yss, &op->w_ydof,
+                          &op->w_xss32, &op->w_yss32, &op->w_xss_df,
                           &op->dense.d_row_ptr, &op->dense.d_col})
     a += b->bytes;
   for (const auto* v : {&op->d_pts64, &op->d_pts32, &op->d_centres, &op->d_tan64, &op->d_tan32, &op->d_far64,
@@ -601,6 +648,7 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
   const int np2 = op->np * op->np;
   size_t e = (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * sb +
              (size_t)op->dense.col.size() * op->block_stride32(op->dense.B) * sb / 2;
+  if (!op->cplx) e += (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * sizeof(float2);  // double-float
   for (int l = 0; l <= op->leaf_level && l < (int)op->far.size(); ++l) {
     const size_t nb = op->far[l].col.size();
     const size_t ncl = (size_t)op->nclusters(l);
@@ -615,7 +663,7 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
   const size_t k = 32;
   size_t lev = 0;
   for (int l = 0; l <= op->leaf_level; ++l) lev += (size_t)op->vd * op->nclusters(l) * op->R;
-  e += 8 * (size_t)op->S * k * sb + 4 * lev * k * sb + 3 * 202 * (size_t)op->N * k * sb;
+  e += 9 * (size_t)op->S * k * sb + 4 * lev * k * sb + 3 * 202 * (size_t)op->N * k * sb;
   *estimate = std::max(e, a);
   return BG_OK;
 }
@@ -1054,6 +1102,15 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
                                 op->block_stride32((int)B), B * B, nb, op->ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(op->ctx->stream);
     if ((st = cuda_status(op->ctx, e, "FP32 near field")) != BG_OK) return st;
+    // (hi, lo) FP32 pairs of the real blocks: the FP64-accurate near field of
+    // BG_PREC_MIXED products runs on the FP32 pipes
+    if (!op->cplx && nb > 0) {
+      const long n = nb * op->block_stride((int)B);
+      e = op->d_dense_df.alloc((size_t)n * sizeof(float2));
+      if (e == cudaSuccess) e = launch_split_df(op->d_dense64.p, n, op->d_dense_df.p, op->ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(op->ctx->stream);
+      if ((st = cuda_status(op->ctx, e, "double-float near field")) != BG_OK) return st;
+    }
   }
   auto t2 = std::chrono::steady_clock::now();
   op->t_far = std::chrono::duration<double>(t1 - t0).count();
@@ -1074,6 +1131,7 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
   BG_CHECK(op->w_yss.alloc((size_t)op->S * nrhs * sb), "work vectors");
   BG_CHECK(op->w_xss32.alloc((size_t)op->S * nrhs * sb / 2), "work vectors");
   BG_CHECK(op->w_yss32.alloc((size_t)op->S * nrhs * sb / 2), "work vectors");
+  if (!op->cplx) BG_CHECK(op->w_xss_df.alloc((size_t)op->S * nrhs * sizeof(float2)), "work vectors");
   while ((int)op->w_y.size() <= op->leaf_level) {
     op->w_y.push_back(new DevBuf());
     op->w_z.push_back(new DevBuf());
@@ -1101,8 +1159,48 @@ bg_status ensure_work(bg_operator* op, int nrhs) {
       BG_CHECK(op->w_binv[l]->alloc(sizeof(float) * 32 * op->nclusters(l)), "work vectors");
     }
   }
+  if (op->fmm_fused) {
+    // arrival counters of the fused upward pass: parents at levels
+    // 0 .. L - 2, per 32-column chunk of the widest product (complex: 2 nrhs)
+    const int chunks = ((op->cplx ? 2 : 1) * nrhs + 31) / 32;
+    long stride = 0;
+    for (int l = 0; l + 2 <= op->leaf_level; ++l) {
+      op->fmm_cnt_off[l] = stride;
+      stride += op->nclusters(l);
+    }
+    op->fmm_cnt_stride = stride;
+    if (stride > 0) {
+      BG_CHECK(op->d_fmm_cnt.alloc((size_t)chunks * stride * sizeof(int)), "work vectors");
+      BG_CHECK(cudaMemsetAsync(op->d_fmm_cnt.p, 0, (size_t)chunks * stride * sizeof(int), op->ctx->stream),
+               "work vectors");
+    }
+    op->fmm_cnt_chunks = chunks;
+  }
   op->cap = nrhs;
   return BG_OK;
+}
+
+// Tables of the fused FMM transforms for one product: x / out the
+// superspace panels, y / z the level coefficients of the operator's work
+// vectors, kk real columns (complex vectors: 2 per right-hand side).
+template <typename T>
+static void fill_fmm(const bg_operator* op, const void* fac, int kk, const void* x, void* out, FmmLevels<T>* f) {
+  f->fac = static_cast<const T*>(fac);
+  f->cmap = op->d_fmm_cmap.as<int>();
+  f->x = static_cast<const T*>(x);
+  f->out = static_cast<T*>(out);
+  for (int l = 0; l <= op->leaf_level; ++l) {
+    f->y[l] = static_cast<T*>(op->w_y[l]->p);
+    f->z[l] = static_cast<const T*>(op->w_z[l]->p);
+  }
+  f->cnt = op->d_fmm_cnt.as<int>();
+  for (int l = 0; l < kMaxFarLevels; ++l) f->cnt_off[l] = op->fmm_cnt_off[l];
+  f->cnt_stride = op->fmm_cnt_stride;
+  f->np = op->np;
+  f->w1 = op->fmm_w1;
+  f->Bq = op->Bq;
+  f->L = op->leaf_level;
+  f->kk = kk;
 }
 
 // One H2 product on row-major FP64 work vectors (H2DenseProduct.hpp:33-165).
@@ -1126,6 +1224,14 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp32(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense32.p,
                         op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss32.p, op->w_yss32.p, nrhs, 0, s, pl.near_kernel); }),
              "near-field product (FP32)");
+  } else if (mixed && !op->cplx && op->d_dense_df.p) {
+    // FP64-accurate near field in double-float: blocks and x as FP32 (hi, lo)
+    // pairs, exact products and compensated sums (about 1e-14 relative)
+    BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df(op->w_xss.p, ss_n, op->w_xss_df.p, s); }),
+             "near-field split of x");
+    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_df(op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense_df.p,
+                        op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss_df.p, op->w_yss.p, nrhs, 0, s); }),
+             "near-field product (double-float)");
   } else {
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
                         op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss.p, op->w_yss.p, nrhs, 0, s); }),
@@ -1178,7 +1284,19 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
                  "forward transfer");
       }
     }
-    for (int c = 0; c < op->vd && !op->maxwell(); ++c) {
+    // scalar operators: one fused launch per direction through the
+    // tensor-product factors, unless the plan asks for the batched GEMMs
+    const bool fused_tr = !op->maxwell() && op->fmm_fused && pl.transforms == 0 &&
+                          ((op->cplx ? 2 : 1) * nrhs + 31) / 32 <= op->fmm_cnt_chunks;
+    FmmLevelsAny fa{};
+    if (fused_tr) {
+      const int kk = (op->cplx ? 2 : 1) * nrhs;
+      if (mixed) fill_fmm<float>(op, op->d_fmm_fac32.p, kk, xc0, yfar, &fa.f32);
+      else fill_fmm<double>(op, op->d_fmm_fac64.p, kk, xc0, yfar, &fa.f64);
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_up(Sfar, fa, op->nclusters(Ll - 1), s); }),
+               "forward transforms (fused)");
+    }
+    for (int c = 0; c < op->vd && !op->maxwell() && !fused_tr; ++c) {
       const void* mom = mixed ? op->d_mom32[c]->p : op->d_mom64[c]->p;
       const char* xc = c == 0 ? xc0 : xc1;
       char* yl = static_cast<char*>(op->w_y[Ll]->p) + (size_t)c * op->nleaf_cl * op->R * nrhs * sfar;
@@ -1391,7 +1509,10 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
                               : launch_moment_bwd(Sfar, mw_mom(blk[t]), np2, op->Bq, nb[t], zin[t], yout[t], nrhs, s); }),
                  "backward moments");
     }
-    for (int c = 0; c < op->vd && !op->maxwell(); ++c) {
+    if (fused_tr)
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_down(Sfar, fa, op->nclusters(Ll - 1), s); }),
+               "backward transforms (fused)");
+    for (int c = 0; c < op->vd && !op->maxwell() && !fused_tr; ++c) {
       for (int l = 0; l < Ll; ++l) {
         const int ncl = op->nclusters(l);
         const char* zpa = static_cast<const char*>(op->w_z[l]->p) + (size_t)c * ncl * op->R * nrhs * sfar;
@@ -1498,7 +1619,8 @@ extern "C" bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precisi
   if (nrhs < 1 || !valid_precision(precision))
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: nrhs must be positive and the precision a bg_precision");
   if (plan->near_kernel < 0 || plan->near_kernel > 3 || plan->split_k_batches < -1 ||
-      plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2)
+      plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2 || plan->transforms < 0 ||
+      plan->transforms > 1)
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: a field is out of range");
   op->plans[bg_operator::plan_key(nrhs, precision)] = *plan;
   op->drop_graphs();
@@ -1600,7 +1722,9 @@ extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precisi
     if (op->cplx && op->dense.B % 4 == 0) v.push_back(3);
     st = sweep(&bg_launch_plan::near_kernel, v);
   }
-  if (st == BG_OK && mixed && op->use_tgemm) st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
+  if (st == BG_OK && op->fmm_fused) st = sweep(&bg_launch_plan::transforms, {1});
+  if (st == BG_OK && mixed && op->use_tgemm && (!op->fmm_fused || cur.transforms == 1))
+    st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
   if (st == BG_OK && mixed && op->d_far_work_alt[0].p) st = sweep(&bg_launch_plan::far_order, {1, 2});
   if (st != BG_OK) {
     restore();

@@ -828,22 +828,28 @@ static double lagrange_value(const std::vector<double>& c, const std::vector<dou
   for (int k = np - 2; k >= 0; --k) v = v * (t - x[k]) + c[k * np + j];
   return v;
 }
-std::vector<double> transfer_matrix(int np) {
-  const int n2 = np * np;
+std::vector<double> transfer_factors(int np) {
   std::vector<double> x = cheb_points(np), c = newton_coefficients(np, x);
-  // E0[i][j] = L_j(x_i / 2), E1[i][j] = L_j(x_i / 2 + 1/2)
-  std::vector<double> E0(np * np), E1(np * np);
+  // E0[i][j] = L_j(x_i / 2), E1[i][j] = L_j(x_i / 2 + 1/2), stored [E0 | E1]
+  std::vector<double> E(2 * (size_t)np * np);
   for (int i = 0; i < np; ++i)
     for (int j = 0; j < np; ++j) {
-      E0[i * np + j] = lagrange_value(c, x, np, j, 0.5 * x[i]);
-      E1[i * np + j] = lagrange_value(c, x, np, j, 0.5 * x[i] + 0.5);
+      E[i * np + j] = lagrange_value(c, x, np, j, 0.5 * x[i]);
+      E[(size_t)np * np + i * np + j] = lagrange_value(c, x, np, j, 0.5 * x[i] + 0.5);
     }
+  return E;
+}
+std::vector<double> transfer_matrix(int np) {
+  const int n2 = np * np;
+  const std::vector<double> E = transfer_factors(np);
+  const double* E0 = E.data();
+  const double* E1 = E.data() + n2;
   // child k (son order) sits in the s-half sx and t-half sy
   static const int sx[4] = {0, 1, 1, 0}, sy[4] = {0, 0, 1, 1};
   std::vector<double> T((size_t)n2 * 4 * n2);
   for (int k = 0; k < 4; ++k) {
-    const std::vector<double>& Es = sx[k] ? E1 : E0;
-    const std::vector<double>& Et = sy[k] ? E1 : E0;
+    const double* Es = sx[k] ? E1 : E0;
+    const double* Et = sy[k] ? E1 : E0;
     for (int ps = 0; ps < np; ++ps)
       for (int pt = 0; pt < np; ++pt)
         for (int cs = 0; cs < np; ++cs)
@@ -887,6 +893,19 @@ static std::vector<double> moment_2d(int P, int cl, int cr, int np, bool ds, boo
                 ms[(size_t)i * w1 + ex * pp + ax] * mt[(size_t)j * w1 + ey * pp + ay];
   }
   return out;
+}
+void moment_factors(int P, int cl, int cr, int np, std::vector<double>* ms, std::vector<double>* mt,
+                    std::vector<int>* cmap) {
+  const int n = 1 << cr, pp = P + 1, p2 = pp * pp;
+  *ms = moment_1d(P, cl, cr, np, false);
+  *mt = moment_1d(P, cl, cr, np, false);
+  cmap->assign((size_t)n * n * p2, 0);
+  for (int k = 0; k < n * n; ++k) {
+    int ex, ey;
+    quadtree_coords(k, cr, &ex, &ey);
+    for (int ay = 0; ay < pp; ++ay)
+      for (int ax = 0; ax < pp; ++ax) (*cmap)[p2 * k + ay * pp + ax] = (ex * pp + ax) | ((ey * pp + ay) << 8);
+  }
 }
 std::vector<std::vector<double>> moment_matrices(bool maxwell, int P, int cl, int cr, int np) {
   std::vector<std::vector<double>> out;

@@ -102,5 +102,13 @@ Csr transpose(const Csr& A);
 std::vector<double> cheb_points(int np);
 std::vector<double> transfer_matrix(int np);
 std::vector<std::vector<double>> moment_matrices(bool maxwell, int P, int cluster_level, int cluster_ref, int np);
+// The 1-D factors of the transfer and (scalar) moment matrices above:
+// E = [E0 | E1] (np x np each, E_h[c][p] = L_p(x_c / 2 + h / 2)); ms, mt the
+// 1-D moments (np x w1, w1 = 2^cluster_ref (P + 1)); cmap[q] = a | (b << 8)
+// for superspace row q of a leaf cluster, so that
+// moments[(i np + j)][q] = ms[i][a] mt[j][b].
+std::vector<double> transfer_factors(int np);
+void moment_factors(int P, int cluster_level, int cluster_ref, int np, std::vector<double>* ms, std::vector<double>* mt,
+                    std::vector<int>* cmap);
 
 }  // namespace bg

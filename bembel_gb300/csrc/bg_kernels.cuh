@@ -200,6 +200,38 @@ cudaError_t launch_split_df_cols(const void* in, long rows, int ld, int c0, int 
                                  cudaStream_t s);
 cudaError_t launch_split_df_cplx_blocks(const void* in, long sin, long B2, long nblocks, long sout, void* out,
                                         cudaStream_t s);
+// Fused FMM transforms through the tensor-product factors (bg_fmm.cu).
+// fac: [E0 np x np][E1 np x np][Ms np x w1][Mt np x w1] with E_h[c][p] the
+// parent polynomial p at child point c of half h, Ms / Mt the 1-D moments;
+// cmap[q] = a | (b << 8): the (s, t) 1-D moment columns of superspace row q of
+// a leaf cluster (Bq = w1^2 rows). y[l] / z[l]: coefficients of level l
+// ([cluster][np^2][kk]); x / out: superspace panels ([leaf cluster][Bq][kk]),
+// out accumulated. cnt: arrival counters of the upward pass, zero between
+// launches, at cnt_off[l] + chunk * cnt_stride + parent for parents at levels
+// 0 .. L - 2 and column chunks of 32.
+constexpr int kFmmMaxNp = 12;
+template <typename T>
+struct FmmLevels {
+  const T* fac;
+  const int* cmap;
+  const T* x;
+  T* out;
+  T* y[kMaxFarLevels];
+  const T* z[kMaxFarLevels];
+  int* cnt;
+  long cnt_off[kMaxFarLevels];
+  long cnt_stride;
+  int np, w1, Bq, L, kk;
+};
+struct FmmLevelsAny {
+  FmmLevels<double> f64;
+  FmmLevels<float> f32;
+};
+// upward pass (moments of the leaf clusters, transfers to level 0) and
+// downward pass (transposed transfers, transposed moments added to out);
+// nparents = clusters of level L - 1; S the bg vector type of the pass
+cudaError_t launch_fmm_up(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s);
+cudaError_t launch_fmm_down(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s);
 // op(A) of an FMM transform, stored transposed: AT[q][i], q < Ki, i < ld
 // (ld a multiple of 4, at least Mo rounded up to 3, zero beyond Mo)
 struct TGemmA {

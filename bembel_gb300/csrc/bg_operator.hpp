@@ -151,6 +151,8 @@ struct bg_operator {
   std::vector<DevBuf*> d_tan64, d_tan32;             // per level, Maxwell: tangents dx, dy of every point
   DevBuf d_dense64;                       // dense blocks (FP64)
   DevBuf d_dense32;                       // FP32 copy of the dense blocks (BG_PREC_FP32)
+  DevBuf d_dense_df;                      // real operators: FP32 (hi, lo) pairs of the dense blocks, the
+                                          // near field of BG_PREC_MIXED products (double-float, FP64 accuracy)
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_far_df;          // per level: FP32 (hi, lo) pairs of d_far64 (real operators)
   std::vector<DevBuf*> d_far_atiles;      // per level: FP16 hi/lo tensor-core tiles of the low-rank blocks
@@ -169,6 +171,16 @@ struct bg_operator {
   };
   TransformMats tm[2];
   bool use_tgemm = false;
+  // fused FMM transforms through the tensor-product factors (scalar
+  // operators): factors per precision ([E0|E1|Ms|Mt]), the superspace-row map
+  // of a leaf cluster, and the upward pass's arrival counters (zero between
+  // launches; fmm_cnt_chunks column chunks of 32)
+  bool fmm_fused = false;
+  int fmm_w1 = 0;
+  DevBuf d_fmm_fac64, d_fmm_fac32, d_fmm_cmap, d_fmm_cnt;
+  long fmm_cnt_off[bg::kMaxFarLevels] = {};
+  long fmm_cnt_stride = 0;
+  int fmm_cnt_chunks = 0;
   // tensor-core far field: (level, row) work list, heaviest rows first, and
   // the two alternative orders of bg_launch_plan::far_order (built only when
   // there are more rows than persistent CTAs)
@@ -183,6 +195,7 @@ struct bg_operator {
   // work vectors (sized for the largest nrhs seen)
   int cap = 0;
   DevBuf w_xdof, w_xss, w_yss, w_ydof, w_xss32, w_yss32;
+  DevBuf w_xss_df;                // real operators: FP32 (hi, lo) split of w_xss for the double-float near field
   std::vector<DevBuf*> w_y, w_z;  // per level
   std::vector<DevBuf*> w_ydf;     // per level: FP32 (hi, lo) split of w_y for the double-float product
   std::vector<DevBuf*> w_yv, w_zv;  // per level, Maxwell: the four kernel columns per right-hand side
@@ -208,7 +221,7 @@ struct bg_operator {
   // launch plans per (nrhs, precision), keyed as the graphs
   std::map<long, bg_launch_plan> plans;
   static long plan_key(int nrhs, int prec) { return (long)nrhs * 4 + prec; }
-  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0}; }
+  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0, 0}; }
   bg_launch_plan plan_for(int nrhs, int prec) const {
     auto it = plans.find(plan_key(nrhs, prec));
     return it == plans.end() ? builtin_plan() : it->second;

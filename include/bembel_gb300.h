@@ -244,6 +244,11 @@ typedef struct bg_launch_plan {
    * second round reversed; 2 heaviest first, each round's items to the CTAs
    * with the least work so far. Results are identical for every order. */
   int far_order;
+  /* FMM transforms of scalar operators: 0 built-in (one fused launch per
+   * direction through the tensor-product factors of the transfer and moment
+   * matrices, where the operator has a transfer level); 1 batched GEMMs with
+   * the assembled matrices, level by level. Results agree to rounding. */
+  int transforms;
 } bg_launch_plan;
 
 typedef struct bg_tune_report {

@@ -203,14 +203,104 @@ class Operator {
 #include <Eigen/Core>
 #include <Eigen/Sparse>
 
+#if defined(BEMBEL_SRC_H2MATRIX_H2MATRIXBASE_HPP_) && defined(BEMBEL_SRC_H2MATRIX_EIGENHELPER_H2DENSEPRODUCT_HPP_)
+// Bembel's H2Matrix module is included: H2MatrixGPU joins Bembel's own H2
+// storage kind (H2Matrix/EigenHelper/Constants.hpp), so every expression
+// Bembel's Eigen glue accepts for H2Matrix works for it too: A * x, and the
+// distributive and associative rewrites (H2 + H2, D + H2, H2 - D, a * H2) of
+// H2DenseProduct.hpp:179-258, which end in H2_time_dense_product_impl below.
 namespace Eigen {
 template <typename Scalar_>
 class H2MatrixGPU;
 namespace internal {
-// Eigen's matrix-free solvers treat the operator like a sparse matrix
-// (the same trick as H2Matrix.hpp:26-56)
+// as traits<H2Matrix<S>> (H2Matrix.hpp:32-45)
+template <typename Scalar_>
+struct traits<H2MatrixGPU<Scalar_>> {
+  typedef Scalar_ Scalar;
+  typedef int StorageIndex;
+  typedef H2 StorageKind;
+  typedef MatrixXpr XprKind;
+  enum {
+    RowsAtCompileTime = Dynamic,
+    ColsAtCompileTime = Dynamic,
+    MaxRowsAtCompileTime = Dynamic,
+    MaxColsAtCompileTime = Dynamic,
+    Flags = NestByRefBit
+  };
+};
+// as is_ref_compatible<H2Matrix<S>> (H2Matrix.hpp:48-54): Eigen's solvers
+// must hold the operator by reference, never copy it into a Ref
+template <typename Scalar_>
+struct is_ref_compatible<H2MatrixGPU<Scalar_>> {
+  enum { value = false };
+};
+template <typename Scalar_>
+struct is_ref_compatible<const H2MatrixGPU<Scalar_>> : is_ref_compatible<H2MatrixGPU<Scalar_>> {};
+}  // namespace internal
+
+template <typename Scalar_>
+class H2MatrixGPU : public H2MatrixBase<H2MatrixGPU<Scalar_>> {
+ public:
+  typedef Scalar_ Scalar;
+  typedef typename NumTraits<Scalar>::Real RealScalar;
+  typedef Index StorageIndex;
+  enum { ColsAtCompileTime = Dynamic, MaxColsAtCompileTime = Dynamic, IsRowMajor = false, Flags = NestByRefBit };
+
+  H2MatrixGPU() {}
+  explicit H2MatrixGPU(std::shared_ptr<bembel_gb300::Operator<Scalar>> op) : op_(std::move(op)) {}
+  Index rows() const { return op_ ? op_->rows() : 0; }
+  Index cols() const { return op_ ? op_->cols() : 0; }
+  template <typename Rhs>
+  Product<H2MatrixGPU, Rhs, AliasFreeProduct> operator*(const MatrixBase<Rhs>& x) const {
+    return Product<H2MatrixGPU, Rhs, AliasFreeProduct>(*this, x.derived());
+  }
+  // precision of the products Eigen's solvers request (bg_precision)
+  void set_precision(int p) { precision_ = p; }
+  int precision() const { return precision_; }
+  const std::shared_ptr<bembel_gb300::Operator<Scalar>>& gpu_operator() const { return op_; }
+  void set_gpu_operator(std::shared_ptr<bembel_gb300::Operator<Scalar>> op) { op_ = std::move(op); }
+
+ private:
+  std::shared_ptr<bembel_gb300::Operator<Scalar>> op_;
+  int precision_ = BG_PREC_FP64;
+};
+
+namespace internal {
+// res += alpha * A * rhs, all columns in one bg_matvec call (the reference
+// runs one H2 product per column, H2DenseProduct.hpp:33-165); reached from
+// generic_product_impl<Lhs, Rhs, H2, DenseShape, ...>::scaleAndAddTo
+// (H2DenseProduct.hpp:260-290) for H2MatrixGPU and every expression of it
+template <typename Scalar_, typename DenseRhsType, typename DenseResType, typename AlphaType>
+struct H2_time_dense_product_impl<H2MatrixGPU<Scalar_>, DenseRhsType, DenseResType, AlphaType, ColMajor, true> {
+  static void run(const H2MatrixGPU<Scalar_>& lhs, const DenseRhsType& rhs, DenseResType& res,
+                  const AlphaType& alpha) {
+    typedef Matrix<Scalar_, Dynamic, Dynamic> Block;
+    const Block x = rhs;  // contiguous, column-major
+    Block y = res;
+    lhs.gpu_operator()->matvec(x.data(), x.rows(), y.data(), y.rows(), (int)x.cols(), Scalar_(alpha), Scalar_(1),
+                               lhs.precision(), false);
+    res = y;
+  }
+};
+}  // namespace internal
+}  // namespace Eigen
+
+#else
+// Eigen alone (no Bembel): a matrix-free operator with SparseMatrix traits
+// (the trick H2Matrix.hpp:16-25 describes), enough for Eigen's iterative
+// solvers; expressions of several operators need Bembel's H2 storage kind.
+namespace Eigen {
+template <typename Scalar_>
+class H2MatrixGPU;
+namespace internal {
 template <typename Scalar_>
 struct traits<H2MatrixGPU<Scalar_>> : public traits<SparseMatrix<Scalar_>> {};
+template <typename Scalar_>
+struct is_ref_compatible<H2MatrixGPU<Scalar_>> {
+  enum { value = false };
+};
+template <typename Scalar_>
+struct is_ref_compatible<const H2MatrixGPU<Scalar_>> : is_ref_compatible<H2MatrixGPU<Scalar_>> {};
 }  // namespace internal
 
 template <typename Scalar_>
@@ -229,7 +319,6 @@ class H2MatrixGPU : public EigenBase<H2MatrixGPU<Scalar_>> {
   Product<H2MatrixGPU, Rhs, AliasFreeProduct> operator*(const MatrixBase<Rhs>& x) const {
     return Product<H2MatrixGPU, Rhs, AliasFreeProduct>(*this, x.derived());
   }
-  // precision of the products Eigen's solvers request (bg_precision)
   void set_precision(int p) { precision_ = p; }
   int precision() const { return precision_; }
   const std::shared_ptr<bembel_gb300::Operator<Scalar>>& gpu_operator() const { return op_; }
@@ -260,9 +349,31 @@ struct generic_product_impl<H2MatrixGPU<Scalar_>, Rhs, SparseShape, DenseShape, 
 };
 }  // namespace internal
 }  // namespace Eigen
+#endif
 
 #if __has_include(<Bembel/AnsatzSpace>) && defined(BEMBEL_SRC_LINEAROPERATOR_DISCRETEOPERATOR_HPP_)
 namespace Bembel {
+namespace gb300_detail {
+// the wavenumber of the Helmholtz and Maxwell operators; Laplace has none.
+// The reference's get_wavenumber() is not const
+// (Helmholtz/SingleLayerOperator.hpp:130, Maxwell/SingleLayerOperator.hpp:141),
+// so it is read from a copy. Overloads instead of `if constexpr`: Bembel
+// builds as C++11 (CMakeLists.txt:74).
+template <typename Derived>
+inline void set_wavenumber(bembel_gb300::Operator<std::complex<double>>& op, const Derived& lin_op) {
+  Derived copy(lin_op);
+  op.set_wavenumber(std::complex<double>(copy.get_wavenumber()));
+}
+template <typename Derived>
+inline void set_wavenumber(bembel_gb300::Operator<double>&, const Derived&) {}
+template <typename Derived>
+inline int op_kind() {
+  return std::is_same<Derived, HelmholtzSingleLayerOperator>::value
+             ? BG_HELMHOLTZ_SL
+             : (std::is_same<Derived, MaxwellSingleLayerOperator>::value ? BG_MAXWELL_SL : BG_LAPLACE_SL);
+}
+}  // namespace gb300_detail
+
 template <typename Derived>
 struct DiscreteOperatorComputer<Eigen::H2MatrixGPU<typename LinearOperatorTraits<Derived>::Scalar>, Derived> {
   typedef typename LinearOperatorTraits<Derived>::Scalar Scalar;
@@ -284,12 +395,10 @@ struct DiscreteOperatorComputer<Eigen::H2MatrixGPU<typename LinearOperatorTraits
       data.insert(data.end(), p.data_.begin(), p.data_.end());
     }
     auto geo = bembel_gb300::Geometry::from_bezier(ctx, px, py, data);
-    constexpr bool helmholtz = std::is_same<Derived, HelmholtzSingleLayerOperator>::value;
-    constexpr bool maxwell = std::is_same<Derived, MaxwellSingleLayerOperator>::value;
-    const int kind = helmholtz ? BG_HELMHOLTZ_SL : (maxwell ? BG_MAXWELL_SL : BG_LAPLACE_SL);
     auto op = std::make_shared<bembel_gb300::Operator<Scalar>>(geo, ansatz_space.get_refinement_level(),
-                                                               ansatz_space.get_polynomial_degree(), kind);
-    if constexpr (helmholtz || maxwell) op->set_wavenumber(std::complex<double>(lin_op.get_wavenumber()));
+                                                               ansatz_space.get_polynomial_degree(),
+                                                               gb300_detail::op_kind<Derived>());
+    gb300_detail::set_wavenumber<Derived>(*op, lin_op);
     op->assemble();
     disc_op->set_gpu_operator(op);
   }

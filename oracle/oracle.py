@@ -65,6 +65,10 @@ def lib():
         L.orc_potential.argtypes = [P, dp, dp, I, dp]
         L.orc_gmres.restype = I
         L.orc_gmres.argtypes = [P, dp, dp, D, I, I]
+        L.orc_set_leaf.restype = I
+        L.orc_set_leaf.argtypes = [P, L_, I, I, dp]
+        L.orc_cg.restype = I
+        L.orc_cg.argtypes = [P, dp, dp, D, I, dp]
         L.orc_create_sampled.restype = P
         L.orc_create_sampled.argtypes = [ctypes.c_char_p, I, I, I, D, D, I, D, I, I]
         L.orc_last_product_split.argtypes = [P, dp]
@@ -216,6 +220,12 @@ class Problem:
             raise RuntimeError("H2 matrix not assembled")
         return buf.T.copy()
 
+    def set_leaf_matrix(self, leaf, F, rc=0, cc=0):
+        """Store leaf matrix F (a problem made with assemble=False)."""
+        buf = np.asfortranarray(F, dtype=self.dtype)
+        if lib().orc_set_leaf(self.h, leaf, rc, cc, _dp(buf.reshape(-1, order="F").view(np.float64))) != 0:
+            raise RuntimeError("leaf index out of range")
+
     def element_pair(self, id1, id2):
         n = self.vd * (self.P + 1) ** 2
         buf = np.zeros((n, n), dtype=self.dtype)
@@ -304,6 +314,16 @@ class Problem:
         x = np.zeros_like(b)
         it = lib().orc_gmres(self.h, _dp(b.view(np.float64)), _dp(x.view(np.float64)), tol, restart, maxit)
         return x, it
+
+    def cg(self, b, tol=1e-8, maxit=None):
+        """Unpreconditioned CG from x = 0 (the reference's Laplace solver); (x, iterations, relres)."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        rr = np.zeros(1)
+        it = lib().orc_cg(self.h, _dp(b), _dp(x), tol, maxit if maxit else 2 * self.N, _dp(rr))
+        if it < 0:
+            raise RuntimeError("CG needs a real symmetric operator")
+        return x, it, float(rr[0])
 
 
 def threads():

@@ -8,7 +8,9 @@
 // Python tests load with ctypes.
 #include <omp.h>
 
+#include <algorithm>
 #include <chrono>
+#include <limits>
 #include <memory>
 
 #include "oracle_space.hpp"
@@ -117,33 +119,47 @@ void h2_product_ss(Problem& p, const S* xss, S* yss) {
       for (int i = 0; i < comp; ++i) X.a[i] = xr[i];
       std::vector<Mat<S>> fwd = forward_transform<S>(momc, p.transfer, steps, X);
       std::vector<S> dst(comp, S(0));
-      std::vector<Mat<S>> bw;
-      for (auto& f : fwd) bw.emplace_back(f.rows, f.cols);
       auto tl0 = std::chrono::steady_clock::now();
-      for (auto& lf : L) {
-        if (lf.F.empty()) continue;  // not assembled (sampled operator)
-        const Mat<S>& F = lf.F[rc * vd + cc];
-        const Node& c1 = p.ss.et.nodes[lf.c1];
-        const Node& c2 = p.ss.et.nodes[lf.c2];
-        if (lf.cc == kDense) {
-          int r0 = n * p.ss.et.cluster_first(lf.c1), c0 = n * p.ss.et.cluster_first(lf.c2);
-          for (int c = 0; c < F.cols; ++c) {
-            S xv = xr[c0 + c];
-            for (int r = 0; r < F.rows; ++r) dst[r0 + r] += F(r, c) * xv;
-          }
-        } else {
-          int lvl = p.bct.max_level - p.bct.mcl - c1.level;
-          Mat<S>& Z = bw[lvl];
-          const Mat<S>& Y = fwd[lvl];
-          for (int c = 0; c < F.cols; ++c) {
-            S yv = Y(c, c2.id);
-            for (int r = 0; r < F.rows; ++r) Z(r, c1.id) += F(r, c) * yv;
+      // The reference's OpenMP structure (H2DenseProduct.hpp:82-150): every
+      // thread owns a full destination and full backward-transform targets,
+      // the leaves are shared out one at a time, each thread runs its own
+      // backward transform, and the destinations are summed in a critical
+      // section. (The reference hands out leaves with `omp single nowait`;
+      // a dynamic loop hands them out the same way with less locking.)
+#pragma omp parallel
+      {
+        std::vector<S> mine(comp, S(0));
+        std::vector<Mat<S>> bw;
+        for (auto& f : fwd) bw.emplace_back(f.rows, f.cols);
+#pragma omp for schedule(dynamic, 8) nowait
+        for (long li = 0; li < (long)L.size(); ++li) {
+          const H2Leaf<S>& lf = L[li];
+          if (lf.F.empty()) continue;  // not assembled (sampled operator)
+          const Mat<S>& F = lf.F[rc * vd + cc];
+          const Node& c1 = p.ss.et.nodes[lf.c1];
+          const Node& c2 = p.ss.et.nodes[lf.c2];
+          if (lf.cc == kDense) {
+            int r0 = n * p.ss.et.cluster_first(lf.c1), c0 = n * p.ss.et.cluster_first(lf.c2);
+            for (int c = 0; c < F.cols; ++c) {
+              S xv = xr[c0 + c];
+              for (int r = 0; r < F.rows; ++r) mine[r0 + r] += F(r, c) * xv;
+            }
+          } else {
+            int lvl = p.bct.max_level - p.bct.mcl - c1.level;
+            Mat<S>& Z = bw[lvl];
+            const Mat<S>& Y = fwd[lvl];
+            for (int c = 0; c < F.cols; ++c) {
+              S yv = Y(c, c2.id);
+              for (int r = 0; r < F.rows; ++r) Z(r, c1.id) += F(r, c) * yv;
+            }
           }
         }
+        std::vector<S> back = backward_transform<S>(p.mom[rc], p.transfer, steps, bw);
+#pragma omp critical
+        for (int i = 0; i < comp; ++i) dst[i] += mine[i] + back[i];
       }
       p.t_leaves += std::chrono::duration<double>(std::chrono::steady_clock::now() - tl0).count();
-      std::vector<S> back = backward_transform<S>(p.mom[rc], p.transfer, steps, bw);
-      for (int i = 0; i < comp; ++i) yss[(size_t)rc * comp + i] += dst[i] + back[i];
+      for (int i = 0; i < comp; ++i) yss[(size_t)rc * comp + i] += dst[i];
     }
 }
 
@@ -444,6 +460,55 @@ int gmres(Problem& p, const S* b, S* x, double tol, int restart, int maxit) {
   return it;
 }
 
+// Conjugate gradient without preconditioning, the solver of the reference's
+// Laplace example (examples/LaplaceSingleLayerH2.cpp:77-80:
+// ConjugateGradient<H2Matrix<double>, Lower | Upper, IdentityPreconditioner>).
+// The iteration is the published Hestenes-Stiefel CG as Eigen 3 implements it
+// (Eigen/src/IterativeLinearSolvers/ConjugateGradient.h, third party, version
+// not pinned by the reference): start at x = 0, stop when
+// ||r||^2 < tol^2 ||b||^2, at most maxit iterations (Eigen's default is
+// 2 N). Returns the iteration count; *relres gets ||r|| / ||b|| of the
+// recursively updated residual, as Eigen's error() does.
+int cg(Problem& p, const double* b, double* x, double tol, int maxit, double* relres) {
+  const int N = p.N();
+  auto dot = [&](const std::vector<double>& u, const std::vector<double>& v) {
+    double s = 0;
+    for (int i = 0; i < N; ++i) s += u[i] * v[i];
+    return s;
+  };
+  std::vector<double> r(b, b + N), d(N), Ad(N);
+  for (int i = 0; i < N; ++i) x[i] = 0;
+  const double bn2 = dot(r, r);
+  *relres = 0;
+  if (bn2 == 0) return 0;
+  const double threshold = std::max(tol * tol * bn2, std::numeric_limits<double>::min());
+  double rn2 = bn2;
+  if (rn2 < threshold) {
+    *relres = std::sqrt(rn2 / bn2);
+    return 0;
+  }
+  d = r;
+  double absnew = rn2;
+  int it = 0;
+  while (it < maxit) {
+    h2_matvec<double>(p, d.data(), Ad.data(), 1);
+    const double alpha = absnew / dot(d, Ad);
+    for (int i = 0; i < N; ++i) {
+      x[i] += alpha * d[i];
+      r[i] -= alpha * Ad[i];
+    }
+    rn2 = dot(r, r);
+    ++it;
+    if (rn2 < threshold) break;
+    const double absold = absnew;
+    absnew = rn2;
+    const double beta = absnew / absold;
+    for (int i = 0; i < N; ++i) d[i] = r[i] + beta * d[i];
+  }
+  *relres = std::sqrt(rn2 / bn2);
+  return it;
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -593,6 +658,36 @@ int orc_leaf_matrix(void* h, long leaf, int rc, int cc, double* out) {
     std::memcpy(out, F.a.data(), F.a.size() * sizeof(double));
   }
   return 0;
+}
+
+// Put a leaf matrix (column-major, the layout orc_leaf_matrix reads) into a
+// problem created without assembly, for timing the CPU products and solves
+// on entries computed elsewhere. The first call sizes the leaf table from the
+// block partition.
+int orc_set_leaf(void* h, long leaf, int rc, int cc, const double* in) {
+  Problem& p = *static_cast<Problem*>(h);
+  const int vd = p.vd(), n = p.ss.p2();
+  if (leaf < 0 || leaf >= (long)p.bct.leaves.size() || rc < 0 || rc >= vd || cc < 0 || cc >= vd) return -1;
+  auto fill = [&](auto& L, auto zero) -> int {
+    using S = decltype(zero);
+    if (L.size() != p.bct.leaves.size()) {
+      L.resize(p.bct.leaves.size());
+      for (size_t li = 0; li < L.size(); ++li) {
+        L[li].cc = p.bct.leaves[li].cc;
+        L[li].c1 = p.bct.leaves[li].c1;
+        L[li].c2 = p.bct.leaves[li].c2;
+      }
+    }
+    const BlockLeaf& bl = p.bct.leaves[leaf];
+    const int rows = bl.cc == kDense ? p.ss.et.cluster_size(bl.c1) * n : p.op.nc() * p.np * p.np;
+    const int cols = bl.cc == kDense ? p.ss.et.cluster_size(bl.c2) * n : p.op.nc() * p.np * p.np;
+    auto& F = L[leaf].F;
+    if (F.size() != (size_t)vd * vd) F.assign(vd * vd, Mat<S>(rows, cols));
+    std::memcpy(static_cast<void*>(F[rc * vd + cc].a.data()), in, (size_t)rows * cols * sizeof(S));
+    return 0;
+  };
+  if (p.op.is_complex()) return fill(p.leaves_c, cplx(0));
+  return fill(p.leaves_r, 0.0);
 }
 
 // intval of evaluateBilinearForm for one element pair ((vd p^2)^2, col-major)
@@ -772,6 +867,11 @@ int orc_gmres(void* h, const double* b, double* x, double tol, int restart, int 
   if (p.op.is_complex())
     return gmres<cplx>(p, reinterpret_cast<const cplx*>(b), reinterpret_cast<cplx*>(x), tol, restart, maxit);
   return gmres<double>(p, b, x, tol, restart, maxit);
+}
+int orc_cg(void* h, const double* b, double* x, double tol, int maxit, double* relres) {
+  Problem& p = *static_cast<Problem*>(h);
+  if (p.op.is_complex()) return -1;
+  return cg(p, b, x, tol, maxit, relres);
 }
 int orc_threads() { return omp_get_max_threads(); }
 

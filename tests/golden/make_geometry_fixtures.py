@@ -23,4 +23,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_geometry_fixtures.py <reference checkout root>")
+    main(sys.argv[1])

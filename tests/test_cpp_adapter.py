@@ -1,5 +1,5 @@
 """The header-style C++ front end (include/bembel_gb300/H2MatrixGPU.hpp):
-compiled with g++ against the library and run (host-only checks on the CPU,
+compiled with g++ as C++11 (the standard Bembel builds with) against the library and run (host-only checks on the CPU,
 assembly + products + solve on a GPU)."""
 import os
 import shutil
@@ -21,7 +21,7 @@ def adapter_exe(tmp_path_factory):
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("adapter") / "adapter_check")
     libdir = os.path.dirname(_lib.LIB_PATH)
-    cmd = [cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "adapter_check.cpp"),
+    cmd = [cxx, "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "adapter_check.cpp"),
            "-L", libdir, "-lbembel_gb300", "-Wl,-rpath," + libdir, "-o", out]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return out

@@ -51,17 +51,25 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch, capsys):
     assert capsys.readouterr().out == ""
 
 
-def test_reference_arm_json_line():
+def test_reference_arm_json_line(monkeypatch, capsys):
     """bench.py --impl reference: one JSON line with the arm's metric, the
     steps and warm-up it was given, the CPU baseline it measured and an e2e
-    block without host-device copies (about 20 s on 8 cores)."""
+    block without host-device copies. Run in-process on a smaller sphere
+    (M = 3, P = 1, n_p = 6) so that it takes seconds; the line's structure is
+    what is checked."""
     import json
-    import subprocess
-    import sys
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
-                        "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
-    assert r.returncode == 0, r.stderr[-2000:]
-    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.setattr(bench, "M", 3)
+    monkeypatch.setattr(bench, "P", 1)
+    monkeypatch.setattr(bench, "NP", 6)
+
+    class Args:
+        gpus, steps, warmup = 1, 2, 1
+    bench.run_reference(Args())
+    out = capsys.readouterr().out
+    lines = [l for l in out.splitlines() if l.startswith("{")]
     assert len(lines) == 1
     j = json.loads(lines[0])
     assert j["impl"] == "reference" and j["unit"] == "solves/s" and j["higher_is_better"] is True
@@ -70,6 +78,8 @@ def test_reference_arm_json_line():
     assert j["cpu_baseline"]["kind"] == "port" and j["cpu_baseline"]["sample"]
     assert j["e2e"] == {"value": j["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert j["config"]["workload"] == "laplace_sl_h2_sphere_M5_P2_np9_32rhs"
+    assert j["full_solve"]["iterations"] > 0 and j["full_solve"]["final_relres"] <= 1e-8
+    assert "measured" in j["cpu_baseline"]["sample"]
 
 
 def test_bench_column_errors():
