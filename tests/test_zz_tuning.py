@@ -5,7 +5,9 @@ orders only permute which persistent CTA computes a row, so the result agrees
 to 1e-9 relative (each row is still summed by one CTA in block order); the
 near-field kernel variants and the split-K threshold change FP32 summation
 orders, so they agree to 1e-5 relative, the tolerance of the other FP32
-product tests. The autotuner's chosen plan is then set on the operator and
+product tests. The two transform paths (fused launches through the
+tensor-product factors, or batched GEMMs with the assembled FMM matrices)
+agree to rounding: 1e-12 for the FP64 product, 1e-5 for FP32. The autotuner's chosen plan is then set on the operator and
 gives the same product. Collected after the other product tests.
 """
 import numpy as np
@@ -55,6 +57,8 @@ def test_every_plan_gives_the_builtin_product(laplace_m4, prec):
     for order in (1, 2):
         d.set_plan(32, prec, far_order=order)
         assert _rel(A.matvec(x, precision=prec), y0) < ORDER_TOL
+    d.set_plan(32, prec, transforms=1)
+    assert _rel(A.matvec(x, precision=prec), y0) < FP32_TOL
     for split in (0, 608):
         d.set_plan(32, prec, split_k_batches=split)
         assert _rel(A.matvec(x, precision=prec), y0) < FP32_TOL
@@ -76,7 +80,7 @@ def test_autotune_sets_a_plan_with_the_same_product(laplace_m4, prec):
     assert r["candidates"] >= 1 and r["builtin_ms"] > 0 and 0 < r["tuned_ms"] <= r["builtin_ms"]
     assert d.get_plan(32, prec) == r["plan"]
     if prec == "fp64":
-        assert r["candidates"] == 1
+        assert r["candidates"] == 2  # the built-in plan and the batched-GEMM transforms
     tol = 1e-12 if prec == "fp64" else FP32_TOL
     assert _rel(A.matvec(x, precision=prec), y0) < tol
     d.set_plan(32, prec)
@@ -94,3 +98,14 @@ def test_complex_near_variants(ctx):
     r = d.autotune(8, "fp32", reps=2)
     assert r["candidates"] >= 3
     assert _rel(A.matvec(x, precision="fp32"), y0) < FP32_TOL
+
+
+def test_fp64_transform_paths_agree(laplace_m4):
+    d = laplace_m4
+    A = d.get_discrete_operator()
+    x = np.random.default_rng(14).uniform(-1, 1, (d.N, 5))
+    d.set_plan(5, "fp64")
+    y0 = A.matvec(x)
+    d.set_plan(5, "fp64", transforms=1)
+    assert _rel(A.matvec(x), y0) < 1e-12
+    d.set_plan(5, "fp64")
