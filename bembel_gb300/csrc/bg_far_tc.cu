@@ -454,18 +454,32 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 // stages of tiles move by 1-D TMA bulk copies; two accumulator buffers.
 constexpr int kH16Stages = 4;
 
+// The coupling (A) tiles store K padded only to the 8-element core-matrix
+// width, KA, while the MMA steps K by 16 up to KP. Where KA < KP the last
+// K step reads one core-matrix column past a row group's end: the first
+// column of the next row group (or, after the last row group, of the next
+// tile in the stage), finite data that meets the zero rows KA .. KP - 1 of
+// the right-hand-side (B) tiles, which keep the full KP. Rows beyond the
+// stored row groups (M = 128 reads 16) only feed output rows >= NP2, which
+// are never read.
 template <int NP2>
 struct H16Shape {
   static constexpr int KP = (NP2 + 15) / 16 * 16;  // K padded to the f16 MMA K step
-  static constexpr int KC = KP / 8;                // 16-byte core-matrix columns (8 halves)
+  static constexpr int KC = KP / 8;                // 16-byte core-matrix columns (8 halves) of a B tile
+  static constexpr int KA = (NP2 + 7) / 8 * 8;     // K stored in the A tiles
+  static constexpr int KCA = KA / 8;
   static constexpr int MG = (NP2 + 7) / 8;
-  static constexpr uint32_t SBO = KC * 128;
-  static constexpr uint32_t A_BYTES = MG * SBO, B_BYTES = 4 * SBO;
+  static constexpr uint32_t SBO = KC * 128;        // B tiles: bytes between 8-row groups
+  static constexpr uint32_t SBOA = KCA * 128;      // A tiles
+  static constexpr uint32_t A_BYTES = MG * SBOA, B_BYTES = 4 * SBO;
   static constexpr uint32_t A2 = 2 * A_BYTES, B2 = 2 * B_BYTES;
   static constexpr uint32_t STAGE = A2 + B2;
   static constexpr uint32_t TILES = kH16Stages * STAGE;
-  static constexpr uint32_t NEED = (kH16Stages - 1) * STAGE + A_BYTES + 16 * SBO;
+  // furthest byte an M = 128 A operand reads, from its start
+  static constexpr uint32_t A_READ = 15 * SBOA + KC * 128;
+  static constexpr uint32_t NEED = (kH16Stages - 1) * STAGE + A_BYTES + A_READ;
   static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
+  static_assert(KP - KA <= 8, "one aliased core-matrix column at most");
 };
 
 // kind::f16 instruction descriptor: D FP32, A and B FP16, both K-major.
@@ -579,7 +593,7 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
           const uint32_t d_hh = tmem + (uint32_t)(64 * ab), d_cr = d_hh + 32;
 #pragma unroll
           for (int pass = 0; pass < 3; ++pass) {
-            uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBO);
+            uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBOA);
             uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
             const uint32_t dd = pass == 0 ? d_hh : d_cr;
 #pragma unroll
@@ -655,7 +669,7 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
 
 // A tiles of nblocks FP64 blocks (column-major, stride bstride): one CTA per
 // block finds the largest coupling, picks sA, writes [hi tile][lo tile] with
-// entry (m, k) in core matrix (m / 8) * KC + k / 8 at row m % 8, element k % 8,
+// entry (m, k) in core matrix (m / 8) * KCA + k / 8 at row m % 8, element k % 8,
 // and 1/sA to ainv[b].
 template <int NP2>
 __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restrict__ F, long bstride,
@@ -676,7 +690,7 @@ __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restri
   __half* out = tiles + b * 2 * AH;
   for (int e = threadIdx.x; e < AH; e += blockDim.x) {
     const int cm = e >> 6, r = (e >> 3) & 7, c = e & 7;
-    const int m = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + c;
+    const int m = (cm / G::KCA) * 8 + r, k = (cm % G::KCA) * 8 + c;
     const double v = (m < NP2 && k < NP2) ? Fb[(long)k * NP2 + m] * (double)sa : 0.0;
     const __half h = __double2half(v);
     out[e] = h;
@@ -818,12 +832,12 @@ constexpr uint32_t kTmemColsC = 256;
 template <int NP2>
 struct H16CShape {
   using R = H16Shape<NP2>;
-  static constexpr uint32_t SBO = R::SBO, A_BYTES = R::A_BYTES, B_BYTES = R::B_BYTES;
+  static constexpr uint32_t SBO = R::SBO, SBOA = R::SBOA, A_BYTES = R::A_BYTES, B_BYTES = R::B_BYTES;
   static constexpr uint32_t A4 = 4 * A_BYTES, B2 = 2 * B_BYTES;
   static constexpr uint32_t STAGE = A4 + B2;
   static constexpr uint32_t TILES = kH16CStages * STAGE;
   // an M = 128 operand read starting at the last A tile of the last stage
-  static constexpr uint32_t NEED = (kH16CStages - 1) * STAGE + 3 * A_BYTES + 16 * SBO;
+  static constexpr uint32_t NEED = (kH16CStages - 1) * STAGE + 3 * A_BYTES + R::A_READ;
   static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
 };
 
@@ -916,7 +930,7 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
             const uint32_t d_hh = tmem + (uint32_t)(128 * ab + 64 * part), d_cr = d_hh + 32;
 #pragma unroll
             for (int pass = 0; pass < 3; ++pass) {
-              uint64_t ad = umma_desc(pass == 2 ? alo : ahi, 128, G::SBO);
+              uint64_t ad = umma_desc(pass == 2 ? alo : ahi, 128, G::SBOA);
               uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
               const uint32_t dd = pass == 0 ? d_hh : d_cr;
 #pragma unroll
@@ -1021,7 +1035,7 @@ __global__ void __launch_bounds__(256) k_build_h16c_atiles(const double2* __rest
   __half* out = tiles + b * 4 * AH;
   for (int e = threadIdx.x; e < AH; e += blockDim.x) {
     const int cm = e >> 6, r = (e >> 3) & 7, c = e & 7;
-    const int m = (cm / G::KC) * 8 + r, k = (cm % G::KC) * 8 + c;
+    const int m = (cm / G::KCA) * 8 + r, k = (cm % G::KCA) * 8 + c;
     double2 v = make_double2(0.0, 0.0);
     if (m < NP2 && k < NP2) v = Fb[(long)k * NP2 + m];
     const double vr = v.x * (double)sa, vi = v.y * (double)sa;
