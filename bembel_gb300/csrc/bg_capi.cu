@@ -464,6 +464,7 @@ static bg_status upload_tables(bg_operator* op) {
         BG_CHECK(op->d_fmm_fac64.upload(fac, s), "upload transforms");
         BG_CHECK(op->d_fmm_fac32.upload(f32, s), "upload transforms");
         BG_CHECK(op->d_fmm_cmap.upload(cmap, s), "upload transforms");
+        op->fmm_hfac = fac;
         op->fmm_w1 = w1;
         op->fmm_fused = true;
       }
@@ -1293,7 +1294,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       const int kk = (op->cplx ? 2 : 1) * nrhs;
       if (mixed) fill_fmm<float>(op, op->d_fmm_fac32.p, kk, xc0, yfar, &fa.f32);
       else fill_fmm<double>(op, op->d_fmm_fac64.p, kk, xc0, yfar, &fa.f64);
-      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_up(Sfar, fa, op->nclusters(Ll - 1), s); }),
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_up(Sfar, fa, op->fmm_hfac.data(), op->nclusters(Ll - 1), s); }),
                "forward transforms (fused)");
     }
     for (int c = 0; c < op->vd && !op->maxwell() && !fused_tr; ++c) {
@@ -1510,7 +1511,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
                  "backward moments");
     }
     if (fused_tr)
-      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_down(Sfar, fa, op->nclusters(Ll - 1), s); }),
+      BG_CHECK(timed_launch(op->ctx, KC_TRANSFORM, [&] { return launch_fmm_down(Sfar, fa, op->fmm_hfac.data(), op->nclusters(Ll - 1), s); }),
                "backward transforms (fused)");
     for (int c = 0; c < op->vd && !op->maxwell() && !fused_tr; ++c) {
       for (int l = 0; l < Ll; ++l) {

@@ -36,6 +36,7 @@
 // Warp w owns output rows w, w + 8, ... of every stage.
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "bg_kernels.cuh"
 
@@ -313,6 +314,311 @@ __global__ void __launch_bounds__(kFmmThreads) k_fmm_down(FmmLevels<T> a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same two passes with the sizes fixed at compile time (n_p and the 1-D
+// moment width w1 of the common discretisations). The 1-D factors travel in
+// the kernel parameters, so with every loop unrolled each multiply-add takes
+// its factor straight from the constant bank; a warp owns one row (or column)
+// of the 2-D coefficient grid per stage and keeps that row's data in
+// registers, so shared memory is read once per operand row, not per
+// multiply-add. One warp per point row: NP warps.
+template <typename T, int NP, int W1>
+struct FmmFactors {
+  T E[2][NP * NP];  // E[h][c * NP + p]
+  T Ms[NP * W1];    // Ms[i * W1 + a]
+  T Mt[NP * W1];
+};
+
+// V[cs][pt] = sum_ct E_H[ct][pt] C[cs][ct]; warp = cs
+template <typename T, int NP, int W1, int H>
+__device__ __forceinline__ void tup1(const FmmFactors<T, NP, W1>& f, const T* C, T* V, int w, int lane) {
+  if (w >= NP) return;
+  T c[NP];
+#pragma unroll
+  for (int ct = 0; ct < NP; ++ct) c[ct] = C[(w * NP + ct) * kFmmCols + lane];
+#pragma unroll
+  for (int pt = 0; pt < NP; ++pt) {
+    T v = T(0);
+#pragma unroll
+    for (int ct = 0; ct < NP; ++ct) v = fma(f.E[H][ct * NP + pt], c[ct], v);
+    V[(w * NP + pt) * kFmmCols + lane] = v;
+  }
+}
+// acc[ps] += sum_cs E_H[cs][ps] V[cs][pt]; warp = pt
+template <typename T, int NP, int W1, int H>
+__device__ __forceinline__ void tup2(const FmmFactors<T, NP, W1>& f, const T* V, T* acc, int w, int lane) {
+  if (w >= NP) return;
+  T v[NP];
+#pragma unroll
+  for (int cs = 0; cs < NP; ++cs) v[cs] = V[(cs * NP + w) * kFmmCols + lane];
+#pragma unroll
+  for (int ps = 0; ps < NP; ++ps) {
+    T a = acc[ps];
+#pragma unroll
+    for (int cs = 0; cs < NP; ++cs) a = fma(f.E[H][cs * NP + ps], v[cs], a);
+    acc[ps] = a;
+  }
+}
+// child K of a parent: both transfer stages, summed into acc
+template <typename T, int NP, int W1, int K>
+__device__ __forceinline__ void tup_child(const FmmFactors<T, NP, W1>& f, const T* C, T* V, T* acc, int w,
+                                          int lane) {
+  constexpr int HT = K >> 1, HS = (K == 1 || K == 2) ? 1 : 0;
+  tup1<T, NP, W1, HT>(f, C, V, w, lane);
+  __syncthreads();
+  tup2<T, NP, W1, HS>(f, V, acc, w, lane);
+  __syncthreads();
+}
+// moments of one leaf cluster: W[i][b] = sum_a Ms[i][a] X[q(a, b)] (warp = b),
+// then C[i][i2] = sum_b Mt[i2][b] W[i][b] (warp = i), written to yout too
+template <typename T, int NP, int W1>
+__device__ __forceinline__ void tmom(const FmmFactors<T, NP, W1>& f, const T* X, const int* q_of, T* W, T* C,
+                                     T* yout, int kk, bool on, int w, int lane) {
+  if (w < W1) {
+    T x[W1];
+#pragma unroll
+    for (int a = 0; a < W1; ++a) x[a] = X[q_of[a * W1 + w] * kFmmCols + lane];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      T v = T(0);
+#pragma unroll
+      for (int a = 0; a < W1; ++a) v = fma(f.Ms[i * W1 + a], x[a], v);
+      W[(i * W1 + w) * kFmmCols + lane] = v;
+    }
+  }
+  __syncthreads();
+  if (w < NP) {
+    T wv[W1];
+#pragma unroll
+    for (int b = 0; b < W1; ++b) wv[b] = W[(w * W1 + b) * kFmmCols + lane];
+#pragma unroll
+    for (int i2 = 0; i2 < NP; ++i2) {
+      T v = T(0);
+#pragma unroll
+      for (int b = 0; b < W1; ++b) v = fma(f.Mt[i2 * W1 + b], wv[b], v);
+      C[(w * NP + i2) * kFmmCols + lane] = v;
+      if (on) yout[(size_t)(w * NP + i2) * kk] = v;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int NP, int W1>
+__global__ void __launch_bounds__(32 * NP) k_fmm_up_t(const __grid_constant__ FmmLevels<T> a, const __grid_constant__ FmmFactors<T, NP, W1> f) {
+  extern __shared__ __align__(16) unsigned char fmm_smem[];
+  constexpr int NP2 = NP * NP, BQ = W1 * W1, NW = NP;
+  // X [4 BQ][32] | W [NP W1][32] | C [NP2][32], then V [NP2][32] after
+  // FRONT rows; the climb reuses the front as Cg [4 NP2][32]
+  constexpr int FRONT = (4 * BQ + NP * W1 + NP2) > 4 * NP2 ? (4 * BQ + NP * W1 + NP2) : 4 * NP2;
+  T* X = reinterpret_cast<T*>(fmm_smem);
+  T* W = X + 4 * BQ * kFmmCols;
+  T* C = W + NP * W1 * kFmmCols;
+  T* V = X + FRONT * kFmmCols;
+  int* q_of = reinterpret_cast<int*>(V + NP2 * kFmmCols);
+  T* Cg = X;
+  const int P = blockIdx.x, chunk = blockIdx.y, c0 = chunk * kFmmCols, kk = a.kk, L = a.L;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool on = c0 + lane < kk;
+  for (int q = threadIdx.x; q < BQ; q += blockDim.x) {
+    const int ab = a.cmap[q];
+    q_of[(ab & 0xFF) * W1 + (ab >> 8)] = q;
+  }
+  for (int r = w; r < 4 * BQ; r += NW)
+    X[r * kFmmCols + lane] = on ? a.x[((size_t)4 * P * BQ + r) * kk + c0 + lane] : T(0);
+  __syncthreads();
+  T acc[NP];
+#pragma unroll
+  for (int u = 0; u < NP; ++u) acc[u] = T(0);
+  auto leaf = [&](auto kc) {
+    constexpr int K = decltype(kc)::value;
+    tmom<T, NP, W1>(f, X + K * BQ * kFmmCols, q_of, W, C, a.y[L] + ((size_t)(4 * P + K) * NP2) * kk + c0 + lane,
+                    kk, on, w, lane);
+    tup_child<T, NP, W1, K>(f, C, V, acc, w, lane);
+  };
+  leaf(std::integral_constant<int, 0>());
+  leaf(std::integral_constant<int, 1>());
+  leaf(std::integral_constant<int, 2>());
+  leaf(std::integral_constant<int, 3>());
+  // warp pt holds column pt of the parent's coefficients
+  auto store = [&](T* dst) {
+    if (w < NP && on)
+#pragma unroll
+      for (int ps = 0; ps < NP; ++ps) dst[(size_t)(ps * NP + w) * kk] = acc[ps];
+  };
+  store(a.y[L - 1] + ((size_t)P * NP2) * kk + c0 + lane);
+  __shared__ int last;
+  int cur = P;
+  for (int l = L - 2; l >= 0; --l) {
+    __syncthreads();  // every store of level l + 1 issued
+    if (threadIdx.x == 0) {
+      __threadfence();
+      int* cnt = a.cnt + a.cnt_off[l] + (size_t)chunk * a.cnt_stride + (cur >> 2);
+      const int old = atomicAdd(cnt, 1);
+      last = old == 3;
+      if (last) {
+        *cnt = 0;  // ready for the next launch
+        __threadfence();
+      }
+    }
+    __syncthreads();
+    if (!last) return;
+    cur >>= 2;
+    const T* src = a.y[l + 1] + ((size_t)4 * cur * NP2) * kk + c0 + lane;
+    for (int r = w; r < 4 * NP2; r += NW) Cg[r * kFmmCols + lane] = on ? __ldcg(src + (size_t)r * kk) : T(0);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < NP; ++u) acc[u] = T(0);
+    tup_child<T, NP, W1, 0>(f, Cg, V, acc, w, lane);
+    tup_child<T, NP, W1, 1>(f, Cg + NP2 * kFmmCols, V, acc, w, lane);
+    tup_child<T, NP, W1, 2>(f, Cg + 2 * NP2 * kFmmCols, V, acc, w, lane);
+    tup_child<T, NP, W1, 3>(f, Cg + 3 * NP2 * kFmmCols, V, acc, w, lane);
+    store(a.y[l] + ((size_t)cur * NP2) * kk + c0 + lane);
+  }
+}
+
+// W[ps][ct] = sum_pt E_H[ct][pt] Z[ps][pt]; warp = ps
+template <typename T, int NP, int W1, int H>
+__device__ __forceinline__ void tdown1(const FmmFactors<T, NP, W1>& f, const T* Z, T* W, int w, int lane) {
+  if (w >= NP) return;
+  T z[NP];
+#pragma unroll
+  for (int pt = 0; pt < NP; ++pt) z[pt] = Z[(w * NP + pt) * kFmmCols + lane];
+#pragma unroll
+  for (int ct = 0; ct < NP; ++ct) {
+    T v = T(0);
+#pragma unroll
+    for (int pt = 0; pt < NP; ++pt) v = fma(f.E[H][ct * NP + pt], z[pt], v);
+    W[(w * NP + ct) * kFmmCols + lane] = v;
+  }
+}
+// out[cs][ct] = base[cs][ct] + sum_ps E_H[cs][ps] W[ps][ct]; warp = ct
+template <typename T, int NP, int W1, int H>
+__device__ __forceinline__ void tdown2(const FmmFactors<T, NP, W1>& f, const T* W, const T* base, int kk, bool on,
+                                       T* out, int w, int lane) {
+  if (w >= NP) return;
+  T v[NP];
+#pragma unroll
+  for (int ps = 0; ps < NP; ++ps) v[ps] = W[(ps * NP + w) * kFmmCols + lane];
+#pragma unroll
+  for (int cs = 0; cs < NP; ++cs) {
+    T o = on ? base[(size_t)(cs * NP + w) * kk] : T(0);
+#pragma unroll
+    for (int ps = 0; ps < NP; ++ps) o = fma(f.E[H][cs * NP + ps], v[ps], o);
+    out[(cs * NP + w) * kFmmCols + lane] = o;
+  }
+}
+template <typename T, int NP, int W1, int K>
+__device__ __forceinline__ void tdown_child(const FmmFactors<T, NP, W1>& f, const T* Zp, T* W, const T* base, int kk,
+                                            bool on, T* out, int w, int lane) {
+  constexpr int HT = K >> 1, HS = (K == 1 || K == 2) ? 1 : 0;
+  tdown1<T, NP, W1, HT>(f, Zp, W, w, lane);
+  __syncthreads();
+  tdown2<T, NP, W1, HS>(f, W, base, kk, on, out, w, lane);
+  __syncthreads();
+}
+
+template <typename T, int NP, int W1>
+__global__ void __launch_bounds__(32 * NP) k_fmm_down_t(const __grid_constant__ FmmLevels<T> a, const __grid_constant__ FmmFactors<T, NP, W1> f) {
+  extern __shared__ __align__(16) unsigned char fmm_smem[];
+  constexpr int NP2 = NP * NP, BQ = W1 * W1, NW = NP;
+  // Zf [NP2][32] | W [NP2][32] | C [NP2][32] | V [NP W1][32]
+  T* Zf = reinterpret_cast<T*>(fmm_smem);
+  T* W = Zf + NP2 * kFmmCols;
+  T* C = W + NP2 * kFmmCols;
+  T* V = C + NP2 * kFmmCols;
+  int* q_of = reinterpret_cast<int*>(V + NP * W1 * kFmmCols);
+  const int P = blockIdx.x, c0 = blockIdx.y * kFmmCols, kk = a.kk, L = a.L;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool on = c0 + lane < kk;
+  for (int q = threadIdx.x; q < BQ; q += blockDim.x) {
+    const int ab = a.cmap[q];
+    q_of[(ab & 0xFF) * W1 + (ab >> 8)] = q;
+  }
+  {
+    const T* z0 = a.z[0] + ((size_t)(P >> (2 * (L - 1))) * NP2) * kk + c0 + lane;
+    for (int r = w; r < NP2; r += NW) Zf[r * kFmmCols + lane] = on ? z0[(size_t)r * kk] : T(0);
+  }
+  __syncthreads();
+  // down the ancestor path to P (Zf is read in stage 1 and rewritten in stage 2)
+  for (int l = 1; l <= L - 1; ++l) {
+    const int al = P >> (2 * (L - 1 - l));
+    const T* base = a.z[l] + ((size_t)al * NP2) * kk + c0 + lane;
+    switch (al & 3) {
+      case 0: tdown_child<T, NP, W1, 0>(f, Zf, W, base, kk, on, Zf, w, lane); break;
+      case 1: tdown_child<T, NP, W1, 1>(f, Zf, W, base, kk, on, Zf, w, lane); break;
+      case 2: tdown_child<T, NP, W1, 2>(f, Zf, W, base, kk, on, Zf, w, lane); break;
+      default: tdown_child<T, NP, W1, 3>(f, Zf, W, base, kk, on, Zf, w, lane); break;
+    }
+  }
+  auto leaf = [&](auto kc) {
+    constexpr int K = decltype(kc)::value;
+    const int lf = 4 * P + K;
+    tdown_child<T, NP, W1, K>(f, Zf, W, a.z[L] + ((size_t)lf * NP2) * kk + c0 + lane, kk, on, C, w, lane);
+    // transposed moments: V[i][b] = sum_j Mt[j][b] C[i][j] (warp = i), then
+    // y[q(a, b)] += sum_i Ms[i][a] V[i][b] (warp = b)
+    if (w < NP) {
+      T c[NP];
+#pragma unroll
+      for (int j = 0; j < NP; ++j) c[j] = C[(w * NP + j) * kFmmCols + lane];
+#pragma unroll
+      for (int b = 0; b < W1; ++b) {
+        T v = T(0);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) v = fma(f.Mt[j * W1 + b], c[j], v);
+        V[(w * W1 + b) * kFmmCols + lane] = v;
+      }
+    }
+    __syncthreads();
+    if (w < W1) {
+      T v[NP];
+#pragma unroll
+      for (int i = 0; i < NP; ++i) v[i] = V[(i * W1 + w) * kFmmCols + lane];
+      T* yo = a.out + ((size_t)lf * BQ) * kk + c0 + lane;
+#pragma unroll
+      for (int aa = 0; aa < W1; ++aa) {
+        T o = T(0);
+#pragma unroll
+        for (int i = 0; i < NP; ++i) o = fma(f.Ms[i * W1 + aa], v[i], o);
+        if (on) {
+          T* dst = yo + (size_t)q_of[aa * W1 + w] * kk;
+          *dst += o;
+        }
+      }
+    }
+    __syncthreads();
+  };
+  leaf(std::integral_constant<int, 0>());
+  leaf(std::integral_constant<int, 1>());
+  leaf(std::integral_constant<int, 2>());
+  leaf(std::integral_constant<int, 3>());
+}
+
+template <typename T, int NP, int W1>
+cudaError_t fmm_launch_t(bool up, const FmmLevels<T>& a, const double* hfac, int nparents, cudaStream_t s) {
+  constexpr int NP2 = NP * NP, BQ = W1 * W1;
+  FmmFactors<T, NP, W1> f;
+  for (int h = 0; h < 2; ++h)
+    for (int e = 0; e < NP2; ++e) f.E[h][e] = (T)hfac[h * NP2 + e];
+  for (int e = 0; e < NP * W1; ++e) {
+    f.Ms[e] = (T)hfac[2 * NP2 + e];
+    f.Mt[e] = (T)hfac[2 * NP2 + NP * W1 + e];
+  }
+  constexpr int FRONT = (4 * BQ + NP * W1 + NP2) > 4 * NP2 ? (4 * BQ + NP * W1 + NP2) : 4 * NP2;
+  const size_t smem = up ? sizeof(T) * kFmmCols * (FRONT + NP2) + sizeof(int) * BQ
+                         : sizeof(T) * kFmmCols * (3 * NP2 + NP * W1) + sizeof(int) * BQ;
+  const dim3 grid(nparents, (a.kk + kFmmCols - 1) / kFmmCols);
+  if (up) {
+    cudaError_t e = smem_limit(k_fmm_up_t<T, NP, W1>, smem);
+    if (e != cudaSuccess) return e;
+    k_fmm_up_t<T, NP, W1><<<grid, 32 * NP, smem, s>>>(a, f);
+  } else {
+    cudaError_t e = smem_limit(k_fmm_down_t<T, NP, W1>, smem);
+    if (e != cudaSuccess) return e;
+    k_fmm_down_t<T, NP, W1><<<grid, 32 * NP, smem, s>>>(a, f);
+  }
+  return cudaGetLastError();
+}
+
 template <typename T>
 size_t fmm_smem_bytes(int np, int w1, int Bq, bool with_x) {
   auto a16 = [](size_t n) { return (n * sizeof(T) + 15) / 16 * 16; };
@@ -323,11 +629,18 @@ size_t fmm_smem_bytes(int np, int w1, int Bq, bool with_x) {
 }
 
 template <typename T>
-cudaError_t fmm_launch(bool up, const FmmLevels<T>& a, int nparents, cudaStream_t s) {
+cudaError_t fmm_launch(bool up, const FmmLevels<T>& a, const double* hfac, int nparents, cudaStream_t s) {
   if (nparents == 0 || a.kk == 0) return cudaSuccess;
   if (a.L < 1 || a.L >= kMaxFarLevels || a.np < 2 || a.np > kFmmMaxNp || a.w1 < 1 || a.w1 * a.w1 != a.Bq ||
       a.w1 > 16)
     return cudaErrorInvalidValue;
+  // compiled sizes: n_p 6, 9, 10 with P = 1, 2 (w1 = 4, 6)
+  if (hfac) {
+#define BG_FMM_T(NPV, W1V) \
+  if (a.np == NPV && a.w1 == W1V) return fmm_launch_t<T, NPV, W1V>(up, a, hfac, nparents, s);
+    BG_FMM_T(6, 4) BG_FMM_T(6, 6) BG_FMM_T(9, 4) BG_FMM_T(9, 6) BG_FMM_T(10, 4) BG_FMM_T(10, 6)
+#undef BG_FMM_T
+  }
   const size_t smem = fmm_smem_bytes<T>(a.np, a.w1, a.Bq, up);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   auto kf = up ? k_fmm_up<T> : k_fmm_down<T>;
@@ -340,13 +653,13 @@ cudaError_t fmm_launch(bool up, const FmmLevels<T>& a, int nparents, cudaStream_
 
 }  // namespace
 
-cudaError_t launch_fmm_up(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s) {
-  if (S < 2) return fmm_launch<double>(true, a.f64, nparents, s);
-  return fmm_launch<float>(true, a.f32, nparents, s);
+cudaError_t launch_fmm_up(int S, const FmmLevelsAny& a, const double* hfac, int nparents, cudaStream_t s) {
+  if (S < 2) return fmm_launch<double>(true, a.f64, hfac, nparents, s);
+  return fmm_launch<float>(true, a.f32, hfac, nparents, s);
 }
-cudaError_t launch_fmm_down(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s) {
-  if (S < 2) return fmm_launch<double>(false, a.f64, nparents, s);
-  return fmm_launch<float>(false, a.f32, nparents, s);
+cudaError_t launch_fmm_down(int S, const FmmLevelsAny& a, const double* hfac, int nparents, cudaStream_t s) {
+  if (S < 2) return fmm_launch<double>(false, a.f64, hfac, nparents, s);
+  return fmm_launch<float>(false, a.f32, hfac, nparents, s);
 }
 
 }  // namespace bg

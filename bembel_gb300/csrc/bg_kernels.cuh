@@ -229,9 +229,11 @@ struct FmmLevelsAny {
 };
 // upward pass (moments of the leaf clusters, transfers to level 0) and
 // downward pass (transposed transfers, transposed moments added to out);
-// nparents = clusters of level L - 1; S the bg vector type of the pass
-cudaError_t launch_fmm_up(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s);
-cudaError_t launch_fmm_down(int S, const FmmLevelsAny& a, int nparents, cudaStream_t s);
+// nparents = clusters of level L - 1; S the bg vector type of the pass;
+// hfac the factors on the host (FP64, layout of fac) for the compiled sizes,
+// whose kernels take them as launch parameters (nullptr: generic kernels)
+cudaError_t launch_fmm_up(int S, const FmmLevelsAny& a, const double* hfac, int nparents, cudaStream_t s);
+cudaError_t launch_fmm_down(int S, const FmmLevelsAny& a, const double* hfac, int nparents, cudaStream_t s);
 // op(A) of an FMM transform, stored transposed: AT[q][i], q < Ki, i < ld
 // (ld a multiple of 4, at least Mo rounded up to 3, zero beyond Mo)
 struct TGemmA {

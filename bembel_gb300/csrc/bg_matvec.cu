@@ -994,96 +994,8 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
   }
 }
 
-// Register-tiled variant for small blocks (the near field: B = 16, 36, 64):
-// thread t owns rows 4 (t / (nrhs/4)) .. +3 and columns 4 (t % (nrhs/4)) .. +3,
-// so each step of j loads 4 coupling pairs (two 16-byte loads, shared by the
-// threads of a row group through L1) and 4 right-hand-side pairs (two 16-byte
-// shared-memory loads) for 16 double-float multiply-adds. Same arithmetic as
-// k_bsr_df; x panels double-buffered with cp.async.
-__device__ __forceinline__ void df_madd(float& s, float& cc, const float2 f, const float2 b) {
-  const float p = f.x * b.x;
-  float e = fmaf(f.x, b.x, -p);
-  e = fmaf(f.x, b.y, e);
-  e = fmaf(f.y, b.x, e);
-  const float tt = s + p, z = tt - s;
-  cc += ((s - (tt - z)) + (p - z)) + e;
-  s = tt;
-}
-__global__ void __launch_bounds__(256) k_bsr_df_tile(const int* __restrict__ row_ptr, const int* __restrict__ col,
-                                                     const float2* __restrict__ blocks, long bstride, int B,
-                                                     const float2* __restrict__ x, double* __restrict__ y, int nrhs,
-                                                     int accumulate) {
-  extern __shared__ __align__(16) float2 xsm[];  // [2][B * nrhs]
-  const int row = blockIdx.x, t = threadIdx.x;
-  const int cgroups = nrhs / 4, i0 = 4 * (t / cgroups), c0 = 4 * (t % cgroups);
-  const bool active = i0 < B;
-  const int panel = B * nrhs;
-  float s[4][4], cc[4][4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) s[r][c] = cc[r][c] = 0.0f;
-  const int kb = row_ptr[row], ke = row_ptr[row + 1];
-  auto issue = [&](int k, int buf) {
-    const float2* src = x + (long)col[k] * panel;
-    float2* dst = xsm + buf * panel;
-    for (int e = 2 * t; e < panel; e += 2 * blockDim.x) cp_async16(dst + e, src + e);
-    cp_async_commit();
-  };
-  if (kb < ke) issue(kb, 0);
-  for (int k = kb; k < ke; ++k) {
-    const int buf = (k - kb) & 1;
-    cp_async_wait<0>();
-    __syncthreads();  // panel k staged; everyone is done with panel k-1
-    if (k + 1 < ke) issue(k + 1, buf ^ 1);
-    if (active) {
-      const float2* F = blocks + (long)k * bstride + i0;
-      const float2* xp = xsm + buf * panel + c0;
-#pragma unroll 2
-      for (int j = 0; j < B; ++j) {
-        const float4 f01 = __ldg(reinterpret_cast<const float4*>(F + (long)j * B));
-        const float4 f23 = __ldg(reinterpret_cast<const float4*>(F + (long)j * B + 2));
-        const float4 x01 = *reinterpret_cast<const float4*>(xp + j * nrhs);
-        const float4 x23 = *reinterpret_cast<const float4*>(xp + j * nrhs + 2);
-        const float2 fv[4] = {make_float2(f01.x, f01.y), make_float2(f01.z, f01.w), make_float2(f23.x, f23.y),
-                              make_float2(f23.z, f23.w)};
-        const float2 xv[4] = {make_float2(x01.x, x01.y), make_float2(x01.z, x01.w), make_float2(x23.x, x23.y),
-                              make_float2(x23.z, x23.w)};
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) df_madd(s[r][c], cc[r][c], fv[r], xv[c]);
-      }
-    }
-  }
-  if (active) {
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      double* yo = y + ((long)row * B + i0 + r) * nrhs + c0;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const double v = (double)s[r][c] + (double)cc[r][c];
-        yo[c] = accumulate ? yo[c] + v : v;
-      }
-    }
-  }
-}
-
 cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
                           const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
-  // small blocks: register tiles of 4 rows x 4 columns (block rows and the
-  // block stride keep every 4-row group 16-byte aligned)
-  if (nrows > 0 && B % 4 == 0 && B <= 64 && nrhs % 4 == 0 && (B / 4) * (nrhs / 4) <= 256 && bstride % 2 == 0 &&
-      (reinterpret_cast<uintptr_t>(blocks) % 16) == 0 && (reinterpret_cast<uintptr_t>(x) % 16) == 0) {
-    const int threads = ((B / 4) * (nrhs / 4) + 31) / 32 * 32;
-    const size_t smem = (size_t)2 * B * nrhs * sizeof(float2);
-    cudaError_t e = smem_limit(k_bsr_df_tile, smem);
-    if (e != cudaSuccess) return e;
-    k_bsr_df_tile<<<nrows, threads, smem, s>>>(row_ptr, col, static_cast<const float2*>(blocks), bstride, B,
-                                               static_cast<const float2*>(x), static_cast<double*>(y), nrhs,
-                                               accumulate);
-    return cudaGetLastError();
-  }
   return launch_bsr_df_cols(row_ptr, col, blocks, bstride, nrows, B, x, y, nrhs, nrhs, 0, accumulate, s);
 }
 cudaError_t launch_bsr_df_cols(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,

@@ -178,6 +178,7 @@ struct bg_operator {
   bool fmm_fused = false;
   int fmm_w1 = 0;
   DevBuf d_fmm_fac64, d_fmm_fac32, d_fmm_cmap, d_fmm_cnt;
+  std::vector<double> fmm_hfac;  // the same factors on the host (launch parameters of the compiled sizes)
   long fmm_cnt_off[bg::kMaxFarLevels] = {};
   long fmm_cnt_stride = 0;
   int fmm_cnt_chunks = 0;

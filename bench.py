@@ -467,10 +467,10 @@ def _read_profile(L, ctx):
 
 def far_tile_bytes(np2):
     """Bytes of the FP16 hi + lo operand tiles of one low-rank block as
-    stored: row groups of 8 targets x K padded to 16 sources, 2 bytes each."""
+    stored: row groups of 8 targets x K padded to 8 sources, 2 bytes each."""
     mg = (np2 + 7) // 8
-    kp = (np2 + 15) // 16 * 16
-    return 2 * mg * 8 * kp * 2
+    ka = (np2 + 7) // 8 * 8
+    return 2 * mg * 8 * ka * 2
 
 
 def far_algorithmic_bytes(np2):
