@@ -295,6 +295,17 @@ class DiscreteOperator:
             self.ctx.check(_lib.load().bg_operator_set_wavenumber(self.h, k.real, k.imag))
         self.ctx.check(_lib.load().bg_operator_assemble(self.h))
 
+    def prepare_wavenumbers(self, kappas):
+        """Near fields of several Helmholtz wavenumbers in one pass
+        (bg_operator_prepare_wavenumbers): compute() after set_wavenumber to
+        one of them reuses its near field and assembles only the far field."""
+        k = np.asarray(kappas, dtype=np.complex128).reshape(-1)
+        re_, im_ = np.ascontiguousarray(k.real), np.ascontiguousarray(k.imag)
+        self.ctx.check(_lib.load().bg_operator_prepare_wavenumbers(self.h, _dp(re_), _dp(im_), len(k)))
+
+    def release_wavenumbers(self):
+        self.ctx.check(_lib.load().bg_operator_release_wavenumbers(self.h))
+
     def assembly_times(self):
         t = np.zeros(3)
         self.ctx.check(_lib.load().bg_operator_assembly_times(self.h, _dp(t)))

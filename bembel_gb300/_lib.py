@@ -105,6 +105,8 @@ def load(build_if_missing=True):
         "bg_operator_destroy": (I, [P]),
         "bg_operator_info": (I, [P, lp]),
         "bg_operator_assembly_times": (I, [P, dp]),
+        "bg_operator_prepare_wavenumbers": (I, [P, dp, dp, I]),
+        "bg_operator_release_wavenumbers": (I, [P]),
         "bg_matvec": (I, [P, P, Lg, P, Lg, I, dp, dp, I, I]),
         "bg_load_vector": (I, [P, I, dp, I, P, I]),
         "bg_solve": (I, [P, P, P, I, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveStats), I]),

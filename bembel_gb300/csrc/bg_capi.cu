@@ -642,6 +642,7 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
                             &tm.mw_f[1], &tm.mw_f[2], &tm.mw_b[0], &tm.mw_b[1], &tm.mw_b[2]})
       a += b->bytes;
   for (const auto& f : op->far) a += f.d_row_ptr.bytes + f.d_col.bytes;
+  for (const auto& c : op->near_cache) a += c.blocks->bytes;
   if (op->solver_ws && op->solver_ws_bytes) a += op->solver_ws_bytes(op->solver_ws);
   *allocated = a;
   // stored fields once assembled
@@ -987,21 +988,19 @@ static bg_status assemble_near_mw(bg_operator* op) {
   return cuda_status(op->ctx, e, "near-field assembly");
 }
 
-static bg_status assemble_near(bg_operator* op) {
-  if (op->maxwell()) return assemble_near_mw(op);
-  cudaStream_t s = op->ctx->stream;
-  const BsrSegment& D = op->dense;
-  const int B = D.B, p2 = op->p2;
-  const int ecl = B / p2;
-  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "near field of vector operators");
-  const size_t sb = op->scalar_bytes(false);
-  const long bstride = op->block_stride(B);
-  BG_CHECK(op->d_dense64.alloc((size_t)D.col.size() * bstride * sb), "near-field storage");
-  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, (size_t)D.col.size() * bstride * sb, s), "near-field storage");
-  // classify every element pair of the dense leaves (host, FP64 like the reference)
-  std::map<int, std::vector<NearPair>> regular;                 // by degree
-  std::map<std::pair<int, int>, std::vector<NearPair>> singular;  // by (case, degree)
+// Element pairs of the dense leaves of a scalar operator, classified on the
+// host (FP64, as the reference): regular pairs by quadrature degree, singular
+// pairs by (case, degree); dst is the entry offset of the pair's block.
+struct NearWork {
+  std::map<int, std::vector<NearPair>> regular;
+  std::map<std::pair<int, int>, std::vector<NearPair>> singular;
   long npairs = 0;
+};
+static NearWork near_work(const bg_operator* op) {
+  NearWork w;
+  const BsrSegment& D = op->dense;
+  const int B = D.B, p2 = op->p2, ecl = B / p2;
+  const long bstride = op->block_stride(B);
   for (int r = 0; r < D.nrows; ++r)
     for (int k = D.row_ptr[r]; k < D.row_ptr[r + 1]; ++k) {
       const int c1 = r, c2 = D.col[k];
@@ -1015,12 +1014,23 @@ static bg_status assemble_near(bg_operator* op) {
           np.rot = (pc.rot1 & 15) | ((pc.rot2 & 15) << 4);
           np.pad = 0;
           np.dst = (long long)k * bstride + (long long)(b * p2) * B + a * p2;
-          if (pc.cs == 0) regular[pc.deg].push_back(np);
-          else singular[{pc.cs, pc.deg}].push_back(np);
-          ++npairs;
+          if (pc.cs == 0) w.regular[pc.deg].push_back(np);
+          else w.singular[{pc.cs, pc.deg}].push_back(np);
+          ++w.npairs;
         }
     }
-  op->near_pairs = npairs;
+  return w;
+}
+
+// Quadrature of the dense leaves for nk wavenumbers into out[q] (zeroed
+// block pools). The regular pairs' per-element tables of surface points are
+// built once per degree and shared; the singular (Duffy) pairs of complex
+// operators evaluate each sample's points, measures and basis values once for
+// up to kDuffyMaxWavenumbers wavenumbers per launch.
+static bg_status near_quadrature(bg_operator* op, const NearWork& w, int nk, const double* kre, const double* kim,
+                                 void* const* out) {
+  cudaStream_t s = op->ctx->stream;
+  const int B = op->dense.B, p2 = op->p2;
   PatchTable pt{op->d_patch_meta.as<int>(), op->d_patch_cp.as<double>()};
   ElementTable et{op->d_el_patch.as<int>(), op->d_el_llc.as<double>(), 1.0 / double(1 << op->M)};
   std::vector<DevBuf*> keep;  // buffers alive until the stream drains
@@ -1029,7 +1039,7 @@ static bg_status assemble_near(bg_operator* op) {
     for (auto b : keep) delete b;
   };
   bg_status st = BG_OK;
-  for (auto& kv : regular) {
+  for (auto& kv : w.regular) {
     const int deg = kv.first, n1 = deg + 1, Q = n1 * n1;
     const Rule1D& gr = gauss_rule(n1);
     std::vector<double> basis((size_t)Q * p2);
@@ -1048,15 +1058,16 @@ static bg_status assemble_near(bg_operator* op) {
     if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
     if (e == cudaSuccess) e = dtab->alloc((size_t)op->ne * Q * sizeof(d4));
     if (e == cudaSuccess) e = launch_quad_table(op->G, pt, et, op->ne, dgx->as<double>(), dgw->as<double>(), n1, dtab->as<d4>(), s);
-    if (e == cudaSuccess)
+    for (int q = 0; q < nk && e == cudaSuccess; ++q)
       e = launch_near_regular(op->P, op->cplx, dpairs->as<NearPair>(), (int)kv.second.size(), dtab->as<d4>(), n1,
-                              dbas->as<double>(), op->kre, op->kim, op->d_dense64.p, B, s);
+                              dbas->as<double>(), kre[q], kim[q], out[q], B, s);
     if ((st = cuda_status(op->ctx, e, "near-field regular pairs")) != BG_OK) {
       cleanup();
       return st;
     }
   }
-  for (auto& kv : singular) {
+  const bool multi = op->cplx && nk > 1 && (op->P == 1 || op->P == 2);
+  for (auto& kv : w.singular) {
     const int cs = kv.first.first, deg = kv.first.second, n1 = deg + 1;
     const Rule1D& gr = gauss_rule(n1);
     DevBuf *dgx = new DevBuf(), *dgw = new DevBuf(), *dpairs = new DevBuf();
@@ -1064,9 +1075,16 @@ static bg_status assemble_near(bg_operator* op) {
     cudaError_t e = dgx->upload(gr.x, s);
     if (e == cudaSuccess) e = dgw->upload(gr.w, s);
     if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
-    if (e == cudaSuccess)
-      e = launch_near_duffy(op->G, op->P, op->cplx, cs, pt, et, dpairs->as<NearPair>(), (int)kv.second.size(),
-                            dgx->as<double>(), dgw->as<double>(), n1, op->kre, op->kim, op->d_dense64.p, B, s);
+    for (int q0 = 0; q0 < nk && e == cudaSuccess;) {
+      const int nb = multi ? std::min(kDuffyMaxWavenumbers, nk - q0) : 1;
+      if (multi)
+        e = launch_near_duffy_multi(op->G, op->P, cs, pt, et, dpairs->as<NearPair>(), (int)kv.second.size(),
+                                    dgx->as<double>(), dgw->as<double>(), n1, nb, kre + q0, kim + q0, out + q0, B, s);
+      else
+        e = launch_near_duffy(op->G, op->P, op->cplx, cs, pt, et, dpairs->as<NearPair>(), (int)kv.second.size(),
+                              dgx->as<double>(), dgw->as<double>(), n1, kre[q0], kim[q0], out[q0], B, s);
+      q0 += nb;
+    }
     if ((st = cuda_status(op->ctx, e, "near-field singular pairs")) != BG_OK) {
       cleanup();
       return st;
@@ -1074,7 +1092,85 @@ static bg_status assemble_near(bg_operator* op) {
   }
   cudaError_t e = cudaStreamSynchronize(s);
   cleanup();
-  if ((st = cuda_status(op->ctx, e, "near-field assembly")) != BG_OK) return st;
+  return cuda_status(op->ctx, e, "near-field assembly");
+}
+
+static bg_status assemble_near(bg_operator* op) {
+  if (op->maxwell()) return assemble_near_mw(op);
+  cudaStream_t s = op->ctx->stream;
+  const BsrSegment& D = op->dense;
+  if (op->vd != 1) return set_error(op->ctx, BG_UNSUPPORTED, "near field of vector operators");
+  const size_t bytes = (size_t)D.col.size() * op->block_stride(D.B) * op->scalar_bytes(false);
+  BG_CHECK(op->d_dense64.alloc(bytes), "near-field storage");
+  // a near field prepared for this wavenumber (bg_operator_prepare_wavenumbers)
+  for (const auto& c : op->near_cache)
+    if (c.kre == op->kre && c.kim == op->kim && c.blocks->bytes == bytes) {
+      BG_CHECK(cudaMemcpyAsync(op->d_dense64.p, c.blocks->p, bytes, cudaMemcpyDeviceToDevice, s), "near field");
+      BG_CHECK(cudaStreamSynchronize(s), "near field");
+      return BG_OK;
+    }
+  BG_CHECK(cudaMemsetAsync(op->d_dense64.p, 0, bytes, s), "near-field storage");
+  const NearWork w = near_work(op);
+  op->near_pairs = w.npairs;
+  void* out = op->d_dense64.p;
+  return near_quadrature(op, w, 1, &op->kre, &op->kim, &out);
+}
+
+extern "C" bg_status bg_operator_prepare_wavenumbers(bg_operator* op, const double* kre, const double* kim, int n) {
+  if (!op || n < 0 || (n > 0 && (!kre || !kim))) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
+  if (!op->cplx || op->maxwell() || op->vd != 1)
+    return set_error(op->ctx, BG_UNSUPPORTED, "prepared wavenumbers: Helmholtz single layer only");
+  for (int q = 0; q < n; ++q)
+    if (!std::isfinite(kre[q]) || !std::isfinite(kim[q]))
+      return set_error(op->ctx, BG_INVALID_ARG, "prepared wavenumbers: wavenumbers must be finite");
+  cudaSetDevice(op->ctx->device);
+  cudaStream_t s = op->ctx->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  const size_t bytes = (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * op->scalar_bytes(false);
+  std::vector<DevBuf*> bufs;
+  std::vector<void*> outs;
+  auto drop = [&]() {
+    for (auto b : bufs) delete b;
+  };
+  for (int q = 0; q < n; ++q) {
+    DevBuf* b = new DevBuf();
+    bufs.push_back(b);
+    cudaError_t e = b->alloc(bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->p, 0, bytes, s);
+    if (e != cudaSuccess) {
+      drop();
+      return cuda_status(op->ctx, e, "prepared near fields");
+    }
+    outs.push_back(b->p);
+  }
+  if (n > 0) {
+    const NearWork w = near_work(op);
+    op->near_pairs = w.npairs;
+    bg_status st = near_quadrature(op, w, n, kre, kim, outs.data());
+    if (st != BG_OK) {
+      drop();
+      return st;
+    }
+  }
+  for (int q = 0; q < n; ++q) {
+    // replace an entry of the same wavenumber
+    for (size_t i = 0; i < op->near_cache.size(); ++i)
+      if (op->near_cache[i].kre == kre[q] && op->near_cache[i].kim == kim[q]) {
+        delete op->near_cache[i].blocks;
+        op->near_cache.erase(op->near_cache.begin() + i);
+        break;
+      }
+    op->near_cache.push_back({kre[q], kim[q], bufs[q]});
+  }
+  op->t_prepare = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_release_wavenumbers(bg_operator* op) {
+  if (!op) return BG_INVALID_ARG;
+  for (auto& c : op->near_cache) delete c.blocks;
+  op->near_cache.clear();
   return BG_OK;
 }
 

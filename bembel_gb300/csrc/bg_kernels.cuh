@@ -63,6 +63,14 @@ cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable&
 // component blocks of every element pair, idiv = -1 / (kappa^2 h^2)
 cudaError_t launch_quad_table_mw(int G, const PatchTable& pt, const ElementTable& et, int ne, const double* gx,
                                  const double* gw, int n1, MwPt* out, cudaStream_t s);
+// complex (Helmholtz) singular pairs for nk wavenumbers at once
+// (1 <= nk <= kDuffyMaxWavenumbers, P = 1 or 2): out[q] receives the blocks of
+// wavenumber kre[q] + i kim[q]
+constexpr int kDuffyMaxWavenumbers = 4;
+cudaError_t launch_near_duffy_multi(int G, int P, int cs, const PatchTable& pt, const ElementTable& et,
+                                    const NearPair* pairs, int npairs, const double* gx, const double* gw, int n1,
+                                    int nk, const double* kre, const double* kim, void* const* out, int B,
+                                    cudaStream_t s);
 cudaError_t launch_near_regular_mw(int P, const NearPairV* pairs, int npairs, const MwPt* tab, int n1,
                                    const double* basis3, double kre, double kim, cd idiv, cd* out, int B,
                                    cudaStream_t s);

@@ -172,6 +172,25 @@ struct WarpAcc {
 #pragma unroll
     for (int m = 0; m < PER; ++m) acc[m] = zero<S>();
   }
+  // NK accumulators at once: acc[k] += c_k(s) phi_a(s) phi_b(s) for the 32
+  // staged samples, sc[k * 32 + s] (the basis products are formed once)
+  template <int NK>
+  static __device__ void add_multi(WarpAcc* acc, const S* sc, const double* sa, const double* sb, bool sym,
+                                   int lane) {
+    for (int s = 0; s < 32; ++s) {
+#pragma unroll
+      for (int m = 0; m < PER; ++m) {
+        const int e = lane + 32 * m;
+        if (e < NE) {
+          const int a = e % P2, b = e / P2;
+          double v = sa[s * P2 + a] * sb[s * P2 + b];
+          if (sym) v = fma(sb[s * P2 + a], sa[s * P2 + b], v);
+#pragma unroll
+          for (int k = 0; k < NK; ++k) acc[k].acc[m] = fmac(acc[k].acc[m], sc[k * 32 + s], v);
+        }
+      }
+    }
+  }
   // add the 32 staged samples c_s phi_a(s) phi_b(s) (+ transposed when sym)
   __device__ void add(const S* sc, const double* sa, const double* sb, bool sym, int lane) {
     for (int s = 0; s < 32; ++s) {
@@ -190,14 +209,23 @@ struct WarpAcc {
   }
 };
 
-template <int G, int P, typename S, int CS>
+// Several wavenumbers per launch (KBatch, NK of them): every Duffy sample's
+// points, surface measures and basis values are evaluated once and shared;
+// each wavenumber has its own kernel values, accumulators and output.
+template <typename S, int NK>
+struct KBatch {
+  double kre[NK], kim[NK];
+  S* out[NK];
+};
+
+template <int G, int P, typename S, int CS, int NK>
 __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable et, const NearPair* __restrict__ pairs,
                                                     const double* __restrict__ gx, const double* __restrict__ gw, int n1,
-                                                    double kre, double kim, S* __restrict__ out, int B) {
+                                                    KBatch<S, NK> kb, int B) {
   constexpr int P2 = (P + 1) * (P + 1);
   constexpr int NE = P2 * P2;
   constexpr int NW = 4;
-  __shared__ S st_c[NW][32];
+  __shared__ S st_c[NW][NK * 32];
   __shared__ double st_a[NW][32 * P2];
   __shared__ double st_b[NW][32 * P2];
   __shared__ PointEval vp[NW][4];        // per-i points of the common-vertex rule
@@ -210,8 +238,9 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
   const double b0 = et.llc[2 * pr.e2], b1 = et.llc[2 * pr.e2 + 1];
   const double h = et.h;
   const int Q = n1 * n1;
-  WarpAcc<P, S> acc;
-  acc.init();
+  WarpAcc<P, S> acc[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) acc[k].init();
   S* sc = st_c[warp];
   double* sa = st_a[warp];
   double* sb = st_b[warp];
@@ -298,11 +327,15 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
         }
         const double d0 = A.x[0] - Bp.x[0], d1 = A.x[1] - Bp.x[1], d2 = A.x[2] - Bp.x[2];
         const double r2 = fma(d0, d0, fma(d1, d1, d2 * d2));
-        S c = scale_of(kernel_val<S>(r2, kre, kim), A.c * Bp.c);
-        if (!valid) c = zero<S>();
-        sc[lane] = c;
+#pragma unroll
+        for (int q = 0; q < NK; ++q) {
+          S c = scale_of(kernel_val<S>(r2, kb.kre[q], kb.kim[q]), A.c * Bp.c);
+          if (!valid) c = zero<S>();
+          sc[q * 32 + lane] = c;
+        }
         __syncwarp();
-        acc.add(sc, sa, sb, CS == 2, lane);
+        if (NK == 1) acc[0].add(sc, sa, sb, CS == 2, lane);
+        else WarpAcc<P, S>::template add_multi<NK>(acc, sc, sa, sb, CS == 2, lane);
         __syncwarp();
       }
     }
@@ -311,22 +344,36 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
   // reduce the warps' accumulators (staging memory reused: NE * sizeof(S)
   // <= 32 * P2 * sizeof(double) for P <= 3) and write the block
   static_assert(NE * sizeof(S) <= 32 * P2 * sizeof(double), "reduction buffer too small");
-  __syncthreads();
   S* red = reinterpret_cast<S*>(&st_a[0][0]);
   const int stride = 32 * P2 * sizeof(double) / sizeof(S);
 #pragma unroll
-  for (int m = 0; m < WarpAcc<P, S>::PER; ++m) {
-    const int e = lane + 32 * m;
-    if (e < NE) red[warp * stride + e] = acc.acc[m];
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
-    S v = red[e];
+  for (int q = 0; q < NK; ++q) {
+    __syncthreads();
 #pragma unroll
-    for (int w2 = 1; w2 < NW; ++w2) v = v + red[w2 * stride + e];
-    const int a = e % P2, b = e / P2;
-    out[pr.dst + (long)b * B + a] = v;
+    for (int m = 0; m < WarpAcc<P, S>::PER; ++m) {
+      const int e = lane + 32 * m;
+      if (e < NE) red[warp * stride + e] = acc[q].acc[m];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+      S v = red[e];
+#pragma unroll
+      for (int w2 = 1; w2 < NW; ++w2) v = v + red[w2 * stride + e];
+      const int a = e % P2, b = e / P2;
+      kb.out[q][pr.dst + (long)b * B + a] = v;
+    }
   }
+}
+
+template <int G, int P, typename S, int NK>
+static cudaError_t run_duffy_k(int cs, const PatchTable& pt, const ElementTable& et, const NearPair* pairs,
+                               int npairs, const double* gx, const double* gw, int n1, const KBatch<S, NK>& kb, int B,
+                               cudaStream_t s) {
+  if (cs == 2) k_near_duffy<G, P, S, 2, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);
+  else if (cs == 3) k_near_duffy<G, P, S, 3, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);
+  else if (cs == 4) k_near_duffy<G, P, S, 4, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
 }
 
 template <int G, int P, typename S>
@@ -334,11 +381,34 @@ static cudaError_t run_duffy(int cs, const PatchTable& pt, const ElementTable& e
                              const double* gx, const double* gw, int n1, double kre, double kim, S* out, int B,
                              cudaStream_t s) {
   if (npairs == 0) return cudaSuccess;
-  if (cs == 2) k_near_duffy<G, P, S, 2><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kre, kim, out, B);
-  else if (cs == 3) k_near_duffy<G, P, S, 3><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kre, kim, out, B);
-  else if (cs == 4) k_near_duffy<G, P, S, 4><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kre, kim, out, B);
-  else return cudaErrorInvalidValue;
-  return cudaGetLastError();
+  KBatch<S, 1> kb{{kre}, {kim}, {out}};
+  return run_duffy_k<G, P, S, 1>(cs, pt, et, pairs, npairs, gx, gw, n1, kb, B, s);
+}
+
+// complex kernels, nk (1 .. kDuffyMaxWavenumbers) wavenumbers per launch
+template <int G, int P>
+static cudaError_t run_duffy_multi(int cs, const PatchTable& pt, const ElementTable& et, const NearPair* pairs,
+                                   int npairs, const double* gx, const double* gw, int n1, int nk, const double* kre,
+                                   const double* kim, void* const* out, int B, cudaStream_t s) {
+  if (npairs == 0) return cudaSuccess;
+  switch (nk) {
+#define BG_DUFK(NKV)                                                                               \
+  case NKV: {                                                                                      \
+    KBatch<cd, NKV> kb;                                                                            \
+    for (int q = 0; q < NKV; ++q) {                                                                \
+      kb.kre[q] = kre[q];                                                                          \
+      kb.kim[q] = kim[q];                                                                          \
+      kb.out[q] = static_cast<cd*>(out[q]);                                                        \
+    }                                                                                              \
+    return run_duffy_k<G, P, cd, NKV>(cs, pt, et, pairs, npairs, gx, gw, n1, kb, B, s);            \
+  }
+    BG_DUFK(1)
+    BG_DUFK(2)
+    BG_DUFK(3)
+    BG_DUFK(4)
+#undef BG_DUFK
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int G>
@@ -367,6 +437,29 @@ cudaError_t launch_near_duffy(int G, int P, bool cplx, int cs, const PatchTable&
     case 2: return duffy_p<2>(P, cplx, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, out, B, s);
     case 3: return duffy_p<3>(P, cplx, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, out, B, s);
     case 5: return duffy_p<5>(P, cplx, cs, pt, et, pairs, npairs, gx, gw, n1, kre, kim, out, B, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int G>
+static cudaError_t duffy_multi_p(int P, int cs, const PatchTable& pt, const ElementTable& et, const NearPair* pairs,
+                                 int npairs, const double* gx, const double* gw, int n1, int nk, const double* kre,
+                                 const double* kim, void* const* out, int B, cudaStream_t s) {
+  switch (P) {
+    case 1: return run_duffy_multi<G, 1>(cs, pt, et, pairs, npairs, gx, gw, n1, nk, kre, kim, out, B, s);
+    case 2: return run_duffy_multi<G, 2>(cs, pt, et, pairs, npairs, gx, gw, n1, nk, kre, kim, out, B, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_near_duffy_multi(int G, int P, int cs, const PatchTable& pt, const ElementTable& et,
+                                    const NearPair* pairs, int npairs, const double* gx, const double* gw, int n1,
+                                    int nk, const double* kre, const double* kim, void* const* out, int B,
+                                    cudaStream_t s) {
+  switch (G) {
+    case 2: return duffy_multi_p<2>(P, cs, pt, et, pairs, npairs, gx, gw, n1, nk, kre, kim, out, B, s);
+    case 3: return duffy_multi_p<3>(P, cs, pt, et, pairs, npairs, gx, gw, n1, nk, kre, kim, out, B, s);
+    case 5: return duffy_multi_p<5>(P, cs, pt, et, pairs, npairs, gx, gw, n1, nk, kre, kim, out, B, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -142,6 +142,15 @@ struct bg_operator {
   long near_pairs = 0;
   bool assembled = false;
   double t_near = 0, t_far = 0, t_total = 0;
+  double t_prepare = 0;  // seconds of the last bg_operator_prepare_wavenumbers
+  // near fields prepared for several wavenumbers in one pass
+  // (bg_operator_prepare_wavenumbers); bg_operator_assemble copies the one of
+  // the current wavenumber instead of running the quadrature
+  struct NearCacheEntry {
+    double kre, kim;
+    DevBuf* blocks;
+  };
+  std::vector<NearCacheEntry> near_cache;
 
   // device tables
   DevBuf d_patch_meta, d_patch_cp, d_el_patch, d_el_llc;
@@ -239,6 +248,7 @@ struct bg_operator {
     for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_tan64, &d_tan32, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv,
                    &d_mom64, &d_mom32, &w_y, &w_z, &w_ydf, &w_btiles, &w_binv, &w_yv, &w_zv})
       for (auto b : *v) delete b;
+    for (auto& c : near_cache) delete c.blocks;
   }
   size_t scalar_bytes(bool fp32) const { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }
   // scalars between consecutive stored FP64 blocks of size B x B: rounded up

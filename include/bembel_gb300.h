@@ -145,6 +145,20 @@ bg_status bg_operator_set_wavenumber(bg_operator* op, double re, double im);
 /* DiscreteOperator::compute -> H2Matrix::init_H2Matrix (H2Matrix/H2Matrix.hpp:93-250):
  * near-field (DuffyTrick) and far-field (interpolateKernel) assembly on the GPU. */
 bg_status bg_operator_assemble(bg_operator* op);
+/* No counterpart in the reference, which assembles one wavenumber per
+ * DiscreteOperator::compute (Helmholtz/SingleLayerOperator.hpp:124-130,
+ * H2Matrix.hpp:93-250). Assembles the near field (the dense leaves) of the
+ * Helmholtz operator for the n wavenumbers kre[i] + i kim[i] in one pass:
+ * every Duffy sample's points, surface measures and basis values are
+ * evaluated once for up to 4 wavenumbers, and the regular pairs share their
+ * per-element quadrature tables. The blocks stay on the device (n near
+ * fields, bg_operator_memory counts them); after bg_operator_set_wavenumber
+ * to one of them, bg_operator_assemble copies that near field instead of
+ * integrating it again and assembles only the far field. A wavenumber
+ * prepared twice keeps the later blocks. BG_UNSUPPORTED for other operators. */
+bg_status bg_operator_prepare_wavenumbers(bg_operator* op, const double* kre, const double* kim, int n);
+/* frees the near fields of bg_operator_prepare_wavenumbers */
+bg_status bg_operator_release_wavenumbers(bg_operator* op);
 bg_status bg_operator_destroy(bg_operator* op);
 /* info[0..15]: rows (= cols, H2Matrix.hpp:76-77), superspace size, elements,
  * dense leaves, low-rank leaves, vector dimension, FMM components, n_p,
