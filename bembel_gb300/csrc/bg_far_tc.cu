@@ -624,6 +624,15 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
       for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
       for (int k = kb; k < ke; ++k, ++it) {
         const int st = it % S, ab = it & 1;
+        // the block's scales do not depend on its MMAs: load them first, so
+        // that their latency overlaps the wait for the accumulators
+        const float sa = __ldg(&ainv[k]);
+        float4 bsc[8];
+        {
+          const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) bsc[q] = __ldg(&sb[q]);
+        }
         int got = 1;
         if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
         got = __shfl_sync(0xffffffffu, got, 0);
@@ -642,11 +651,9 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(&free_bar[ab]);
-        const float sa = __ldg(&ainv[k]);
-        const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const float4 b4 = __ldg(&sb[q]);
+          const float4 b4 = bsc[q];
           neumaier(sum[4 * q + 0], comp[4 * q + 0], (hh[4 * q + 0] + cr[4 * q + 0]) * (sa * b4.x));
           neumaier(sum[4 * q + 1], comp[4 * q + 1], (hh[4 * q + 1] + cr[4 * q + 1]) * (sa * b4.y));
           neumaier(sum[4 * q + 2], comp[4 * q + 2], (hh[4 * q + 2] + cr[4 * q + 2]) * (sa * b4.z));
@@ -962,6 +969,20 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
       for (int n = 0; n < kNC; ++n) sre[n] = cre[n] = sim[n] = cim[n] = 0.0f;
       for (int k = kb; k < ke; ++k, ++it) {
         const int st = it % S, ab = it & 1;
+        // the block's scales, loaded before the wait for its accumulators
+        const float sa = __ldg(&ainv[k]);
+        float sbv[32];
+        {
+          const float4* sb4 = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 b4 = __ldg(&sb4[q]);
+            sbv[4 * q] = sa * b4.x;
+            sbv[4 * q + 1] = sa * b4.y;
+            sbv[4 * q + 2] = sa * b4.z;
+            sbv[4 * q + 3] = sa * b4.w;
+          }
+        }
         int got = 1;
         if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
         got = __shfl_sync(0xffffffffu, got, 0);
@@ -974,15 +995,13 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        const float sa = __ldg(&ainv[k]);
-        const float* sb = binv + (long)col[k] * kN;
         float p[32];
         {
           float hh[32], cr[32];
           tmem_ld32(lane_base + (uint32_t)(128 * ab), hh);
           tmem_ld32(lane_base + (uint32_t)(128 * ab + 32), cr);
 #pragma unroll
-          for (int n = 0; n < 32; ++n) p[n] = (hh[n] + cr[n]) * (sa * __ldg(&sb[n]));
+          for (int n = 0; n < 32; ++n) p[n] = (hh[n] + cr[n]) * sbv[n];
         }
         float hh[32], cr[32];
         tmem_ld32(lane_base + (uint32_t)(128 * ab + 64), hh);
@@ -992,8 +1011,8 @@ __global__ void __launch_bounds__(kStoredThreads, 1)
         if (lane == 0) mbar_arrive(&free_bar[ab]);
 #pragma unroll
         for (int n = 0; n < kNC; ++n) {
-          const float q_re = (hh[n] + cr[n]) * (sa * __ldg(&sb[n]));
-          const float q_im = (hh[kNC + n] + cr[kNC + n]) * (sa * __ldg(&sb[kNC + n]));
+          const float q_re = (hh[n] + cr[n]) * sbv[n];
+          const float q_im = (hh[kNC + n] + cr[kNC + n]) * sbv[kNC + n];
           neumaier(sre[n], cre[n], p[n] - q_im);
           neumaier(sim[n], cim[n], p[kNC + n] + q_re);
         }

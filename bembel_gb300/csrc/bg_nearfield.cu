@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
       const bool valid = j < Q;
       const double e0 = valid ? gx[j / n1] : 0.5, e1 = valid ? gx[j % n1] : 0.5;
       const double wj = valid ? gw[j / n1] * gw[j % n1] : 0.0;
-      constexpr int NK = CS == 2 ? 4 : (CS == 3 ? 6 : 4);
+      constexpr int NSUB = CS == 2 ? 4 : (CS == 3 ? 6 : 4);  // point pairs per (outer, inner) sample
       // common-vertex: the inner points are shared by the four samples
       PointEval q5, q6;
       double phi5[P2], phi6[P2];
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
         eval_point<G, P>(pt, p1, a0, a1, h, uv[0], uv[1], wj, &q6, phi6);
       }
 #pragma unroll 1
-      for (int k = 0; k < NK; ++k) {
+      for (int k = 0; k < NSUB; ++k) {
         PointEval A, Bp;
         double* pa = sa + lane * P2;
         double* pb = sb + lane * P2;
