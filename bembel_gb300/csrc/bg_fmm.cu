@@ -491,32 +491,38 @@ __device__ __forceinline__ void tdown1(const FmmFactors<T, NP, W1>& f, const T* 
     W[(w * NP + ct) * kFmmCols + lane] = v;
   }
 }
-// out[cs][ct] = base[cs][ct] + sum_ps E_H[cs][ps] W[ps][ct]; warp = ct
+// out[cs][ct] = base[cs] + sum_ps E_H[cs][ps] W[ps][ct]; warp = ct, base[cs]
+// the far-field result of row (cs, ct), already in registers
 template <typename T, int NP, int W1, int H>
-__device__ __forceinline__ void tdown2(const FmmFactors<T, NP, W1>& f, const T* W, const T* base, int kk, bool on,
-                                       T* out, int w, int lane) {
+__device__ __forceinline__ void tdown2(const FmmFactors<T, NP, W1>& f, const T* W, const T* base, T* out, int w,
+                                       int lane) {
   if (w >= NP) return;
   T v[NP];
 #pragma unroll
   for (int ps = 0; ps < NP; ++ps) v[ps] = W[(ps * NP + w) * kFmmCols + lane];
 #pragma unroll
   for (int cs = 0; cs < NP; ++cs) {
-    T o = on ? base[(size_t)(cs * NP + w) * kk] : T(0);
+    T o = base[cs];
 #pragma unroll
     for (int ps = 0; ps < NP; ++ps) o = fma(f.E[H][cs * NP + ps], v[ps], o);
     out[(cs * NP + w) * kFmmCols + lane] = o;
   }
 }
 template <typename T, int NP, int W1, int K>
-__device__ __forceinline__ void tdown_child(const FmmFactors<T, NP, W1>& f, const T* Zp, T* W, const T* base, int kk,
-                                            bool on, T* out, int w, int lane) {
+__device__ __forceinline__ void tdown_child(const FmmFactors<T, NP, W1>& f, const T* Zp, T* W, const T* base, T* out,
+                                            int w, int lane) {
   constexpr int HT = K >> 1, HS = (K == 1 || K == 2) ? 1 : 0;
   tdown1<T, NP, W1, HT>(f, Zp, W, w, lane);
   __syncthreads();
-  tdown2<T, NP, W1, HS>(f, W, base, kk, on, out, w, lane);
+  tdown2<T, NP, W1, HS>(f, W, base, out, w, lane);
   __syncthreads();
 }
 
+// The downward pass as one sequence of steps: the L - 1 ancestors below
+// level 0 (full coefficients in Zf, updated in place), then the 4 leaf
+// clusters (into C, then the transposed moments). Each step's far-field rows
+// are loaded into registers one step ahead, and each leaf's superspace rows
+// before its transfer, so that global-memory latency overlaps the arithmetic.
 template <typename T, int NP, int W1>
 __global__ void __launch_bounds__(32 * NP) k_fmm_down_t(const __grid_constant__ FmmLevels<T> a, const __grid_constant__ FmmFactors<T, NP, W1> f) {
   extern __shared__ __align__(16) unsigned char fmm_smem[];
@@ -538,22 +544,46 @@ __global__ void __launch_bounds__(32 * NP) k_fmm_down_t(const __grid_constant__ 
     const T* z0 = a.z[0] + ((size_t)(P >> (2 * (L - 1))) * NP2) * kk + c0 + lane;
     for (int r = w; r < NP2; r += NW) Zf[r * kFmmCols + lane] = on ? z0[(size_t)r * kk] : T(0);
   }
-  __syncthreads();
-  // down the ancestor path to P (Zf is read in stage 1 and rewritten in stage 2)
-  for (int l = 1; l <= L - 1; ++l) {
-    const int al = P >> (2 * (L - 1 - l));
-    const T* base = a.z[l] + ((size_t)al * NP2) * kk + c0 + lane;
-    switch (al & 3) {
-      case 0: tdown_child<T, NP, W1, 0>(f, Zf, W, base, kk, on, Zf, w, lane); break;
-      case 1: tdown_child<T, NP, W1, 1>(f, Zf, W, base, kk, on, Zf, w, lane); break;
-      case 2: tdown_child<T, NP, W1, 2>(f, Zf, W, base, kk, on, Zf, w, lane); break;
-      default: tdown_child<T, NP, W1, 3>(f, Zf, W, base, kk, on, Zf, w, lane); break;
+  const int nsteps = L - 1 + 4;
+  // far-field rows (cs, w) of step st: ancestor level st + 1, then leaf st - (L - 1)
+  auto rows_of = [&](int st) -> const T* {
+    if (st < L - 1) {
+      const int l = st + 1;
+      return a.z[l] + ((size_t)(P >> (2 * (L - 1 - l))) * NP2) * kk + c0 + lane;
     }
-  }
-  auto leaf = [&](auto kc) {
-    constexpr int K = decltype(kc)::value;
-    const int lf = 4 * P + K;
-    tdown_child<T, NP, W1, K>(f, Zf, W, a.z[L] + ((size_t)lf * NP2) * kk + c0 + lane, kk, on, C, w, lane);
+    return a.z[L] + ((size_t)(4 * P + st - (L - 1)) * NP2) * kk + c0 + lane;
+  };
+  T nb[NP];
+  auto load_rows = [&](int st) {
+    const T* p = rows_of(st);
+#pragma unroll
+    for (int cs = 0; cs < NP; ++cs) nb[cs] = (on && w < NP) ? p[(size_t)(cs * NP + w) * kk] : T(0);
+  };
+  load_rows(0);
+  __syncthreads();
+  for (int st = 0; st < nsteps; ++st) {
+    T cb[NP];
+#pragma unroll
+    for (int cs = 0; cs < NP; ++cs) cb[cs] = nb[cs];
+    if (st + 1 < nsteps) load_rows(st + 1);
+    const bool leaf = st >= L - 1;
+    const int lf = 4 * P + st - (L - 1);
+    // this leaf's superspace rows, read-modify-written by warp b < W1
+    T yv[W1];
+    T* yo = a.out + ((size_t)lf * BQ) * kk + c0 + lane;
+    if (leaf && w < W1 && on) {
+#pragma unroll
+      for (int aa = 0; aa < W1; ++aa) yv[aa] = yo[(size_t)q_of[aa * W1 + w] * kk];
+    }
+    const int k = leaf ? st - (L - 1) : ((P >> (2 * (L - 2 - st))) & 3);
+    T* dst = leaf ? C : Zf;
+    switch (k) {
+      case 0: tdown_child<T, NP, W1, 0>(f, Zf, W, cb, dst, w, lane); break;
+      case 1: tdown_child<T, NP, W1, 1>(f, Zf, W, cb, dst, w, lane); break;
+      case 2: tdown_child<T, NP, W1, 2>(f, Zf, W, cb, dst, w, lane); break;
+      default: tdown_child<T, NP, W1, 3>(f, Zf, W, cb, dst, w, lane); break;
+    }
+    if (!leaf) continue;
     // transposed moments: V[i][b] = sum_j Mt[j][b] C[i][j] (warp = i), then
     // y[q(a, b)] += sum_i Ms[i][a] V[i][b] (warp = b)
     if (w < NP) {
@@ -573,24 +603,16 @@ __global__ void __launch_bounds__(32 * NP) k_fmm_down_t(const __grid_constant__ 
       T v[NP];
 #pragma unroll
       for (int i = 0; i < NP; ++i) v[i] = V[(i * W1 + w) * kFmmCols + lane];
-      T* yo = a.out + ((size_t)lf * BQ) * kk + c0 + lane;
 #pragma unroll
       for (int aa = 0; aa < W1; ++aa) {
         T o = T(0);
 #pragma unroll
         for (int i = 0; i < NP; ++i) o = fma(f.Ms[i * W1 + aa], v[i], o);
-        if (on) {
-          T* dst = yo + (size_t)q_of[aa * W1 + w] * kk;
-          *dst += o;
-        }
+        if (on) yo[(size_t)q_of[aa * W1 + w] * kk] = yv[aa] + o;
       }
     }
     __syncthreads();
-  };
-  leaf(std::integral_constant<int, 0>());
-  leaf(std::integral_constant<int, 1>());
-  leaf(std::integral_constant<int, 2>());
-  leaf(std::integral_constant<int, 3>());
+  }
 }
 
 template <typename T, int NP, int W1>
