@@ -1433,7 +1433,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
                "right-hand-side tiles");
       BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->far_work(pl.far_order), op->n_far_work,
-                                                                       np2, nrhs, op->d_err.as<int>(), s); }),
+                                                                       np2, nrhs, op->d_err.as<int>(), s, pl.far_ctas); }),
                "far-field product (stored FP16 tiles, tensor cores)");
     } else if (tcc) {
       // complex kernel: stored FP16 tiles of Re K and Im K, 16 complex columns
@@ -1717,7 +1717,7 @@ extern "C" bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precisi
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: nrhs must be positive and the precision a bg_precision");
   if (plan->near_kernel < 0 || plan->near_kernel > 3 || plan->split_k_batches < -1 ||
       plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2 || plan->transforms < 0 ||
-      plan->transforms > 1)
+      plan->transforms > 1 || plan->far_ctas < 0 || plan->far_ctas > 2)
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: a field is out of range");
   op->plans[bg_operator::plan_key(nrhs, precision)] = *plan;
   op->drop_graphs();
@@ -1820,6 +1820,7 @@ extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precisi
     st = sweep(&bg_launch_plan::near_kernel, v);
   }
   if (st == BG_OK && op->fmm_fused) st = sweep(&bg_launch_plan::transforms, {1});
+  if (st == BG_OK && mixed && !op->cplx && op->far_tiles) st = sweep(&bg_launch_plan::far_ctas, {2});
   if (st == BG_OK && mixed && op->use_tgemm && (!op->fmm_fused || cur.transforms == 1))
     st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
   if (st == BG_OK && mixed && op->d_far_work_alt[0].p) st = sweep(&bg_launch_plan::far_order, {1, 2});

@@ -462,7 +462,7 @@ constexpr int kH16Stages = 4;
 // the right-hand-side (B) tiles, which keep the full KP. Rows beyond the
 // stored row groups (M = 128 reads 16) only feed output rows >= NP2, which
 // are never read.
-template <int NP2>
+template <int NP2, int NSTAGE = kH16Stages>
 struct H16Shape {
   static constexpr int KP = (NP2 + 15) / 16 * 16;  // K padded to the f16 MMA K step
   static constexpr int KC = KP / 8;                // 16-byte core-matrix columns (8 halves) of a B tile
@@ -474,10 +474,10 @@ struct H16Shape {
   static constexpr uint32_t A_BYTES = MG * SBOA, B_BYTES = 4 * SBO;
   static constexpr uint32_t A2 = 2 * A_BYTES, B2 = 2 * B_BYTES;
   static constexpr uint32_t STAGE = A2 + B2;
-  static constexpr uint32_t TILES = kH16Stages * STAGE;
+  static constexpr uint32_t TILES = NSTAGE * STAGE;
   // furthest byte an M = 128 A operand reads, from its start
   static constexpr uint32_t A_READ = 15 * SBOA + KC * 128;
-  static constexpr uint32_t NEED = (kH16Stages - 1) * STAGE + A_BYTES + A_READ;
+  static constexpr uint32_t NEED = (NSTAGE - 1) * STAGE + A_BYTES + A_READ;
   static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
   static_assert(KP - KA <= 8, "one aliased core-matrix column at most");
 };
@@ -503,14 +503,17 @@ __device__ __forceinline__ float h16_scale(float max_abs) {
   return ldexpf(1.0f, 14 - e);
 }
 
-template <int NP2>
-__global__ void __launch_bounds__(kStoredThreads, 1)
+// NSTAGE shared-memory stages, MINB CTAs per SM: 4 stages and one CTA per SM
+// (built-in), or 2 stages and two CTAs per SM (two producers, issuers and
+// epilogues per SM; launch plan far_ctas = 2)
+template <int NP2, int NSTAGE, int MINB>
+__global__ void __launch_bounds__(kStoredThreads, MINB)
     k_far_h16(FarH16Tiles T, const int2* __restrict__ work, int nwork, int nrhs, int* __restrict__ err) {
   // Persistent: CTA c takes the rows c, c + gridDim.x, ... of the work list
   // (sorted by block count) and all three roles walk the same flattened
   // sequence of blocks, so the copy pipeline runs on across row boundaries.
-  using G = H16Shape<NP2>;
-  constexpr int S = kH16Stages;
+  using G = H16Shape<NP2, NSTAGE>;
+  constexpr int S = NSTAGE;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t full_bar[S], done_bar[S], free_bar[2];
   __shared__ uint32_t tmem_slot;
@@ -798,7 +801,7 @@ cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int
 }
 
 cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                           cudaStream_t s) {
+                           cudaStream_t s, int ctas_per_sm) {
   if (nwork == 0) return cudaSuccess;
   if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
   // one persistent CTA per SM (the shared-memory plan allows one)
@@ -809,11 +812,19 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
   switch (np2) {
 #define BG_T(N)                                                                                             \
   case N: {                                                                                                 \
+    if (ctas_per_sm == 2) {                                                                                 \
+      constexpr uint32_t smem = H16Shape<N, 2>::SMEM;                                                       \
+      static_assert(2 * smem <= 220 * 1024, "FP16 far field: two CTAs per SM do not fit");                  \
+      cudaError_t e = smem_limit(k_far_h16<N, 2, 2>, smem);                                                 \
+      if (e != cudaSuccess) return e;                                                                       \
+      k_far_h16<N, 2, 2><<<std::min(nwork, 2 * nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err); \
+      return cudaGetLastError();                                                                            \
+    }                                                                                                       \
     constexpr uint32_t smem = H16Shape<N>::SMEM;                                                            \
     static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
-    cudaError_t e = smem_limit(k_far_h16<N>, smem); \
+    cudaError_t e = smem_limit(k_far_h16<N, kH16Stages, 1>, smem);                                          \
     if (e != cudaSuccess) return e;                                                                         \
-    k_far_h16<N><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err);            \
+    k_far_h16<N, kH16Stages, 1><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err); \
     return cudaGetLastError();                                                                              \
   }
     BG_H16_SHAPES(BG_T)

@@ -263,6 +263,10 @@ typedef struct bg_launch_plan {
    * matrices, where the operator has a transfer level); 1 batched GEMMs with
    * the assembled matrices, level by level. Results agree to rounding. */
   int transforms;
+  /* stored-tile far field of real operators (BG_PREC_MIXED, BG_PREC_FP32):
+   * 0 or 1 built-in (one persistent CTA of four shared-memory stages per SM);
+   * 2 two CTAs of two stages per SM. Results are identical. */
+  int far_ctas;
 } bg_launch_plan;
 
 typedef struct bg_tune_report {
