@@ -1820,7 +1820,7 @@ extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precisi
     st = sweep(&bg_launch_plan::near_kernel, v);
   }
   if (st == BG_OK && op->fmm_fused) st = sweep(&bg_launch_plan::transforms, {1});
-  if (st == BG_OK && mixed && !op->cplx && op->far_tiles) st = sweep(&bg_launch_plan::far_ctas, {2});
+  if (st == BG_OK && mixed && !op->cplx && op->far_tiles) st = sweep(&bg_launch_plan::far_ctas, {1, 2});
   if (st == BG_OK && mixed && op->use_tgemm && (!op->fmm_fused || cur.transforms == 1))
     st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
   if (st == BG_OK && mixed && op->d_far_work_alt[0].p) st = sweep(&bg_launch_plan::far_order, {1, 2});

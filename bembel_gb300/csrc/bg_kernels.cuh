@@ -161,9 +161,10 @@ size_t far_h16_btile_bytes(int np2);  // per cluster
 cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long nblocks, void* tiles, float* ainv,
                                     cudaStream_t s);
 cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s);
-// ctas_per_sm: 2 runs two CTAs of two stages per SM, otherwise one of four
+// ctas_per_sm: 1 one CTA of four stages per SM, 2 two CTAs of two stages,
+// otherwise the built-in choice (2 when there are at least 2 x SMs rows)
 cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                           cudaStream_t s, int ctas_per_sm = 1);
+                           cudaStream_t s, int ctas_per_sm = 0);
 // watchdog self-test: a bounded wait that cannot complete; sets *err = 99 when it runs out
 cudaError_t launch_wait_selftest(long long limit_cycles, int* err, cudaStream_t s);
 // real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32

@@ -264,7 +264,8 @@ typedef struct bg_launch_plan {
    * the assembled matrices, level by level. Results agree to rounding. */
   int transforms;
   /* stored-tile far field of real operators (BG_PREC_MIXED, BG_PREC_FP32):
-   * 0 or 1 built-in (one persistent CTA of four shared-memory stages per SM);
+   * 0 built-in (2 when there are at least twice as many far-field rows as
+   * SMs, else 1); 1 one persistent CTA of four shared-memory stages per SM;
    * 2 two CTAs of two stages per SM. Results are identical. */
   int far_ctas;
 } bg_launch_plan;
