@@ -303,6 +303,14 @@ class DiscreteOperator:
         re_, im_ = np.ascontiguousarray(k.real), np.ascontiguousarray(k.imag)
         self.ctx.check(_lib.load().bg_operator_prepare_wavenumbers(self.h, _dp(re_), _dp(im_), len(k)))
 
+    def quadrature_counts(self):
+        """Near-field quadrature work (bg_operator_quadrature_counts): pairs and
+        integrand evaluations per rule (regular, identical, edge, vertex)."""
+        out = np.zeros(8, dtype=np.int64)
+        self.ctx.check(_lib.load().bg_operator_quadrature_counts(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long))))
+        names = ("regular", "identical", "edge", "vertex")
+        return {n: {"pairs": int(out[2 * i]), "evaluations": int(out[2 * i + 1])} for i, n in enumerate(names)}
+
     def release_wavenumbers(self):
         self.ctx.check(_lib.load().bg_operator_release_wavenumbers(self.h))
 
@@ -342,17 +350,17 @@ class DiscreteOperator:
 
     # -- launch plans and the autotuner --
     def set_plan(self, nrhs, precision="mixed", near_kernel=0, split_k_batches=-1, far_order=0, transforms=0,
-                 far_ctas=0):
+                 far_ctas=0, mixed_near=0):
         """Kernel variants and schedules of products with nrhs right-hand
-        sides at precision (bg_launch_plan; {0, -1, 0, 0, 0} is the built-in plan)."""
-        p = _lib.LaunchPlan(near_kernel, split_k_batches, far_order, transforms, far_ctas)
+        sides at precision (bg_launch_plan; {0, -1, 0, 0, 0, 0} is the built-in plan)."""
+        p = _lib.LaunchPlan(near_kernel, split_k_batches, far_order, transforms, far_ctas, mixed_near)
         self.ctx.check(_lib.load().bg_operator_set_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
 
     def get_plan(self, nrhs, precision="mixed"):
         p = _lib.LaunchPlan()
         self.ctx.check(_lib.load().bg_operator_get_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
         return {"near_kernel": p.near_kernel, "split_k_batches": p.split_k_batches, "far_order": p.far_order,
-                "transforms": p.transforms, "far_ctas": p.far_ctas}
+                "transforms": p.transforms, "far_ctas": p.far_ctas, "mixed_near": p.mixed_near}
 
     def autotune(self, nrhs, precision="mixed", reps=5):
         """Time the product's kernel variants for nrhs right-hand sides at
@@ -362,7 +370,7 @@ class DiscreteOperator:
         return {"candidates": r.candidates, "builtin_ms": r.builtin_ms, "tuned_ms": r.tuned_ms,
                 "plan": {"near_kernel": r.plan.near_kernel, "split_k_batches": r.plan.split_k_batches,
                          "far_order": r.plan.far_order, "transforms": r.plan.transforms,
-                         "far_ctas": r.plan.far_ctas}}
+                         "far_ctas": r.plan.far_ctas, "mixed_near": r.plan.mixed_near}}
 
     # -- inspection --
     def elements(self):

@@ -36,7 +36,8 @@ class SolveStats(ctypes.Structure):
 
 class LaunchPlan(ctypes.Structure):
     _fields_ = [("near_kernel", ctypes.c_int), ("split_k_batches", ctypes.c_int), ("far_order", ctypes.c_int),
-                ("transforms", ctypes.c_int), ("far_ctas", ctypes.c_int)]
+                ("transforms", ctypes.c_int), ("far_ctas", ctypes.c_int),
+                ("mixed_near", ctypes.c_int)]
 
 
 class TuneReport(ctypes.Structure):
@@ -107,6 +108,7 @@ def load(build_if_missing=True):
         "bg_operator_assembly_times": (I, [P, dp]),
         "bg_operator_prepare_wavenumbers": (I, [P, dp, dp, I]),
         "bg_operator_release_wavenumbers": (I, [P]),
+        "bg_operator_quadrature_counts": (I, [P, lp]),
         "bg_matvec": (I, [P, P, Lg, P, Lg, I, dp, dp, I, I]),
         "bg_load_vector": (I, [P, I, dp, I, P, I]),
         "bg_solve": (I, [P, P, P, I, ctypes.POINTER(SolveParams), ctypes.POINTER(SolveStats), I]),

@@ -628,7 +628,8 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
   size_t a = 0;
   for (const DevBuf* b : {&op->d_patch_meta, &op->d_patch_cp, &op->d_el_patch, &op->d_el_llc, &op->d_T_ptr,
                           &op->d_T_idx, &op->d_T_val, &op->d_Tt_ptr, &op->d_Tt_idx, &op->d_Tt_val, &op->d_cheb,
-                          &op->d_dense64, &op->d_dense32, &op->d_dense_df, &op->d_tr64, &op->d_tr32,
+                          &op->d_dense64, &op->d_dense32, &op->d_dense_df, &op->d_oz_tiles, &op->d_oz_rexp,
+                          &op->w_oz_panels, &op->w_oz_fmax, &op->d_tr64, &op->d_tr32,
                           &op->d_far_work, &op->d_err, &op->w_xdof, &op->w_xss, &op->w_yss, &op->w_ydof,
                           &op->w_xss32, &op->w_yss32, &op->w_xss_df,
                           &op->dense.d_row_ptr, &op->dense.d_col})
@@ -651,6 +652,9 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
   size_t e = (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * sb +
              (size_t)op->dense.col.size() * op->block_stride32(op->dense.B) * sb / 2;
   if (!op->cplx) e += (size_t)op->dense.col.size() * op->block_stride(op->dense.B) * sizeof(float2);  // double-float
+  if (!op->cplx && oz_supported(op->dense.B))  // tensor-core digit tiles, row exponents, x digit panels
+    e += oz_tile_bytes(op->dense.B, (long)op->dense.col.size()) + (size_t)op->dense.nrows * op->dense.B * sizeof(int) +
+         oz_panel_bytes(op->dense.B, op->S / op->dense.B) + 32 * sizeof(int);
   for (int l = 0; l <= op->leaf_level && l < (int)op->far.size(); ++l) {
     const size_t nb = op->far[l].col.size();
     const size_t ncl = (size_t)op->nclusters(l);
@@ -1116,6 +1120,30 @@ static bg_status assemble_near(bg_operator* op) {
   return near_quadrature(op, w, 1, &op->kre, &op->kim, &out);
 }
 
+extern "C" bg_status bg_operator_quadrature_counts(const bg_operator* op, long* counts8) {
+  if (!op || !counts8) return BG_INVALID_ARG;
+  for (int i = 0; i < 8; ++i) counts8[i] = 0;
+  if (op->maxwell() || op->vd != 1)
+    return set_error(op->ctx, BG_UNSUPPORTED, "quadrature counts: scalar operators only");
+  const NearWork w = near_work(op);
+  for (const auto& kv : w.regular) {
+    const long q = (long)(kv.first + 1) * (kv.first + 1);
+    counts8[0] += (long)kv.second.size();
+    counts8[1] += (long)kv.second.size() * q * q;
+  }
+  // point pairs per (outer, inner) Gauss sample of the reference's rules:
+  // identical 8 (integrate2.hpp), common edge 6 (integrate3.hpp), common vertex 4 (integrate4.hpp)
+  for (const auto& kv : w.singular) {
+    const int cs = kv.first.first;
+    const long q = (long)(kv.first.second + 1) * (kv.first.second + 1);
+    const int slot = cs == 2 ? 2 : (cs == 3 ? 4 : 6);
+    const long per = cs == 2 ? 8 : (cs == 3 ? 6 : 4);
+    counts8[slot] += (long)kv.second.size();
+    counts8[slot + 1] += (long)kv.second.size() * q * q * per;
+  }
+  return BG_OK;
+}
+
 extern "C" bg_status bg_operator_prepare_wavenumbers(bg_operator* op, const double* kre, const double* kim, int n) {
   if (!op || n < 0 || (n > 0 && (!kre || !kim))) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
@@ -1207,6 +1235,22 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
       if (e == cudaSuccess) e = launch_split_df(op->d_dense64.p, n, op->d_dense_df.p, op->ctx->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(op->ctx->stream);
       if ((st = cuda_status(op->ctx, e, "double-float near field")) != BG_OK) return st;
+    }
+    // integer digits of the real blocks for the tensor-core near field of
+    // BG_PREC_MIXED products (and their per-product scratch: x digit panels,
+    // zero where no digit is written, and column exponents)
+    if (!op->cplx && nb > 0 && oz_supported((int)B) && (long)op->dense.nrows * B == (long)op->S) {
+      const int nrows = op->dense.nrows;
+      e = op->d_oz_tiles.alloc(oz_tile_bytes((int)B, nb));
+      if (e == cudaSuccess) e = op->d_oz_rexp.alloc((size_t)nrows * B * sizeof(int));
+      if (e == cudaSuccess) e = op->w_oz_panels.alloc(oz_panel_bytes((int)B, op->S / B));
+      if (e == cudaSuccess) e = op->w_oz_fmax.alloc(32 * sizeof(int));
+      if (e == cudaSuccess) e = cudaMemsetAsync(op->w_oz_panels.p, 0, op->w_oz_panels.bytes, op->ctx->stream);
+      if (e == cudaSuccess)
+        e = launch_oz_build(op->dense.d_row_ptr.as<int>(), op->d_dense64.as<double>(), op->block_stride((int)B), nrows,
+                            (int)B, op->d_oz_rexp.as<int>(), op->d_oz_tiles.p, nb, op->ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(op->ctx->stream);
+      if ((st = cuda_status(op->ctx, e, "tensor-core near field digits")) != BG_OK) return st;
     }
   }
   auto t2 = std::chrono::steady_clock::now();
@@ -1321,13 +1365,31 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp32(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense32.p,
                         op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss32.p, op->w_yss32.p, nrhs, 0, s, pl.near_kernel); }),
              "near-field product (FP32)");
+  } else if (mixed && !op->cplx && op->d_oz_tiles.p && pl.mixed_near == 0) {
+    // FP64-accurate near field on the tensor cores: 8 integer digits of 7
+    // bits per operand, exact integer accumulation, one rounding at the end
+    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] {
+               return launch_near_oz(op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->dense.nrows,
+                                     op->dense.B, op->d_oz_tiles.p, op->d_oz_rexp.as<int>(), op->w_xss.as<double>(),
+                                     op->S, nrhs, op->w_oz_panels.p, op->w_oz_fmax.as<int>(), op->w_yss.as<double>(),
+                                     nrhs, nrhs, op->d_err.as<int>(), s); }),
+             "near-field product (tensor cores, integer digits)");
   } else if (mixed && !op->cplx && op->d_dense_df.p) {
     // FP64-accurate near field in double-float: blocks and x as FP32 (hi, lo)
     // pairs, exact products and compensated sums (about 1e-14 relative)
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df(op->w_xss.p, ss_n, op->w_xss_df.p, s); }),
              "near-field split of x");
-    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_df(op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense_df.p,
-                        op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss_df.p, op->w_yss.p, nrhs, 0, s); }),
+    // launch plan: 32 columns with a quarter of them on the FP64 pipe, the
+    // rest in double-float
+    const bool both_pipes = pl.mixed_near == 2 && nrhs == 32 && op->dense.B <= 42;
+    BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] {
+               return both_pipes
+                          ? launch_bsr_near_mix(op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense_df.p,
+                                                op->d_dense64.p, op->block_stride(op->dense.B), op->dense.nrows, op->dense.B,
+                                                op->w_xss_df.p, op->w_xss.p, op->w_yss.p, s)
+                          : launch_bsr_df(op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense_df.p,
+                                          op->block_stride(op->dense.B), op->dense.nrows, op->dense.B, op->w_xss_df.p,
+                                          op->w_yss.p, nrhs, 0, s); }),
              "near-field product (double-float)");
   } else {
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp64(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense64.p,
@@ -1717,7 +1779,8 @@ extern "C" bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precisi
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: nrhs must be positive and the precision a bg_precision");
   if (plan->near_kernel < 0 || plan->near_kernel > 3 || plan->split_k_batches < -1 ||
       plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2 || plan->transforms < 0 ||
-      plan->transforms > 1 || plan->far_ctas < 0 || plan->far_ctas > 2)
+      plan->transforms > 1 || plan->far_ctas < 0 || plan->far_ctas > 2 || plan->mixed_near < 0 ||
+      plan->mixed_near > 2)
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: a field is out of range");
   op->plans[bg_operator::plan_key(nrhs, precision)] = *plan;
   op->drop_graphs();
@@ -1821,6 +1884,7 @@ extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precisi
   }
   if (st == BG_OK && op->fmm_fused) st = sweep(&bg_launch_plan::transforms, {1});
   if (st == BG_OK && mixed && !op->cplx && op->far_tiles) st = sweep(&bg_launch_plan::far_ctas, {1, 2});
+  if (st == BG_OK && mixed && !near32 && !op->cplx && op->d_dense_df.p) st = sweep(&bg_launch_plan::mixed_near, {1, 2});
   if (st == BG_OK && mixed && op->use_tgemm && (!op->fmm_fused || cur.transforms == 1))
     st = sweep(&bg_launch_plan::split_k_batches, {0, 304, 608});
   if (st == BG_OK && mixed && op->d_far_work_alt[0].p) st = sweep(&bg_launch_plan::far_order, {1, 2});

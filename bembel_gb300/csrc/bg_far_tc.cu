@@ -33,10 +33,13 @@
 #include <cstdint>
 
 #include "bg_kernels.cuh"
+#include "bg_tcgen05.cuh"
 
 namespace bg {
 
 namespace {
+
+using namespace tc;
 
 constexpr int kGenWarps = 16;                 // warps generating the tiles
 constexpr int kGenThreads = 32 * kGenWarps;   // the MMA warp follows them
@@ -45,67 +48,11 @@ constexpr int kN = 32;                        // MMA N: right-hand sides per til
 constexpr int kYStride = 40;                  // floats per staged Y_j row (conflict-free reads)
 // FP32 accumulators: 2 buffers x {hi*hi, hi*lo + lo*hi} x 32 columns
 constexpr uint32_t kTmemCols = 128;
-constexpr long long kWaitCycles = 2000000000LL;  // about one second at 2 GHz
 constexpr float kFar = 1.0e18f;                  // padding points: finite r^2 (< 1.2e37), weight 0
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// K-major, no swizzle: LBO = byte distance of core matrices adjacent in K,
-// SBO = byte distance of core matrices adjacent in M (or N); version 1.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;  // base offset 0, relative LBO, layout SWIZZLE_NONE
-}
-
-// kind::tf32 instruction descriptor: D FP32, A and B TF32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
 
 // round to the nearest TF32 value (10 explicit mantissa bits), ties away
 __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// bounded wait for the completion of the phase with the given parity
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = smem_u32(bar);
-  const long long t0 = clock64();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
-  }
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
-               : "memory");
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -116,17 +63,6 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 }
 
 __device__ __forceinline__ void gen_sync() { asm volatile("bar.sync 1, %0;\n" ::"n"(kGenThreads) : "memory"); }
-
-// 32 lanes x 8 consecutive FP32 columns of tensor memory, one lane per thread
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 // 1/sqrt(x) by the hardware approximation (relative error below 2^-22); x is
 // a squared distance of admissible clusters or a padding value, never subnormal
@@ -415,34 +351,6 @@ static cudaError_t launch_np(const FarTcLevels& L, const int2* work, int nwork, 
 // Stored-tile helpers: 1-D TMA bulk copies and wide tensor-memory loads.
 constexpr int kStoredThreads = 192;
 
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// 1-D bulk copy global -> shared, completion counted on bar (16-byte aligned
-// addresses, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // ---------------------------------------------------------------------------
 // FP16 stored-tile variant (the one the product uses). Each low-rank block is
 // scaled by a power of two sA (largest coupling in [2^13, 2^14)) and split into
@@ -462,17 +370,27 @@ constexpr int kH16Stages = 4;
 // the right-hand-side (B) tiles, which keep the full KP. Rows beyond the
 // stored row groups (M = 128 reads 16) only feed output rows >= NP2, which
 // are never read.
-template <int NP2, int NSTAGE = kH16Stages>
+// EDGE (real operators, n_p^2 >= 16): the MMA covers K = KM, n_p^2 rounded
+// down to the K step of 16, and the last E = n_p^2 - KM source columns are
+// applied on the CUDA cores in FP32: their couplings follow the tiles of a
+// block in global memory (EDGE_BYTES, [e][m]), read by the epilogue, so no
+// K padding is stored or streamed (n_p = 9: 80 + 1 columns; 28 496 bytes
+// per block instead of 30 976).
+template <int NP2, int NSTAGE = kH16Stages, bool EDGE = false>
 struct H16Shape {
-  static constexpr int KP = (NP2 + 15) / 16 * 16;  // K padded to the f16 MMA K step
+  static constexpr bool SPLIT = EDGE && NP2 >= 16;
+  static constexpr int KP = SPLIT ? NP2 / 16 * 16 : (NP2 + 15) / 16 * 16;  // K of the MMA steps and B tiles
+  static constexpr int E = SPLIT ? NP2 - KP : 0;                            // source columns on the CUDA cores
   static constexpr int KC = KP / 8;                // 16-byte core-matrix columns (8 halves) of a B tile
-  static constexpr int KA = (NP2 + 7) / 8 * 8;     // K stored in the A tiles
+  static constexpr int KA = SPLIT ? KP : (NP2 + 7) / 8 * 8;  // K stored in the A tiles
   static constexpr int KCA = KA / 8;
   static constexpr int MG = (NP2 + 7) / 8;
   static constexpr uint32_t SBO = KC * 128;        // B tiles: bytes between 8-row groups
   static constexpr uint32_t SBOA = KCA * 128;      // A tiles
   static constexpr uint32_t A_BYTES = MG * SBOA, B_BYTES = 4 * SBO;
   static constexpr uint32_t A2 = 2 * A_BYTES, B2 = 2 * B_BYTES;
+  static constexpr uint32_t EDGE_BYTES = (uint32_t)(E * NP2 * 4 + 15) / 16 * 16;
+  static constexpr uint32_t ASTRIDE = A2 + EDGE_BYTES;  // global bytes per block: hi, lo, edge couplings
   static constexpr uint32_t STAGE = A2 + B2;
   static constexpr uint32_t TILES = NSTAGE * STAGE;
   // furthest byte an M = 128 A operand reads, from its start
@@ -481,19 +399,6 @@ struct H16Shape {
   static constexpr uint32_t SMEM = TILES > NEED ? TILES : NEED;
   static_assert(KP - KA <= 8, "one aliased core-matrix column at most");
 };
-
-// kind::f16 instruction descriptor: D FP32, A and B FP16, both K-major.
-__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
-  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                        uint32_t accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
 
 // power of two s with max_abs * s in [2^13, 2^14) (1 for zero or non-finite)
 __device__ __forceinline__ float h16_scale(float max_abs) {
@@ -514,7 +419,7 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
   // Persistent: CTA c takes the rows c, c + gridDim.x, ... of the work list
   // (sorted by block count) and all three roles walk the same flattened
   // sequence of blocks, so the copy pipeline runs on across row boundaries.
-  using G = H16Shape<NP2, NSTAGE>;
+  using G = H16Shape<NP2, NSTAGE, true>;
   constexpr int S = NSTAGE;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t full_bar[S], done_bar[S], free_bar[2];
@@ -561,7 +466,7 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
           }
           if (*abort_v) break;
           unsigned char* sm = smem + st * G::STAGE;
-          const unsigned char* ga = atiles + (size_t)k * G::A2;
+          const unsigned char* ga = atiles + (size_t)k * G::ASTRIDE;
           const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
           // hi and lo tiles are contiguous in global and shared memory: one copy each for A and B
           mbar_expect_tx(&full_bar[st], G::STAGE);
@@ -624,19 +529,49 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
       const int* col = T.col[lev];
       const float* ainv = T.ainv[lev];
       const float* binv = T.binv[lev];
+      const unsigned char* atiles = T.a[lev];
+      const float* ylev = T.y[lev];
       float sum[32], comp[32];
 #pragma unroll
       for (int n = 0; n < 32; ++n) sum[n] = comp[n] = 0.0f;
       for (int k = kb; k < ke; ++k, ++it) {
         const int st = it % S, ab = it & 1;
-        // the block's scales do not depend on its MMAs: load them first, so
-        // that their latency overlaps the wait for the accumulators
+        // the block's scales and edge columns do not depend on its MMAs: load
+        // them first, so that their latency overlaps the wait for the
+        // accumulators
         const float sa = __ldg(&ainv[k]);
         float4 bsc[8];
         {
           const float4* sb = reinterpret_cast<const float4*>(binv + (long)col[k] * kN);
 #pragma unroll
           for (int q = 0; q < 8; ++q) bsc[q] = __ldg(&sb[q]);
+        }
+        // source columns KP .. NP2 - 1 in FP32, f Y[KP + e][n] added to the
+        // compensation term of the row sums (the edge is a 1 / n_p^2 share of
+        // a block's contribution, so plain FP32 sums keep its error below
+        // the tiles' own)
+        if (G::E > 0) {
+          const float* edge = reinterpret_cast<const float*>(atiles + (size_t)k * G::ASTRIDE + G::A2);
+          const float* ye = ylev + ((long)col[k] * NP2 + G::KP) * nrhs;
+#pragma unroll
+          for (int e = 0; e < G::E; ++e) {
+            const float f = m < NP2 ? __ldg(edge + e * NP2 + m) : 0.0f;
+            if (nrhs == kN) {
+              const float4* y4 = reinterpret_cast<const float4*>(ye + e * kN);
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {
+                const float4 v = __ldg(&y4[q]);
+                comp[4 * q + 0] = fmaf(f, v.x, comp[4 * q + 0]);
+                comp[4 * q + 1] = fmaf(f, v.y, comp[4 * q + 1]);
+                comp[4 * q + 2] = fmaf(f, v.z, comp[4 * q + 2]);
+                comp[4 * q + 3] = fmaf(f, v.w, comp[4 * q + 3]);
+              }
+            } else {
+#pragma unroll
+              for (int n = 0; n < 32; ++n)
+                if (n < nrhs) comp[n] = fmaf(f, __ldg(ye + e * nrhs + n), comp[n]);
+            }
+          }
         }
         int got = 1;
         if (lane == 0) got = mbar_wait(&done_bar[st], (uint32_t)((it / S) & 1)) ? 1 : 0;
@@ -686,7 +621,7 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
 template <int NP2>
 __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restrict__ F, long bstride,
                                                           __half* __restrict__ tiles, float* __restrict__ ainv) {
-  using G = H16Shape<NP2>;
+  using G = H16Shape<NP2, kH16Stages, true>;
   constexpr int AH = G::A_BYTES / 2;  // halves per tile
   __shared__ float red[8];
   const long b = blockIdx.x;
@@ -699,7 +634,7 @@ __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restri
   mx = red[0];
   for (int i = 1; i < (int)(blockDim.x >> 5); ++i) mx = fmaxf(mx, red[i]);
   const float sa = h16_scale(mx * 1.0000001f);
-  __half* out = tiles + b * 2 * AH;
+  __half* out = tiles + b * (G::ASTRIDE / 2);
   for (int e = threadIdx.x; e < AH; e += blockDim.x) {
     const int cm = e >> 6, r = (e >> 3) & 7, c = e & 7;
     const int m = (cm / G::KCA) * 8 + r, k = (cm % G::KCA) * 8 + c;
@@ -708,6 +643,9 @@ __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restri
     out[e] = h;
     out[AH + e] = __double2half(v - (double)__half2float(h));
   }
+  // the edge columns KP .. NP2 - 1, unscaled FP32, [e][m]
+  float* edge = reinterpret_cast<float*>(out + 2 * AH);
+  for (int t = threadIdx.x; t < G::E * NP2; t += blockDim.x) edge[t] = (float)Fb[(long)G::KP * NP2 + t];
   if (threadIdx.x == 0) ainv[b] = 1.0f / sa;
 }
 
@@ -716,7 +654,7 @@ __global__ void __launch_bounds__(256) k_build_h16_atiles(const double* __restri
 // 1/sB[n] to binv (32 per cluster, zero-padded columns have scale 1).
 template <int NP2>
 __global__ void __launch_bounds__(256) k_build_h16_btiles(FarH16Tiles T, int nlev, int nrhs) {
-  using G = H16Shape<NP2>;
+  using G = H16Shape<NP2, kH16Stages, true>;
   constexpr int BH = G::B_BYTES / 2;
   __shared__ float cmax[8][kN];
   __shared__ float scale[kN];
@@ -756,7 +694,7 @@ __global__ void __launch_bounds__(256) k_build_h16_btiles(FarH16Tiles T, int nle
 size_t far_h16_atile_bytes(int np2) {
   switch (np2) {
 #define BG_T(N) \
-  case N: return H16Shape<N>::A2;
+  case N: return H16Shape<N, kH16Stages, true>::ASTRIDE;
     BG_H16_SHAPES(BG_T)
 #undef BG_T
     default: return 0;
@@ -765,7 +703,7 @@ size_t far_h16_atile_bytes(int np2) {
 size_t far_h16_btile_bytes(int np2) {
   switch (np2) {
 #define BG_T(N) \
-  case N: return H16Shape<N>::B2;
+  case N: return H16Shape<N, kH16Stages, true>::B2;
     BG_H16_SHAPES(BG_T)
 #undef BG_T
     default: return 0;
@@ -806,25 +744,25 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
                            cudaStream_t s, int ctas_per_sm) {
   if (nwork == 0) return cudaSuccess;
   if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
-  // one persistent CTA per SM (the shared-memory plan allows one)
+  // persistent CTAs: one or two per SM
   int dev = 0, nsm = 0;
   cudaError_t ea = cudaGetDevice(&dev);
   if (ea == cudaSuccess) ea = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (ea != cudaSuccess) return ea;
-  switch (np2) {
   // built-in: two CTAs per SM when every CTA still gets a row
   if (ctas_per_sm != 1 && ctas_per_sm != 2) ctas_per_sm = nwork >= 2 * nsm ? 2 : 1;
+  switch (np2) {
 #define BG_T(N)                                                                                             \
   case N: {                                                                                                 \
     if (ctas_per_sm == 2) {                                                                                 \
-      constexpr uint32_t smem = H16Shape<N, 2>::SMEM;                                                       \
+      constexpr uint32_t smem = H16Shape<N, 2, true>::SMEM;                                                 \
       static_assert(2 * smem <= 220 * 1024, "FP16 far field: two CTAs per SM do not fit");                  \
       cudaError_t e = smem_limit(k_far_h16<N, 2, 2>, smem);                                                 \
       if (e != cudaSuccess) return e;                                                                       \
       k_far_h16<N, 2, 2><<<std::min(nwork, 2 * nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err); \
       return cudaGetLastError();                                                                            \
     }                                                                                                       \
-    constexpr uint32_t smem = H16Shape<N>::SMEM;                                                            \
+    constexpr uint32_t smem = H16Shape<N, kH16Stages, true>::SMEM;                                          \
     static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
     cudaError_t e = smem_limit(k_far_h16<N, kH16Stages, 1>, smem);                                          \
     if (e != cudaSuccess) return e;                                                                         \

@@ -200,6 +200,29 @@ cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks
                           const void* x, void* y, int nrhs, int accumulate, cudaStream_t s);
 // out[t] = (hi, lo) of in[t] (FP64), t < n
 cudaError_t launch_split_df(const void* in, long n, void* out, cudaStream_t s);
+// FP64-accurate near field on the tensor cores (bg_near_tc.cu) for real
+// operators with leaf blocks of B = 4, 16 or 36 rows: oz_supported(B);
+// bytes of the digit tiles of nblocks blocks and of the x digit panels of
+// nclusters clusters; launch_oz_build turns the FP64 blocks (column-major,
+// stride bstride) into row exponents rexp [nrows * B] and digit tiles;
+// launch_near_oz writes y (rows of ldy entries, nrhs columns) = A x for x
+// FP64 [xrows][ldx], panels and fmax (32 ints) its scratch, err the bounded
+// waits' flag
+bool oz_supported(int B);
+size_t oz_tile_bytes(int B, long nblocks);
+size_t oz_panel_bytes(int B, long nclusters);
+cudaError_t launch_oz_build(const int* row_ptr, const double* blocks, long bstride, int nrows, int B, int* rexp,
+                            void* tiles, long nblocks, cudaStream_t s);
+cudaError_t launch_near_oz(const int* row_ptr, const int* col, int nrows, int B, const void* tiles,
+                           const int* rexp, const double* x, long xrows, int ldx, void* panels, int* fmax,
+                           double* y, int ldy, int nrhs, int* err, cudaStream_t s);
+// FP64-accurate near field of real operators for exactly 32 right-hand
+// sides (B <= 42): columns 0 .. 23 in double-float from the (hi, lo) pairs
+// and the split x, columns 24 .. 31 in FP64 from blocks64 and x64 (row-major
+// [rows][32], 16-byte aligned); y written (not accumulated)
+cudaError_t launch_bsr_near_mix(const int* row_ptr, const int* col, const void* pairs, const void* blocks64,
+                                long bstride, int nrows, int B, const void* xdf, const void* x64, void* y,
+                                cudaStream_t s);
 // as launch_bsr_df, writing columns y0 .. y0 + nrhs - 1 of y rows of ldy entries
 cudaError_t launch_bsr_df_cols(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
                                const void* x, void* y, int nrhs, int ldy, int y0, int accumulate, cudaStream_t s);

@@ -994,6 +994,113 @@ __global__ void __launch_bounds__(352) k_bsr_df(const int* __restrict__ row_ptr,
   }
 }
 
+// FP64-accurate near field for 32 right-hand sides on both pipes at once:
+// the double-float arithmetic of k_bsr_df runs on the FP32 pipe and the FP64
+// pipe sits idle, so a quarter of the columns (24 .. 31) go to native FP64
+// fma on the FP64 pipe in warps of their own. Per CTA (one block row):
+// warps 0-3 are the double-float role (thread = block row i x 8 of columns
+// 0 .. 23, 3 B threads active), warps 4-5 the FP64 role (thread = block row
+// i x columns 24 .. 31). Both read the same block: its (hi, lo) pairs and its
+// FP64 entries (same element stride); x arrives split (columns 0 .. 23) and in
+// FP64 (columns 24 .. 31), both panels double-buffered with cp.async.
+constexpr int kMixThreads = 192, kMixDfThreads = 128, kMixCols = 32, kMixDfCols = 24;
+__global__ void __launch_bounds__(kMixThreads) k_bsr_near_mix(const int* __restrict__ row_ptr,
+                                                             const int* __restrict__ col,
+                                                             const float2* __restrict__ pairs,
+                                                             const double* __restrict__ blocks64, long bstride,
+                                                             int B, const float2* __restrict__ xdf,
+                                                             const double* __restrict__ x64,
+                                                             double* __restrict__ y) {
+  extern __shared__ __align__(16) unsigned char mix_smem[];
+  float2* xs = reinterpret_cast<float2*>(mix_smem);  // [2][B][24] split x
+  double* xd = reinterpret_cast<double*>(xs + 2 * B * kMixDfCols);  // [2][B][8] FP64 x
+  constexpr int NF = kMixCols - kMixDfCols;
+  const int row = blockIdx.x, t = threadIdx.x;
+  const int kb = row_ptr[row], ke = row_ptr[row + 1];
+  auto issue = [&](int k, int buf) {
+    const long r0 = (long)col[k] * B;
+    // split columns 0 .. 23: 24 pairs = 192 bytes per row, 12 x 16 bytes
+    for (int e = t; e < B * 12; e += kMixThreads) {
+      const int r = e / 12, q = e - r * 12;
+      cp_async16(xs + (buf * B + r) * kMixDfCols + 2 * q, xdf + (r0 + r) * kMixCols + 2 * q);
+    }
+    // FP64 columns 24 .. 31: 64 bytes per row, 4 x 16 bytes
+    for (int e = t; e < B * 4; e += kMixThreads) {
+      const int r = e >> 2, q = e & 3;
+      cp_async16(xd + (buf * B + r) * NF + 2 * q, x64 + (r0 + r) * kMixCols + kMixDfCols + 2 * q);
+    }
+    cp_async_commit();
+  };
+  const bool df = t < kMixDfThreads;
+  const int tt = df ? t : t - kMixDfThreads;
+  const int i = df ? tt % B : tt, cg = df ? tt / B : 0;
+  const bool active = df ? (tt < 3 * B) : (tt < B);
+  float s[8], cc[8];
+  double a[NF];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s[c] = cc[c] = 0.0f;
+#pragma unroll
+  for (int c = 0; c < NF; ++c) a[c] = 0.0;
+  if (kb < ke) issue(kb, 0);
+  for (int k = kb; k < ke; ++k) {
+    const int buf = (k - kb) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // panels k staged; everyone is done with panels k-1
+    if (k + 1 < ke) issue(k + 1, buf ^ 1);
+    if (active && df) {
+      const float2* F = pairs + (long)k * bstride + i;
+      const float2* xp = xs + buf * B * kMixDfCols + 8 * cg;
+      for (int j = 0; j < B; ++j) {
+        const float2 f = __ldg(F + (long)j * B);
+        const float2* xv = xp + j * kMixDfCols;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const float2 b = xv[c];
+          const float p = f.x * b.x;
+          float e = fmaf(f.x, b.x, -p);
+          e = fmaf(f.x, b.y, e);
+          e = fmaf(f.y, b.x, e);
+          const float ts = s[c] + p, z = ts - s[c];
+          cc[c] += ((s[c] - (ts - z)) + (p - z)) + e;
+          s[c] = ts;
+        }
+      }
+    } else if (active) {
+      const double* F = blocks64 + (long)k * bstride + i;
+      const double* xp = xd + buf * B * NF;
+      for (int j = 0; j < B; ++j) {
+        const double f = __ldg(F + (long)j * B);
+#pragma unroll
+        for (int c = 0; c < NF; ++c) a[c] = fma(f, xp[j * NF + c], a[c]);
+      }
+    }
+  }
+  if (!active) return;
+  double* yo = y + ((long)row * B + i) * kMixCols;
+  if (df) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) yo[8 * cg + c] = (double)s[c] + (double)cc[c];
+  } else {
+#pragma unroll
+    for (int c = 0; c < NF; ++c) yo[kMixDfCols + c] = a[c];
+  }
+}
+
+cudaError_t launch_bsr_near_mix(const int* row_ptr, const int* col, const void* pairs, const void* blocks64,
+                                long bstride, int nrows, int B, const void* xdf, const void* x64, void* y,
+                                cudaStream_t s) {
+  if (nrows == 0) return cudaSuccess;
+  if (B < 1 || 3 * B > kMixDfThreads || B > kMixThreads - kMixDfThreads) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)2 * B * (kMixDfCols * sizeof(float2) + (kMixCols - kMixDfCols) * sizeof(double));
+  cudaError_t e = smem_limit(k_bsr_near_mix, smem);
+  if (e != cudaSuccess) return e;
+  k_bsr_near_mix<<<nrows, kMixThreads, smem, s>>>(row_ptr, col, static_cast<const float2*>(pairs),
+                                                  static_cast<const double*>(blocks64), bstride, B,
+                                                  static_cast<const float2*>(xdf), static_cast<const double*>(x64),
+                                                  static_cast<double*>(y));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_bsr_df(const int* row_ptr, const int* col, const void* blocks, long bstride, int nrows, int B,
                           const void* x, void* y, int nrhs, int accumulate, cudaStream_t s) {
   return launch_bsr_df_cols(row_ptr, col, blocks, bstride, nrows, B, x, y, nrhs, nrhs, 0, accumulate, s);

@@ -162,6 +162,11 @@ struct bg_operator {
   DevBuf d_dense32;                       // FP32 copy of the dense blocks (BG_PREC_FP32)
   DevBuf d_dense_df;                      // real operators: FP32 (hi, lo) pairs of the dense blocks, the
                                           // near field of BG_PREC_MIXED products (double-float, FP64 accuracy)
+  // real operators, leaf blocks of 4, 16 or 36 rows: the near field as 8
+  // FP16 integer digits per entry in tensor-core tiles (bg_near_tc.cu), the
+  // exponent of every block-row row, and the per-product x digit panels and
+  // column exponents
+  DevBuf d_oz_tiles, d_oz_rexp, w_oz_panels, w_oz_fmax;
   std::vector<DevBuf*> d_far64;           // per level
   std::vector<DevBuf*> d_far_df;          // per level: FP32 (hi, lo) pairs of d_far64 (real operators)
   std::vector<DevBuf*> d_far_atiles;      // per level: FP16 hi/lo tensor-core tiles of the low-rank blocks
@@ -231,7 +236,7 @@ struct bg_operator {
   // launch plans per (nrhs, precision), keyed as the graphs
   std::map<long, bg_launch_plan> plans;
   static long plan_key(int nrhs, int prec) { return (long)nrhs * 4 + prec; }
-  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0, 0, 0}; }
+  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0, 0, 0, 0}; }
   bg_launch_plan plan_for(int nrhs, int prec) const {
     auto it = plans.find(plan_key(nrhs, prec));
     return it == plans.end() ? builtin_plan() : it->second;

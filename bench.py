@@ -45,12 +45,13 @@ METRIC = "solves/s (32-RHS batched Laplace SL H2 solves to rel.err 1e-8, mixed p
 # FP32 FMA throughput of one GB300 measured with an FMA-chain probe (TFLOP/s)
 FP32_FMA_TFLOPS = 75.0
 # DRAM bytes (read + write) per low-rank block of k_far_h16, from one ncu
-# capture of the same kernel on the M=4 sphere (619.7 MB for 17 616 blocks:
-# 35 178 bytes per block against 33 792 bytes of operand tiles; the rest is
-# right-hand-side tiles missing L2 and the output)
-FAR_TILE_DRAM_BYTES_PER_BLOCK = 619.68e6 / 17616
-INNER_DESC = {"mixed": "inner GMRES(near field FP64-accurate (double-float), far field FP16 hi/lo tensor cores, "
-                       "FP32 accumulation)",
+# capture of the same kernel on the M=4 sphere (512.2 MB read + 7.2 MB
+# written for 17 616 blocks: 29 484 bytes per block against 28 496 bytes of
+# stored tiles and edge couplings; the rest is right-hand-side tiles missing
+# L2 and the output)
+FAR_TILE_DRAM_BYTES_PER_BLOCK = (512.184e6 + 7.199e6) / 17616
+INNER_DESC = {"mixed": "inner GMRES(near field FP64-accurate (tensor cores, 8 integer digits per operand, exact "
+                       "integer sums), far field FP16 hi/lo tensor cores, FP32 accumulation)",
               "fp32": "inner GMRES(near field FP32, far field FP16 hi/lo tensor cores, FP32 accumulation)"}
 
 
@@ -276,6 +277,7 @@ def run_gpu(args):
     op.compute()
     asm = op.assembly_times()
     asm["wall_s"] = time.time() - t0
+    quad = op.quadrature_counts()
     # launch plans of the 32-column products: built-in, or timed by the
     # library's autotuner (outside the timed region)
     plans = {"launch_plans": "built-in"}
@@ -432,6 +434,7 @@ def run_gpu(args):
                        "fp32_products_per_s_32rhs": mv32, "fp64_matvec_per_s": mv64 * NRHS,
                        "mixed_matvec_per_s": mvmx * NRHS, "fp32_matvec_per_s": mv32 * NRHS},
             "assembly_s": asm,
+            "assembly_roofline": assembly_roofline(quad, asm["near_s"], P, fp64_peak_tflops()),
             "kernel_ms_per_solve": {k: round(v, 3) for k, v in breakdown["ms"].items()},
             "kernel_launches_per_solve": breakdown["launches"]}
     if world == 1 and not args.no_cpu:
@@ -465,12 +468,67 @@ def _read_profile(L, ctx):
             "launches_total": sum(ln[i] for i in range(8))}
 
 
+def near_flops_per_evaluation(P):
+    """FP64 flops of one near-field integrand evaluation of a real scalar
+    kernel (Laplace), the minimal work of the reference's evaluateIntegrand
+    (Laplace/SingleLayerOperator.hpp:44-85 and its basis interaction,
+    AnsatzSpace/SuperSpace.hpp:173-178): the kernel value 1/(4 pi r) times the two
+    weights (3 differences, r^2 by one multiply and two FMAs, reciprocal
+    square root and scaling: 14 flops) and the rank-one update of the
+    (P+1)^2 x (P+1)^2 element-pair block, one multiply and one FMA per
+    entry (3 (P+1)^4 flops). Surface points, measures and basis values are
+    not counted: they can be shared between samples (the kernels share
+    most of them)."""
+    return 3 * (P + 1) ** 4 + 14
+
+
+def fp64_peak_tflops():
+    """Measured FP64 rate of this GPU: cuBLAS DGEMM (torch.matmul, 4096^3,
+    best of 5, CUDA events)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    best = None
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def assembly_roofline(quad, near_s, P, peak):
+    """Near-field assembly against the FP64 pipe: integrand evaluations of the
+    reference's rules (bg_operator_quadrature_counts: regular pairs
+    integrate0/1, identical integrate2, common edge integrate3, common vertex
+    integrate4) x near_flops_per_evaluation(P), over the near-field assembly
+    time (all rules, one launch sequence)."""
+    evals = sum(v["evaluations"] for v in quad.values())
+    fpe = near_flops_per_evaluation(P)
+    tf = evals * fpe / near_s / 1e12
+    return {"bound": "fp64", "evaluations": {k: v["evaluations"] for k, v in quad.items()},
+            "pairs": {k: v["pairs"] for k, v in quad.items()}, "near_s": near_s,
+            "evaluations_per_s": evals / near_s, "fp64_flops_per_evaluation": fpe,
+            "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+            "peak_source": "cuBLAS DGEMM 4096^3 on this GPU (torch.matmul float64, best of 5)"}
+
+
 def far_tile_bytes(np2):
-    """Bytes of the FP16 hi + lo operand tiles of one low-rank block as
-    stored: row groups of 8 targets x K padded to 8 sources, 2 bytes each."""
+    """Bytes of one low-rank block as stored for the tensor-core far field:
+    FP16 hi + lo tiles of row groups of 8 targets x K sources (K = n_p^2
+    rounded down to 16 when n_p^2 >= 16, else up to 8), then the remaining
+    source columns as FP32 couplings (rounded up to 16 bytes)."""
     mg = (np2 + 7) // 8
-    ka = (np2 + 7) // 8 * 8
-    return 2 * mg * 8 * ka * 2
+    if np2 >= 16:
+        km = np2 // 16 * 16
+        edge = ((np2 - km) * np2 * 4 + 15) // 16 * 16
+    else:
+        km, edge = (np2 + 7) // 8 * 8, 0
+    return 2 * mg * 8 * km * 2 + edge
 
 
 def far_algorithmic_bytes(np2):

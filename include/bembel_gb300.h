@@ -157,6 +157,13 @@ bg_status bg_operator_assemble(bg_operator* op);
  * integrating it again and assembles only the far field. A wavenumber
  * prepared twice keeps the later blocks. BG_UNSUPPORTED for other operators. */
 bg_status bg_operator_prepare_wavenumbers(bg_operator* op, const double* kre, const double* kim, int n);
+/* Near-field quadrature work of a scalar operator, the counts of the
+ * reference's rules (LinearOperatorBase.hpp:56-89, DuffyTrick/integrate0-4.hpp):
+ * counts8 = [regular pairs, their integrand evaluations (n+1)^4 each,
+ * identical pairs, evaluations 8 (n+1)^4 each, common-edge pairs, 6 (n+1)^4
+ * each, common-vertex pairs, 4 (n+1)^4 each]. No counterpart in the
+ * reference; host only, no device work. */
+bg_status bg_operator_quadrature_counts(const bg_operator* op, long* counts8);
 /* frees the near fields of bg_operator_prepare_wavenumbers */
 bg_status bg_operator_release_wavenumbers(bg_operator* op);
 bg_status bg_operator_destroy(bg_operator* op);
@@ -268,6 +275,14 @@ typedef struct bg_launch_plan {
    * SMs, else 1); 1 one persistent CTA of four shared-memory stages per SM;
    * 2 two CTAs of two stages per SM. Results are identical. */
   int far_ctas;
+  /* FP64-accurate near field of BG_PREC_MIXED products of real operators:
+   * 0 built-in (the tensor-core product on 8 integer digits of 7 bits per
+   * operand, exact integer accumulation, where the leaf block size allows
+   * it: 4, 16 or 36 rows; else 1); 1 double-float on the FP32 pipes; 2 the
+   * double-float product with a quarter of 32 columns on the FP64 pipe
+   * (32 columns only, else 1). All agree with the FP64 product to about
+   * 1e-14 relative or better. */
+  int mixed_near;
 } bg_launch_plan;
 
 typedef struct bg_tune_report {

@@ -67,6 +67,64 @@ def test_matvec_fp64_and_mixed(ctx, oracle, geo, M, P, kind, kappa, np_):
         assert np.linalg.norm(yf - ref) / np.linalg.norm(ref) < FP32_TOL
 
 
+@pytest.mark.parametrize("geo,P", [(SPHERE, 2), (TORUS, 1), (SPHERE, 0)])
+def test_mixed_near_field_digits_fp64_accurate(ctx, oracle, geo, P):
+    """The tensor-core near field of the mixed product (8 integer digits of 7
+    bits per operand, exact integer sums; leaf blocks of 36, 16 and 4 rows)
+    against the FP64 product on operators without far field (M = 1), where
+    the product is the near field alone: FP64 accuracy, within 5e-14 per
+    column of the FP64 product (whose own rounding is of that order, about
+    1e-14 measured), for 1, 32 and 45 columns (two passes of 32), with a zero column and
+    columns 1e-150 and 1e+150 times the others. The double-float near field
+    (launch plan mixed_near = 1, about 1e-13) is held to 1e-12 on the columns
+    FP32 pairs can represent."""
+    d, o = _pair(ctx, oracle, geo, 1, P, 0)
+    assert d.n_lowrank == 0
+    A = d.get_discrete_operator()
+    rng = np.random.default_rng(23)
+    for nrhs in (1, 32, 45):
+        x = rng.uniform(-1, 1, (d.N, nrhs))
+        if nrhs > 4:
+            x[:, 1] = 0.0
+            x[:, 2] *= 1e-150
+            x[:, 3] *= 1e150
+        ref = o.matvec(x)
+        y64 = A.matvec(x)
+        ymx = A.matvec(x, precision="mixed")
+        d.set_plan(nrhs, "mixed", mixed_near=1)
+        ydf = A.matvec(x, precision="mixed")
+        d.set_plan(nrhs, "mixed")
+        for c in range(nrhs):
+            n = np.linalg.norm(y64[:, c])
+            if n == 0.0:
+                assert not ymx[:, c].any() and not ydf[:, c].any()
+                continue
+            assert np.linalg.norm(ymx[:, c] - y64[:, c]) / n < 5e-14, (nrhs, c)
+            if nrhs <= 4 or c > 3:  # FP32 pairs cannot hold 1e+-150
+                assert np.linalg.norm(ydf[:, c] - y64[:, c]) / n < 1e-12, (nrhs, c)
+        assert np.linalg.norm(y64 - ref) / np.linalg.norm(ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("mixed_near", [0, 1, 2])
+def test_mixed_matvec_32_columns(ctx, oracle, mixed_near):
+    """32 columns with far field, every near-field variant of the mixed
+    product (tensor-core digits, double-float, double-float with a quarter of
+    the columns on the FP64 pipe): every column meets the FP32 bound, and the
+    variants differ only by the near field's rounding (the far field is the
+    same), far below it."""
+    d, o = _pair(ctx, oracle, SPHERE, 2, 2, 0, 0.0, 9)
+    x = np.random.default_rng(17).uniform(-1, 1, (d.N, 32))
+    ref = o.matvec(x)
+    A = d.get_discrete_operator()
+    y0 = A.matvec(x, precision="mixed")
+    d.set_plan(32, "mixed", mixed_near=mixed_near)
+    y = A.matvec(x, precision="mixed")
+    d.set_plan(32, "mixed")
+    err = np.max(np.linalg.norm(y - ref, axis=0) / np.linalg.norm(ref, axis=0))
+    assert err < FP32_TOL, err
+    assert np.max(np.linalg.norm(y - y0, axis=0) / np.linalg.norm(ref, axis=0)) < 1e-12
+
+
 def test_matvec_alpha_beta(ctx, oracle):
     d, o = _pair(ctx, oracle, SPHERE, 2, 1, 0)
     rng = np.random.default_rng(8)

@@ -179,14 +179,15 @@ def test_launch_plans_round_trip_and_validation(bg_host):
     from bembel_gb300 import BembelError, _lib
     bg, ctx = bg_host
     d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 2, 2), bg.LaplaceSingleLayerOperator())
-    builtin = {"near_kernel": 0, "split_k_batches": -1, "far_order": 0, "transforms": 0, "far_ctas": 0}
+    builtin = {"near_kernel": 0, "split_k_batches": -1, "far_order": 0, "transforms": 0, "far_ctas": 0,
+               "mixed_near": 0}
     assert d.get_plan(32, "mixed") == builtin
-    d.set_plan(32, "fp32", near_kernel=2, split_k_batches=608, far_order=2, transforms=1, far_ctas=2)
+    d.set_plan(32, "fp32", near_kernel=2, split_k_batches=608, far_order=2, transforms=1, far_ctas=2, mixed_near=2)
     assert d.get_plan(32, "fp32") == {"near_kernel": 2, "split_k_batches": 608, "far_order": 2, "transforms": 1,
-                                      "far_ctas": 2}
+                                      "far_ctas": 2, "mixed_near": 2}
     assert d.get_plan(32, "mixed") == builtin and d.get_plan(16, "fp32") == builtin
     for bad in ({"near_kernel": 4}, {"near_kernel": -1}, {"split_k_batches": -2}, {"far_order": 3}, {"transforms": 2},
-                {"transforms": -1}, {"far_ctas": 3}, {"far_ctas": -1}):
+                {"transforms": -1}, {"far_ctas": 3}, {"far_ctas": -1}, {"mixed_near": 3}, {"mixed_near": -1}):
         with pytest.raises(BembelError):
             d.set_plan(8, "mixed", **bad)
     with pytest.raises(BembelError):
@@ -282,3 +283,19 @@ def test_abi_entry_points_refuse_null_arguments(bg_host):
             assert st in statuses, (name, with_handles, st)
             if not with_handles:
                 assert st == _lib.BG_INVALID_ARG, name
+
+
+def test_quadrature_counts(bg_host):
+    """Near-field quadrature work on the host: every element pair of the dense
+    leaves is counted once, evaluations follow the reference's rules."""
+    bg, ctx = bg_host
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 2, 1), bg.LaplaceSingleLayerOperator())
+    info = d.info()
+    c = d.quadrature_counts()
+    pairs = sum(v["pairs"] for v in c.values())
+    assert pairs == int(info[3]) * int(info[11]) ** 2
+    assert c["identical"]["pairs"] == d.ne
+    for name, per in (("identical", 8), ("edge", 6), ("vertex", 4)):
+        if c[name]["pairs"]:
+            q4 = c[name]["evaluations"] // (per * c[name]["pairs"])
+            assert q4 * per * c[name]["pairs"] == c[name]["evaluations"] and round(q4 ** 0.25) ** 4 == q4
