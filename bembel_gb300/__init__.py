@@ -76,6 +76,19 @@ class Geometry:
         self.h = h
         self.filename = str(filename)
 
+    @classmethod
+    def cube_sphere(cls, context=None):
+        """The unit sphere as six analytic patches, each the image x/|x| of one
+        face of the cube [-1, 1]^3 (no control points; the reference's patches
+        are rational B-splines only, Patch.hpp:63-104)."""
+        self = cls.__new__(cls)
+        self.ctx = context or default_context()
+        h = ctypes.c_void_p()
+        self.ctx.check(_lib.load().bg_geometry_cube_sphere(self.ctx.h, ctypes.byref(h)))
+        self.h = h
+        self.filename = None
+        return self
+
     def surface_point(self, patch, s, t):
         out = np.zeros(12)
         self.ctx.check(_lib.load().bg_geometry_surface_point(self.h, patch, s, t, _dp(out)))

@@ -98,6 +98,7 @@ def load(build_if_missing=True):
         "bg_profile_classes": (I, [P, ctypes.c_uint]),
         "bg_geometry_load_dat": (I, [P, ctypes.c_char_p, PP]),
         "bg_geometry_load_igs": (I, [P, ctypes.c_char_p, PP]),
+        "bg_geometry_cube_sphere": (I, [P, PP]),
         "bg_geometry_destroy": (I, [P]),
         "bg_geometry_surface_point": (I, [P, I, D, D, dp]),
         "bg_operator_create": (I, [P, P, I, I, I, ctypes.POINTER(H2Params), PP]),

@@ -199,9 +199,21 @@ bg_status bg_geometry_from_bezier(bg_context* ctx, int npatch, const int* px, co
   *out = g;
   return BG_OK;
 }
+bg_status bg_geometry_cube_sphere(bg_context* ctx, bg_geometry** out) {
+  if (!ctx || !out || ctx->closing) return BG_INVALID_ARG;
+  *out = nullptr;
+  bg_geometry* g = new (std::nothrow) bg_geometry();
+  if (!g) return BG_OOM;
+  cube_sphere(&g->g);
+  g->ctx = ctx;
+  context_retain(ctx);
+  *out = g;
+  return BG_OK;
+}
 bg_status bg_geometry_patch_data(const bg_geometry* g, int patch, int* px, int* py, double* data) {
   if (!g || !px || !py || patch < 0 || patch >= (int)g->g.patches.size()) return BG_INVALID_ARG;
   const PatchData& P = g->g.patches[patch];
+  if (P.face >= 0) return BG_UNSUPPORTED;  // analytic patch: no control points
   *px = P.px;
   *py = P.py;
   if (data) std::copy(P.cp.begin(), P.cp.end(), data);
@@ -335,7 +347,9 @@ static bg_status upload_tables(bg_operator* op) {
   std::vector<int> meta;
   std::vector<double> cp;
   for (const auto& P : op->geo.patches) {
-    meta.insert(meta.end(), {P.px, P.py, (int)cp.size()});
+    // analytic cube-sphere face: px = 0 marks it, py holds the face
+    if (P.face >= 0) meta.insert(meta.end(), {0, P.face, 0});
+    else meta.insert(meta.end(), {P.px, P.py, (int)cp.size()});
     cp.insert(cp.end(), P.cp.begin(), P.cp.end());
     while (cp.size() % 4) cp.push_back(0.0);
   }

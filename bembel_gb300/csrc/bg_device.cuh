@@ -111,11 +111,39 @@ struct PatchTable {
   const double* cp;
 };
 
+// Analytic cube-sphere face f (meta px = 0, py = f): the unit-sphere image
+// c / |c| of c(s, t) = sg e_k + (2 s - 1) e_a + (2 t - 1) e_b, k = f / 2,
+// sg = +1 for even f (a, b = k + 1, k + 2 mod 3), -1 for odd f (a, b =
+// k + 2, k + 1 mod 3), so e_a x e_b points outwards;
+// dx/ds = 2 (e_a - x x_a) / |c|, dx/dt = 2 (e_b - x x_b) / |c|.
+__device__ inline void cube_face_frame(int f, double s, double t, double* x, double* dx, double* dy) {
+  const int k = f >> 1;
+  const bool pos = (f & 1) == 0;
+  const int a = pos ? (k + 1) % 3 : (k + 2) % 3, b = pos ? (k + 2) % 3 : (k + 1) % 3;
+  double c[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) c[j] = j == k ? (pos ? 1.0 : -1.0) : (j == a ? fma(2.0, s, -1.0) : fma(2.0, t, -1.0));
+  const double ir = rsqrt_nr(fma(c[0], c[0], fma(c[1], c[1], c[2] * c[2])));
+#pragma unroll
+  for (int j = 0; j < 3; ++j) x[j] = c[j] * ir;
+  const double xa = x[0] * (a == 0) + x[1] * (a == 1) + x[2] * (a == 2);
+  const double xb = x[0] * (b == 0) + x[1] * (b == 1) + x[2] * (b == 2);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dx[j] = 2.0 * ((j == a ? 1.0 : 0.0) - x[j] * xa) * ir;
+    dy[j] = 2.0 * ((j == b ? 1.0 : 0.0) - x[j] * xb) * ir;
+  }
+}
+
 // Surface point at patch coordinates (s, t): x, dx, dy (9 doubles)
 template <int G>
 __device__ inline void surface_frame(const PatchTable& pt, int patch, double s, double t, double* x, double* dx,
                                      double* dy) {
   const int px = __ldg(&pt.meta[3 * patch]), py = __ldg(&pt.meta[3 * patch + 1]);
+  if (px == 0) {
+    cube_face_frame(py, s, t, x, dx, dy);
+    return;
+  }
   const double* cp = pt.cp + __ldg(&pt.meta[3 * patch + 2]);
   double bs[G], dbs[G], bt[G], dbt[G];
   bern_der<G>(px - 1, s, bs, dbs);

@@ -233,12 +233,41 @@ static void patch_accumulate(const PatchData& P, double s, double t, double* h, 
       }
     }
 }
+void cube_face_frame(int face, double s, double t, double* out) {
+  const int k = face / 2;
+  const bool pos = face % 2 == 0;
+  const int a = pos ? (k + 1) % 3 : (k + 2) % 3, b = pos ? (k + 2) % 3 : (k + 1) % 3;
+  double c[3];
+  c[k] = pos ? 1.0 : -1.0;
+  c[a] = 2.0 * s - 1.0;
+  c[b] = 2.0 * t - 1.0;
+  const double ir = 1.0 / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  for (int j = 0; j < 3; ++j) out[j] = c[j] * ir;
+  for (int j = 0; j < 3; ++j) {
+    out[3 + j] = 2.0 * ((j == a ? 1.0 : 0.0) - out[j] * out[a]) * ir;
+    out[6 + j] = 2.0 * ((j == b ? 1.0 : 0.0) - out[j] * out[b]) * ir;
+  }
+}
+void cube_sphere(Geometry* g) {
+  g->patches.assign(6, PatchData());
+  for (int f = 0; f < 6; ++f) g->patches[f].face = f;
+}
 void patch_point(const PatchData& P, double s, double t, double* x3) {
+  if (P.face >= 0) {
+    double f[9];
+    cube_face_frame(P.face, s, t, f);
+    for (int k = 0; k < 3; ++k) x3[k] = f[k];
+    return;
+  }
   double h[4], hs[4], ht[4];
   patch_accumulate(P, s, t, h, hs, ht);
   for (int k = 0; k < 3; ++k) x3[k] = h[k] / h[3];
 }
 void patch_frame(const PatchData& P, double s, double t, double* out) {
+  if (P.face >= 0) {
+    cube_face_frame(P.face, s, t, out);
+    return;
+  }
   double h[4], hs[4], ht[4];
   patch_accumulate(P, s, t, h, hs, ht);
   double iw = 1.0 / h[3], iw2 = iw * iw;

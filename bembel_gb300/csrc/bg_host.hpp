@@ -17,9 +17,15 @@ constexpr double kPi = 3.14159265358979323846;
 // One rational Bezier patch in homogeneous coordinates:
 // cp[4 * (ix * py + iy) + k], k = x, y, z, w; px/py = number of control
 // points (degree + 1) per direction (Geometry/Patch.hpp:63-104).
+//
+// A patch with face >= 0 is instead the analytic cube-sphere map of face
+// `face` (no control points): the unit-sphere image x / |x| of one face of
+// the cube [-1, 1]^3 (see cube_face_frame). The reference's patches are all
+// rational B-splines (Patch.hpp:63-104); this kind is an addition.
 struct PatchData {
   int px = 0, py = 0;
   std::vector<double> cp;
+  int face = -1;
 };
 struct Geometry {
   std::vector<PatchData> patches;
@@ -39,6 +45,15 @@ void bernstein_der(int p, double x, double* b);  // derivative, p+1 values
 void patch_point(const PatchData& P, double s, double t, double* x3);
 // Patch::updateSurfacePoint (Patch.hpp:294-365): out[0..8] = x, dx, dy
 void patch_frame(const PatchData& P, double s, double t, double* out9);
+// The unit sphere as six analytic patches: face f lies on the cube plane
+// x_k = sg (k = f / 2, sg = +1 for even f, -1 for odd f) and is parametrised
+// by c(s, t) = sg e_k + (2 s - 1) e_a + (2 t - 1) e_b with (a, b) = (k + 1,
+// k + 2) mod 3 for sg = +1 and (k + 2, k + 1) mod 3 for sg = -1, so that
+// e_a x e_b is the outward normal; the surface point is c / |c|.
+void cube_sphere(Geometry* g);
+// x, dx/ds, dx/dt of face f at (s, t): x = c / |c|,
+// dx/ds = 2 (e_a - x x_a) / |c|, dx/dt = 2 (e_b - x x_b) / |c|.
+void cube_face_frame(int face, double s, double t, double* out9);
 
 // Gauss-Legendre rule with n points on [0,1], ascending nodes.
 struct Rule1D {

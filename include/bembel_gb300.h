@@ -117,6 +117,14 @@ bg_status bg_geometry_load_dat(bg_context* ctx, const char* path, bg_geometry** 
  * the rational B-spline surfaces (entity 128) of an IGES file; single-span
  * (Bezier) surfaces only, other entities and interior knots give BG_INVALID_ARG. */
 bg_status bg_geometry_load_igs(bg_context* ctx, const char* path, bg_geometry** out);
+/* The unit sphere as six analytic patches: patch f is the image x / |x| of
+ * one face of the cube [-1, 1]^3, parametrised over [0, 1]^2 with an outward
+ * normal (face f on the plane x_{f/2} = +1 for even f, -1 for odd f). No
+ * reference counterpart: Bembel's patches are rational B-splines only
+ * (Geometry/Patch.hpp:63-104); this kind stands beside them and is accepted
+ * wherever a geometry is. bg_geometry_patch_data returns BG_UNSUPPORTED for
+ * its patches (they have no control points). */
+bg_status bg_geometry_cube_sphere(bg_context* ctx, bg_geometry** out);
 bg_status bg_geometry_destroy(bg_geometry* g);
 /* Geometry(const PatchVector&) (Geometry/Geometry.hpp:60-63) from Bezier
  * patches already in memory, so an existing Bembel::Geometry can be handed

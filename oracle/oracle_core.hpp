@@ -181,12 +181,45 @@ struct SurfacePoint {
 
 // Patch in Bezier form (Geometry/Patch.hpp:63-104). Only single-Bezier
 // patches (knot vectors without interior knots) are supported here.
+//
+// face >= 0 marks an analytic cube-sphere patch instead (no reference
+// counterpart; the benchmark's sphere is defined this way): the unit-sphere
+// image c / |c| of c(s, t) = sg e_k + (2 s - 1) e_a + (2 t - 1) e_b on the
+// cube face x_k = sg, k = face / 2, sg = +1 for even faces with (a, b) =
+// (k + 1, k + 2) mod 3 and sg = -1 for odd faces with (a, b) = (k + 2, k + 1)
+// mod 3; its derivatives follow from d(c / |c|) = (I - u u^T) dc / |c|.
 struct Patch {
   std::vector<double> data;  // [(ix*py + iy)*4 + k], k in {x,y,z,w}
   int px = 0, py = 0;        // orders (degree + 1) in x and y
+  int face = -1;
+
+  void cube_face(double s, double t, V3* x, V3* ds, V3* dt) const {
+    const int k = face / 2;
+    const bool pos = face % 2 == 0;
+    const int a = pos ? (k + 1) % 3 : (k + 2) % 3, b = pos ? (k + 2) % 3 : (k + 1) % 3;
+    double c[3];
+    c[k] = pos ? 1.0 : -1.0;
+    c[a] = 2 * s - 1;
+    c[b] = 2 * t - 1;
+    const double ir = 1.0 / std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    double u[3], da[3], db[3];
+    for (int j = 0; j < 3; ++j) u[j] = c[j] * ir;
+    for (int j = 0; j < 3; ++j) {
+      da[j] = 2.0 * ((j == a ? 1.0 : 0.0) - u[j] * u[a]) * ir;
+      db[j] = 2.0 * ((j == b ? 1.0 : 0.0) - u[j] * u[b]) * ir;
+    }
+    *x = V3(u[0], u[1], u[2]);
+    *ds = V3(da[0], da[1], da[2]);
+    *dt = V3(db[0], db[1], db[2]);
+  }
 
   // Patch::eval (Patch.hpp:115-155)
   V3 eval(double s, double t) const {
+    if (face >= 0) {
+      V3 x, ds, dt;
+      cube_face(s, t, &x, &ds, &dt);
+      return x;
+    }
     double xb[32], yb[32];
     bernstein_basis(px - 1, s, xb);
     bernstein_basis(py - 1, t, yb);
@@ -209,6 +242,20 @@ struct Patch {
   // Patch::updateSurfacePoint (Patch.hpp:294-365)
   void update(SurfacePoint* sp, double s, double t, double w, double xi0,
               double xi1) const {
+    if (face >= 0) {
+      V3 x, ds, dt;
+      cube_face(s, t, &x, &ds, &dt);
+      sp->v[0] = xi0;
+      sp->v[1] = xi1;
+      sp->v[2] = w;
+      const V3* f[3] = {&x, &ds, &dt};
+      for (int r = 0; r < 3; ++r) {
+        sp->v[3 + 3 * r] = f[r]->x;
+        sp->v[4 + 3 * r] = f[r]->y;
+        sp->v[5 + 3 * r] = f[r]->z;
+      }
+      return;
+    }
     double xb[32], yb[32], xbd[32], ybd[32];
     bernstein_basis(px - 1, s, xb);
     bernstein_basis(py - 1, t, yb);
@@ -237,8 +284,17 @@ struct Patch {
   }
 };
 
+// The six analytic cube-sphere faces (see Patch::face).
+inline std::vector<Patch> cube_sphere() {
+  std::vector<Patch> out(6);
+  for (int f = 0; f < 6; ++f) out[f].face = f;
+  return out;
+}
+
 // LoadGeometryFileDAT (Geometry/GeometryIO.hpp:25-122): Octave NURBS text.
+// The name "analytic:cube_sphere" selects the analytic cube sphere instead.
 inline std::vector<Patch> load_dat(const std::string& path) {
+  if (path == "analytic:cube_sphere") return cube_sphere();
   std::ifstream f(path);
   if (!f) throw std::runtime_error("cannot open geometry file " + path);
   std::string row;

@@ -9,6 +9,15 @@ if ROOT not in sys.path:
 GEO = os.path.join(ROOT, "tests", "golden", "geo")
 SPHERE = os.path.join(GEO, "sphere.dat")
 TORUS = os.path.join(GEO, "torus.dat")
+# The analytic cube sphere (six x/|x| images of the cube faces): the product
+# builds it with Geometry.cube_sphere(), the oracle under this name.
+CUBE = "analytic:cube_sphere"
+
+
+def geometry(bg, geo, ctx):
+    """The product's geometry for a test geometry name or file."""
+    return bg.Geometry.cube_sphere(ctx) if geo == CUBE else bg.Geometry(geo, ctx)
+
 
 # The unit-square screen of the reference's unit tests (z = 0, bilinear map).
 SCREEN_DAT = """# nurbs mesh v.2.1

@@ -6,7 +6,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT, SPHERE, TORUS
+from conftest import CUBE, ROOT, SPHERE, TORUS, geometry
 
 
 @pytest.fixture(scope="module")
@@ -27,10 +27,11 @@ def test_library_exports_every_declared_symbol():
     assert not missing
 
 
-@pytest.mark.parametrize("geo,M,P", [(SPHERE, 3, 1), (SPHERE, 2, 2), (TORUS, 2, 2), (SPHERE, 1, 0), (SPHERE, 0, 1)])
+@pytest.mark.parametrize("geo,M,P", [(SPHERE, 3, 1), (SPHERE, 2, 2), (TORUS, 2, 2), (SPHERE, 1, 0), (SPHERE, 0, 1),
+                                     (CUBE, 3, 1), (CUBE, 2, 2)])
 def test_tables_match_oracle(bg_host, oracle, geo, M, P):
     bg, ctx = bg_host
-    g = bg.Geometry(geo, ctx)
+    g = geometry(bg, geo, ctx)
     d = bg.DiscreteOperator(bg.AnsatzSpace(g, M, P), bg.LaplaceSingleLayerOperator(), n_p=6)
     o = oracle.Problem(geo, M, P, oracle.LAPLACE, np_=6, assemble=False)
     assert (d.N, d.S, d.n_dense, d.n_lowrank) == (o.N, o.S, o.n_dense, o.n_lowrank)
@@ -53,7 +54,8 @@ def test_tables_match_oracle(bg_host, oracle, geo, M, P):
     assert np.abs(a[2] - b[2]).max() < 1e-13
 
 
-@pytest.mark.parametrize("geo,M,P", [(SPHERE, 1, 1), (SPHERE, 2, 2), (TORUS, 1, 3), ("screen", 1, 2), ("screen", 2, 1)])
+@pytest.mark.parametrize("geo,M,P", [(SPHERE, 1, 1), (SPHERE, 2, 2), (TORUS, 1, 3), ("screen", 1, 2), ("screen", 2, 1),
+                                     (CUBE, 2, 2)])
 def test_divconforming_transform_matches_oracle(bg_host, oracle, screen_path, geo, M, P):
     """Maxwell's T = Projector * Glue (div-conforming gluing across patch
     edges, boundary functions of an open surface dropped), against the oracle."""
@@ -61,7 +63,7 @@ def test_divconforming_transform_matches_oracle(bg_host, oracle, screen_path, ge
     geo = screen_path if geo == "screen" else geo
     lin = bg.MaxwellSingleLayerOperator()
     lin.set_wavenumber(1.0)
-    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(geo, ctx), M, P), lin, n_p=4)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(geometry(bg, geo, ctx), M, P), lin, n_p=4)
     o = oracle.Problem(geo, M, P, oracle.MAXWELL, kappa=1.0, np_=4, assemble=False)
     assert (d.N, d.S) == (o.N, o.S)
     a, b = d.transform_csr(), o.transform_csr()
@@ -299,3 +301,46 @@ def test_quadrature_counts(bg_host):
         if c[name]["pairs"]:
             q4 = c[name]["evaluations"] // (per * c[name]["pairs"])
             assert q4 * per * c[name]["pairs"] == c[name]["evaluations"] and round(q4 ** 0.25) ** 4 == q4
+
+
+def test_cube_sphere_patches(bg_host, oracle):
+    """The analytic cube sphere: points on the unit sphere, derivatives equal
+    to central differences, outward normals, surface area 4 pi by Gauss
+    quadrature, faces meeting along the cube edges, and the same frames as the
+    oracle's restatement."""
+    bg, ctx = bg_host
+    g = bg.Geometry.cube_sphere(ctx)
+    o = oracle.Problem(CUBE, 0, 0, oracle.LAPLACE, np_=6, assemble=False)
+    rng = np.random.default_rng(11)
+    h = 1e-6
+    for _ in range(60):
+        p, s, t = int(rng.integers(6)), rng.uniform(0.01, 0.99), rng.uniform(0.01, 0.99)
+        f = g.surface_point(p, s, t)
+        x, dx, dy = f[3:6], f[6:9], f[9:12]
+        assert abs(np.linalg.norm(x) - 1.0) < 1e-15
+        fd_s = (g.surface_point(p, s + h, t)[3:6] - g.surface_point(p, s - h, t)[3:6]) / (2 * h)
+        fd_t = (g.surface_point(p, s, t + h)[3:6] - g.surface_point(p, s, t - h)[3:6]) / (2 * h)
+        assert np.abs(fd_s - dx).max() < 1e-8 and np.abs(fd_t - dy).max() < 1e-8
+        assert np.dot(np.cross(dx, dy), x) > 0
+        assert np.abs(f[3:] - o.surface_point(p, s, t)[3:]).max() < 1e-15
+    xg, wg = np.polynomial.legendre.leggauss(24)
+    xg, wg = (xg + 1) / 2, wg / 2
+    area = 0.0
+    for p in range(6):
+        for s, ws in zip(xg, wg):
+            for t, wt in zip(xg, wg):
+                f = g.surface_point(p, s, t)
+                area += ws * wt * np.linalg.norm(np.cross(f[6:9], f[9:12]))
+    assert abs(area - 4 * np.pi) < 1e-9
+    # every patch corner is a cube corner direction, shared by three faces
+    corners = {}
+    for p in range(6):
+        for s, t in ((0, 0), (1, 0), (1, 1), (0, 1)):
+            key = tuple(np.round(g.surface_point(p, s, t)[3:6] * np.sqrt(3), 12))
+            corners[key] = corners.get(key, 0) + 1
+    assert len(corners) == 8 and set(corners.values()) == {3}
+    # analytic patches have no control points to hand out
+    import ctypes
+    px, py = ctypes.c_int(), ctypes.c_int()
+    st = bg._lib.load().bg_geometry_patch_data(g.h, 0, ctypes.byref(px), ctypes.byref(py), None)
+    assert st == bg._lib.BG_UNSUPPORTED
