@@ -365,10 +365,307 @@ __global__ void __launch_bounds__(128) k_near_duffy(PatchTable pt, ElementTable 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Common-edge and common-vertex pairs with the inner sum factorised (one
+// wavenumber per launch, P <= 2, n1 <= 16).
+//
+// Common edge (integrate3.hpp:45-76): with outer node (x0, x1) and inner
+// node (e0, e1), every one of the six point pairs has one point that does not
+// depend on e1: sub-rules 0-3 the point on the first element, ((1 -) x0 (1 -
+// x1), x1 e0) and ((1 -) x0 (1 - x1 e0), x1), sub-rules 4, 5 the point on the
+// second, ((1 -) x0 (1 - x1 e0), x1). So each sub-rule's contribution is
+//   sum_e0 phi(fixed(e0)) (x) [sum_e1 c(e0, e1) phi(varying(e0, e1))],
+// a rank-one update per (outer node, e0, sub-rule) instead of one per sample:
+// one fixed point evaluation and one basis outer product per n1 samples. In
+// sub-rules 0, 1 the varying point depends on e1 alone and is evaluated once
+// per outer node (a per-warp cache). The weights are split the same way: the
+// fixed point carries the outer weight, the e0 weight and the (1 - x1) or
+// (1 - x1 e0) factor, the varying point the e1 weight.
+// Common vertex (integrate4.hpp:49-58): the four pairs are (qp1, qp5), (qp2,
+// qp5), (qp6, qp3), (qp6, qp4), where qp1-qp4 depend on the outer node only;
+// so sum_j c_k(j) phi(qp5 or qp6 at j) is accumulated per lane over all inner
+// nodes and each outer node ends with four rank-one updates.
+// The sums are the reference's in another order: leaf blocks agree with the
+// per-sample kernel to rounding.
+constexpr int kEdgeNW = 4;
+
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline cd warp_sum(cd v) { return {warp_sum(v.re), warp_sum(v.im)}; }
+
+template <int P, typename S>
+struct RankOneStage {
+  static constexpr int P2 = (P + 1) * (P + 1);
+  double f[kEdgeNW][32 * P2];  // basis values of the fixed point per lane
+  S v[kEdgeNW][32 * P2];       // inner sums per lane
+  int o[kEdgeNW][32];          // 0: fixed point on the first element (rows), 1: on the second (columns)
+};
+
+// acc(a, b) += f_s(a) v_s(b) (o = 0) or v_s(a) f_s(b) (o = 1) for the 32
+// staged lanes s of this warp; the p^2 x p^2 block is distributed over the
+// lanes, entry lane + 32 m.
+template <int P, typename S, int PER>
+__device__ inline void add_rank_one(S* acc, const RankOneStage<P, S>& st, int warp, int lane) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  constexpr int NE = P2 * P2;
+  for (int s = 0; s < 32; ++s) {
+    const int o = st.o[warp][s];
+    const double* f = &st.f[warp][s * P2];
+    const S* v = &st.v[warp][s * P2];
+#pragma unroll
+    for (int m = 0; m < PER; ++m) {
+      const int e = lane + 32 * m;
+      if (e < NE) {
+        const int a = e % P2, b = e / P2;
+        acc[m] = o ? fmac(acc[m], v[a], f[b]) : fmac(acc[m], v[b], f[a]);
+      }
+    }
+  }
+}
+
+template <int P, typename S>
+__device__ inline void stage_rank_one(RankOneStage<P, S>& st, int warp, int lane, bool act, int o, const double* f,
+                                      const S* v) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  st.o[warp][lane] = act ? o : 0;
+#pragma unroll
+  for (int t = 0; t < P2; ++t) {
+    st.f[warp][lane * P2 + t] = act ? f[t] : 0.0;
+    st.v[warp][lane * P2 + t] = act ? v[t] : zero<S>();
+  }
+}
+
+// sum the warps' accumulators (staging memory reused) and write the block
+template <int P, typename S, int PER>
+__device__ inline void write_block(S* acc, RankOneStage<P, S>& st, int warp, int lane, S* out, long long dst, int B) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  constexpr int NE = P2 * P2;
+  static_assert(NE <= 32 * P2, "reduction buffer too small");
+  S* red = &st.v[0][0];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < PER; ++m) {
+    const int e = lane + 32 * m;
+    if (e < NE) red[warp * 32 * P2 + e] = acc[m];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    S v = red[e];
+#pragma unroll
+    for (int w2 = 1; w2 < kEdgeNW; ++w2) v = v + red[w2 * 32 * P2 + e];
+    out[dst + (long)(e / P2) * B + e % P2] = v;
+  }
+}
+
+template <int G, int P, typename S>
+__global__ void __launch_bounds__(128) k_near_edge(PatchTable pt, ElementTable et, const NearPair* __restrict__ pairs,
+                                                   const double* __restrict__ gx, const double* __restrict__ gw,
+                                                   int n1, double kre, double kim, S* __restrict__ out, int B) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  constexpr int NE = P2 * P2;
+  constexpr int PER = (NE + 31) / 32;
+  __shared__ RankOneStage<P, S> st;
+  __shared__ PointEval cpt[kEdgeNW][32];  // sub-rules 0, 1: the e1-only points on the second element
+  __shared__ double cphi[kEdgeNW][32 * P2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const NearPair pr = pairs[blockIdx.x];
+  const int rot1 = pr.rot & 15, rot2 = pr.rot >> 4;
+  const int p1 = et.patch[pr.e1], p2 = et.patch[pr.e2];
+  const double a0 = et.llc[2 * pr.e1], a1 = et.llc[2 * pr.e1 + 1];
+  const double b0 = et.llc[2 * pr.e2], b1 = et.llc[2 * pr.e2 + 1];
+  const double h = et.h;
+  const int Q = n1 * n1;
+  S acc[PER];
+#pragma unroll
+  for (int m = 0; m < PER; ++m) acc[m] = zero<S>();
+  // sub-rules 0, 1: a warp per outer node; lane = (sub-rule, e0 node) for the
+  // fixed point, cache lane = (sub-rule, e1 node) for the varying one
+  for (int i = warp; i < Q; i += kEdgeNW) {
+    const double x0 = gx[i / n1], x1 = gx[i % n1], wi = gw[i / n1] * gw[i % n1];
+    const double w = h * h * wi * x1 * x1;
+    const double t1 = x0 * (1 - x1), t2 = (1 - x0) * (1 - x1);
+    const bool act = lane < 2 * n1;
+    const int k = act ? lane / n1 : 0, m0 = act ? lane % n1 : 0;
+    double uv[2];
+    if (act) {
+      tau(k ? 1 - t2 : t2, x1 * gx[m0], rot2, uv);
+      eval_point<G, P>(pt, p2, b0, b1, h, uv[0], uv[1], gw[m0], &cpt[warp][lane], &cphi[warp][lane * P2]);
+    }
+    __syncwarp();
+    tau(k ? 1 - t1 : t1, x1 * gx[m0], rot1, uv);
+    PointEval F;
+    double phF[P2];
+    eval_point<G, P>(pt, p1, a0, a1, h, uv[0], uv[1], w * gw[m0] * (1 - x1), &F, phF);
+    S v[P2];
+#pragma unroll
+    for (int t = 0; t < P2; ++t) v[t] = zero<S>();
+    if (act) {
+      for (int m = 0; m < n1; ++m) {
+        const PointEval& V = cpt[warp][k * n1 + m];
+        const double d0 = F.x[0] - V.x[0], d1 = F.x[1] - V.x[1], d2 = F.x[2] - V.x[2];
+        const S c = scale_of(kernel_val<S>(fma(d0, d0, fma(d1, d1, d2 * d2)), kre, kim), F.c * V.c);
+        const double* ph = &cphi[warp][(k * n1 + m) * P2];
+#pragma unroll
+        for (int t = 0; t < P2; ++t) v[t] = fmac(v[t], c, ph[t]);
+      }
+    }
+    stage_rank_one<P, S>(st, warp, lane, act, 0, phF, v);
+    __syncwarp();
+    add_rank_one<P, S, PER>(acc, st, warp, lane);
+    __syncwarp();
+  }
+  // sub-rules 2-5: units (outer node, e0 node, sub-rule) over all threads
+  const int U = Q * n1 * 4;
+  for (int base = 0; base < U; base += blockDim.x) {
+    const int u = base + threadIdx.x;
+    const bool act = u < U;
+    const int uu = act ? u : 0;
+    const int i = uu / (4 * n1), rem = uu % (4 * n1), m0 = rem >> 2, k = (rem & 3) + 2;
+    const double x0 = gx[i / n1], x1 = gx[i % n1], wi = gw[i / n1] * gw[i % n1];
+    const double w = h * h * wi * x1 * x1;
+    const double f0 = x1 * gx[m0];
+    const double t3 = x0 * (1 - f0), t4 = (1 - x0) * (1 - f0);
+    // sub-rules 2, 3: fixed on the first element at ((1 -) t3, x1), varying on
+    // the second at ((1 -) t4, x1 e1); sub-rules 4, 5: the other way round
+    const bool flip = k & 1, onA = k < 4;
+    const int pf = onA ? p1 : p2, pv = onA ? p2 : p1, rf = onA ? rot1 : rot2, rv = onA ? rot2 : rot1;
+    const double lf0 = onA ? a0 : b0, lf1 = onA ? a1 : b1, lv0 = onA ? b0 : a0, lv1 = onA ? b1 : a1;
+    const double vt = flip ? 1 - t4 : t4;
+    double uv[2];
+    tau(flip ? 1 - t3 : t3, x1, rf, uv);
+    PointEval F;
+    double phF[P2];
+    eval_point<G, P>(pt, pf, lf0, lf1, h, uv[0], uv[1], w * gw[m0] * (1 - f0), &F, phF);
+    S v[P2];
+#pragma unroll
+    for (int t = 0; t < P2; ++t) v[t] = zero<S>();
+    for (int m = 0; m < n1; ++m) {
+      tau(vt, x1 * gx[m], rv, uv);
+      PointEval V;
+      double phV[P2];
+      eval_point<G, P>(pt, pv, lv0, lv1, h, uv[0], uv[1], gw[m], &V, phV);
+      const double d0 = F.x[0] - V.x[0], d1 = F.x[1] - V.x[1], d2 = F.x[2] - V.x[2];
+      const S c = scale_of(kernel_val<S>(fma(d0, d0, fma(d1, d1, d2 * d2)), kre, kim), F.c * V.c);
+#pragma unroll
+      for (int t = 0; t < P2; ++t) v[t] = fmac(v[t], c, phV[t]);
+    }
+    stage_rank_one<P, S>(st, warp, lane, act, onA ? 0 : 1, phF, v);
+    __syncwarp();
+    add_rank_one<P, S, PER>(acc, st, warp, lane);
+    __syncwarp();
+  }
+  write_block<P, S, PER>(acc, st, warp, lane, out, pr.dst, B);
+}
+
+template <int G, int P, typename S>
+__global__ void __launch_bounds__(128) k_near_vertex(PatchTable pt, ElementTable et, const NearPair* __restrict__ pairs,
+                                                     const double* __restrict__ gx, const double* __restrict__ gw,
+                                                     int n1, double kre, double kim, S* __restrict__ out, int B) {
+  constexpr int P2 = (P + 1) * (P + 1);
+  constexpr int NE = P2 * P2;
+  constexpr int PER = (NE + 31) / 32;
+  __shared__ RankOneStage<P, S> st;  // only st.v (inner sums of the 4 pairs) and the final reduction
+  __shared__ PointEval vp[kEdgeNW][4];
+  __shared__ double vphi[kEdgeNW][4 * P2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const NearPair pr = pairs[blockIdx.x];
+  const int rot1 = pr.rot & 15, rot2 = pr.rot >> 4;
+  const int p1 = et.patch[pr.e1], p2 = et.patch[pr.e2];
+  const double a0 = et.llc[2 * pr.e1], a1 = et.llc[2 * pr.e1 + 1];
+  const double b0 = et.llc[2 * pr.e2], b1 = et.llc[2 * pr.e2 + 1];
+  const double h = et.h;
+  const int Q = n1 * n1;
+  S acc[PER];
+#pragma unroll
+  for (int m = 0; m < PER; ++m) acc[m] = zero<S>();
+  S* sv = &st.v[warp][0];
+  for (int i = warp; i < Q; i += kEdgeNW) {
+    const double x0 = gx[i / n1], x1 = gx[i % n1], wi = gw[i / n1] * gw[i % n1];
+    const double w = h * h * wi * (x0 * x0 * x0);
+    const double y1 = x1 * x0;
+    if (lane < 4) {
+      double uv[2];
+      const int r = (lane < 2) ? rot1 : rot2;
+      if (lane == 0 || lane == 2) tau(x0, y1, r, uv); else tau(y1, x0, r, uv);
+      if (lane < 2) eval_point<G, P>(pt, p1, a0, a1, h, uv[0], uv[1], w, &vp[warp][lane], &vphi[warp][lane * P2]);
+      else eval_point<G, P>(pt, p2, b0, b1, h, uv[0], uv[1], w, &vp[warp][lane], &vphi[warp][lane * P2]);
+    }
+    __syncwarp();
+    // pass 0: qp5 (second element) against qp1, qp2; pass 1: qp6 (first
+    // element) against qp3, qp4 -- every inner point is evaluated once
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+      S v[2][P2];
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int t = 0; t < P2; ++t) v[k][t] = zero<S>();
+      for (int jj = 0; jj < Q; jj += 32) {
+        const int j = jj + lane;
+        const bool valid = j < Q;
+        const double e0 = valid ? gx[j / n1] : 0.5, e1 = valid ? gx[j % n1] : 0.5;
+        const double wj = valid ? gw[j / n1] * gw[j % n1] : 0.0;
+        double uv[2];
+        PointEval q;
+        double phq[P2];
+        tau(x0 * e0, x0 * e1, pass ? rot1 : rot2, uv);
+        eval_point<G, P>(pt, pass ? p1 : p2, pass ? a0 : b0, pass ? a1 : b1, h, uv[0], uv[1], wj, &q, phq);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const PointEval& Fk = vp[warp][2 * pass + k];
+          const double d0 = Fk.x[0] - q.x[0], d1 = Fk.x[1] - q.x[1], d2 = Fk.x[2] - q.x[2];
+          S c = scale_of(kernel_val<S>(fma(d0, d0, fma(d1, d1, d2 * d2)), kre, kim), Fk.c * q.c);
+          if (!valid) c = zero<S>();
+#pragma unroll
+          for (int t = 0; t < P2; ++t) v[k][t] = fmac(v[k][t], c, phq[t]);
+        }
+      }
+      // sum the lanes' inner sums (every lane ends with the totals)
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int t = 0; t < P2; ++t) v[k][t] = warp_sum(v[k][t]);
+#pragma unroll
+      for (int q = 0; q < 2 * P2; ++q)
+        if ((q & 31) == lane) sv[2 * pass * P2 + q] = v[q / P2][q % P2];
+    }
+    __syncwarp();
+    // pairs 0, 1: fixed point on the first element; 2, 3: on the second
+#pragma unroll
+    for (int m = 0; m < PER; ++m) {
+      const int e = lane + 32 * m;
+      if (e < NE) {
+        const int a = e % P2, b = e / P2;
+        const double* f = vphi[warp];
+        acc[m] = fmac(acc[m], sv[b], f[a]);
+        acc[m] = fmac(acc[m], sv[P2 + b], f[P2 + a]);
+        acc[m] = fmac(acc[m], sv[2 * P2 + a], f[2 * P2 + b]);
+        acc[m] = fmac(acc[m], sv[3 * P2 + a], f[3 * P2 + b]);
+      }
+    }
+    __syncwarp();
+  }
+  write_block<P, S, PER>(acc, st, warp, lane, out, pr.dst, B);
+}
+
 template <int G, int P, typename S, int NK>
 static cudaError_t run_duffy_k(int cs, const PatchTable& pt, const ElementTable& et, const NearPair* pairs,
                                int npairs, const double* gx, const double* gw, int n1, const KBatch<S, NK>& kb, int B,
                                cudaStream_t s) {
+  if constexpr (NK == 1 && P <= 2) {
+    // factorised common-edge / common-vertex kernels (cache of 2 n1 points per warp)
+    if (cs == 3 && 2 * n1 <= 32) {
+      k_near_edge<G, P, S><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb.kre[0], kb.kim[0], kb.out[0], B);
+      return cudaGetLastError();
+    }
+    if (cs == 4) {
+      k_near_vertex<G, P, S><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb.kre[0], kb.kim[0], kb.out[0], B);
+      return cudaGetLastError();
+    }
+  }
   if (cs == 2) k_near_duffy<G, P, S, 2, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);
   else if (cs == 3) k_near_duffy<G, P, S, 3, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);
   else if (cs == 4) k_near_duffy<G, P, S, 4, NK><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb, B);

@@ -5,7 +5,9 @@ Five wavenumbers are prepared together (one launch of 4 and one of 1 per
 Duffy rule). For two of them the operator is then assembled with the
 prepared near field, and its leaf blocks and products are compared with an
 operator assembled for that wavenumber alone: the batched kernels evaluate
-the same samples in the same order, so the blocks agree to 1e-14 relative.
+the same samples, in the same order for regular and identical pairs and in
+another (the single-wavenumber kernels factorise the common-edge and
+common-vertex rules' inner sums), so the blocks agree to 1e-13 relative.
 One wavenumber is also checked against the oracle (1e-12, the bound of the
 other leaf-block tests).
 """
@@ -17,7 +19,7 @@ from conftest import SPHERE, TORUS
 pytestmark = pytest.mark.gpu
 
 KAPPAS = [0.7, 2.0, 3.5, 5.1, 6.0]
-SAME_TOL = 1e-14
+SAME_TOL = 1e-13
 FP64_TOL = 1e-12
 
 
