@@ -182,6 +182,88 @@ __device__ inline void surface_frame(const PatchTable& pt, int patch, double s, 
   }
 }
 
+// Surface points along a line of one fixed patch coordinate: the control
+// points are contracted along the fixed direction once (values with the
+// Bernstein basis and its derivative there), so every point of the line
+// costs one G-term contraction instead of G^2 (the sums of
+// Patch::updateSurfacePoint, Patch.hpp:294-365, associated the other way).
+// Analytic patches keep the fixed coordinate and evaluate in closed form.
+template <int G>
+struct SurfaceLine {
+  double q[G][4], qd[G][4];  // q_m = sum_n B_n(fixed) P, qd_m = sum_n B'_n(fixed) P
+  double c;                  // the fixed coordinate
+  int n, face;               // terms along the free direction; n = 0: analytic face
+  bool fix_s;
+};
+
+template <int G>
+__device__ inline void surface_line(const PatchTable& pt, int patch, bool fix_s, double c, SurfaceLine<G>& L) {
+  const int px = __ldg(&pt.meta[3 * patch]), py = __ldg(&pt.meta[3 * patch + 1]);
+  L.fix_s = fix_s;
+  L.c = c;
+  if (px == 0) {
+    L.n = 0;
+    L.face = py;
+    return;
+  }
+  const double* cp = pt.cp + __ldg(&pt.meta[3 * patch + 2]);
+  const int nf = fix_s ? px : py;
+  L.n = fix_s ? py : px;
+  double b[G], db[G];
+  bern_der<G>(nf - 1, c, b, db);
+#pragma unroll
+  for (int m = 0; m < G; ++m) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L.q[m][k] = L.qd[m][k] = 0.0;
+    if (m < L.n) {
+#pragma unroll
+      for (int n = 0; n < G; ++n) {
+        if (n < nf) {
+          const d4 P = *reinterpret_cast<const d4*>(cp + 4 * (fix_s ? n * py + m : m * py + n));
+          L.q[m][0] = fma(P.x, b[n], L.q[m][0]); L.q[m][1] = fma(P.y, b[n], L.q[m][1]);
+          L.q[m][2] = fma(P.z, b[n], L.q[m][2]); L.q[m][3] = fma(P.w, b[n], L.q[m][3]);
+          L.qd[m][0] = fma(P.x, db[n], L.qd[m][0]); L.qd[m][1] = fma(P.y, db[n], L.qd[m][1]);
+          L.qd[m][2] = fma(P.z, db[n], L.qd[m][2]); L.qd[m][3] = fma(P.w, db[n], L.qd[m][3]);
+        }
+      }
+    }
+  }
+}
+
+// x, dx/ds, dx/dt at the free coordinate v of the line
+template <int G>
+__device__ inline void surface_line_point(const SurfaceLine<G>& L, double v, double* x, double* dx, double* dy) {
+  if (L.n == 0) {
+    if (L.fix_s) cube_face_frame(L.face, L.c, v, x, dx, dy);
+    else cube_face_frame(L.face, v, L.c, x, dx, dy);
+    return;
+  }
+  double b[G], db[G];
+  bern_der<G>(L.n - 1, v, b, db);
+  double h[4] = {0, 0, 0, 0}, hf[4] = {0, 0, 0, 0}, hv[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int m = 0; m < G; ++m) {
+    if (m < L.n) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        h[k] = fma(b[m], L.q[m][k], h[k]);
+        hf[k] = fma(b[m], L.qd[m][k], hf[k]);
+        hv[k] = fma(db[m], L.q[m][k], hv[k]);
+      }
+    }
+  }
+  const double iw = rcp_nr(h[3]);
+  const double iw2 = iw * iw;
+  const double hs3 = L.fix_s ? hf[3] : hv[3], ht3 = L.fix_s ? hv[3] : hf[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double hsk = L.fix_s ? hf[k] : hv[k], htk = L.fix_s ? hv[k] : hf[k];
+    x[k] = h[k] * iw;
+    dx[k] = (hsk * h[3] - h[k] * hs3) * iw2;
+    dy[k] = (htk * h[3] - h[k] * ht3) * iw2;
+  }
+}
+
 // surface measure |dx x dy|
 __device__ inline double surface_measure(const double* dx, const double* dy) {
   double n0 = dx[1] * dy[2] - dx[2] * dy[1];

@@ -539,6 +539,12 @@ __global__ void __launch_bounds__(128) k_near_edge(PatchTable pt, ElementTable e
     PointEval F;
     double phF[P2];
     eval_point<G, P>(pt, pf, lf0, lf1, h, uv[0], uv[1], w * gw[m0] * (1 - f0), &F, phF);
+    // the varying points (vt, x1 e1) lie on one line of the patch: rotations
+    // 1 and 3 fix the patch's t, the others its s
+    const bool fs = !(rv == 1 || rv == 3);
+    tau(vt, 0.0, rv, uv);
+    SurfaceLine<G> line;
+    surface_line<G>(pt, pv, fs, fs ? lv0 + h * uv[0] : lv1 + h * uv[1], line);
     S v[P2];
 #pragma unroll
     for (int t = 0; t < P2; ++t) v[t] = zero<S>();
@@ -546,7 +552,12 @@ __global__ void __launch_bounds__(128) k_near_edge(PatchTable pt, ElementTable e
       tau(vt, x1 * gx[m], rv, uv);
       PointEval V;
       double phV[P2];
-      eval_point<G, P>(pt, pv, lv0, lv1, h, uv[0], uv[1], gw[m], &V, phV);
+      {
+        double dx[3], dy[3];
+        surface_line_point<G>(line, fs ? lv1 + h * uv[1] : lv0 + h * uv[0], V.x, dx, dy);
+        V.c = gw[m] * surface_measure(dx, dy);
+        tensor_basis<P>(uv[0], uv[1], phV);
+      }
       const double d0 = F.x[0] - V.x[0], d1 = F.x[1] - V.x[1], d2 = F.x[2] - V.x[2];
       const S c = scale_of(kernel_val<S>(fma(d0, d0, fma(d1, d1, d2 * d2)), kre, kim), F.c * V.c);
 #pragma unroll
