@@ -31,11 +31,21 @@ __device__ inline double addv(double a, double b) { return a + b; }
 __device__ inline cd addv(cd a, cd b) { return a + b; }
 
 // out[i][c] = sum_n conj(V[i][n][c]) w[n][c] for i < nv (one CTA per i)
+// (any k: with more columns than threads each thread sums whole columns)
 template <typename S>
 __global__ void k_mdot(const S* __restrict__ V, long vstride, const S* __restrict__ w, int N, int k, S* __restrict__ out) {
   __shared__ S red[256];
   const int i = blockIdx.x;
   const int kp = k;  // columns
+  if (kp > (int)blockDim.x) {
+    const S* v = V + (long)i * vstride;
+    for (int c = threadIdx.x; c < kp; c += blockDim.x) {
+      S acc = zero<S>();
+      for (int n = 0; n < N; ++n) acc = addv(acc, conj_mul(v[(long)n * k + c], w[(long)n * k + c]));
+      out[(long)i * k + c] = acc;
+    }
+    return;
+  }
   const int groups = blockDim.x / kp;
   const int c = threadIdx.x % kp, g = threadIdx.x / kp;
   S acc = zero<S>();
@@ -59,9 +69,18 @@ __global__ void k_mdot_part(const S* __restrict__ V, long vstride, const S* __re
                             S* __restrict__ part) {
   __shared__ S red[256];
   const int i = blockIdx.x, ch = blockIdx.y, nch = gridDim.y;
+  const int n0 = ch * rows_per, n1 = min(N, n0 + rows_per);
+  if (k > (int)blockDim.x) {  // more columns than threads: each thread sums whole columns of the chunk
+    const S* v = V + (long)i * vstride;
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+      S acc = zero<S>();
+      for (int n = n0; n < n1; ++n) acc = addv(acc, conj_mul(v[(long)n * k + c], w[(long)n * k + c]));
+      part[((long)i * nch + ch) * k + c] = acc;
+    }
+    return;
+  }
   const int groups = blockDim.x / k;
   const int c = threadIdx.x % k, g = threadIdx.x / k;
-  const int n0 = ch * rows_per, n1 = min(N, n0 + rows_per);
   S acc = zero<S>();
   if (g < groups) {
     const S* v = V + (long)i * vstride;
@@ -298,6 +317,14 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
     std::fill(Hm.begin(), Hm.end(), H(0));
     std::fill(g.begin(), g.end(), H(0));
     for (int c = 0; c < k; ++c) g[c] = beta[c];
+    // step count at which each column met the tolerance in this cycle (-1:
+    // not yet): its update uses those steps only, so that columns that
+    // converge early are not iterated further on a basis that keeps growing
+    // for the others (with one Gram-Schmidt pass and a low-precision operator
+    // that extra iteration spoils their directions)
+    std::vector<int> jconv(k, -1);
+    for (int c = 0; c < k; ++c)
+      if (!(beta[c] > tol * bn[c] && bn[c] > 0)) jconv[c] = 0;
     // Arnoldi steps with the host one step behind (without an inner solve):
     // step jj+1 is launched (it needs only device data) before the host reads
     // step jj's Hessenberg column from its pinned slot, so the GPU does not wait
@@ -354,12 +381,12 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
             return cudaGetLastError();
           });
           timed_launch(op->ctx, KC_KRYLOV, [&] {
-            k_reduce_parts<S><<<1, 256, 0, s>>>(K.part.as<S>(), 1, nch, k, h3);
+            k_reduce_parts<S><<<(k + 255) / 256, 256, 0, s>>>(K.part.as<S>(), 1, nch, k, h3);
             return cudaGetLastError();
           });
         }
         timed_launch(op->ctx, KC_KRYLOV, [&] {
-          k_inv_norm<S><<<1, 64, 0, s>>>(h3, k, K.inv.as<double>());
+          k_inv_norm<S><<<(k + 63) / 64, 64, 0, s>>>(h3, k, K.inv.as<double>());
           return cudaGetLastError();
         });
         timed_launch(op->ctx, KC_KRYLOV, [&] {
@@ -411,7 +438,8 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
         H gj = g[(size_t)j * k + c];
         g[(size_t)(j + 1) * k + c] = -cj(ss) * gj;
         g[(size_t)j * k + c] = cc * gj;
-        if (std::abs(g[(size_t)(j + 1) * k + c]) > tol * bn[c] && hn[c] > 0) all_done = false;
+        if (jconv[c] < 0 && !(std::abs(g[(size_t)(j + 1) * k + c]) > tol * bn[c] && hn[c] > 0)) jconv[c] = j + 1;
+        if (jconv[c] < 0) all_done = false;
       }
       *all_done_out = all_done;
       return BG_OK;
@@ -443,9 +471,10 @@ bg_status fgmres(Krylov& K, int prec, Krylov* inner, int inner_prec, double inne
     std::vector<H> y((size_t)j * k, H(0));
     for (int c = 0; c < k; ++c) {
       const H* hc = &Hm[(size_t)c * (m + 1) * m];
-      for (int i = j - 1; i >= 0; --i) {
+      const int jc = jconv[c] >= 0 ? std::min(jconv[c], j) : j;
+      for (int i = jc - 1; i >= 0; --i) {
         H acc = g[(size_t)i * k + c];
-        for (int q = i + 1; q < j; ++q) acc -= hc[(size_t)q * (m + 1) + i] * y[(size_t)q * k + c];
+        for (int q = i + 1; q < jc; ++q) acc -= hc[(size_t)q * (m + 1) + i] * y[(size_t)q * k + c];
         H diag = hc[(size_t)i * (m + 1) + i];
         y[(size_t)i * k + c] = std::abs(diag) > 0 ? acc / diag : H(0);
       }
@@ -505,6 +534,51 @@ bg_status solve_typed(bg_operator* op, const void* bdof, void* xdof, int k, cons
 
 }  // namespace
 
+static bg_status solve_chunks(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params& prm,
+                              bg_solve_stats* stats, int on_device, int chunk);
+
+// Batched wavenumbers: the columns form nk blocks of nr, block q with
+// wavenumber q, and every batch the solver runs must hold an equal slice of
+// every block in block order (the product maps its columns that way). The
+// columns are permuted on the device so that slice j (columns c0 .. c0 + w - 1
+// of every block) is contiguous, solved in chunks of nk w columns (at most
+// 256), and permuted back.
+static bg_status solve_wavenumber_slices(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params& prm,
+                                         bg_solve_stats* stats, int on_device) {
+  const int nk = (int)op->kslots.size();
+  if (nrhs % nk)
+    return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+  const int nr = nrhs / nk, w = std::max(1, std::min(nr, 256 / nk));
+  cudaStream_t s = op->ctx->stream;
+  const size_t col = (size_t)op->N * (op->cplx ? 16 : 8);
+  DevBuf bp, xp;
+  cudaError_t e = bp.alloc(col * nrhs);
+  if (e == cudaSuccess) e = xp.alloc(col * nrhs);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve staging");
+  // block q, columns c0 .. c0 + ws - 1  <->  permuted columns c0 nk + q ws
+  auto permute = [&](bool in) -> cudaError_t {
+    for (int c0 = 0; c0 < nr; c0 += w) {
+      const int ws = std::min(w, nr - c0);
+      for (int q = 0; q < nk; ++q) {
+        const size_t user = (size_t)(q * nr + c0) * col, perm = (size_t)(c0 * nk + q * ws) * col;
+        cudaError_t ee =
+            in ? cudaMemcpyAsync(static_cast<char*>(bp.p) + perm, static_cast<const char*>(b) + user, ws * col,
+                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s)
+               : cudaMemcpyAsync(static_cast<char*>(x) + user, static_cast<const char*>(xp.p) + perm, ws * col,
+                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s);
+        if (ee != cudaSuccess) return ee;
+      }
+    }
+    return cudaSuccess;
+  };
+  if ((e = permute(true)) != cudaSuccess) return cuda_status(op->ctx, e, "solve staging");
+  const bg_status st = solve_chunks(op, bp.p, xp.p, nrhs, prm, stats, 1, nk * w);
+  if (st != BG_OK && st != BG_NOT_CONVERGED && st != BG_TIMEOUT) return st;
+  if ((e = permute(false)) == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(op->ctx, e, "solve copy-out");
+  return st;
+}
+
 extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params* params,
                               bg_solve_stats* stats, int on_device) {
   if (!op || nrhs < 0) return BG_INVALID_ARG;
@@ -522,12 +596,19 @@ extern "C" bg_status bg_solve(bg_operator* op, const void* b, void* x, int nrhs,
       prm.inner_precision > BG_PREC_FP32)
     return set_error(op->ctx, BG_INVALID_ARG, "solve parameters");
   cudaSetDevice(op->ctx->device);
+  if (op->kbatched()) return solve_wavenumber_slices(op, b, x, nrhs, prm, stats, on_device);
+  return solve_chunks(op, b, x, nrhs, prm, stats, on_device, 32);
+}
+
+// Column chunks of at most `chunk` columns, each solved as one batch.
+static bg_status solve_chunks(bg_operator* op, const void* b, void* x, int nrhs, const bg_solve_params& prm,
+                              bg_solve_stats* stats, int on_device, int chunk) {
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;
   bg_solve_stats total{0, 0, 0, 0, 0.0};
   bg_status result = BG_OK;
-  for (int c0 = 0; c0 < nrhs; c0 += 32) {
-    const int k = std::min(32, nrhs - c0);
+  for (int c0 = 0; c0 < nrhs; c0 += chunk) {
+    const int k = std::min(chunk, nrhs - c0);
     bg_status st = ensure_work(op, k);
     if (st != BG_OK) return st;
     const long nk = (long)op->N * k;

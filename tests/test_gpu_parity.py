@@ -170,6 +170,28 @@ def test_solve_reaches_tolerance(ctx, oracle, inner):
         assert np.linalg.norm(r) / np.linalg.norm(b[:, c]) < 2e-8
 
 
+@pytest.mark.parametrize("inner", ["fp64", "fp32"])
+def test_solve_many_columns(ctx, oracle, inner):
+    """300 right-hand sides in one batched solve (more columns than the
+    threads of one reduction block): every column reaches the FP64 residual
+    1e-8, and the first 8 columns agree with an 8-column solve of the same
+    data within what two solutions at that residual may differ by (the
+    condition number here is about 8e3)."""
+    d, o = _pair(ctx, oracle, SPHERE, 2, 1, 0, 0.0, 6)
+    rng = np.random.default_rng(12)
+    dirs = rng.normal(size=(300, 3))
+    x0 = dirs / np.linalg.norm(dirs, axis=1, keepdims=True) * rng.uniform(1.5, 3.0, (300, 1))
+    b = d.load_vector(0, x0)
+    A = d.get_discrete_operator()
+    x, st = A.solve(b, tol=1e-8, inner=inner)
+    assert st["converged"]
+    r = b - o.matvec(x)
+    res = np.linalg.norm(r, axis=0) / np.linalg.norm(b, axis=0)
+    assert res.max() < 2e-8, res.max()
+    x8, _ = A.solve(b[:, :8], tol=1e-8, inner=inner)
+    assert np.max(np.linalg.norm(x[:, :8] - x8, axis=0) / np.linalg.norm(x8, axis=0)) < 1e-3
+
+
 # Maxwell single layer (div-conforming vector basis, kappa = 2 as in the EFIE
 # workload): all four component blocks of every leaf, the product, the dipole
 # excitation and a solve.
