@@ -327,6 +327,23 @@ class DiscreteOperator:
     def release_wavenumbers(self):
         self.ctx.check(_lib.load().bg_operator_release_wavenumbers(self.h))
 
+    def assemble_wavenumbers(self):
+        """Assemble every prepared wavenumber side by side
+        (bg_operator_assemble_wavenumbers): afterwards products, solves, load
+        vectors and potentials take n * k columns, block q (k columns) with
+        wavenumber q in preparation order."""
+        self.ctx.check(_lib.load().bg_operator_assemble_wavenumbers(self.h))
+
+    def wavenumbers(self):
+        """The batched wavenumbers in column-block order (empty when the
+        operator holds one)."""
+        n = ctypes.c_int()
+        self.ctx.check(_lib.load().bg_operator_num_wavenumbers(self.h, ctypes.byref(n), None, None))
+        re_, im_ = np.zeros(n.value), np.zeros(n.value)
+        if n.value:
+            self.ctx.check(_lib.load().bg_operator_num_wavenumbers(self.h, ctypes.byref(n), _dp(re_), _dp(im_)))
+        return re_ + 1j * im_
+
     def assembly_times(self):
         t = np.zeros(3)
         self.ctx.check(_lib.load().bg_operator_assembly_times(self.h, _dp(t)))

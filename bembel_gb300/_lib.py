@@ -109,6 +109,8 @@ def load(build_if_missing=True):
         "bg_operator_assembly_times": (I, [P, dp]),
         "bg_operator_prepare_wavenumbers": (I, [P, dp, dp, I]),
         "bg_operator_release_wavenumbers": (I, [P]),
+        "bg_operator_assemble_wavenumbers": (I, [P]),
+        "bg_operator_num_wavenumbers": (I, [P, ip, dp, dp]),
         "bg_operator_quadrature_counts": (I, [P, lp]),
         "bg_matvec": (I, [P, P, Lg, P, Lg, I, dp, dp, I, I]),
         "bg_load_vector": (I, [P, I, dp, I, P, I]),

@@ -658,6 +658,13 @@ extern "C" bg_status bg_operator_memory(const bg_operator* op, size_t* allocated
       a += b->bytes;
   for (const auto& f : op->far) a += f.d_row_ptr.bytes + f.d_col.bytes;
   for (const auto& c : op->near_cache) a += c.blocks->bytes;
+  for (const auto& k : op->kslots) {  // batched wavenumbers (the active slot's fields are counted above)
+    if (&k == &op->kslots[0] + op->kslot_active) continue;
+    a += k.dense64.bytes + k.dense32.bytes;
+    for (const auto* v : {&k.far64, &k.far_df, &k.atiles, &k.ainv})
+      for (const DevBuf* b : *v) a += b->bytes;
+  }
+  a += op->w_kx.bytes + op->w_ky.bytes;
   if (op->solver_ws && op->solver_ws_bytes) a += op->solver_ws_bytes(op->solver_ws);
   *allocated = a;
   // stored fields once assembled
@@ -1113,6 +1120,8 @@ static bg_status near_quadrature(bg_operator* op, const NearWork& w, int nk, con
   return cuda_status(op->ctx, e, "near-field assembly");
 }
 
+static void fresh_far_fields(bg_operator* op);
+
 static bg_status assemble_near(bg_operator* op) {
   if (op->maxwell()) return assemble_near_mw(op);
   cudaStream_t s = op->ctx->stream;
@@ -1213,7 +1222,101 @@ extern "C" bg_status bg_operator_release_wavenumbers(bg_operator* op) {
   if (!op) return BG_INVALID_ARG;
   for (auto& c : op->near_cache) delete c.blocks;
   op->near_cache.clear();
+  if (!op->kslots.empty()) {
+    op->drop_graphs();
+    op->free_slots();
+    fresh_far_fields(op);
+    op->assembled = false;
+  }
   return BG_OK;
+}
+
+extern "C" bg_status bg_operator_assemble(bg_operator* op);
+
+extern "C" bg_status bg_operator_assemble_wavenumbers(bg_operator* op) {
+  if (!op) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
+  if (!op->cplx || op->maxwell() || op->vd != 1)
+    return set_error(op->ctx, BG_UNSUPPORTED, "batched wavenumbers: Helmholtz single layer only");
+  if (op->near_cache.empty())
+    return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: prepare the wavenumbers first");
+  std::vector<std::pair<double, double>> ks;
+  for (const auto& c : op->near_cache) ks.emplace_back(c.kre, c.kim);
+  const double kre0 = op->kre, kim0 = op->kim;
+  std::vector<bg_operator::KSlot> slots;
+  auto fail = [&](bg_status st) {
+    for (auto& k : slots)
+      for (auto v : {&k.far64, &k.far_df, &k.atiles, &k.ainv})
+        for (auto b : *v) delete b;
+    op->kre = kre0;
+    op->kim = kim0;
+    op->assembled = false;
+    return st;
+  };
+  double t_far = 0, t_near = 0;
+  for (const auto& k : ks) {
+    op->kre = k.first;
+    op->kim = k.second;
+    bg_status st = bg_operator_assemble(op);  // copies the prepared near field, assembles the far field
+    if (st != BG_OK) return fail(st);
+    t_far += op->t_far;
+    t_near += op->t_near;
+    bg_operator::KSlot slot;
+    slot.kre = k.first;
+    slot.kim = k.second;
+    std::swap(slot.dense64, op->d_dense64);
+    std::swap(slot.dense32, op->d_dense32);
+    std::swap(slot.far64, op->d_far64);
+    std::swap(slot.far_df, op->d_far_df);
+    std::swap(slot.atiles, op->d_far_atiles);
+    std::swap(slot.ainv, op->d_far_ainv);
+    slot.far_tiles = op->far_tiles;
+    fresh_far_fields(op);
+    // the prepared copy of this near field is no longer needed
+    for (size_t i = 0; i < op->near_cache.size(); ++i)
+      if (op->near_cache[i].kre == k.first && op->near_cache[i].kim == k.second) {
+        delete op->near_cache[i].blocks;
+        op->near_cache.erase(op->near_cache.begin() + i);
+        break;
+      }
+    slots.push_back(std::move(slot));
+  }
+  op->drop_graphs();
+  op->kslots = std::move(slots);
+  op->kslot_active = -1;
+  op->kre = kre0;
+  op->kim = kim0;
+  op->t_far = t_far;
+  op->t_near = t_near;
+  op->t_total = t_far + t_near;
+  op->assembled = true;
+  return BG_OK;
+}
+
+extern "C" bg_status bg_operator_num_wavenumbers(const bg_operator* op, int* n, double* kre, double* kim) {
+  if (!op || !n) return BG_INVALID_ARG;
+  *n = (int)op->kslots.size();
+  for (int q = 0; q < *n; ++q) {
+    // the active slot's wavenumber sits in the operator while it is swapped in
+    const bool act = q == op->kslot_active;
+    if (kre) kre[q] = act ? op->kre : op->kslots[q].kre;
+    if (kim) kim[q] = act ? op->kim : op->kslots[q].kim;
+  }
+  return BG_OK;
+}
+
+// the per-level far-field buffers of the current wavenumber, empty (after
+// they moved into a wavenumber slot or the slots were freed)
+static void fresh_far_fields(bg_operator* op) {
+  const size_t L = op->d_pts64.size();
+  for (auto v : {&op->d_far64, &op->d_far_df, &op->d_far_atiles, &op->d_far_ainv}) {
+    for (auto b : *v) delete b;
+    v->clear();
+    for (size_t l = 0; l < L; ++l) v->push_back(new DevBuf());
+  }
+  op->far_tiles = false;
+  op->d_dense64.release();
+  op->d_dense32.release();
 }
 
 extern "C" bg_status bg_operator_assemble(bg_operator* op) {
@@ -1226,6 +1329,10 @@ extern "C" bg_status bg_operator_assemble(bg_operator* op) {
   cudaSetDevice(op->ctx->device);
   op->assembled = false;
   op->drop_graphs();  // assembly may move the stored fields
+  if (!op->kslots.empty()) {
+    op->free_slots();
+    fresh_far_fields(op);
+  }
   auto t0 = std::chrono::steady_clock::now();
   bg_status st = assemble_far(op);
   if (st != BG_OK) return st;
@@ -1717,7 +1824,35 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
 // precision) as a CUDA graph and replayed; growing the work vectors or
 // re-assembling the operator drops the graphs. A capture that fails falls back
 // to direct launches for this operator.
+// Batched wavenumbers: column block q of the row-major dof vectors (nrhs /
+// nslots columns) goes through slot q's operator.
+static bg_status apply_wavenumber_blocks(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
+  const int nk = (int)op->kslots.size();
+  if (nrhs % nk) return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+  const int nr = nrhs / nk;
+  const size_t usz = op->scalar_bytes(false), blk = (size_t)op->N * nr * usz;
+  cudaStream_t s = op->ctx->stream;
+  if (op->w_kx.bytes < blk) {
+    BG_CHECK(op->w_kx.alloc(blk), "wavenumber column blocks");
+    BG_CHECK(op->w_ky.alloc(blk), "wavenumber column blocks");
+  }
+  bg_status st = BG_OK;
+  for (int q = 0; q < nk && st == BG_OK; ++q) {
+    const size_t off = (size_t)q * nr * usz, pitch = (size_t)nrhs * usz;
+    BG_CHECK(cudaMemcpy2DAsync(op->w_kx.p, nr * usz, static_cast<const char*>(xdof) + off, pitch, nr * usz, op->N,
+                               cudaMemcpyDeviceToDevice, s), "wavenumber column block");
+    op->activate_slot(q);
+    st = apply_operator(op, nr, prec, op->w_kx.p, op->w_ky.p);
+    if (st == BG_OK)
+      BG_CHECK(cudaMemcpy2DAsync(static_cast<char*>(ydof) + off, pitch, op->w_ky.p, nr * usz, nr * usz, op->N,
+                                 cudaMemcpyDeviceToDevice, s), "wavenumber column block");
+  }
+  op->activate_slot(-1);
+  return st;
+}
+
 bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
+  if (op->kbatched()) return apply_wavenumber_blocks(op, nrhs, prec, xdof, ydof);
   cudaStream_t s = op->ctx->stream;
   const int S64 = op->stype(false);
   BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
@@ -1728,7 +1863,8 @@ bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, 
   if (ctx->profiling || !op->use_graphs) {
     st = apply_middle(op, nrhs, prec);
   } else {
-    const long key = bg_operator::plan_key(nrhs, prec);
+    // one graph per shape and wavenumber slot (the slots' fields differ)
+    const long key = bg_operator::plan_key(nrhs, prec) + ((long)(op->kslot_active + 1) << 40);
     auto it = op->graphs.find(key);
     if (it == op->graphs.end() && !op->graph_seen.count(key)) {
       // first product of this shape: direct launches (they also raise the
@@ -1814,6 +1950,7 @@ extern "C" bg_status bg_operator_autotune(bg_operator* op, int nrhs, int precisi
     return set_error(ctx, BG_INVALID_ARG, "autotune: nrhs must be positive, reps in [0, 1000]");
   if (ctx->device < 0) return set_error(ctx, BG_UNSUPPORTED, "host-only context: the autotuner needs a GPU");
   if (!op->assembled) return set_error(ctx, BG_INVALID_ARG, "autotune: the operator is not assembled");
+  if (op->kbatched()) return set_error(ctx, BG_UNSUPPORTED, "autotune: tune one wavenumber, not a batch");
   if (reps == 0) reps = 5;
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
@@ -1939,6 +2076,21 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
   if (!op->cplx && (alpha[1] != 0.0 || beta[1] != 0.0))
     return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
   cudaSetDevice(op->ctx->device);
+  if (op->kbatched()) {
+    // column block q through wavenumber slot q
+    const int nk = (int)op->kslots.size();
+    if (nrhs % nk)
+      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+    const int nr = nrhs / nk;
+    bg_status st = BG_OK;
+    for (int q = 0; q < nk && st == BG_OK; ++q) {
+      op->activate_slot(q);
+      st = bg_matvec(op, static_cast<const char*>(x) + (size_t)q * nr * ldx * 16, ldx,
+                     static_cast<char*>(y) + (size_t)q * nr * ldy * 16, ldy, nr, alpha, beta, precision, on_device);
+    }
+    op->activate_slot(-1);
+    return st;
+  }
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;
   const int uS = op->cplx ? 1 : 0;

@@ -237,6 +237,8 @@ extern "C" bg_status bg_matvec_noalloc(bg_operator* op, const void* x, void* y, 
   if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED) return set_error(op->ctx, BG_INVALID_ARG, "precision");
   if (op->maxwell())
     return set_error(op->ctx, BG_UNSUPPORTED, "bg_matvec_noalloc: the Maxwell operator is not supported; use bg_matvec");
+  if (op->kbatched())
+    return set_error(op->ctx, BG_UNSUPPORTED, "bg_matvec_noalloc: batched wavenumbers are not supported; use bg_matvec");
   const bool mixed = precision == BG_PREC_MIXED;
   const ScratchPlan sp = plan_scratch(op, mixed);
   if (sp.total > kNoallocScratchBytes)

@@ -152,6 +152,47 @@ struct bg_operator {
   };
   std::vector<NearCacheEntry> near_cache;
 
+  // Several wavenumbers assembled side by side (bg_operator_assemble_wavenumbers):
+  // slot q holds wavenumber q's near field, far field and tensor-core tiles.
+  // While no slot is active, products, load vectors, potentials and solves
+  // take nslots column blocks of equal width and apply slot q to block q, by
+  // swapping the slot's fields into the operator's (activate_slot).
+  struct KSlot {
+    double kre = 0.0, kim = 0.0;
+    DevBuf dense64, dense32;
+    std::vector<DevBuf*> far64, far_df, atiles, ainv;
+    bool far_tiles = false;
+  };
+  std::vector<KSlot> kslots;
+  int kslot_active = -1;
+  DevBuf w_kx, w_ky;  // one column block of a batched product (row-major dof vectors)
+  bool kbatched() const { return !kslots.empty() && kslot_active < 0; }
+  void swap_slot(int q) {
+    KSlot& k = kslots[q];
+    std::swap(kre, k.kre);
+    std::swap(kim, k.kim);
+    std::swap(d_dense64, k.dense64);
+    std::swap(d_dense32, k.dense32);
+    std::swap(d_far64, k.far64);
+    std::swap(d_far_df, k.far_df);
+    std::swap(d_far_atiles, k.atiles);
+    std::swap(d_far_ainv, k.ainv);
+    std::swap(far_tiles, k.far_tiles);
+  }
+  void activate_slot(int q) {
+    if (q == kslot_active) return;
+    if (kslot_active >= 0) swap_slot(kslot_active);
+    if (q >= 0) swap_slot(q);
+    kslot_active = q;
+  }
+  void free_slots() {
+    activate_slot(-1);
+    for (auto& k : kslots)
+      for (auto v : {&k.far64, &k.far_df, &k.atiles, &k.ainv})
+        for (auto b : *v) delete b;
+    kslots.clear();
+  }
+
   // device tables
   DevBuf d_patch_meta, d_patch_cp, d_el_patch, d_el_llc;
   DevBuf d_T_ptr, d_T_idx, d_T_val, d_Tt_ptr, d_Tt_idx, d_Tt_val;
@@ -249,6 +290,7 @@ struct bg_operator {
 
   ~bg_operator() {
     drop_graphs();
+    free_slots();
     if (solver_ws && solver_ws_free) solver_ws_free(solver_ws);
     for (auto v : {&d_pts64, &d_pts32, &d_centres, &d_tan64, &d_tan32, &d_far64, &d_far_df, &d_far_atiles, &d_far_ainv,
                    &d_mom64, &d_mom32, &w_y, &w_z, &w_ydf, &w_btiles, &w_binv, &w_yv, &w_zv})

@@ -383,6 +383,21 @@ extern "C" bg_status bg_load_vector(bg_operator* op, int kind, const double* prm
   const int npr = kind == 3 ? 6 : 3;  // parameters per right-hand side
   if (!op->cplx && kind != 0) return set_error(op->ctx, BG_INVALID_ARG, "complex data for a real operator");
   cudaSetDevice(op->ctx->device);
+  if (op->kbatched()) {
+    // batched wavenumbers: column block q with wavenumber q
+    const int nk = (int)op->kslots.size();
+    if (nrhs % nk)
+      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+    const int nr = nrhs / nk;
+    bg_status st = BG_OK;
+    for (int q = 0; q < nk && st == BG_OK; ++q) {
+      op->activate_slot(q);
+      st = bg_load_vector(op, kind, prm + (size_t)npr * q * nr, nr, static_cast<char*>(out) + (size_t)q * nr * op->N * 16,
+                          on_device);
+    }
+    op->activate_slot(-1);
+    return st;
+  }
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;
   const Rule1D& gr = gauss_rule(op->P + 2);
@@ -473,6 +488,21 @@ extern "C" bg_status bg_potential(bg_operator* op, const void* rho, int nrhs, co
   if (!rho || !pts || !out) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: potentials need a GPU");
   cudaSetDevice(op->ctx->device);
+  if (op->kbatched()) {
+    // batched wavenumbers: column block q with wavenumber q
+    const int nk = (int)op->kslots.size();
+    if (nrhs % nk)
+      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+    const int nr = nrhs / nk;
+    bg_status st = BG_OK;
+    for (int q = 0; q < nk && st == BG_OK; ++q) {
+      op->activate_slot(q);
+      st = bg_potential(op, static_cast<const char*>(rho) + (size_t)q * nr * op->N * 16, nr, pts, npts,
+                        static_cast<char*>(out) + (size_t)q * nr * npts * 16);
+    }
+    op->activate_slot(-1);
+    return st;
+  }
   if (op->maxwell()) return potential_mw(op, rho, nrhs, pts, npts, out);
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;

@@ -172,8 +172,28 @@ bg_status bg_operator_prepare_wavenumbers(bg_operator* op, const double* kre, co
  * each, common-vertex pairs, 4 (n+1)^4 each]. No counterpart in the
  * reference; host only, no device work. */
 bg_status bg_operator_quadrature_counts(const bg_operator* op, long* counts8);
-/* frees the near fields of bg_operator_prepare_wavenumbers */
+/* frees the near fields of bg_operator_prepare_wavenumbers and the
+ * wavenumber slots of bg_operator_assemble_wavenumbers (the operator is then
+ * unassembled) */
 bg_status bg_operator_release_wavenumbers(bg_operator* op);
+/* No counterpart in the reference (one wavenumber per
+ * DiscreteOperator::compute, Helmholtz/SingleLayerOperator.hpp:124-130).
+ * Assembles every wavenumber prepared by bg_operator_prepare_wavenumbers
+ * side by side: wavenumber q (in preparation order) gets a slot with its near
+ * field (the prepared blocks, which are then freed), its far field and the
+ * far field's tensor-core tiles. Afterwards bg_matvec, bg_solve,
+ * bg_load_vector and bg_potential take nrhs = n k columns (n wavenumbers,
+ * k columns each) and apply wavenumber q to columns q k .. q k + k - 1: one
+ * call, and for bg_solve one flexible GMRES over all n k columns, covers
+ * every wavenumber. Other column counts give BG_INVALID_ARG;
+ * bg_matvec_noalloc and bg_operator_autotune give BG_UNSUPPORTED.
+ * bg_operator_assemble (after bg_operator_set_wavenumber) returns the
+ * operator to one wavenumber. Helmholtz single layer only. */
+bg_status bg_operator_assemble_wavenumbers(bg_operator* op);
+/* the wavenumbers of the slots of bg_operator_assemble_wavenumbers, in
+ * column-block order (*n = 0 when the operator holds none); kre, kim may be
+ * NULL or hold *n values */
+bg_status bg_operator_num_wavenumbers(const bg_operator* op, int* n, double* kre, double* kim);
 bg_status bg_operator_destroy(bg_operator* op);
 /* info[0..15]: rows (= cols, H2Matrix.hpp:76-77), superspace size, elements,
  * dense leaves, low-rank leaves, vector dimension, FMM components, n_p,

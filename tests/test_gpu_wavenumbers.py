@@ -67,3 +67,73 @@ def test_prepared_near_field_against_oracle(ctx, oracle):
         a, b = d.leaf_block(li), o.leaf_matrix(li)
         worst = max(worst, np.linalg.norm(a - b) / np.linalg.norm(b))
     assert worst < FP64_TOL, worst
+
+
+def test_batched_wavenumbers(ctx):
+    """Three wavenumbers assembled side by side
+    (bg_operator_assemble_wavenumbers): one call of the product, the load
+    vector, the potential and the solve covers all three, column block q with
+    wavenumber q, and each block equals the single-wavenumber operator's
+    result (products 1e-13 as above; the mixed and FP32 products to 1e-12).
+    The batched solve is one flexible GMRES over the 3 x 4 columns; every
+    block meets the FP64 residual 2e-8 of its own wavenumber's operator, also
+    with 3 x 90 columns, which the solver takes in two slices of every
+    block."""
+    import bembel_gb300 as bg
+    ks = [0.7, 2.0, 3.5]
+    nr = 4
+    d, lin = _op(ctx, SPHERE, 2, 1, ks[0])
+    d.prepare_wavenumbers(ks)
+    d.assemble_wavenumbers()
+    assert np.allclose(d.wavenumbers(), ks)
+    refs = []
+    for k in ks:
+        r, _ = _op(ctx, SPHERE, 2, 1, k)
+        r.compute()
+        refs.append(r)
+    rng = np.random.default_rng(41)
+    x = rng.uniform(-1, 1, (d.N, 3 * nr)) + 1j * rng.uniform(-1, 1, (d.N, 3 * nr))
+    A = d.get_discrete_operator()
+    for prec, tol in (("fp64", 1e-13), ("mixed", 1e-12), ("fp32", 1e-12)):
+        y = A.matvec(x, precision=prec)
+        for q in range(3):
+            yr = refs[q].get_discrete_operator().matvec(x[:, q * nr:(q + 1) * nr], precision=prec)
+            assert np.linalg.norm(y[:, q * nr:(q + 1) * nr] - yr) / np.linalg.norm(yr) < tol, (prec, q)
+    dirs = rng.normal(size=(3 * nr, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    b = d.load_vector(2, dirs)
+    for q in range(3):
+        br = refs[q].load_vector(2, dirs[q * nr:(q + 1) * nr])
+        assert np.linalg.norm(b[:, q * nr:(q + 1) * nr] - br) / np.linalg.norm(br) < 1e-14
+    xs, st = A.solve(b, tol=1e-8, inner="fp32")
+    assert st["converged"]
+    pts = rng.uniform(-0.3, 0.3, (5, 3))
+    pot = d.potential(xs, pts)
+    for q in range(3):
+        Aq = refs[q].get_discrete_operator()
+        bq, xq = b[:, q * nr:(q + 1) * nr], xs[:, q * nr:(q + 1) * nr]
+        res = np.linalg.norm(bq - Aq.matvec(xq), axis=0) / np.linalg.norm(bq, axis=0)
+        assert res.max() < 2e-8, (q, res)
+        pr = refs[q].potential(xq, pts)
+        assert np.linalg.norm(pot[:, q * nr:(q + 1) * nr] - pr) / np.linalg.norm(pr) < 1e-14
+    with pytest.raises(bg.BembelError):
+        A.matvec(x[:, :5])
+    # 90 columns per wavenumber: the solve runs in slices of 85 and 5 columns
+    # of every block (two batches); each block still solves its own system
+    big = 90
+    dirs = rng.normal(size=(big, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    bb = d.load_vector(2, np.tile(dirs, (3, 1)))
+    xb, st = A.solve(bb, tol=1e-8, inner="fp32")
+    assert st["converged"]
+    for q in range(3):
+        Aq = refs[q].get_discrete_operator()
+        bq, xq = bb[:, q * big:(q + 1) * big], xb[:, q * big:(q + 1) * big]
+        res = np.linalg.norm(bq - Aq.matvec(xq), axis=0) / np.linalg.norm(bq, axis=0)
+        assert res.max() < 2e-8, (q, res.max())
+    d.release_wavenumbers()
+    lin.set_wavenumber(ks[1])
+    d.compute()
+    y = d.get_discrete_operator().matvec(x[:, :nr])
+    yr = refs[1].get_discrete_operator().matvec(x[:, :nr])
+    assert np.linalg.norm(y - yr) / np.linalg.norm(yr) < 1e-12
