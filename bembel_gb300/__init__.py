@@ -449,8 +449,9 @@ class Server:
     """Serving loop of the library (bg_server_*): worker threads, each with
     its own stream on the context's GPU, solve queued requests, batching
     requests for the same operator; assembled operators are cached per
-    (geometry, kind, M, P, wavenumber), sharded over the workers and admitted
-    by device memory (least recently used evicted).
+    (geometry, kind, M, P, wavenumber) on the worker that assembled them and
+    admitted by device memory against one budget for all workers (least
+    recently used idle operators evicted).
 
         srv = Server(ctx, hbm_budget_bytes=200e9, workers=4)
         g = srv.add_geometry(Geometry("sphere.dat", ctx))

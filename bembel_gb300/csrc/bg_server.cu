@@ -1,7 +1,7 @@
 // Serving loop over the C ABI: a request queue drained by worker threads on
 // the context's GPU (each with its own context and stream), batching of
-// requests that share an operator, and per-worker caches of assembled
-// operators with admission by device memory.
+// requests that share an operator, and caches of assembled operators with
+// admission by device memory against one budget shared by all workers.
 //
 // The reference has no serving layer (its examples assemble once and solve
 // once); this file is the runtime around the operator for a stream of solves
@@ -39,7 +39,9 @@ struct OpKey {
 struct CacheEntry {
   OpKey key;
   bg_operator* op;
-  size_t bytes;  // admitted footprint (estimate at admission, raised to the measured one after use)
+  size_t bytes;       // admitted footprint (estimate at admission, raised to the measured one after use)
+  long last_use = 0;  // server-wide use stamp (least recently used across workers is evicted first)
+  bool busy = false;  // its worker is solving with it
 };
 
 struct Job {
@@ -62,16 +64,17 @@ bool batchable(const bg_request& a, const bg_request& b) {
 
 }  // namespace
 
-// One worker: its own context (stream, pinned staging) on the server's GPU,
-// its own operator cache and its share of the memory budget. Operators are
-// sharded over the workers by key, so an operator only ever runs on the
-// stream of the context that created it.
+// One worker: its own context (stream, pinned staging) on the server's GPU
+// and the operators it created. An operator only ever runs on the stream of
+// the context that created it, so requests for a cached operator go to its
+// worker (owner); requests for an operator that no worker holds go to the
+// first worker that is free, which then owns it. The memory budget is one for
+// all workers: admission evicts the least recently used idle operator of any
+// worker.
 struct Worker {
   int id = 0;
   bg_context* ctx = nullptr;
-  size_t budget = 0;
-  std::list<CacheEntry> cache;  // front: most recently used
-  size_t in_use = 0;
+  std::list<CacheEntry> cache;  // front: most recently used by this worker
   DevBuf b_dev, x_dev;
   std::thread th;
 };
@@ -90,78 +93,149 @@ struct bg_server {
   bg_server_stats st{};
   std::chrono::steady_clock::time_point t0;
   std::vector<Worker*> workers;
+  std::map<OpKey, int> owner;       // worker holding (or assembling) the operator of a key
+  size_t in_use = 0;                // admitted bytes of all workers, reservations included
+  long use_stamp = 0;
+  int reserving = 0;                // admissions between reservation and cache entry
+  std::condition_variable cv_idle;  // an operator stopped being busy, or a reservation ended
+  std::mutex ops_mu;                // operator creation and destruction (context reference counts)
 
   double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
 
-  int shard(const OpKey& k) const {
-    size_t h = std::hash<int>()(k.geo) * 1000003u ^ std::hash<int>()(k.kind * 131 + k.M * 17 + k.P);
-    h = h * 1000003u ^ std::hash<double>()(k.kre) ^ (std::hash<double>()(k.kim) << 1);
-    return (int)(h % workers.size());
-  }
-
   void update_usage() {  // caller holds mu
-    size_t u = 0;
     int n = 0;
-    for (const Worker* w : workers) {
-      u += w->in_use;
-      n += (int)w->cache.size();
-    }
-    st.bytes_in_use = u;
+    for (const Worker* w : workers) n += (int)w->cache.size();
+    st.bytes_in_use = in_use;
     st.cached_operators = n;
   }
 
-  void evict_back(Worker& w) {
-    CacheEntry& e = w.cache.back();
-    bg_operator_destroy(e.op);
-    std::lock_guard<std::mutex> lk(mu);
-    w.in_use -= e.bytes;
-    w.cache.pop_back();
-    ++st.evictions;
-    update_usage();
+  void destroy_op(bg_operator* op) {
+    std::lock_guard<std::mutex> lk(ops_mu);
+    bg_operator_destroy(op);
   }
 
-  // operator of key k, assembled; nullptr and *status on failure
-  bg_operator* acquire(Worker& w, const OpKey& k, bool* hit, bg_status* status) {
-    for (auto it = w.cache.begin(); it != w.cache.end(); ++it)
-      if (it->key == k) {
-        std::lock_guard<std::mutex> lk(mu);
-        w.cache.splice(w.cache.begin(), w.cache, it);
-        *hit = true;
-        return w.cache.front().op;
+  // Reserve est bytes of the shared budget (caller holds lk on mu): evict
+  // idle operators of any worker, least recently used first, and wait for
+  // busy ones or other admissions when nothing idle is left. False if est
+  // cannot fit even with every other operator gone.
+  bool reserve(std::unique_lock<std::mutex>& lk, size_t est) {
+    if (est > budget) return false;
+    for (;;) {
+      if (in_use + est <= budget) {
+        in_use += est;
+        ++reserving;
+        update_usage();
+        return true;
       }
-    *hit = false;
-    if (k.geo < 0 || k.geo >= (int)geos.size()) {
-      *status = BG_INVALID_ARG;
-      return nullptr;
+      Worker* vw = nullptr;
+      std::list<CacheEntry>::iterator victim;
+      bool any_busy = reserving > 0;
+      for (Worker* o : workers)
+        for (auto it = o->cache.begin(); it != o->cache.end(); ++it) {
+          if (it->busy) {
+            any_busy = true;
+            continue;
+          }
+          if (!vw || it->last_use < victim->last_use) {
+            vw = o;
+            victim = it;
+          }
+        }
+      if (vw) {
+        bg_operator* op = victim->op;
+        in_use -= victim->bytes;
+        owner.erase(victim->key);
+        vw->cache.erase(victim);
+        ++st.evictions;
+        update_usage();
+        lk.unlock();
+        destroy_op(op);
+        lk.lock();
+        continue;
+      }
+      if (!any_busy) return false;  // nothing to evict and nothing will be freed
+      cv_idle.wait(lk);
     }
+  }
+
+  // operator of key k, assembled and marked busy; nullptr and *status on failure
+  bg_operator* acquire(Worker& w, const OpKey& k, bool* hit, bg_status* status) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      for (auto it = w.cache.begin(); it != w.cache.end(); ++it)
+        if (it->key == k) {
+          w.cache.splice(w.cache.begin(), w.cache, it);
+          w.cache.front().busy = true;
+          w.cache.front().last_use = ++use_stamp;
+          *hit = true;
+          return w.cache.front().op;
+        }
+    }
+    *hit = false;
+    {
+      // another worker may have evicted this key since it was routed here
+      std::lock_guard<std::mutex> lk(mu);
+      owner[k] = w.id;
+    }
+    auto give_up = [&](bg_status s) {
+      std::lock_guard<std::mutex> lk(mu);
+      owner.erase(k);
+      *status = s;
+      return nullptr;
+    };
+    if (k.geo < 0 || k.geo >= (int)geos.size()) return give_up(BG_INVALID_ARG);
     bg_h2_params prm;
     bg_h2_params_default(&prm);
     prm.keep_fp64_blocks = 0;  // the cache holds only what the products read
     bg_operator* op = nullptr;
-    bg_status s = bg_operator_create(w.ctx, geos[k.geo], k.M, k.P, k.kind, &prm, &op);
+    bg_status s;
+    {
+      std::lock_guard<std::mutex> lk(ops_mu);
+      s = bg_operator_create(w.ctx, geos[k.geo], k.M, k.P, k.kind, &prm, &op);
+    }
     if (s == BG_OK && k.kind != BG_LAPLACE_SL) s = bg_operator_set_wavenumber(op, k.kre, k.kim);
     size_t alloc = 0, est = 0;
     if (s == BG_OK) s = bg_operator_memory(op, &alloc, &est);
-    if (s == BG_OK && est > w.budget) s = BG_OOM;
-    if (s != BG_OK) {
-      if (op) bg_operator_destroy(op);
-      *status = s;
-      return nullptr;
+    if (s == BG_OK) {
+      std::unique_lock<std::mutex> lk(mu);
+      if (!reserve(lk, est)) s = BG_OOM;
     }
-    while (!w.cache.empty() && w.in_use + est > w.budget) evict_back(w);
+    if (s != BG_OK) {
+      if (op) destroy_op(op);
+      return give_up(s);
+    }
     const double t = now();
     s = bg_operator_assemble(op);
-    std::lock_guard<std::mutex> lk(mu);
+    std::unique_lock<std::mutex> lk(mu);
     st.assembly_s += now() - t;
+    --reserving;
     if (s != BG_OK) {
-      bg_operator_destroy(op);
+      in_use -= est;
+      update_usage();
+      owner.erase(k);
+      lk.unlock();
+      cv_idle.notify_all();
+      destroy_op(op);
       *status = s;
       return nullptr;
     }
-    w.cache.push_front(CacheEntry{k, op, est});
-    w.in_use += est;
+    CacheEntry e{k, op, est};
+    e.busy = true;
+    e.last_use = ++use_stamp;
+    w.cache.push_front(e);
     update_usage();
+    lk.unlock();
+    cv_idle.notify_all();
     return op;
+  }
+
+  // the worker is done with its front operator
+  void release_op(Worker& w) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      if (!w.cache.empty()) w.cache.front().busy = false;
+    }
+    cv_idle.notify_all();
   }
 
   void finish(Worker& w, std::vector<Job>& batch, bg_status status, int N, double t_start, bool hit, int tot,
@@ -205,6 +279,11 @@ struct bg_server {
       finish(w, batch, status, 0, t_start, hit, 0, stats);
       return;
     }
+    struct Release {  // the operator stops being busy however process returns
+      bg_server* s;
+      Worker& w;
+      ~Release() { s->release_op(w); }
+    } release{this, w};
     const int N = op->N;
     const size_t usz = op->cplx ? 16 : 8;
     int tot = 0;
@@ -246,8 +325,9 @@ struct bg_server {
       std::lock_guard<std::mutex> lk(mu);
       st.solve_s += now() - ts;
       if (measured && alloc > w.cache.front().bytes) {
-        w.in_use += alloc - w.cache.front().bytes;
+        in_use += alloc - w.cache.front().bytes;
         w.cache.front().bytes = alloc;
+        update_usage();
       }
     }
     finish(w, batch, status, N, t_start, hit, tot, stats);
@@ -259,14 +339,18 @@ struct bg_server {
       std::vector<Job> batch;
       {
         std::unique_lock<std::mutex> lk(mu);
+        // the oldest request whose operator this worker holds or no worker holds
         auto mine = [&] {
-          for (auto it = queue.begin(); it != queue.end(); ++it)
-            if (shard(key_of(it->req)) == w.id) return it;
+          for (auto it = queue.begin(); it != queue.end(); ++it) {
+            auto o = owner.find(key_of(it->req));
+            if (o == owner.end() || o->second == w.id) return it;
+          }
           return queue.end();
         };
         cv_work.wait(lk, [&] { return stop || mine() != queue.end(); });
         auto first = mine();
         if (first == queue.end()) break;  // stopping and nothing left for this worker
+        owner[key_of(first->req)] = w.id;
         batch.push_back(std::move(*first));
         queue.erase(first);
         int tot = batch[0].req.nrhs;
@@ -281,8 +365,20 @@ struct bg_server {
         }
       }
       process(w, batch);
+      cv_work.notify_all();  // requests for operators this worker gave up may be anyone's now
     }
-    while (!w.cache.empty()) evict_back(w);
+    std::unique_lock<std::mutex> lk(mu);
+    while (!w.cache.empty()) {
+      bg_operator* op = w.cache.back().op;
+      in_use -= w.cache.back().bytes;
+      owner.erase(w.cache.back().key);
+      w.cache.pop_back();
+      ++st.evictions;
+      update_usage();
+      lk.unlock();
+      destroy_op(op);
+      lk.lock();
+    }
   }
 };
 
@@ -304,7 +400,6 @@ bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers
       return BG_OOM;
     }
     w->id = i;
-    w->budget = hbm_budget_bytes / workers;
     bg_status st = bg_context_create(ctx->device, &w->ctx);
     if (st != BG_OK) {
       delete w;

@@ -376,8 +376,13 @@ typedef struct {
 } bg_server_stats;
 
 /* workers: 1 .. 16 worker threads, each with its own context (stream) on
- * ctx's device and budget / workers bytes; operators are sharded over them by
- * key, so solves on different operators overlap on the GPU */
+ * ctx's device; solves on different operators overlap on the GPU. An
+ * operator runs on the worker that assembled it (requests for it wait for
+ * that worker); a request for an operator no worker holds goes to the first
+ * free worker. hbm_budget_bytes is shared by all workers: an operator is
+ * admitted once its estimated footprint fits, after evicting the least
+ * recently used idle operators of any worker (waiting for busy ones when
+ * nothing idle is left); one larger than the whole budget fails with BG_OOM. */
 bg_status bg_server_create(bg_context* ctx, size_t hbm_budget_bytes, int workers, bg_server** out);
 /* stops the workers after the queue drains and frees every cached operator;
  * no other thread may be inside a bg_server_* call on srv meanwhile */

@@ -96,6 +96,39 @@ def test_server_evicts_under_budget(ctx):
         assert _residual(ctx, SPHERE, "laplace", M, 1, 0.0, 0, data, x) < 1e-7
 
 
+def test_server_budget_is_shared_by_workers(ctx):
+    """Two workers, a budget with room for the larger of two operators but
+    not for both, and less than twice it: the larger operator is admitted
+    (the budget is not split between the workers), and alternating requests
+    evict each other's operators across workers."""
+    import ctypes
+    import bembel_gb300 as bg
+    from bembel_gb300 import _lib
+    sizes = []
+    for M in (2, 3):
+        d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), M, 1), bg.LaplaceSingleLayerOperator(),
+                                keep_fp64_blocks=False)
+        a, e = ctypes.c_size_t(), ctypes.c_size_t()
+        ctx.check(_lib.load().bg_operator_memory(d.h, ctypes.byref(a), ctypes.byref(e)))
+        sizes.append(e.value)
+    budget = int(max(sizes) + min(sizes) // 2)
+    assert budget < 2 * max(sizes)
+    srv = bg.Server(ctx, budget, workers=2)
+    g = srv.add_geometry(bg.Geometry(SPHERE, ctx))
+    data = 3.0 * np.array([[0.0, 0.6, 0.8], [1.0, 0.0, 0.0]])
+    res = []
+    for M in (3, 2, 3, 2):
+        x, info = srv.wait(srv.submit(g, "laplace", M, 1, 0, data), timeout=300)
+        res.append((M, x, info))
+    st = srv.stats()
+    srv.close()
+    assert st["failed"] == 0 and st["evictions"] >= 3, st
+    assert st["bytes_in_use"] <= st["bytes_budget"]
+    for M, x, info in res:
+        assert info["status"] == 0
+        assert _residual(ctx, SPHERE, "laplace", M, 1, 0.0, 0, data, x) < 1e-7
+
+
 def test_server_rejects_operator_above_budget(ctx):
     import bembel_gb300 as bg
     from bembel_gb300 import _lib
