@@ -17,6 +17,8 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
 LAPLACE, HELMHOLTZ, MAXWELL, DUMMY = 0, 1, 2, 3
+# the analytic cube sphere (six x/|x| images of the cube faces) as a geometry name
+CUBE_SPHERE = "analytic:cube_sphere"
 DENSE, LOWRANK = 2, 1
 
 
