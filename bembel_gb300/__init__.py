@@ -380,17 +380,19 @@ class DiscreteOperator:
 
     # -- launch plans and the autotuner --
     def set_plan(self, nrhs, precision="mixed", near_kernel=0, split_k_batches=-1, far_order=0, transforms=0,
-                 far_ctas=0, mixed_near=0):
+                 far_ctas=0, mixed_near=0, far_tiles=0):
         """Kernel variants and schedules of products with nrhs right-hand
-        sides at precision (bg_launch_plan; {0, -1, 0, 0, 0, 0} is the built-in plan)."""
-        p = _lib.LaunchPlan(near_kernel, split_k_batches, far_order, transforms, far_ctas, mixed_near)
+        sides at precision (bg_launch_plan; all zeros but split_k_batches = -1
+        is the built-in plan)."""
+        p = _lib.LaunchPlan(near_kernel, split_k_batches, far_order, transforms, far_ctas, mixed_near, far_tiles)
         self.ctx.check(_lib.load().bg_operator_set_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
 
     def get_plan(self, nrhs, precision="mixed"):
         p = _lib.LaunchPlan()
         self.ctx.check(_lib.load().bg_operator_get_plan(self.h, nrhs, _prec_code(precision), ctypes.byref(p)))
         return {"near_kernel": p.near_kernel, "split_k_batches": p.split_k_batches, "far_order": p.far_order,
-                "transforms": p.transforms, "far_ctas": p.far_ctas, "mixed_near": p.mixed_near}
+                "transforms": p.transforms, "far_ctas": p.far_ctas, "mixed_near": p.mixed_near,
+                "far_tiles": p.far_tiles}
 
     def autotune(self, nrhs, precision="mixed", reps=5):
         """Time the product's kernel variants for nrhs right-hand sides at
@@ -400,7 +402,8 @@ class DiscreteOperator:
         return {"candidates": r.candidates, "builtin_ms": r.builtin_ms, "tuned_ms": r.tuned_ms,
                 "plan": {"near_kernel": r.plan.near_kernel, "split_k_batches": r.plan.split_k_batches,
                          "far_order": r.plan.far_order, "transforms": r.plan.transforms,
-                         "far_ctas": r.plan.far_ctas, "mixed_near": r.plan.mixed_near}}
+                         "far_ctas": r.plan.far_ctas, "mixed_near": r.plan.mixed_near,
+                         "far_tiles": r.plan.far_tiles}}
 
     # -- inspection --
     def elements(self):

@@ -37,7 +37,7 @@ class SolveStats(ctypes.Structure):
 class LaunchPlan(ctypes.Structure):
     _fields_ = [("near_kernel", ctypes.c_int), ("split_k_batches", ctypes.c_int), ("far_order", ctypes.c_int),
                 ("transforms", ctypes.c_int), ("far_ctas", ctypes.c_int),
-                ("mixed_near", ctypes.c_int)]
+                ("mixed_near", ctypes.c_int), ("far_tiles", ctypes.c_int)]
 
 
 class TuneReport(ctypes.Structure):

@@ -1616,7 +1616,8 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16_btiles(T, op->leaf_level + 1, np2, nrhs, s); }),
                "right-hand-side tiles");
       BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16(T, op->far_work(pl.far_order), op->n_far_work,
-                                                                       np2, nrhs, op->d_err.as<int>(), s, pl.far_ctas); }),
+                                                                       np2, nrhs, op->d_err.as<int>(), s, pl.far_ctas,
+                                                                       pl.far_tiles == 1); }),
                "far-field product (stored FP16 tiles, tensor cores)");
     } else if (tcc) {
       // complex kernel: stored FP16 tiles of Re K and Im K, 16 complex columns
@@ -1930,7 +1931,7 @@ extern "C" bg_status bg_operator_set_plan(bg_operator* op, int nrhs, int precisi
   if (plan->near_kernel < 0 || plan->near_kernel > 3 || plan->split_k_batches < -1 ||
       plan->split_k_batches > (1 << 24) || plan->far_order < 0 || plan->far_order > 2 || plan->transforms < 0 ||
       plan->transforms > 1 || plan->far_ctas < 0 || plan->far_ctas > 2 || plan->mixed_near < 0 ||
-      plan->mixed_near > 2)
+      plan->mixed_near > 2 || plan->far_tiles < 0 || plan->far_tiles > 1)
     return set_error(op->ctx, BG_INVALID_ARG, "launch plan: a field is out of range");
   op->plans[bg_operator::plan_key(nrhs, precision)] = *plan;
   op->drop_graphs();

@@ -413,7 +413,8 @@ __device__ __forceinline__ float h16_scale(float max_abs) {
 // SM, twice the blocks in flight: 0.469 -> 0.363 ms per launch at c2). The
 // built-in choice takes two CTAs per SM when there are at least as many rows
 // as CTAs (launch plan far_ctas)
-template <int NP2, int NSTAGE, int MINB>
+// HI: the hi coupling tiles only (hi*hi and hi*lo, the lo tiles not read)
+template <int NP2, int NSTAGE, int MINB, bool HI>
 __global__ void __launch_bounds__(kStoredThreads, MINB)
     k_far_h16(FarH16Tiles T, const int2* __restrict__ work, int nwork, int nrhs, int* __restrict__ err) {
   // Persistent: CTA c takes the rows c, c + gridDim.x, ... of the work list
@@ -469,8 +470,8 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
           const unsigned char* ga = atiles + (size_t)k * G::ASTRIDE;
           const unsigned char* gb = btiles + (size_t)col[k] * G::B2;
           // hi and lo tiles are contiguous in global and shared memory: one copy each for A and B
-          mbar_expect_tx(&full_bar[st], G::STAGE);
-          bulk_g2s(sm, ga, G::A2, &full_bar[st]);
+          mbar_expect_tx(&full_bar[st], (HI ? G::A_BYTES : G::A2) + G::B2);
+          bulk_g2s(sm, ga, HI ? G::A_BYTES : G::A2, &full_bar[st]);
           bulk_g2s(sm + G::A2, gb, G::B2, &full_bar[st]);
         }
       }
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(kStoredThreads, MINB)
           const uint32_t b0 = a0 + G::A2, b1 = b0 + G::B_BYTES;
           const uint32_t d_hh = tmem + (uint32_t)(64 * ab), d_cr = d_hh + 32;
 #pragma unroll
-          for (int pass = 0; pass < 3; ++pass) {
+          for (int pass = 0; pass < (HI ? 2 : 3); ++pass) {
             uint64_t ad = umma_desc(pass == 2 ? a1 : a0, 128, G::SBOA);
             uint64_t bd = umma_desc(pass == 1 ? b1 : b0, 128, G::SBO);
             const uint32_t dd = pass == 0 ? d_hh : d_cr;
@@ -740,8 +741,27 @@ cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int
   return cudaGetLastError();
 }
 
+template <int N, bool HI>
+static cudaError_t far_h16_launch(const FarH16Tiles& T, const int2* work, int nwork, int nrhs, int* err,
+                                  cudaStream_t s, int ctas_per_sm, int nsm) {
+  if (ctas_per_sm == 2) {
+    constexpr uint32_t smem = H16Shape<N, 2, true>::SMEM;
+    static_assert(2 * smem <= 220 * 1024, "FP16 far field: two CTAs per SM do not fit");
+    cudaError_t e = smem_limit(k_far_h16<N, 2, 2, HI>, smem);
+    if (e != cudaSuccess) return e;
+    k_far_h16<N, 2, 2, HI><<<std::min(nwork, 2 * nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err);
+    return cudaGetLastError();
+  }
+  constexpr uint32_t smem = H16Shape<N, kH16Stages, true>::SMEM;
+  static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");
+  cudaError_t e = smem_limit(k_far_h16<N, kH16Stages, 1, HI>, smem);
+  if (e != cudaSuccess) return e;
+  k_far_h16<N, kH16Stages, 1, HI><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                           cudaStream_t s, int ctas_per_sm) {
+                           cudaStream_t s, int ctas_per_sm, bool hi_only) {
   if (nwork == 0) return cudaSuccess;
   if (!far_tc_supported(false, np2, nrhs)) return cudaErrorInvalidValue;
   // persistent CTAs: one or two per SM
@@ -752,23 +772,10 @@ cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, in
   // built-in: two CTAs per SM when every CTA still gets a row
   if (ctas_per_sm != 1 && ctas_per_sm != 2) ctas_per_sm = nwork >= 2 * nsm ? 2 : 1;
   switch (np2) {
-#define BG_T(N)                                                                                             \
-  case N: {                                                                                                 \
-    if (ctas_per_sm == 2) {                                                                                 \
-      constexpr uint32_t smem = H16Shape<N, 2, true>::SMEM;                                                 \
-      static_assert(2 * smem <= 220 * 1024, "FP16 far field: two CTAs per SM do not fit");                  \
-      cudaError_t e = smem_limit(k_far_h16<N, 2, 2>, smem);                                                 \
-      if (e != cudaSuccess) return e;                                                                       \
-      k_far_h16<N, 2, 2><<<std::min(nwork, 2 * nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err); \
-      return cudaGetLastError();                                                                            \
-    }                                                                                                       \
-    constexpr uint32_t smem = H16Shape<N, kH16Stages, true>::SMEM;                                          \
-    static_assert(smem <= 227 * 1024, "FP16 far field: shared memory plan too large");                      \
-    cudaError_t e = smem_limit(k_far_h16<N, kH16Stages, 1>, smem);                                          \
-    if (e != cudaSuccess) return e;                                                                         \
-    k_far_h16<N, kH16Stages, 1><<<std::min(nwork, nsm), kStoredThreads, smem, s>>>(T, work, nwork, nrhs, err); \
-    return cudaGetLastError();                                                                              \
-  }
+#define BG_T(N)                                                                                            \
+  case N:                                                                                                  \
+    return hi_only ? far_h16_launch<N, true>(T, work, nwork, nrhs, err, s, ctas_per_sm, nsm)              \
+                   : far_h16_launch<N, false>(T, work, nwork, nrhs, err, s, ctas_per_sm, nsm);
     BG_H16_SHAPES(BG_T)
 #undef BG_T
     default: return cudaErrorInvalidValue;

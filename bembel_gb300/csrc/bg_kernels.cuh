@@ -163,8 +163,9 @@ cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long
 cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s);
 // ctas_per_sm: 1 one CTA of four stages per SM, 2 two CTAs of two stages,
 // otherwise the built-in choice (2 when there are at least 2 x SMs rows)
+// hi_only: the FP16 hi coupling tiles only (two products per block instead of three)
 cudaError_t launch_far_h16(const FarH16Tiles& T, const int2* work, int nwork, int np2, int nrhs, int* err,
-                           cudaStream_t s, int ctas_per_sm = 0);
+                           cudaStream_t s, int ctas_per_sm = 0, bool hi_only = false);
 // watchdog self-test: a bounded wait that cannot complete; sets *err = 99 when it runs out
 cudaError_t launch_wait_selftest(long long limit_cycles, int* err, cudaStream_t s);
 // real kernels, n_p^2 <= 128 within the shared-memory limit, nrhs <= 32

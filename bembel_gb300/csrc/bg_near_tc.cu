@@ -221,23 +221,41 @@ __global__ void k_oz_col_exp(const double* __restrict__ x, long rows, int ld, in
 }
 
 // x digit tiles: cluster J = row / B, local row j = row % B, digit t, column
-// c at J PANEL_X + t XBLK + kmajor_off(c, j, SBO_X); columns >= nc get zeros
+// c at J PANEL_X + t XBLK + kmajor_off(c, j, SBO_X); columns >= nc and rows
+// j >= B of a cluster get zeros. A thread takes 8 consecutive rows of one
+// column (one 16-byte core-matrix row per digit), so a warp's stores are
+// whole 128-byte core matrices and its loads whole rows of x.
 template <int B>
 __global__ void k_oz_split_x(const double* __restrict__ x, long rows, int ld, int c0, int nc,
                              const int* __restrict__ fmax, __half* __restrict__ panels) {
   using G = OzShape<B>;
+  constexpr int NG = (B + 7) / 8;  // groups of 8 rows holding the cluster's rows
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= rows * kOzCols) return;
-  const long row = t >> 5;
+  const long ncl = rows / B;
+  if (t >= ncl * NG * kOzCols) return;
   const int c = (int)(t & 31);
-  const double v = c < nc ? x[row * ld + c0 + c] : 0.0;
-  int d[kOzDigits];
-  oz_digits(v, fmax[c] - 1021, d);
-  const long J = row / B;
-  const int j = (int)(row - J * B);
-  unsigned char* base = reinterpret_cast<unsigned char*>(panels) + (size_t)J * G::PANEL_X + kmajor_off(c, j, G::SBO_X);
+  const long q = t >> 5;
+  const long J = q / NG;
+  const int g = (int)(q - J * NG);
+  const int f = fmax[c] - 1021;
+  uint32_t w[kOzDigits][4];
 #pragma unroll
-  for (int s = 0; s < kOzDigits; ++s) *reinterpret_cast<__half*>(base + s * G::XBLK) = __int2half_rn(d[s]);
+  for (int i = 0; i < 8; ++i) {
+    const int j = g * 8 + i;
+    const double v = (j < B && c < nc) ? x[(J * B + j) * ld + c0 + c] : 0.0;
+    int d[kOzDigits];
+    oz_digits(v, f, d);
+#pragma unroll
+    for (int s = 0; s < kOzDigits; ++s) {
+      const uint32_t h = (uint32_t)__half_as_ushort(__int2half_rn(d[s]));
+      if (i & 1) w[s][i >> 1] |= h << 16;
+      else w[s][i >> 1] = h;
+    }
+  }
+  unsigned char* base = reinterpret_cast<unsigned char*>(panels) + (size_t)J * G::PANEL_X + kmajor_off(c, g * 8, G::SBO_X);
+#pragma unroll
+  for (int s = 0; s < kOzDigits; ++s)
+    *reinterpret_cast<uint4*>(base + s * G::XBLK) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
 template <int B>
@@ -496,7 +514,7 @@ cudaError_t launch_near_oz(const int* row_ptr, const int* col, int nrows, int B,
     e = cudaMemsetAsync(fmax, 0, kOzCols * sizeof(int), s);
     if (e != cudaSuccess) return e;
     k_oz_col_exp<<<2 * nsm, 256, 0, s>>>(x, xrows, ldx, c0, nc, fmax);
-    const long nt = xrows * kOzCols;
+    const long nt = (xrows / B) * ((B + 7) / 8) * kOzCols;
     const unsigned blocks = (unsigned)((nt + 255) / 256);
     switch (B) {
 #define BG_C(N)                                                                                                 \

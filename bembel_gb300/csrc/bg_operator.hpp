@@ -277,7 +277,7 @@ struct bg_operator {
   // launch plans per (nrhs, precision), keyed as the graphs
   std::map<long, bg_launch_plan> plans;
   static long plan_key(int nrhs, int prec) { return (long)nrhs * 4 + prec; }
-  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0, 0, 0, 0}; }
+  static bg_launch_plan builtin_plan() { return bg_launch_plan{0, -1, 0, 0, 0, 0, 0}; }
   bg_launch_plan plan_for(int nrhs, int prec) const {
     auto it = plans.find(plan_key(nrhs, prec));
     return it == plans.end() ? builtin_plan() : it->second;

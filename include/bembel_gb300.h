@@ -311,6 +311,13 @@ typedef struct bg_launch_plan {
    * (32 columns only, else 1). All agree with the FP64 product to about
    * 1e-14 relative or better. */
   int mixed_near;
+  /* couplings of the stored-tile far field of real operators (BG_PREC_MIXED,
+   * BG_PREC_FP32): 0 built-in, the FP16 hi and lo tiles (three products per
+   * block, about 22 bits of every coupling, product error about 2e-7);
+   * 1 the FP16 hi tiles only (two products, half the bytes streamed, about
+   * 11 bits, product error about 1e-4): an inner operator for solvers that
+   * refine in FP64, which absorb the error in their outer iterations. */
+  int far_tiles;
 } bg_launch_plan;
 
 typedef struct bg_tune_report {

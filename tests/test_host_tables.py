@@ -182,14 +182,16 @@ def test_launch_plans_round_trip_and_validation(bg_host):
     bg, ctx = bg_host
     d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 2, 2), bg.LaplaceSingleLayerOperator())
     builtin = {"near_kernel": 0, "split_k_batches": -1, "far_order": 0, "transforms": 0, "far_ctas": 0,
-               "mixed_near": 0}
+               "mixed_near": 0, "far_tiles": 0}
     assert d.get_plan(32, "mixed") == builtin
-    d.set_plan(32, "fp32", near_kernel=2, split_k_batches=608, far_order=2, transforms=1, far_ctas=2, mixed_near=2)
+    d.set_plan(32, "fp32", near_kernel=2, split_k_batches=608, far_order=2, transforms=1, far_ctas=2, mixed_near=2,
+               far_tiles=1)
     assert d.get_plan(32, "fp32") == {"near_kernel": 2, "split_k_batches": 608, "far_order": 2, "transforms": 1,
-                                      "far_ctas": 2, "mixed_near": 2}
+                                      "far_ctas": 2, "mixed_near": 2, "far_tiles": 1}
     assert d.get_plan(32, "mixed") == builtin and d.get_plan(16, "fp32") == builtin
     for bad in ({"near_kernel": 4}, {"near_kernel": -1}, {"split_k_batches": -2}, {"far_order": 3}, {"transforms": 2},
-                {"transforms": -1}, {"far_ctas": 3}, {"far_ctas": -1}, {"mixed_near": 3}, {"mixed_near": -1}):
+                {"transforms": -1}, {"far_ctas": 3}, {"far_ctas": -1}, {"mixed_near": 3}, {"mixed_near": -1},
+                {"far_tiles": 2}, {"far_tiles": -1}):
         with pytest.raises(BembelError):
             d.set_plan(8, "mixed", **bad)
     with pytest.raises(BembelError):
