@@ -768,6 +768,8 @@ extern "C" bg_status bg_operator_leaf_block(const bg_operator* op, long leaf, in
       cc >= op->vd)
     return BG_INVALID_ARG;
   if (op->ctx->device < 0 || !op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
+  if (op->kbatched())
+    return set_error(op->ctx, BG_UNSUPPORTED, "leaf blocks of batched wavenumbers: assemble one wavenumber to inspect");
   const int cls = op->part.leaf_list[4 * leaf];
   const BsrSegment* seg = nullptr;
   const DevBuf* data = nullptr;
@@ -1233,6 +1235,39 @@ extern "C" bg_status bg_operator_release_wavenumbers(bg_operator* op) {
 
 extern "C" bg_status bg_operator_assemble(bg_operator* op);
 
+// Batched products in one pass over all wavenumbers: right-hand-side tile
+// buffers per (wavenumber, level) and the far-field work list over those
+// indexes (every row of every wavenumber, heaviest first as in the
+// one-wavenumber list). Left unset, so that low-precision products go one
+// wavenumber at a time, when a wavenumber has no tiles or the indexes exceed
+// the tile bound.
+static bg_status setup_kbatch(bg_operator* op) {
+  const int nk = (int)op->kslots.size(), nlev = op->leaf_level + 1, np2 = op->np * op->np;
+  op->kb_nwork = 0;
+  if (op->n_far_work == 0 || nk * nlev > kMaxTileLevels) return BG_OK;
+  for (const auto& k : op->kslots)
+    if (!k.far_tiles) return BG_OK;
+  const size_t tb = far_h16c_btile_bytes(np2);
+  if (tb == 0) return BG_OK;
+  for (int q = 0; q < nk; ++q)
+    for (int l = 0; l < nlev; ++l) {
+      op->kb_btiles.push_back(new DevBuf());
+      op->kb_binv.push_back(new DevBuf());
+      BG_CHECK(op->kb_btiles.back()->alloc(tb * op->nclusters(l)), "batched right-hand-side tiles");
+      BG_CHECK(op->kb_binv.back()->alloc(sizeof(float) * 32 * op->nclusters(l)), "batched right-hand-side tiles");
+    }
+  std::vector<int2> base(op->n_far_work), work;
+  BG_CHECK(cudaMemcpy(base.data(), op->d_far_work.p, base.size() * sizeof(int2), cudaMemcpyDeviceToHost),
+           "far-field work list");
+  work.reserve(base.size() * nk);
+  for (const int2& it : base)
+    for (int q = 0; q < nk; ++q) work.push_back(make_int2(q * nlev + it.x, it.y));
+  BG_CHECK(op->kb_work.upload(work, op->ctx->stream), "far-field work list");
+  BG_CHECK(cudaStreamSynchronize(op->ctx->stream), "far-field work list");
+  op->kb_nwork = (int)work.size();
+  return BG_OK;
+}
+
 extern "C" bg_status bg_operator_assemble_wavenumbers(bg_operator* op) {
   if (!op) return BG_INVALID_ARG;
   if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: assembly needs a GPU");
@@ -1286,6 +1321,11 @@ extern "C" bg_status bg_operator_assemble_wavenumbers(bg_operator* op) {
   op->kslot_active = -1;
   op->kre = kre0;
   op->kim = kim0;
+  if (bg_status st = setup_kbatch(op)) {
+    op->free_slots();
+    op->assembled = false;
+    return st;
+  }
   op->t_far = t_far;
   op->t_near = t_near;
   op->t_total = t_far + t_near;
@@ -1480,7 +1520,31 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
   const bg_launch_plan pl = op->plan_for(nrhs, prec);
   bool any_far = false;
   for (const auto& f : op->far) any_far |= !f.col.empty();
-  if (near32) {
+  if (op->kbatched()) {
+    // batched wavenumbers: wavenumber q's near field on column block q (the
+    // block is copied out of the row-major superspace vectors and back)
+    const int nk = (int)op->kslots.size(), nr = nrhs / nk;
+    if (near32)
+      BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
+    const size_t es = op->scalar_bytes(near32);
+    const char* xs = static_cast<const char*>(near32 ? op->w_xss32.p : op->w_xss.p);
+    char* ys = static_cast<char*>(near32 ? op->w_yss32.p : op->w_yss.p);
+    for (int q = 0; q < nk; ++q) {
+      BG_CHECK(cudaMemcpy2DAsync(op->kb_xs.p, nr * es, xs + (size_t)q * nr * es, (size_t)nrhs * es, nr * es, op->S,
+                                 cudaMemcpyDeviceToDevice, s), "near-field column block");
+      const bg_operator::KSlot& k = op->kslots[q];
+      BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] {
+                 return near32 ? launch_bsr_fp32(true, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), k.dense32.p,
+                                                 op->block_stride32(op->dense.B), op->dense.nrows, op->dense.B,
+                                                 op->kb_xs.p, op->kb_ys.p, nr, 0, s, pl.near_kernel)
+                               : launch_bsr_fp64(true, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), k.dense64.p,
+                                                 op->block_stride(op->dense.B), op->dense.nrows, op->dense.B,
+                                                 op->kb_xs.p, op->kb_ys.p, nr, 0, s); }),
+               "near-field product (batched wavenumbers)");
+      BG_CHECK(cudaMemcpy2DAsync(ys + (size_t)q * nr * es, (size_t)nrhs * es, op->kb_ys.p, nr * es, nr * es, op->S,
+                                 cudaMemcpyDeviceToDevice, s), "near-field column block");
+    }
+  } else if (near32) {
     // FP32 near field into the FP32 accumulator the far field adds to
     BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_convert(S64, Sfar, op->w_xss.p, ss_n, op->w_xss32.p, s); }), "x to FP32");
     BG_CHECK(timed_launch(op->ctx, KC_NEAR, [&] { return launch_bsr_fp32(op->cplx, op->dense.d_row_ptr.as<int>(), op->dense.d_col.as<int>(), op->d_dense32.p,
@@ -1598,7 +1662,35 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
     const bool tc = mixed && op->vd == 1 && op->nc == 1 && op->leaf_level < kMaxFarLevels &&
                     far_tc_supported(op->cplx, np2, nrhs);
     const bool tcc = mixed && op->cplx && op->far_tiles && op->leaf_level < kMaxFarLevels;
-    if (tc && op->far_tiles) {
+    const bool tcc_kb = mixed && op->kbatched() && op->kb_nwork > 0;
+    if (tcc_kb) {
+      // batched wavenumbers: one launch per 16 columns covers every
+      // wavenumber's stored tiles (level index q (L + 1) + l), each applied
+      // to its own column block of Y
+      const int nk = (int)op->kslots.size(), nr = nrhs / nk, nlev = op->leaf_level + 1;
+      FarH16Tiles T{};
+      for (int q = 0; q < nk; ++q)
+        for (int l = 0; l < nlev; ++l) {
+          const int v = q * nlev + l;
+          T.row_ptr[v] = op->far[l].d_row_ptr.as<int>();
+          T.col[v] = op->far[l].d_col.as<int>();
+          T.a[v] = static_cast<const unsigned char*>(op->kslots[q].atiles[l]->p);
+          T.ainv[v] = op->kslots[q].ainv[l]->as<float>();
+          T.b[v] = static_cast<unsigned char*>(op->kb_btiles[v]->p);
+          T.binv[v] = op->kb_binv[v]->as<float>();
+          T.y[v] = reinterpret_cast<const float*>(static_cast<const char*>(op->w_y[l]->p) + (size_t)q * nr * sfar);
+          T.z[v] = reinterpret_cast<float*>(static_cast<char*>(op->w_z[l]->p) + (size_t)q * nr * sfar);
+          T.ncl[v] = op->nclusters(l);
+        }
+      for (int c0 = 0; c0 < nr; c0 += 16) {
+        const int nc = std::min(16, nr - c0);
+        BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_build_h16c_btiles(T, nk * nlev, np2, nrhs, c0, nc, s); }),
+                 "right-hand-side tiles");
+        BG_CHECK(timed_launch(op->ctx, KC_FAR_FUSED, [&] { return launch_far_h16c(T, op->kb_work.as<int2>(), op->kb_nwork,
+                                                                           np2, nrhs, c0, nc, op->d_err.as<int>(), s); }),
+                 "far-field product (batched wavenumbers, stored complex FP16 tiles, tensor cores)");
+      }
+    } else if (tc && op->far_tiles) {
       // stored FP16 tiles streamed by TMA bulk copies; all levels in one
       // launch, which writes every row of Z
       FarH16Tiles T{};
@@ -1682,14 +1774,15 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
     }
     // complex FP64 far product of level l on the double-float pipes: z (rows
     // of ld complex entries) = K y, 16 columns per pass, Kr split(y) + Ki split(i y)
-    auto far64_cplx = [&](int l, const void* y, int ld, void* z) -> bg_status {
+    // (columns cb .. cb + ncols - 1 of rows of ld, with the pairs df)
+    auto far64_cplx = [&](int l, const DevBuf* df, const void* y, int ld, int cb, int ncols, void* z) -> bg_status {
       const BsrSegment& f = op->far[l];
       const long sdf = ((long)f.B * f.B + 1) / 2 * 2;
-      const float2* kr = op->d_far_df[l]->as<float2>();
+      const float2* kr = df->as<float2>();
       const float2* ki = kr + (long)f.col.size() * sdf;
       const long rows = (long)op->nclusters(l) * f.B;
-      for (int c0 = 0; c0 < ld; c0 += 16) {
-        const int nc = std::min(16, ld - c0);
+      for (int c0 = cb; c0 < cb + ncols; c0 += 16) {
+        const int nc = std::min(16, cb + ncols - c0);
         for (int part = 0; part < 2; ++part) {
           BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df_cols(y, rows, ld, c0, nc, part,
                                                                                   op->w_ydf[l]->p, s); }),
@@ -1703,7 +1796,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
       }
       return BG_OK;
     };
-    for (int l = 0; l <= op->leaf_level && !tc && !tcc; ++l) {
+    for (int l = 0; l <= op->leaf_level && !tc && !tcc && !tcc_kb; ++l) {
       const BsrSegment& f = op->far[l];
       if (f.col.empty()) {
         BG_CHECK(cudaMemsetAsync(op->w_z[l]->p, 0, (size_t)op->vd * op->nclusters(l) * op->R * nrhs * sfar, s),
@@ -1729,7 +1822,7 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
                                       op->w_yv[l]->p, op->w_zv[l]->p, 4 * nr, s); }),
                      "far-field product (FP32 fused, Maxwell)");
           else if (op->d_far_df[l]->p) {
-            bg_status st = far64_cplx(l, op->w_yv[l]->p, 4 * nr, op->w_zv[l]->p);
+            bg_status st = far64_cplx(l, op->d_far_df[l], op->w_yv[l]->p, 4 * nr, 0, 4 * nr, op->w_zv[l]->p);
             if (st != BG_OK) return st;
           } else
             BG_CHECK(timed_launch(op->ctx, KC_FAR64, [&] { return launch_bsr_fp64(true, f.d_row_ptr.as<int>(), f.d_col.as<int>(), op->d_far64[l]->p,
@@ -1749,8 +1842,15 @@ static bg_status apply_middle(bg_operator* op, int nrhs, int prec) {
                  "far-field product (FP32 fused)");
       } else {
         if (!op->store_far) return set_error(op->ctx, BG_UNSUPPORTED, "the FP64 product needs the stored far field");
-        if (op->cplx && op->d_far_df[l]->p) {
-          bg_status st = far64_cplx(l, op->w_y[l]->p, nrhs, op->w_z[l]->p);
+        if (op->kbatched()) {
+          // batched wavenumbers: wavenumber q's double-float pairs on column block q
+          const int nk = (int)op->kslots.size(), nr = nrhs / nk;
+          for (int q = 0; q < nk; ++q) {
+            bg_status st = far64_cplx(l, op->kslots[q].far_df[l], op->w_y[l]->p, nrhs, q * nr, nr, op->w_z[l]->p);
+            if (st != BG_OK) return st;
+          }
+        } else if (op->cplx && op->d_far_df[l]->p) {
+          bg_status st = far64_cplx(l, op->d_far_df[l], op->w_y[l]->p, nrhs, 0, nrhs, op->w_z[l]->p);
           if (st != BG_OK) return st;
         } else if (!op->cplx && op->d_far_df[l]->p) {
           BG_CHECK(timed_launch(op->ctx, KC_OTHER, [&] { return launch_split_df(op->w_y[l]->p, (long)op->nclusters(l) * op->R * nrhs,
@@ -1852,8 +1952,33 @@ static bg_status apply_wavenumber_blocks(bg_operator* op, int nrhs, int prec, co
   return st;
 }
 
+// Whether a product of batched wavenumbers can run as one pass over all of
+// them: the FP64 product needs every wavenumber's double-float far field, the
+// low-precision ones the tile setup of bg_operator_assemble_wavenumbers.
+static bool kbatch_one_pass(const bg_operator* op, int prec) {
+  bool any_far = false;
+  for (const auto& f : op->far) any_far |= !f.col.empty();
+  if (!any_far) return true;
+  if (prec != BG_PREC_FP64) return op->kb_nwork > 0;
+  for (const auto& k : op->kslots)
+    for (int l = 0; l <= op->leaf_level; ++l)
+      if (!op->far[l].col.empty() && ((int)k.far_df.size() <= l || !k.far_df[l]->p)) return false;
+  return true;
+}
+
 bg_status apply_operator(bg_operator* op, int nrhs, int prec, const void* xdof, void* ydof) {
-  if (op->kbatched()) return apply_wavenumber_blocks(op, nrhs, prec, xdof, ydof);
+  if (op->kbatched()) {
+    if (!kbatch_one_pass(op, prec)) return apply_wavenumber_blocks(op, nrhs, prec, xdof, ydof);
+    const int nk = (int)op->kslots.size();
+    if (nrhs % nk)
+      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+    const size_t blk = (size_t)op->S * (nrhs / nk) * op->scalar_bytes(false);
+    if (op->kb_xs.bytes < blk) {
+      op->drop_graphs();  // the column blocks of the near fields move
+      BG_CHECK(op->kb_xs.alloc(blk), "near-field column blocks");
+      BG_CHECK(op->kb_ys.alloc(blk), "near-field column blocks");
+    }
+  }
   cudaStream_t s = op->ctx->stream;
   const int S64 = op->stype(false);
   BG_CHECK(timed_launch(op->ctx, KC_TAPPLY, [&] { return launch_csr_apply(S64, op->d_T_ptr.as<int>(), op->d_T_idx.as<int>(), op->d_T_val.as<double>(), op->S, xdof,
@@ -2062,41 +2187,14 @@ static bg_status stage_host(bg_context* ctx, DevBuf* buf, const void* host, long
   return cuda_status(ctx, e, "host to device copy");
 }
 
-extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
-                               const double* alpha, const double* beta, int precision, int on_device) {
-  if (!op || nrhs < 0) return BG_INVALID_ARG;
-  if (nrhs == 0) return BG_OK;  // no columns: nothing to do (as Eigen's empty product)
-  if (!x || !y || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
-  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
-  if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
-  if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED && precision != BG_PREC_FP32)
-    return set_error(op->ctx, BG_INVALID_ARG, "precision");
-  const double one[2] = {1.0, 0.0}, zero2[2] = {0.0, 0.0};
-  if (!alpha) alpha = one;
-  if (!beta) beta = zero2;
-  if (!op->cplx && (alpha[1] != 0.0 || beta[1] != 0.0))
-    return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
-  cudaSetDevice(op->ctx->device);
-  if (op->kbatched()) {
-    // column block q through wavenumber slot q
-    const int nk = (int)op->kslots.size();
-    if (nrhs % nk)
-      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
-    const int nr = nrhs / nk;
-    bg_status st = BG_OK;
-    for (int q = 0; q < nk && st == BG_OK; ++q) {
-      op->activate_slot(q);
-      st = bg_matvec(op, static_cast<const char*>(x) + (size_t)q * nr * ldx * 16, ldx,
-                     static_cast<char*>(y) + (size_t)q * nr * ldy * 16, ldy, nr, alpha, beta, precision, on_device);
-    }
-    op->activate_slot(-1);
-    return st;
-  }
+// The product in chunks of at most `chunk` columns.
+static bg_status matvec_chunks(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
+                               const double* alpha, const double* beta, int precision, int on_device, int chunk) {
   cudaStream_t s = op->ctx->stream;
   const size_t usz = op->cplx ? 16 : 8;
   const int uS = op->cplx ? 1 : 0;
-  for (int c0 = 0; c0 < nrhs; c0 += 32) {
-    const int k = std::min(32, nrhs - c0);
+  for (int c0 = 0; c0 < nrhs; c0 += chunk) {
+    const int k = std::min(chunk, nrhs - c0);
     bg_status st = ensure_work(op, k);
     if (st != BG_OK) return st;
     const char* xp = static_cast<const char*>(x) + (size_t)c0 * ldx * usz;
@@ -2122,4 +2220,72 @@ extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y
   }
   BG_CHECK(cudaStreamSynchronize(s), "H2 matvec");
   return check_device_flag(op);
+}
+
+extern "C" bg_status bg_matvec(bg_operator* op, const void* x, long ldx, void* y, long ldy, int nrhs,
+                               const double* alpha, const double* beta, int precision, int on_device) {
+  if (!op || nrhs < 0) return BG_INVALID_ARG;
+  if (nrhs == 0) return BG_OK;  // no columns: nothing to do (as Eigen's empty product)
+  if (!x || !y || ldx < op->N || ldy < op->N) return BG_INVALID_ARG;
+  if (op->ctx->device < 0) return set_error(op->ctx, BG_UNSUPPORTED, "host-only context: products need a GPU");
+  if (!op->assembled) return set_error(op->ctx, BG_INVALID_ARG, "operator not assembled");
+  if (precision != BG_PREC_FP64 && precision != BG_PREC_MIXED && precision != BG_PREC_FP32)
+    return set_error(op->ctx, BG_INVALID_ARG, "precision");
+  const double one[2] = {1.0, 0.0}, zero2[2] = {0.0, 0.0};
+  if (!alpha) alpha = one;
+  if (!beta) beta = zero2;
+  if (!op->cplx && (alpha[1] != 0.0 || beta[1] != 0.0))
+    return set_error(op->ctx, BG_INVALID_ARG, "complex scalars for a real operator");
+  cudaSetDevice(op->ctx->device);
+  if (op->kbatched()) {
+    const int nk = (int)op->kslots.size();
+    if (nrhs % nk)
+      return set_error(op->ctx, BG_INVALID_ARG, "batched wavenumbers: columns must be a multiple of the wavenumbers");
+    const int nr = nrhs / nk;
+    if (!kbatch_one_pass(op, precision)) {
+      // column block q through wavenumber slot q, one wavenumber at a time
+      bg_status st = BG_OK;
+      for (int q = 0; q < nk && st == BG_OK; ++q) {
+        op->activate_slot(q);
+        st = bg_matvec(op, static_cast<const char*>(x) + (size_t)q * nr * ldx * 16, ldx,
+                       static_cast<char*>(y) + (size_t)q * nr * ldy * 16, ldy, nr, alpha, beta, precision, on_device);
+      }
+      op->activate_slot(-1);
+      return st;
+    }
+    // one pass over all wavenumbers per chunk: the columns are permuted on the
+    // device so that every chunk holds an equal slice of every block, in
+    // block order (what the batched product expects), then permuted back
+    cudaStream_t s = op->ctx->stream;
+    const int w = std::max(1, std::min(nr, 32 / nk));
+    const size_t col = (size_t)op->N * 16;
+    const bool by = beta[0] != 0.0 || beta[1] != 0.0;
+    DevBuf xp, yp;
+    BG_CHECK(xp.alloc(col * nrhs), "product staging");
+    BG_CHECK(yp.alloc(col * nrhs), "product staging");
+    auto permute = [&](const void* src, long lds, void* dst, long ldd, bool to_slices, cudaMemcpyKind kind) {
+      for (int c0 = 0; c0 < nr; c0 += w) {
+        const int ws = std::min(w, nr - c0);
+        for (int q = 0; q < nk; ++q) {
+          const long user = q * nr + c0, perm = (long)c0 * nk + (long)q * ws;
+          const long cs = to_slices ? user : perm, cd = to_slices ? perm : user;
+          cudaError_t e = cudaMemcpy2DAsync(static_cast<char*>(dst) + (size_t)cd * ldd * 16, ldd * 16,
+                                            static_cast<const char*>(src) + (size_t)cs * lds * 16, lds * 16, col, ws,
+                                            kind, s);
+          if (e != cudaSuccess) return e;
+        }
+      }
+      return cudaSuccess;
+    };
+    const cudaMemcpyKind in = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    BG_CHECK(permute(x, ldx, xp.p, op->N, true, in), "product staging");
+    if (by) BG_CHECK(permute(y, ldy, yp.p, op->N, true, in), "product staging");
+    bg_status st = matvec_chunks(op, xp.p, op->N, yp.p, op->N, nrhs, alpha, beta, precision, 1, nk * w);
+    if (st != BG_OK) return st;
+    BG_CHECK(permute(yp.p, op->N, y, ldy, false, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost),
+             "product staging");
+    BG_CHECK(cudaStreamSynchronize(s), "H2 matvec");
+    return BG_OK;
+  }
+  return matvec_chunks(op, x, ldx, y, ldy, nrhs, alpha, beta, precision, on_device, 32);
 }

@@ -727,7 +727,7 @@ cudaError_t launch_build_h16_atiles(int np2, const double* F, long bstride, long
 }
 
 cudaError_t launch_build_h16_btiles(const FarH16Tiles& T, int nlev, int np2, int nrhs, cudaStream_t s) {
-  if (nlev < 1 || nlev > kMaxFarLevels || nrhs < 1 || nrhs > kN) return cudaErrorInvalidValue;
+  if (nlev < 1 || nlev > kMaxTileLevels || nrhs < 1 || nrhs > kN) return cudaErrorInvalidValue;
   int ncl_total = 0;
   for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
   if (ncl_total == 0) return cudaSuccess;
@@ -1110,7 +1110,7 @@ cudaError_t launch_build_h16c_atiles(int np2, const void* F, long bstride, long 
 
 cudaError_t launch_build_h16c_btiles(const FarH16Tiles& T, int nlev, int np2, int ldy, int y0, int nc,
                                      cudaStream_t s) {
-  if (nlev < 1 || nlev > kMaxFarLevels || nc < 1 || nc > kNC || y0 < 0 || y0 + nc > ldy) return cudaErrorInvalidValue;
+  if (nlev < 1 || nlev > kMaxTileLevels || nc < 1 || nc > kNC || y0 < 0 || y0 + nc > ldy) return cudaErrorInvalidValue;
   int ncl_total = 0;
   for (int l = 0; l < nlev; ++l) ncl_total += T.ncl[l];
   if (ncl_total == 0) return cudaSuccess;

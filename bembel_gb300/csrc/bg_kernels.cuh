@@ -144,17 +144,20 @@ struct FarTcLevels {
 // tiles (a) and their inverse scales (ainv, one per block), the right-hand-side
 // tiles of every cluster (b) and inverse column scales (binv, 32 per cluster),
 // both rebuilt per product from y by launch_build_h16_btiles, the product's
-// output (z) and the cluster count (ncl)
+// output (z) and the cluster count (ncl). A "level" here may also be one
+// level of one wavenumber of a batch (index q (L + 1) + l), hence the larger
+// bound (the structure is a kernel parameter of about 4.4 KB).
+constexpr int kMaxTileLevels = 64;
 struct FarH16Tiles {
-  const int* row_ptr[kMaxFarLevels];
-  const int* col[kMaxFarLevels];
-  const unsigned char* a[kMaxFarLevels];
-  const float* ainv[kMaxFarLevels];
-  unsigned char* b[kMaxFarLevels];
-  float* binv[kMaxFarLevels];
-  const float* y[kMaxFarLevels];
-  float* z[kMaxFarLevels];
-  int ncl[kMaxFarLevels];
+  const int* row_ptr[kMaxTileLevels];
+  const int* col[kMaxTileLevels];
+  const unsigned char* a[kMaxTileLevels];
+  const float* ainv[kMaxTileLevels];
+  unsigned char* b[kMaxTileLevels];
+  float* binv[kMaxTileLevels];
+  const float* y[kMaxTileLevels];
+  float* z[kMaxTileLevels];
+  int ncl[kMaxTileLevels];
 };
 size_t far_h16_atile_bytes(int np2);  // per low-rank block (0: shape not supported)
 size_t far_h16_btile_bytes(int np2);  // per cluster

@@ -166,6 +166,13 @@ struct bg_operator {
   std::vector<KSlot> kslots;
   int kslot_active = -1;
   DevBuf w_kx, w_ky;  // one column block of a batched product (row-major dof vectors)
+  // the batched product in one pass over all wavenumbers (kb_nwork > 0): per
+  // (wavenumber q, level l), index q (leaf_level + 1) + l, the right-hand-side
+  // tiles of the tensor-core far field; its work list over those indexes;
+  // superspace column blocks for the per-wavenumber near fields
+  std::vector<DevBuf*> kb_btiles, kb_binv;
+  DevBuf kb_work, kb_xs, kb_ys;
+  int kb_nwork = 0;
   bool kbatched() const { return !kslots.empty() && kslot_active < 0; }
   void swap_slot(int q) {
     KSlot& k = kslots[q];
@@ -191,6 +198,14 @@ struct bg_operator {
       for (auto v : {&k.far64, &k.far_df, &k.atiles, &k.ainv})
         for (auto b : *v) delete b;
     kslots.clear();
+    for (auto v : {&kb_btiles, &kb_binv}) {
+      for (auto b : *v) delete b;
+      v->clear();
+    }
+    kb_work.release();
+    kb_xs.release();
+    kb_ys.release();
+    kb_nwork = 0;
   }
 
   // device tables

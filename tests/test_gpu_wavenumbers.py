@@ -75,6 +75,9 @@ def test_batched_wavenumbers(ctx):
     vector, the potential and the solve covers all three, column block q with
     wavenumber q, and each block equals the single-wavenumber operator's
     result (products 1e-13 as above; the mixed and FP32 products to 1e-12).
+    The products run as one pass over all wavenumbers (one tensor-core
+    far-field launch per 16 columns of every block), also with 3 x 40 columns,
+    which the product takes in slices of 10 columns of every block.
     The batched solve is one flexible GMRES over the 3 x 4 columns; every
     block meets the FP64 residual 2e-8 of its own wavenumber's operator, also
     with 3 x 90 columns, which the solver takes in two slices of every
@@ -116,8 +119,17 @@ def test_batched_wavenumbers(ctx):
         assert res.max() < 2e-8, (q, res)
         pr = refs[q].potential(xq, pts)
         assert np.linalg.norm(pot[:, q * nr:(q + 1) * nr] - pr) / np.linalg.norm(pr) < 1e-14
+    # 40 columns per wavenumber: four slices of 10 columns of every block
+    xw = rng.uniform(-1, 1, (d.N, 3 * 40)) + 1j * rng.uniform(-1, 1, (d.N, 3 * 40))
+    for prec, tol in (("fp64", 1e-13), ("mixed", 1e-12)):
+        y = A.matvec(xw, precision=prec)
+        for q in range(3):
+            yr = refs[q].get_discrete_operator().matvec(xw[:, q * 40:(q + 1) * 40], precision=prec)
+            assert np.linalg.norm(y[:, q * 40:(q + 1) * 40] - yr) / np.linalg.norm(yr) < tol, (prec, q)
     with pytest.raises(bg.BembelError):
         A.matvec(x[:, :5])
+    with pytest.raises(bg.BembelError):
+        d.leaf_block(0)
     # 90 columns per wavenumber: the solve runs in slices of 85 and 5 columns
     # of every block (two batches); each block still solves its own system
     big = 90
