@@ -185,7 +185,10 @@ bg_status bg_operator_release_wavenumbers(bg_operator* op);
  * bg_load_vector and bg_potential take nrhs = n k columns (n wavenumbers,
  * k columns each) and apply wavenumber q to columns q k .. q k + k - 1: one
  * call, and for bg_solve one flexible GMRES over all n k columns, covers
- * every wavenumber. Other column counts give BG_INVALID_ARG;
+ * every wavenumber. A product makes one pass over all wavenumbers (the
+ * tensor-core far field of every wavenumber in one launch per 16 columns)
+ * when each has its tiles, else applies them one after another. Other
+ * column counts give BG_INVALID_ARG;
  * bg_matvec_noalloc and bg_operator_autotune give BG_UNSUPPORTED.
  * bg_operator_assemble (after bg_operator_set_wavenumber) returns the
  * operator to one wavenumber. Helmholtz single layer only. */
