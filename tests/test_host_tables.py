@@ -346,3 +346,18 @@ def test_cube_sphere_patches(bg_host, oracle):
     px, py = ctypes.c_int(), ctypes.c_int()
     st = bg._lib.load().bg_geometry_patch_data(g.h, 0, ctypes.byref(px), ctypes.byref(py), None)
     assert st == bg._lib.BG_UNSUPPORTED
+
+
+def test_batched_wavenumbers_host_only(bg_host):
+    """On a host-only context the batched-wavenumber entry points refuse to
+    assemble (no device), and an operator holds no wavenumber slots."""
+    from bembel_gb300 import BembelError
+    bg, ctx = bg_host
+    lin = bg.HelmholtzSingleLayerOperator()
+    lin.set_wavenumber(1.0)
+    d = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(SPHERE, ctx), 1, 1), lin, n_p=4)
+    assert len(d.wavenumbers()) == 0
+    with pytest.raises(BembelError):
+        d.assemble_wavenumbers()
+    d.release_wavenumbers()  # nothing to release: a no-op
+    assert len(d.wavenumbers()) == 0
