@@ -1102,9 +1102,14 @@ static bg_status near_quadrature(bg_operator* op, const NearWork& w, int nk, con
     cudaError_t e = dgx->upload(gr.x, s);
     if (e == cudaSuccess) e = dgw->upload(gr.w, s);
     if (e == cudaSuccess) e = dpairs->upload(kv.second, s);
+    // the common-edge and common-vertex rules have factorised one-wavenumber
+    // kernels (P <= 2, n1 <= 16), faster than sharing per-sample work over
+    // several wavenumbers; the identical-element rule shares it
+    const bool factorised = (cs == 3 || cs == 4) && op->P <= 2 && 2 * n1 <= 32;
     for (int q0 = 0; q0 < nk && e == cudaSuccess;) {
-      const int nb = multi ? std::min(kDuffyMaxWavenumbers, nk - q0) : 1;
-      if (multi)
+      const bool mk = multi && !factorised;
+      const int nb = mk ? std::min(kDuffyMaxWavenumbers, nk - q0) : 1;
+      if (mk)
         e = launch_near_duffy_multi(op->G, op->P, cs, pt, et, dpairs->as<NearPair>(), (int)kv.second.size(),
                                     dgx->as<double>(), dgw->as<double>(), n1, nb, kre + q0, kim + q0, out + q0, B, s);
       else

@@ -157,9 +157,10 @@ bg_status bg_operator_assemble(bg_operator* op);
  * DiscreteOperator::compute (Helmholtz/SingleLayerOperator.hpp:124-130,
  * H2Matrix.hpp:93-250). Assembles the near field (the dense leaves) of the
  * Helmholtz operator for the n wavenumbers kre[i] + i kim[i] in one pass:
- * every Duffy sample's points, surface measures and basis values are
- * evaluated once for up to 4 wavenumbers, and the regular pairs share their
- * per-element quadrature tables. The blocks stay on the device (n near
+ * the identical-element rule evaluates every Duffy sample's points, surface
+ * measures and basis values once for up to 4 wavenumbers, the common-edge
+ * and common-vertex rules run their factorised kernels per wavenumber, and
+ * the regular pairs share their per-element quadrature tables. The blocks stay on the device (n near
  * fields, bg_operator_memory counts them); after bg_operator_set_wavenumber
  * to one of them, bg_operator_assemble copies that near field instead of
  * integrating it again and assembles only the far field. A wavenumber
