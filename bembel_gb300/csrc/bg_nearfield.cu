@@ -395,6 +395,8 @@ __device__ inline double warp_sum(double v) {
   return v;
 }
 __device__ inline cd warp_sum(cd v) { return {warp_sum(v.re), warp_sum(v.im)}; }
+__device__ inline double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ inline cd shfl_xor(cd v, int o) { return {shfl_xor(v.re, o), shfl_xor(v.im, o)}; }
 
 template <int P, typename S>
 struct RankOneStage {
@@ -662,6 +664,158 @@ __global__ void __launch_bounds__(128) k_near_vertex(PatchTable pt, ElementTable
   write_block<P, S, PER>(acc, st, warp, lane, out, pr.dst, B);
 }
 
+// Identical element (integrate2.hpp:41-60), one wavenumber, P <= 2,
+// n1 <= 16. With t1 = e0 (1 - x0), t3 = t1 + x0 (depending on e0) and
+// t2 = e1 (1 - x0 x1), t4 = t2 + x0 x1 (depending on e1), the four point
+// pairs are A = (t1, t2), B = (t3, t4); A = (t1, t4), B = (t3, t2);
+// A = (t2, t1), B = (t4, t3); A = (t2, t3), B = (t4, t1). For a fixed
+// (outer node, e0) every point lies on one of four patch lines (s fixed at
+// t1 or t3, or t fixed at t1 or t3), contracted once (SurfaceLine), and each
+// basis product splits into an e0 part and an e1 part, e.g. pair 0:
+// phi_a(A) phi_b(B) = [B_ax(t1) B_bx(t3)] [B_ay(t2) B_by(t4)]. So the e1 sums
+// are accumulated as three p^2-vectors per (outer node, e0) and added to the
+// block as Kronecker products; the symmetric half (the pairs with A and B
+// exchanged) is the transpose, added once at the end. A half-warp takes one
+// e0 node, its lanes the e1 nodes.
+template <int G, int P, typename S>
+__global__ void __launch_bounds__(128) k_near_identical(PatchTable pt, ElementTable et,
+                                                        const NearPair* __restrict__ pairs,
+                                                        const double* __restrict__ gx, const double* __restrict__ gw,
+                                                        int n1, double kre, double kim, S* __restrict__ out, int B) {
+  constexpr int P1 = P + 1, P2 = P1 * P1, NE = P2 * P2;
+  constexpr int PER = (NE + 31) / 32;
+  __shared__ RankOneStage<P, S> st;  // final reduction only
+  __shared__ SurfaceLine<G> lines[kEdgeNW][2][4];
+  __shared__ double fb[kEdgeNW][2][2 * P1];  // per half: Bernstein values at t1, t3
+  __shared__ S fv[kEdgeNW][2][3 * P2];       // per half: the three e1 sums
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, half = lane >> 4, l16 = lane & 15;
+  const NearPair pr = pairs[blockIdx.x];
+  const int p1 = et.patch[pr.e1];
+  const double a0 = et.llc[2 * pr.e1], a1 = et.llc[2 * pr.e1 + 1];
+  const double h = et.h;
+  const int Q = n1 * n1;
+  S acc[PER];
+#pragma unroll
+  for (int m = 0; m < PER; ++m) acc[m] = zero<S>();
+  for (int i = warp; i < Q; i += kEdgeNW) {
+    const double x0 = gx[i / n1], x1 = gx[i % n1], wi = gw[i / n1] * gw[i % n1];
+    const double w = h * h * wi * x0 * (1 - x0) * (1 - x0 * x1);
+    for (int e0b = 0; e0b < n1; e0b += 2) {
+      const int m0 = e0b + half;
+      const bool act0 = m0 < n1;
+      const double t1 = act0 ? gx[m0] * (1 - x0) : 0.5, t3 = t1 + x0;
+      // lines 0: s = t1, 1: s = t3, 2: t = t1, 3: t = t3 (element coordinates)
+      if (act0 && l16 < 4)
+        surface_line<G>(pt, p1, l16 < 2, (l16 < 2 ? a0 : a1) + h * ((l16 & 1) ? t3 : t1), lines[warp][half][l16]);
+      if (act0 && l16 >= 4 && l16 < 6) {
+        double b[P1];
+        bern<P1>(P, l16 == 4 ? t1 : t3, b);
+#pragma unroll
+        for (int q = 0; q < P1; ++q) fb[warp][half][(l16 - 4) * P1 + q] = b[q];
+      }
+      __syncwarp();
+      const bool act = act0 && l16 < n1;
+      const int m1 = act ? l16 : 0;
+      const double t2 = gx[m1] * (1 - x0 * x1), t4 = t2 + x0 * x1;
+      const double wj = act ? w * gw[m0 < n1 ? m0 : 0] * gw[m1] : 0.0;
+      S vL[P2], v2[P2], v3[P2];
+#pragma unroll
+      for (int q = 0; q < P2; ++q) vL[q] = v2[q] = v3[q] = zero<S>();
+      if (act) {
+        const SurfaceLine<G>* L = lines[warp][half];
+        // points and surface measures: L1(t2), L3(t4), L1(t4), L3(t2), M1(t2), M3(t4), M3(t2), M1(t4)
+        double X[8][3], J[8];
+        const int li[8] = {0, 1, 0, 1, 2, 3, 3, 2};
+        const double tv[8] = {t2, t4, t4, t2, t2, t4, t2, t4};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          double dx[3], dy[3];
+          surface_line_point<G>(L[li[k]], (li[k] < 2 ? a1 : a0) + h * tv[k], X[k], dx, dy);
+          J[k] = surface_measure(dx, dy);
+        }
+        double b2[P1], b4[P1];
+        bern<P1>(P, t2, b2);
+        bern<P1>(P, t4, b4);
+        S c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int ia = 2 * k, ib = 2 * k + 1;
+          const double d0 = X[ia][0] - X[ib][0], d1 = X[ia][1] - X[ib][1], d2 = X[ia][2] - X[ib][2];
+          c[k] = scale_of(kernel_val<S>(fma(d0, d0, fma(d1, d1, d2 * d2)), kre, kim), wj * J[ia] * J[ib]);
+        }
+#pragma unroll
+        for (int ya = 0; ya < P1; ++ya)
+#pragma unroll
+          for (int yb = 0; yb < P1; ++yb) {
+            const int q = ya * P1 + yb;
+            // pairs 0, 1 vary in the second coordinate: (A, B) = (t2, t4) and (t4, t2)
+            vL[q] = fmac(fmac(vL[q], c[0], b2[ya] * b4[yb]), c[1], b4[ya] * b2[yb]);
+            // pairs 2, 3 vary in the first coordinate: (A, B) = (t2, t4)
+            v2[q] = fmac(v2[q], c[2], b2[ya] * b4[yb]);
+            v3[q] = fmac(v3[q], c[3], b2[ya] * b4[yb]);
+          }
+      }
+      // sums over the half-warp's e1 nodes
+#pragma unroll
+      for (int q = 0; q < P2; ++q) {
+#pragma unroll
+        for (int o = 8; o; o >>= 1) {
+          vL[q] = vL[q] + shfl_xor(vL[q], o);
+          v2[q] = v2[q] + shfl_xor(v2[q], o);
+          v3[q] = v3[q] + shfl_xor(v3[q], o);
+        }
+      }
+      if (l16 == 0 && act0) {
+#pragma unroll
+        for (int q = 0; q < P2; ++q) {
+          fv[warp][half][q] = vL[q];
+          fv[warp][half][P2 + q] = v2[q];
+          fv[warp][half][2 * P2 + q] = v3[q];
+        }
+      }
+      __syncwarp();
+      // block S(a, b), a = ay P1 + ax, b = by P1 + bx:
+      //   F_L(ax, bx) vL(ay, by) + v2(ax, bx) F2(ay, by) + v3(ax, bx) F3(ay, by)
+      // with F_L(x, y) = F2(x, y) = B_x(t1) B_y(t3), F3(x, y) = B_x(t3) B_y(t1)
+#pragma unroll
+      for (int hf = 0; hf < 2; ++hf) {
+        if (e0b + hf >= n1) break;
+        const double* f1 = fb[warp][hf];
+        const double* f3 = f1 + P1;
+        const S* v = fv[warp][hf];
+#pragma unroll
+        for (int m = 0; m < PER; ++m) {
+          const int e = lane + 32 * m;
+          if (e < NE) {
+            const int a = e % P2, b = e / P2;
+            const int ax = a % P1, ay = a / P1, bx = b % P1, by = b / P1;
+            acc[m] = fmac(acc[m], v[ay * P1 + by], f1[ax] * f3[bx]);
+            acc[m] = fmac(acc[m], v[P2 + ax * P1 + bx], f1[ay] * f3[by]);
+            acc[m] = fmac(acc[m], v[2 * P2 + ax * P1 + bx], f3[ay] * f1[by]);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // sum the warps, then add the transpose (the pairs with A and B exchanged)
+  S* red = &st.v[0][0];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < PER; ++m) {
+    const int e = lane + 32 * m;
+    if (e < NE) red[warp * 32 * P2 + e] = acc[m];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < NE; e += blockDim.x) {
+    const int a = e % P2, b = e / P2, et2 = b + a * P2;
+    S v = red[e] + red[et2];
+#pragma unroll
+    for (int w2 = 1; w2 < kEdgeNW; ++w2) v = v + red[w2 * 32 * P2 + e] + red[w2 * 32 * P2 + et2];
+    out[pr.dst + (long)b * B + a] = v;
+  }
+}
+
 template <int G, int P, typename S, int NK>
 static cudaError_t run_duffy_k(int cs, const PatchTable& pt, const ElementTable& et, const NearPair* pairs,
                                int npairs, const double* gx, const double* gw, int n1, const KBatch<S, NK>& kb, int B,
@@ -674,6 +828,10 @@ static cudaError_t run_duffy_k(int cs, const PatchTable& pt, const ElementTable&
     }
     if (cs == 4) {
       k_near_vertex<G, P, S><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb.kre[0], kb.kim[0], kb.out[0], B);
+      return cudaGetLastError();
+    }
+    if (cs == 2 && 2 * n1 <= 32) {
+      k_near_identical<G, P, S><<<npairs, 128, 0, s>>>(pt, et, pairs, gx, gw, n1, kb.kre[0], kb.kim[0], kb.out[0], B);
       return cudaGetLastError();
     }
   }
