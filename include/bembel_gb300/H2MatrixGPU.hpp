@@ -110,6 +110,13 @@ class Geometry {
                   ctx.get());
     return Geometry(ctx, g);
   }
+  // the unit sphere as six analytic patches x/|x| of the cube faces (no
+  // Bembel counterpart; see bg_geometry_cube_sphere)
+  static Geometry cube_sphere(const Context& ctx) {
+    bg_geometry* g = nullptr;
+    detail::check(bg_geometry_cube_sphere(ctx.get(), &g), ctx.get());
+    return Geometry(ctx, g);
+  }
   int num_patches() const {
     int n = 0;
     detail::check(bg_geometry_num_patches(h_.get(), &n), ctx_.get());

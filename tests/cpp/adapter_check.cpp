@@ -75,6 +75,20 @@ int main(int argc, char** argv) {
     threw = e.status() == BG_INVALID_ARG;
   }
   if (!threw) return fail("invalid launch plan not reported");
+  // the analytic cube sphere: six patches without control data, an operator
+  // on it has the same unknowns as on the NURBS sphere
+  Geometry cs = Geometry::cube_sphere(ctx);
+  if (cs.num_patches() != 6) return fail("cube sphere patches");
+  threw = false;
+  try {
+    int a = 0, b = 0;
+    cs.patch_data(0, &a, &b);
+  } catch (const Error& e) {
+    threw = e.status() == BG_UNSUPPORTED;
+  }
+  if (!threw) return fail("cube sphere patch data not refused");
+  Operator<double> C(cs, 3, 1, BG_LAPLACE_SL);
+  if (C.rows() != A.rows()) return fail("cube sphere dofs");
   if (gpu) {
     Operator<double> B(h, 2, 1, BG_LAPLACE_SL);
     B.assemble();
