@@ -1047,6 +1047,24 @@ def run_profile_case(args):
         print(json.dumps({"profile": "matvec", "workload": "maxwell", "precision": args.precision, "M": m, "N": op.N,
                           "products": 5}))
         return
+    if args.profile == "batched":
+        # Helmholtz on the torus (M = --profile-m, default 3), 4 wavenumbers
+        # assembled side by side, three mixed products of 4 x 16 columns
+        lin = bg.HelmholtzSingleLayerOperator()
+        lin.set_wavenumber(1.0)
+        mb = args.profile_m if args.profile_m is not None else 3
+        op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(os.path.join(ROOT, "tests", "golden", "geo", "torus.dat"),
+                                                            ctx), mb, P), lin, n_p=10)
+        ks = [1.0, 2.0, 3.0, 4.0]
+        op.prepare_wavenumbers(ks)
+        op.assemble_wavenumbers()
+        A = op.get_discrete_operator()
+        x = torch.randn(op.N, 4 * 16, dtype=torch.complex128, device="cuda")
+        for _ in range(3):
+            A.matvec(x, precision="mixed")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "batched", "M": mb, "N": op.N, "kappas": ks, "columns": 64, "products": 3}))
+        return
     op = bg.DiscreteOperator(bg.AnsatzSpace(bg.Geometry(GEO, ctx), m, P), bg.LaplaceSingleLayerOperator(), n_p=NP,
                              store_fp64_far=store)
     op.compute()
@@ -1073,7 +1091,7 @@ def main():
     ap.add_argument("--inner", default="mixed", choices=["mixed", "fp32"],
                     help="precision of the inner (preconditioning) operator: mixed (near field FP64-accurate, the "
                          "workload's mixed form) or fp32 (near field FP32 as well)")
-    ap.add_argument("--profile", choices=["matvec", "solve"], default=None,
+    ap.add_argument("--profile", choices=["matvec", "solve", "batched"], default=None,
                     help="run a small fixed case for ncu instead of the benchmark")
     ap.add_argument("--precision", default="fp32", choices=["fp64", "mixed", "fp32"],
                     help="product precision of --profile matvec")
